@@ -1,0 +1,128 @@
+/*
+ * sssi_gb300.h -- C ABI of libsssi_gb300, a GB300 (sm_103a) implementation of
+ * SSSI's acoustic finite-difference time-domain core with a convolutional
+ * perfectly matched layer (CPML) and the reverse-time-migration imaging
+ * condition.
+ *
+ * Conventions shared by every entry point
+ *   - Arrays are column-major (MATLAB order) double precision unless stated:
+ *     v[z + x*nz], source[z + x*nz + t*nz*nx], data[x + t*nx],
+ *     snapshot[z + x*nz + t*nz*nx]; 3D adds y after x.
+ *   - nz, nx (, ny) are the sizes of the model handed over, i.e. already padded
+ *     by extBoundary (src/extBoundary.m:22-39): nBoundary damping cells on the
+ *     bottom, left and right (and front/rear); the top is a free surface.
+ *   - Pointers may be host memory or device memory of the current CUDA device;
+ *     the library detects which.  Host inputs are copied in and host outputs
+ *     copied back inside the call.  Optional outputs may be NULL.
+ *   - Every function returns SSSI_OK (0) or an SSSI_ERR_* code;
+ *     sssi_last_error() gives the message of the calling thread's last failure.
+ *   - Calls are synchronous: outputs are complete when the call returns.
+ */
+#ifndef SSSI_GB300_H
+#define SSSI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SSSI_OK 0
+#define SSSI_ERR_ARG 1      /* invalid argument (sizes, orders, pointers) */
+#define SSSI_ERR_CUDA 2     /* CUDA runtime error, or no usable GPU */
+#define SSSI_ERR_NOMEM 3    /* device or host allocation failed */
+#define SSSI_ERR_UNSTABLE 4 /* the wavefield became non-finite (CFL violated) */
+#define SSSI_ERR_BUSY 5     /* admission refused: not enough device memory now */
+#define SSSI_ERR_INTERNAL 6
+
+/* ---- arithmetic modes ---- */
+/* FP64 with the reference's rounding sequence (no fused multiply-add,
+ * c_k*(a-b)/d per term): results are bit-identical to the reference C
+ * gateways compiled without contraction. */
+#define SSSI_MODE_FP64_STRICT 0
+/* FP64 with folded coefficients w_k = c_k/d and fused multiply-adds:
+ * same algorithm, rounding differs from the reference at the 1e-16 level. */
+#define SSSI_MODE_FP64 1
+/* FP32 wavefield, FP64 CPML memory variables and FP64 imaging sums. */
+#define SSSI_MODE_FP32 2
+
+/* Message of the calling thread's last failure ("" after a success). */
+const char *sssi_last_error(void);
+
+/* Library version as 10000*major + 100*minor + patch. */
+int sssi_version(void);
+
+/* Number of CUDA kernels this library has launched so far in this process. */
+int64_t sssi_launch_count(void);
+
+/* Releases device and pinned host buffers cached between calls. */
+int sssi_release_cache(void);
+
+/* Stream the library launches on (a cudaStream_t; NULL = legacy default). */
+int sssi_set_stream(void *stream);
+
+/* ---- host-side building blocks ---- */
+
+/* Staggered-grid first-derivative coefficients of half-order `order`
+ * (1..8): solves A c = e1 with A_ij = (2j-1)^(2i-1) by LU with partial
+ * pivoting.  Replaces dCoef(order, "s"), src/fd_cmex/finiteDifference.c:24-82,
+ * which calls MATLAB's mldivide. */
+int sssi_dCoef(int order, double *coeff);
+
+/* CPML damping d = -(3v)/(2L) * ln(1e-6) * (u/L)^2 for `count` cells.
+ * Replaces dampPml, src/fd_cmex/finiteDifference.c:253-280. */
+int sssi_dampPml(const double *u, const double *v, int64_t count, double L, double *d);
+
+/* ---- drop-in propagators (the MEX gateways' work, plain pointers) ---- */
+
+/* 2D forward modelling.  v: nz x nx; source: nz x nx x nt (dense, as the
+ * MEX takes it); outputs data: nx x nt (top interior row of every step),
+ * snapshot: nz x nx x nt (interior of every step), either may be NULL.
+ * Replaces fwdTimeCpmlFor2dAw_mex, src/fd_cmex/fwdTimeCpmlFor2dAw_mex.c:39-290. */
+int sssi_fwdTimeCpmlFor2dAw(const double *v, const double *source, int64_t nz, int64_t nx, int64_t nt,
+                            int nDiffOrder, int nBoundary, double dz, double dx, double dt, double *data,
+                            double *snapshot, int mode);
+
+/* 2D reverse propagation: data (nx x nt) injected on the top interior row
+ * with time running nt-1..0.  model: (nz+2l) x (nx+2l), l = 2*nDiffOrder-1,
+ * the padded wavefield one step before the last one computed (as the
+ * reference returns it); snapshot: nz x nx x nt.
+ * Replaces rvsTimeCpmlFor2dAw_mex, src/fd_cmex/rvsTimeCpmlFor2dAw_mex.c:38-287. */
+int sssi_rvsTimeCpmlFor2dAw(const double *v, const double *data, int64_t nz, int64_t nx, int64_t nt,
+                            int nDiffOrder, int nBoundary, double dz, double dx, double dt, double *model,
+                            double *snapshot, int mode);
+
+/* ---- native forms (sparse sources, fused imaging) ---- */
+
+/* 2D forward modelling with point sources: source s sits at interior cell
+ * (src_iz[s], src_ix[s]) with amplitude wavelets[s*nt + t] at step t.
+ * data / snapshot as sssi_fwdTimeCpmlFor2dAw (either may be NULL). */
+int sssi_fwdTimeCpmlFor2dAwPoint(const double *v, int64_t nz, int64_t nx, int64_t nt, int nDiffOrder,
+                                  int nBoundary, double dz, double dx, double dt, int nsrc,
+                                  const int64_t *src_iz, const int64_t *src_ix, const double *wavelets,
+                                  double *data, double *snapshot, int mode);
+
+/* One reverse-time-migration shot, the work of
+ * applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:156-166,252-275,315
+ * done on the device: forward modelling of the point source in v (true
+ * model) and vs (migration model), reverse propagation of
+ * dataTrue - dataSmooth in v, and the zero-lag imaging condition
+ *     image = M ./ s2,  M = sum_t f_t .* r_t,  s2 = epsilon + sum_t f_t.^2
+ * with f the forward field in vs and r the reverse field.
+ * SSSI_MODE_FP64_STRICT / SSSI_MODE_FP64 keep every forward snapshot in FP64
+ * and image every step.  SSSI_MODE_FP32 stores the forward field every
+ * `snap_stride` steps in FP16 with one power-of-two scale per snapshot and
+ * images those steps (sums scaled by snap_stride), with FP64 accumulators.
+ * image: nz x nx; data_true / data_smooth: nx x nt (may be NULL). */
+int sssi_rtmTimeCpmlFor2dAw(const double *v, const double *vs, int64_t nz, int64_t nx, int64_t nt,
+                            int nDiffOrder, int nBoundary, double dz, double dx, double dt,
+                            const double *wavelet, int64_t src_iz, int64_t src_ix, double epsilon, int mode,
+                            int snap_stride, double *image, double *data_true, double *data_smooth);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SSSI_GB300_H */

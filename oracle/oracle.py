@@ -1,0 +1,552 @@
+"""CPU oracle for SSSI's acoustic CPML finite-difference hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg import this module, and only as the checker;
+the product (``sssi_gb300``) never imports it.
+
+Three layers, each pinned against the next:
+
+* :class:`RefMex` -- the reference's own C gateways
+  (``src/fd_cmex/fwdTimeCpmlFor2dAw_mex.c``, ``rvsTimeCpmlFor2dAw_mex.c``)
+  compiled unmodified against the project's ``mex.h`` shim into
+  ``oracle/_ref/`` (``make -C oracle ref``).  Available only where the
+  reference tree exists; it pins the two restatements below and generates the
+  committed golden vectors in ``tests/golden/``.
+* :class:`COracle` -- ``oracle/sssi_oracle.c``, a C99 restatement of the same
+  algorithm (2D forward/reverse, 3D forward, imaging), bit-identical to
+  :class:`RefMex` on every case the tests run.  It is the checker on machines
+  without the reference tree and the CPU baseline timed by ``bench.py``.
+* the numpy functions below -- a vectorised restatement of the MATLAB twins
+  (``src/fd_matlab/fwdTimeCpmlFor2dAw.m:88-119``,
+  ``src/fd_matlab/rvsTimeCpmlFor2dAw.m:82-127``, ``src/fwdTimeCpmlFor3dAw.m:110-147``)
+  with the same operation order, used for small cases and for the 3D path,
+  which has no C in the reference.
+
+Array conventions follow MATLAB: a model ``v`` is indexed ``v[z, x]`` (or
+``v[z, x, y]``), sources ``source[z, x, t]``, data ``data[x, t]``, snapshots
+``snapshot[z, x, t]``; all are handed to C as column-major (Fortran) memory.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+BUILD_DIR = ORACLE_DIR / "_build"
+REF_DIR = ORACLE_DIR / "_ref"
+REFERENCE_SRC = Path(os.environ.get("SSSI_REFERENCE_SRC", "/root/reference/src/fd_cmex"))
+
+_i64 = ctypes.c_int64
+# glibc's log/exp, as the C gateways use (numpy's vectorised loops may round differently)
+_LOGR = math.log(1e-6)
+_exp = np.vectorize(math.exp, otypes=[float])
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the C restatement (always) and the reference gateways (when the
+    reference tree is present, or when ``reference`` is True)."""
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "all"], check=True)
+    if reference is None:
+        reference = (REFERENCE_SRC / "fwdTimeCpmlFor2dAw_mex.c").exists()
+    if reference:
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF_SRC={REFERENCE_SRC}"], check=True)
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+# --------------------------------------------------------------------------
+# C restatement
+# --------------------------------------------------------------------------
+class COracle:
+    """ctypes view of ``oracle/_build/liboracle.so`` (build it with :func:`build`)."""
+
+    def __init__(self, path: Path | None = None):
+        path = Path(path or BUILD_DIR / "liboracle.so")
+        if not path.exists():
+            build(reference=False)
+        self.lib = ctypes.CDLL(str(path))
+        L = self.lib
+        L.orc_dcoef.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_damp_pml.argtypes = [_dp, _dp, _i64, ctypes.c_double, _dp]
+        L.orc_damping_2d.argtypes = [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, _dp, _dp]
+        L.orc_damping_3d.argtypes = [_dp, _i64, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]
+        L.orc_fwd2d.argtypes = [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp]
+        L.orc_rvs2d.argtypes = [_dp, _dp, _i64, _i64, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _dp]
+        L.orc_fwd3d.argtypes = [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64, _i64, _i64, ctypes.c_int,
+                                ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                _dp, _dp]
+        L.orc_image_accum.argtypes = [_dp, _dp, _i64, _dp, _dp]
+        L.orc_image_stack.argtypes = [_dp, _dp, _i64, _dp]
+        L.orc_num_threads.restype = ctypes.c_int
+        L.orc_set_num_threads.argtypes = [ctypes.c_int]
+
+    def set_threads(self, n: int) -> None:
+        self.lib.orc_set_num_threads(int(n))
+
+    def threads(self) -> int:
+        return int(self.lib.orc_num_threads())
+
+    def dcoef(self, order: int) -> np.ndarray:
+        c = np.zeros(order)
+        if self.lib.orc_dcoef(order, 1, _ptr(c)):
+            raise ValueError("order out of range")
+        return c
+
+    def damping_2d(self, v, nB, dz, dx, dt):
+        v = _f64(v)
+        nz, nx = v.shape
+        xb = np.zeros((nz, nx), order="F")
+        zb = np.zeros((nz, nx), order="F")
+        self.lib.orc_damping_2d(_ptr(v), nz, nx, nB, dz, dx, dt, _ptr(xb), _ptr(zb))
+        return xb, zb
+
+    def damping_3d(self, v, nB, dt):
+        v = _f64(v)
+        nz, nx, ny = v.shape
+        out = [np.zeros((nz, nx, ny), order="F") for _ in range(3)]
+        self.lib.orc_damping_3d(_ptr(v), nz, nx, ny, nB, dt, *[_ptr(a) for a in out])
+        return tuple(out)
+
+    def fwd2d(self, v, source, N, nB, dz, dx, dt, *, nt=None, point=None, want_snapshot=True):
+        """Forward modelling.  ``source`` dense (nz, nx, nt), or None with
+        ``point=(trace, iz, ix)`` for a single point source."""
+        v = _f64(v)
+        nz, nx = v.shape
+        if source is not None:
+            source = _f64(source)
+            nt = source.shape[2]
+            trace, iz, ix = None, 0, 0
+        else:
+            trace, iz, ix = point
+            trace = np.ascontiguousarray(trace, dtype=np.float64)
+            nt = nt or trace.shape[0]
+        data = np.zeros((nx, nt), order="F")
+        snap = np.zeros((nz, nx, nt), order="F") if want_snapshot else None
+        rc = self.lib.orc_fwd2d(_ptr(v), _ptr(source), _ptr(trace), iz, ix, nz, nx, nt, N, nB, dz, dx, dt,
+                                _ptr(data), _ptr(snap))
+        if rc:
+            raise ValueError("orc_fwd2d failed")
+        return data, snap
+
+    def rvs2d(self, v, data, N, nB, dz, dx, dt, *, want_snapshot=True, fwd_snapshot=None):
+        v = _f64(v)
+        data = _f64(data)
+        nz, nx = v.shape
+        nt = data.shape[1]
+        l = 2 * N - 1
+        model = np.zeros((nz + 2 * l, nx + 2 * l), order="F")
+        snap = np.zeros((nz, nx, nt), order="F") if want_snapshot else None
+        m = s2 = None
+        if fwd_snapshot is not None:
+            fwd_snapshot = _f64(fwd_snapshot)
+            m = np.zeros((nz, nx), order="F")
+            s2 = np.zeros((nz, nx), order="F")
+        rc = self.lib.orc_rvs2d(_ptr(v), _ptr(data), nz, nx, nt, N, nB, dz, dx, dt, _ptr(model), _ptr(snap),
+                                _ptr(fwd_snapshot), _ptr(m), _ptr(s2))
+        if rc:
+            raise ValueError("orc_rvs2d failed")
+        if fwd_snapshot is not None:
+            return model, snap, m, s2
+        return model, snap
+
+    def fwd3d(self, v, source, N, nB, dz, dx, dy, dt, *, nt=None, point=None, want_snapshot=True):
+        v = _f64(v)
+        nz, nx, ny = v.shape
+        if source is not None:
+            source = _f64(source)
+            nt = source.shape[3]
+            trace, iz, ix, iy = None, 0, 0, 0
+        else:
+            trace, iz, ix, iy = point
+            trace = np.ascontiguousarray(trace, dtype=np.float64)
+            nt = nt or trace.shape[0]
+        data = np.zeros((nx, ny, nt), order="F")
+        snap = np.zeros((nz, nx, ny, nt), order="F") if want_snapshot else None
+        rc = self.lib.orc_fwd3d(_ptr(v), _ptr(source), _ptr(trace), iz, ix, iy, nz, nx, ny, nt, N, nB, dz, dx, dy,
+                                dt, _ptr(data), _ptr(snap))
+        if rc:
+            raise ValueError("orc_fwd3d failed")
+        return data, snap
+
+    def image(self, fwd_snap, rvs_snap, epsilon):
+        """M./s2 with the sums taken in ascending time order
+        (mainRtmTimeCpmlFor2dAw.m:268-275)."""
+        f = _f64(fwd_snap)
+        r = _f64(rvs_snap)
+        nz, nx, nt = f.shape
+        m = np.zeros((nz, nx), order="F")
+        s2 = np.full((nz, nx), float(epsilon), order="F")
+        for t in range(nt):
+            ft = np.asfortranarray(f[:, :, t])
+            rt = np.asfortranarray(r[:, :, t])
+            self.lib.orc_image_accum(_ptr(ft), _ptr(rt), nz * nx, _ptr(m), _ptr(s2))
+        return m, s2
+
+    def rtm2d(self, v, vs, trace, src_iz, src_ix, N, nB, dz, dx, dt, epsilon):
+        """One reference RTM shot (mainRtmTimeCpmlFor2dAw.m:156-166,252-275,315):
+        data in V and VS, reverse propagation of their difference in V, zero-lag
+        imaging against the VS forward snapshots.  Returns (image, dataTrue,
+        dataSmooth) with image = M ./ s2 (one shot's contribution to Stacked)."""
+        d_true, _ = self.fwd2d(v, None, N, nB, dz, dx, dt, point=(trace, src_iz, src_ix), want_snapshot=False)
+        d_smooth, f_snap = self.fwd2d(vs, None, N, nB, dz, dx, dt, point=(trace, src_iz, src_ix))
+        delta = d_true - d_smooth
+        _, r_snap = self.rvs2d(v, delta, N, nB, dz, dx, dt)
+        m, s2 = self.image(f_snap, r_snap, epsilon)
+        stacked = np.zeros_like(m, order="F")
+        self.lib.orc_image_stack(_ptr(m), _ptr(s2), m.size, _ptr(stacked))
+        return stacked, d_true, d_smooth
+
+
+# --------------------------------------------------------------------------
+# reference gateways on the shim
+# --------------------------------------------------------------------------
+class RefMex:
+    """One reference MEX gateway compiled from the reference tree on the shim.
+
+    ``name`` is the gateway file stem, e.g. ``fwdTimeCpmlFor2dAw_mex``;
+    ``variant`` is "" (parity build), "_o3" (reference flags) or "openmp".
+    """
+
+    def __init__(self, name: str, variant: str = ""):
+        if variant == "openmp":
+            stem = name.replace("_mex", "_openmp_mex")
+        else:
+            stem = name + variant
+        path = REF_DIR / f"{stem}.so"
+        if not path.exists():
+            raise FileNotFoundError(f"{path} (build with `make -C oracle ref` where the reference tree exists)")
+        self.lib = load_shim_library(path)
+
+    def call(self, nlhs: int, *args):
+        return shim_call(self.lib, nlhs, *args)
+
+    def dcoef(self, order: int) -> np.ndarray:
+        self.lib.dCoef.restype = _dp
+        self.lib.dCoef.argtypes = [ctypes.c_int, ctypes.c_char_p]
+        p = self.lib.dCoef(order, b"s")
+        return np.array([p[i] for i in range(order)])
+
+
+def available_reference() -> bool:
+    return (REF_DIR / "fwdTimeCpmlFor2dAw_mex.so").exists()
+
+
+def load_shim_library(path) -> ctypes.CDLL:
+    """Load a gateway library linked with the shim and declare the harness."""
+    lib = ctypes.CDLL(str(path), mode=ctypes.RTLD_LOCAL)
+    vp = ctypes.c_void_p
+    lib.shim_array_new.restype = vp
+    lib.shim_array_new.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    lib.shim_array_borrow.restype = vp
+    lib.shim_array_borrow.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), _dp]
+    lib.shim_array_free.argtypes = [vp]
+    lib.shim_array_data.restype = _dp
+    lib.shim_array_data.argtypes = [vp]
+    lib.shim_array_ndim.restype = ctypes.c_int
+    lib.shim_array_ndim.argtypes = [vp]
+    lib.shim_array_dim.restype = ctypes.c_longlong
+    lib.shim_array_dim.argtypes = [vp, ctypes.c_int]
+    lib.shim_last_error.restype = ctypes.c_char_p
+    lib.shim_call.restype = ctypes.c_int
+    lib.shim_call.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(vp)]
+    return lib
+
+
+class MexError(RuntimeError):
+    pass
+
+
+def shim_call(lib, nlhs: int, *args):
+    """Call ``mexFunction`` of ``lib`` with numpy arguments (scalars become 1x1).
+    Returns a tuple of nlhs Fortran-ordered arrays; raises MexError with the
+    gateway's message when it calls mexErrMsgTxt."""
+    keep = []
+    prhs = (ctypes.c_void_p * max(len(args), 1))()
+    for k, a in enumerate(args):
+        arr = _f64(np.atleast_1d(a) if np.ndim(a) == 0 else a)
+        keep.append(arr)
+        dims = (ctypes.c_longlong * max(arr.ndim, 2))(*(list(arr.shape) + [1] * (2 - arr.ndim)))
+        prhs[k] = lib.shim_array_borrow(max(arr.ndim, 2), dims, _ptr(arr))
+    plhs = (ctypes.c_void_p * max(nlhs, 2))()
+    try:
+        rc = lib.shim_call(nlhs, plhs, len(args), prhs)
+        if rc:
+            raise MexError(lib.shim_last_error().decode())
+        outs = []
+        for k in range(max(nlhs, 1)):
+            a = plhs[k]
+            if not a:
+                outs.append(None)
+                continue
+            nd = lib.shim_array_ndim(a)
+            shape = tuple(lib.shim_array_dim(a, i) for i in range(nd))
+            n = int(np.prod(shape))
+            out = np.empty(shape, order="F")
+            if n:
+                ctypes.memmove(out.ctypes.data, lib.shim_array_data(a), n * 8)
+            outs.append(out)
+        return tuple(outs)
+    finally:
+        for k in range(len(args)):
+            lib.shim_array_free(prhs[k])
+        for k in range(max(nlhs, 2)):
+            if plhs[k]:
+                lib.shim_array_free(plhs[k])
+
+
+# --------------------------------------------------------------------------
+# numpy restatement (MATLAB twins)
+# --------------------------------------------------------------------------
+def dcoef(order: int) -> np.ndarray:
+    """dCoef(order, 's') by LU with partial pivoting (src/dCoef.m:35-48)."""
+    n = order
+    A = np.array([[float((2 * j + 1) ** (2 * i + 1)) for j in range(n)] for i in range(n)])
+    x = np.zeros(n)
+    x[0] = 1.0
+    piv = list(range(n))
+    for k in range(n):
+        p = k + int(np.argmax(np.abs(A[k:, k])))
+        piv[k] = p
+        if p != k:
+            A[[k, p], :] = A[[p, k], :]
+        if A[k, k] != 0.0:
+            r = 1.0 / A[k, k]
+            A[k + 1:, k] *= r
+        for j in range(k + 1, n):
+            t = -A[k, j]
+            A[k + 1:, j] += A[k + 1:, k] * t
+    for k in range(n):
+        if piv[k] != k:
+            x[k], x[piv[k]] = x[piv[k]], x[k]
+    for k in range(n):
+        if x[k] != 0.0:
+            x[k + 1:] -= x[k] * A[k + 1:, k]
+    for k in range(n - 1, -1, -1):
+        if x[k] != 0.0:
+            x[k] /= A[k, k]
+            x[:k] -= x[k] * A[:k, k]
+    return x
+
+
+def damp_pml_c(u, v, L):
+    """finiteDifference.c:253-280 operation order."""
+    d0 = -(3.0 * v) / (2 * L) * _LOGR
+    return d0 * (u / L) * (u / L)
+
+
+def damp_pml_m(u, v, L):
+    """src/dampPml.m:16-18 operation order."""
+    d0 = -(3 * v) / (2 * L) * _LOGR
+    q = u / L
+    return d0 * (q * q)
+
+
+def ext_boundary(V, nB: int, dim: int = 2) -> np.ndarray:
+    """Pad left/right (and front/rear in 3D) by edge replication and the bottom
+    by repeating the last row; no top padding (src/extBoundary.m:22-39)."""
+    V = np.asarray(V, dtype=np.float64)
+    if dim == 2:
+        W = np.concatenate([np.repeat(V[:, :1], nB, 1), V, np.repeat(V[:, -1:], nB, 1)], axis=1)
+        return np.concatenate([W, np.repeat(W[-1:, :], nB, 0)], axis=0)
+    W = np.concatenate([np.repeat(V[:, :1, :], nB, 1), V, np.repeat(V[:, -1:, :], nB, 1)], axis=1)
+    W = np.concatenate([np.repeat(W[:, :, :1], nB, 2), W, np.repeat(W[:, :, -1:], nB, 2)], axis=2)
+    return np.concatenate([W, np.repeat(W[-1:, :, :], nB, 0)], axis=0)
+
+
+def ricker(f: float, n: int, dt: float, t0: float | None = None) -> np.ndarray:
+    """Causal Ricker wavelet peaking at t0 = 1/f (src/ricker.m:61-71)."""
+    t0 = 1.0 / f if t0 is None else t0
+    t = np.arange(n) * dt
+    tau = t - t0
+    return (1 - 2 * tau * tau * f ** 2 * np.pi ** 2) * np.exp(-(tau ** 2) * np.pi ** 2 * f ** 2)
+
+
+def _diff(data: np.ndarray, c: np.ndarray, d: float, axis: int) -> np.ndarray:
+    """diffOperator.m: out = sum_ii c(ii)*(data(idx1)-data(idx2))/d, shrinking
+    ``axis`` by 2N-1 (src/fd_matlab/diffOperator.m:29-66)."""
+    order = len(c)
+    k = 2 * order - 1
+    n = data.shape[axis]
+    m = n - k
+    out = np.zeros(data.shape[:axis] + (m,) + data.shape[axis + 1:])
+    base = np.arange(order, order + m)
+    for ii in range(order):
+        a = np.take(data, base + ii, axis=axis)
+        b = np.take(data, base - ii - 1, axis=axis)
+        out = out + c[ii] * (a - b) / d
+    return out
+
+
+def fwd2d_np(v, source, N, nB, dz, dx, dt):
+    """fwdTimeCpmlFor2dAw with the C gateway's damping order; returns (data, snapshot)."""
+    return _run2d(v, source, None, N, nB, dz, dx, dt)
+
+
+def rvs2d_np(v, data, N, nB, dz, dx, dt):
+    """rvsTimeCpmlFor2dAw; returns (model, snapshot)."""
+    return _run2d(v, None, data, N, nB, dz, dx, dt)
+
+
+def _run2d(v, source, rdata, N, nB, dz, dx, dt):
+    v = np.asarray(v, dtype=np.float64)
+    nz, nx = v.shape
+    nt = source.shape[2] if source is not None else rdata.shape[1]
+    c = dcoef(N)
+    k = 2 * N - 1
+    xd = np.zeros((nz, nx))
+    zd = np.zeros((nz, nx))
+    if nB:
+        xd[:, :nB] = damp_pml_c(np.tile(np.arange(nB, 0, -1) * dx, (nz, 1)), v[:, :nB], nB * dx)
+        xd[:, nx - nB:] = damp_pml_c(np.tile(np.arange(1, nB + 1) * dx, (nz, 1)), v[:, nx - nB:], nB * dx)
+        zd[nz - nB:, :] = damp_pml_c(np.tile((np.arange(1, nB + 1) * dz)[:, None], (1, nx)), v[nz - nB:, :],
+                                     nB * dz)
+    xb = _exp(-xd * dt)
+    zb = _exp(-zd * dt)
+    fdm = np.zeros((3, nz + 2 * k, nx + 2 * k))
+    zPhi = np.zeros((nz + 2 * k, nx))
+    xPhi = np.zeros((nz, nx + 2 * k))
+    zA = np.zeros((nz + 2 * k, nx))
+    xA = np.zeros((nz, nx + 2 * k))
+    zPsi = np.zeros((nz + k, nx))
+    xPsi = np.zeros((nz, nx + k))
+    zP = np.zeros((nz + k, nx))
+    xP = np.zeros((nz, nx + k))
+    vdtSq = (v * dt) * (v * dt)
+    izi = slice(k, nz + k)
+    ixi = slice(k, nx + k)
+    izl = np.arange(N - 1, nz + 2 * k - N)
+    ixl = np.arange(N - 1, nx + 2 * k - N)
+    data = np.zeros((nx, nt))
+    snapshot = np.zeros((nz, nx, nt))
+    steps = range(nt) if source is not None else range(nt - 1, -1, -1)
+    for it in steps:
+        if source is not None:
+            src = source[:, :, it]
+        else:
+            src = np.zeros((nz, nx))
+            src[0, :] = rdata[:, it]
+        cur = fdm[1]
+        zPhi[izi, :] = zb * zPhi[izi, :] + (zb - 1) * _diff(cur[izl + 1][:, ixi], c, dz, 0)
+        xPhi[:, ixi] = xb * xPhi[:, ixi] + (xb - 1) * _diff(cur[izi][:, ixl + 1], c, dx, 1)
+        zA[izl, :] = _diff(cur[:, ixi], c, dz, 0) + zPhi[izl, :]
+        xA[:, ixl] = _diff(cur[izi, :], c, dx, 1) + xPhi[:, ixl]
+        dzA = _diff(zA[izl, :], c, dz, 0)
+        dxA = _diff(xA[:, ixl], c, dx, 1)
+        zPsi[izi, :] = zb * zPsi[izi, :] + (zb - 1) * dzA
+        xPsi[:, ixi] = xb * xPsi[:, ixi] + (xb - 1) * dxA
+        zP[izi, :] = dzA + zPsi[izi, :]
+        xP[:, ixi] = dxA + xPsi[:, ixi]
+        fdm[2][izi, ixi] = vdtSq * (zP[izi, :] + xP[:, ixi] + src) + 2 * fdm[1][izi, ixi] - fdm[0][izi, ixi]
+        fdm[0] = fdm[1].copy()
+        fdm[1] = fdm[2].copy()
+        data[:, it] = fdm[1][k, ixi]
+        snapshot[:, :, it] = fdm[1][izi, ixi]
+    if source is not None:
+        return data, snapshot
+    return fdm[0].copy(), snapshot
+
+
+def fwd3d_np(v, source, N, nB, dz, dx, dy, dt):
+    """fwdTimeCpmlFor3dAw.m restated (src/fwdTimeCpmlFor3dAw.m:37-147)."""
+    v = np.asarray(v, dtype=np.float64)
+    nz, nx, ny = v.shape
+    nt = source.shape[3]
+    c = dcoef(N)
+    k = 2 * N - 1
+    xd = np.zeros((nz, nx, ny))
+    yd = np.zeros((nz, nx, ny))
+    zd = np.zeros((nz, nx, ny))
+    if nB:
+        L = float(nB)
+        xl = damp_pml_m(np.tile(np.arange(nB, 0, -1, dtype=float), (nz, 1)), v[:, :nB, 0], L)
+        xr = damp_pml_m(np.tile(np.arange(1, nB + 1, dtype=float), (nz, 1)), v[:, nx - nB:, 0], L)
+        xd[:, :nB, :] = xl[:, :, None]
+        xd[:, nx - nB:, :] = xr[:, :, None]
+        yf = damp_pml_m(np.tile(np.arange(nB, 0, -1, dtype=float), (nx, 1)), v[0, :, :nB], L)
+        yr = damp_pml_m(np.tile(np.arange(1, nB + 1, dtype=float), (nx, 1)), v[0, :, ny - nB:], L)
+        yd[:, :, :nB] = yf[None, :, :]
+        yd[:, :, ny - nB:] = yr[None, :, :]
+        zdn = damp_pml_m(np.tile(np.arange(1, nB + 1, dtype=float)[:, None], (1, nx)), v[nz - nB:, :, 0], L)
+        zd[nz - nB:, :, :] = zdn[:, :, None]
+    xb = _exp(-xd * dt)
+    yb = _exp(-yd * dt)
+    zb = _exp(-zd * dt)
+    fdm = np.zeros((3, nz + 2 * k, nx + 2 * k, ny + 2 * k))
+    zPhi = np.zeros((nz + 2 * k, nx, ny))
+    xPhi = np.zeros((nz, nx + 2 * k, ny))
+    yPhi = np.zeros((nz, nx, ny + 2 * k))
+    zA = np.zeros((nz + 2 * k, nx, ny))
+    xA = np.zeros((nz, nx + 2 * k, ny))
+    yA = np.zeros((nz, nx, ny + 2 * k))
+    zPsi = np.zeros((nz + k, nx, ny))
+    xPsi = np.zeros((nz, nx + k, ny))
+    yPsi = np.zeros((nz, nx, ny + k))
+    zP = np.zeros((nz + k, nx, ny))
+    xP = np.zeros((nz, nx + k, ny))
+    yP = np.zeros((nz, nx, ny + k))
+    vdtSq = (v * dt) * (v * dt)
+    izi, ixi, iyi = slice(k, nz + k), slice(k, nx + k), slice(k, ny + k)
+    izl = np.arange(N - 1, nz + 2 * k - N)
+    ixl = np.arange(N - 1, nx + 2 * k - N)
+    iyl = np.arange(N - 1, ny + 2 * k - N)
+    data = np.zeros((nx, ny, nt))
+    snapshot = np.zeros((nz, nx, ny, nt))
+    for it in range(nt):
+        cur = fdm[1]
+        zPhi[izi] = zb * zPhi[izi] + (zb - 1) * _diff(cur[izl + 1][:, ixi][:, :, iyi], c, dz, 0)
+        xPhi[:, ixi] = xb * xPhi[:, ixi] + (xb - 1) * _diff(cur[izi][:, ixl + 1][:, :, iyi], c, dx, 1)
+        yPhi[:, :, iyi] = yb * yPhi[:, :, iyi] + (yb - 1) * _diff(cur[izi][:, ixi][:, :, iyl + 1], c, dy, 2)
+        zA[izl] = _diff(cur[:, ixi, iyi], c, dz, 0) + zPhi[izl]
+        xA[:, ixl] = _diff(cur[izi][:, :, iyi], c, dx, 1) + xPhi[:, ixl]
+        yA[:, :, iyl] = _diff(cur[izi, ixi, :], c, dy, 2) + yPhi[:, :, iyl]
+        dzA = _diff(zA[izl], c, dz, 0)
+        dxA = _diff(xA[:, ixl], c, dx, 1)
+        dyA = _diff(yA[:, :, iyl], c, dy, 2)
+        zPsi[izi] = zb * zPsi[izi] + (zb - 1) * dzA
+        xPsi[:, ixi] = xb * xPsi[:, ixi] + (xb - 1) * dxA
+        yPsi[:, :, iyi] = yb * yPsi[:, :, iyi] + (yb - 1) * dyA
+        zP[izi] = dzA + zPsi[izi]
+        xP[:, ixi] = dxA + xPsi[:, ixi]
+        yP[:, :, iyi] = dyA + yPsi[:, :, iyi]
+        fdm[2][izi, ixi, iyi] = vdtSq * (zP[izi] + xP[:, ixi] + yP[:, :, iyi] + source[:, :, :, it]) \
+            + 2 * fdm[1][izi, ixi, iyi] - fdm[0][izi, ixi, iyi]
+        fdm[0] = fdm[1].copy()
+        fdm[1] = fdm[2].copy()
+        data[:, :, it] = fdm[1][k, ixi, iyi]
+        snapshot[:, :, :, it] = fdm[1][izi, ixi, iyi]
+    return data, snapshot
+
+
+def image_np(fwd_snap, rvs_snap, epsilon):
+    """M = sum_t f.*r, s2 = epsilon + sum_t f.^2 in ascending t; returns M./s2."""
+    m = np.zeros(fwd_snap.shape[:2])
+    s2 = np.full(fwd_snap.shape[:2], float(epsilon))
+    for t in range(fwd_snap.shape[2]):
+        m = fwd_snap[:, :, t] * rvs_snap[:, :, t] + m
+        s2 = fwd_snap[:, :, t] ** 2 + s2
+    return m / s2
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = float(np.linalg.norm(b.ravel()))
+    num = float(np.linalg.norm((a - b).ravel()))
+    return num / den if den else num

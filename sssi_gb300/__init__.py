@@ -1,0 +1,23 @@
+"""sssi_gb300 -- SSSI's acoustic CPML finite-difference core on GB300 (sm_103a).
+
+Host side of the drop-in: the MATLAB-shaped functions in :mod:`sssi_gb300.api`
+call the C ABI of ``libsssi_gb300.so`` (``include/sssi_gb300.h``), whose
+kernels are hand-written CUDA for sm_103a.  Import never touches the GPU;
+the first call loads the library and fails loudly if it is not built.
+"""
+from .api import (  # noqa: F401
+    MODES,
+    dampPml,
+    dCoef,
+    fwdTimeCpmlFor2dAw,
+    fwdTimeCpmlFor2dAwPoint,
+    fwdTimeCpmlFor3dAw,
+    launch_count,
+    release_cache,
+    rtmTimeCpmlFor2dAw,
+    rvsTimeCpmlFor2dAw,
+    set_stream,
+)
+from ._native import SSSIError  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,202 @@
+"""MATLAB-shaped entry points of the SSSI acoustic CPML core on the GPU.
+
+The functions mirror the MATLAB wrappers the application scripts call
+(``src/fd_cmex/fwdTimeCpmlFor2dAw.m:37``, ``src/fd_cmex/rvsTimeCpmlFor2dAw.m:31``,
+``src/fwdTimeCpmlFor3dAw.m:1``): same names, same positional arguments, same
+array shapes, MATLAB (column-major) index order ``v[z, x]``,
+``source[z, x, t]``, ``data[x, t]``, ``snapshot[z, x, t]``.  Inputs may be
+numpy arrays (host) or CUDA torch tensors (device; they must be Fortran
+ordered, i.e. ``t.T.contiguous().T`` / created via ``permute``); outputs come
+back as the same kind.
+
+``mode`` selects the arithmetic (``"fp64-strict"``: the reference's rounding
+sequence, bit-identical to the reference C; ``"fp64"``: folded coefficients
+and fused multiply-adds; ``"fp32"``: FP32 wavefield with FP64 CPML memory).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from ._native import check, lib
+
+MODES = {"fp64-strict": 0, "fp64": 1, "fp32": 2}
+
+
+def _mode(mode) -> int:
+    if isinstance(mode, int):
+        return mode
+    try:
+        return MODES[mode]
+    except KeyError:
+        raise ValueError(f"unknown mode {mode!r}; expected one of {sorted(MODES)}") from None
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _in(a, name: str):
+    """(address, keepalive, shape) of an input array as column-major float64."""
+    if a is None:
+        return None, None, None
+    if _is_torch(a):
+        import torch
+
+        if a.dtype != torch.float64:
+            raise TypeError(f"{name}: expected a float64 tensor")
+        if a.dim() >= 2 and not a.is_contiguous() and not a.T.is_contiguous():
+            raise ValueError(f"{name}: tensor must be column-major (Fortran ordered)")
+        if a.dim() >= 2 and a.is_contiguous() and not a.T.is_contiguous():
+            raise ValueError(f"{name}: tensor must be column-major (Fortran ordered)")
+        return a.data_ptr(), a, tuple(a.shape)
+    arr = np.asfortranarray(np.asarray(a, dtype=np.float64))
+    return arr.ctypes.data, arr, arr.shape
+
+
+def _out_like(ref, shape):
+    """A zeroed column-major float64 output on the same side (host/device) as ``ref``."""
+    if ref is not None and _is_torch(ref):
+        import torch
+
+        t = torch.zeros(tuple(reversed(shape)), dtype=torch.float64, device=ref.device)
+        return t.permute(*reversed(range(len(shape)))), t
+    arr = np.zeros(shape, order="F")
+    return arr, arr
+
+
+def _addr(a):
+    if a is None:
+        return None
+    if _is_torch(a):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def dCoef(order: int) -> np.ndarray:
+    """Staggered-grid coefficients c_1..c_N (src/dCoef.m, finiteDifference.c:24-82)."""
+    c = np.zeros(order)
+    check(lib().sssi_dCoef(int(order), c.ctypes.data))
+    return c
+
+
+def dampPml(u, v, L: float) -> np.ndarray:
+    """d = -(3v)/(2L) ln(1e-6) (u/L)^2 elementwise (finiteDifference.c:253-280)."""
+    u = np.asfortranarray(np.asarray(u, dtype=np.float64))
+    v = np.asfortranarray(np.asarray(v, dtype=np.float64))
+    if u.shape != v.shape:
+        raise ValueError("u and v must have the same shape")
+    d = np.zeros(u.shape, order="F")
+    check(lib().sssi_dampPml(u.ctypes.data, v.ctypes.data, u.size, float(L), d.ctypes.data))
+    return d
+
+
+def fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64-strict", want_snapshot=True):
+    """[data, snapshot] = fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt)."""
+    pv, kv, vshape = _in(v, "v")
+    ps, ks, sshape = _in(source, "source")
+    if vshape is None or len(vshape) != 2:
+        raise ValueError("v must be nz x nx")
+    nz, nx = vshape
+    if sshape is None or len(sshape) != 3 or sshape[:2] != (nz, nx):
+        raise ValueError("source must be nz x nx x nt with the grid of v")
+    nt = sshape[2]
+    data, dkeep = _out_like(v, (nx, nt))
+    snap, skeep = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeCpmlFor2dAw(pv, ps, nz, nx, nt, int(nDiffOrder), int(nBoundary), float(dz), float(dx),
+                                        float(dt), _addr(data), _addr(snap), _mode(mode)))
+    return data, snap
+
+
+def fwdTimeCpmlFor2dAwPoint(v, nt, src_iz, src_ix, wavelets, nDiffOrder, nBoundary, dz, dx, dt, *,
+                            mode="fp64-strict", want_snapshot=False):
+    """Forward modelling with point sources: source s at interior (src_iz[s], src_ix[s])
+    with amplitude wavelets[s, t].  Returns (data, snapshot or None)."""
+    pv, kv, vshape = _in(v, "v")
+    nz, nx = vshape
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or len(ix) != len(iz):
+        raise ValueError("wavelets must be nsrc x nt and src_iz/src_ix of length nsrc")
+    data, _ = _out_like(v, (nx, nt))
+    snap, _ = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeCpmlFor2dAwPoint(pv, nz, nx, int(nt), int(nDiffOrder), int(nBoundary), float(dz),
+                                             float(dx), float(dt), len(iz), iz.ctypes.data, ix.ctypes.data,
+                                             w.ctypes.data, _addr(data), _addr(snap), _mode(mode)))
+    return data, snap
+
+
+def rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64-strict", want_snapshot=True):
+    """[model, snapshot] = rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt)."""
+    pv, kv, vshape = _in(v, "v")
+    pd, kd, dshape = _in(data, "data")
+    if vshape is None or len(vshape) != 2:
+        raise ValueError("v must be nz x nx")
+    nz, nx = vshape
+    if dshape is None or len(dshape) != 2 or dshape[0] != nx:
+        raise ValueError("data must be nx x nt")
+    nt = dshape[1]
+    l = 2 * int(nDiffOrder) - 1
+    model, _ = _out_like(v, (nz + 2 * l, nx + 2 * l))
+    snap, _ = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_rvsTimeCpmlFor2dAw(pv, pd, nz, nx, nt, int(nDiffOrder), int(nBoundary), float(dz), float(dx),
+                                        float(dt), _addr(model), _addr(snap), _mode(mode)))
+    return model, snap
+
+
+def fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt, *, mode="fp64-strict",
+                       want_snapshot=True):
+    """[data, snapshot] = fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt)."""
+    pv, kv, vshape = _in(v, "v")
+    ps, ks, sshape = _in(source, "source")
+    if vshape is None or len(vshape) != 3:
+        raise ValueError("v must be nz x nx x ny")
+    nz, nx, ny = vshape
+    if sshape is None or len(sshape) != 4 or sshape[:3] != (nz, nx, ny):
+        raise ValueError("source must be nz x nx x ny x nt with the grid of v")
+    nt = sshape[3]
+    data, _ = _out_like(v, (nx, ny, nt))
+    snap, _ = _out_like(v, (nz, nx, ny, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeCpmlFor3dAw(pv, ps, nz, nx, ny, nt, int(nDiffOrder), int(nBoundary), float(dz), float(dx),
+                                        float(dy), float(dt), _addr(data), _addr(snap), _mode(mode)))
+    return data, snap
+
+
+def rtmTimeCpmlFor2dAw(v, vs, wavelet, src_iz, src_ix, nDiffOrder, nBoundary, dz, dx, dt, *, epsilon=1e-3,
+                       mode="fp64-strict", snap_stride=4, want_data=False):
+    """One RTM shot: image = M./s2 of mainRtmTimeCpmlFor2dAw.m:268-275,315 for a
+    point source at interior (src_iz, src_ix).  Returns image, or (image,
+    dataTrue, dataSmooth) with ``want_data``."""
+    pv, kv, vshape = _in(v, "v")
+    pvs, kvs, vsshape = _in(vs, "vs")
+    pw, kw, wshape = _in(wavelet, "wavelet")
+    if vshape != vsshape or len(vshape) != 2:
+        raise ValueError("v and vs must be nz x nx of the same size")
+    nz, nx = vshape
+    nt = wshape[0]
+    image, _ = _out_like(v, (nz, nx))
+    dt_, _ = _out_like(v, (nx, nt)) if want_data else (None, None)
+    ds_, _ = _out_like(v, (nx, nt)) if want_data else (None, None)
+    check(lib().sssi_rtmTimeCpmlFor2dAw(pv, pvs, nz, nx, nt, int(nDiffOrder), int(nBoundary), float(dz), float(dx),
+                                        float(dt), pw, int(src_iz), int(src_ix), float(epsilon), _mode(mode),
+                                        int(snap_stride), _addr(image), _addr(dt_), _addr(ds_)))
+    if want_data:
+        return image, dt_, ds_
+    return image
+
+
+def set_stream(stream) -> None:
+    """Make the library launch on ``stream`` (a torch.cuda.Stream, a raw handle, or None)."""
+    handle = getattr(stream, "cuda_stream", stream) or 0
+    check(lib().sssi_set_stream(ctypes.c_void_p(handle)))
+
+
+def release_cache() -> None:
+    check(lib().sssi_release_cache())
+
+
+def launch_count() -> int:
+    return _native.launch_count()

@@ -1,0 +1,152 @@
+// Internal declarations shared by the translation units of libsssi_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "sssi_gb300.h"
+
+namespace sssi {
+
+// ---------------------------------------------------------------- errors
+// Every C-ABI entry point returns a status code; the text of the last failure
+// of the calling thread is kept for sssi_last_error().
+void set_error(const char* fmt, ...);
+void clear_error();
+
+struct Error {
+    int code;
+};
+
+#define SSSI_CHECK_CUDA(expr)                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            ::sssi::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, \
+                              __LINE__);                                                        \
+            throw ::sssi::Error{SSSI_ERR_CUDA};                                                 \
+        }                                                                                       \
+    } while (0)
+
+#define SSSI_REQUIRE(cond, code, ...)      \
+    do {                                   \
+        if (!(cond)) {                     \
+            ::sssi::set_error(__VA_ARGS__); \
+            throw ::sssi::Error{code};     \
+        }                                  \
+    } while (0)
+
+// Runs f, translating exceptions into a status code (C-ABI boundary helper).
+template <typename F>
+int guarded(F&& f) {
+    clear_error();
+    try {
+        f();
+        return SSSI_OK;
+    } catch (const Error& e) {
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return SSSI_ERR_NOMEM;
+    } catch (...) {
+        set_error("unexpected C++ exception");
+        return SSSI_ERR_INTERNAL;
+    }
+}
+
+// ---------------------------------------------------------------- runtime
+void count_launch(int n = 1);
+cudaStream_t current_stream();
+bool is_device_pointer(const void* p);
+void ensure_device();
+
+// Device memory from a per-process cache keyed by size: buffers are returned to
+// the cache at the end of a call and reused by the next call of the same shape.
+class DeviceBuffer {
+  public:
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t bytes) { allocate(bytes); }
+    ~DeviceBuffer() { release(); }
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) {
+        o.ptr_ = nullptr;
+        o.bytes_ = 0;
+    }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
+        if (this != &o) {
+            release();
+            ptr_ = o.ptr_;
+            bytes_ = o.bytes_;
+            o.ptr_ = nullptr;
+            o.bytes_ = 0;
+        }
+        return *this;
+    }
+    void allocate(size_t bytes);
+    void release();
+    void zero(cudaStream_t s);
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(ptr_);
+    }
+    void* get() const { return ptr_; }
+    size_t bytes() const { return bytes_; }
+
+  private:
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// Releases every cached buffer (sssi_release_cache).
+void pool_trim();
+size_t pool_cached_bytes();
+
+// Pinned host staging buffer (reused across calls).
+class PinnedBuffer {
+  public:
+    PinnedBuffer() = default;
+    ~PinnedBuffer();
+    void reserve(size_t bytes);
+    void* get() const { return ptr_; }
+
+  private:
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// ---------------------------------------------------------------- host setup
+// Staggered-grid coefficients of half-order N: A c = e1, A_ij = (2j-1)^(2i-1),
+// by LU with partial pivoting (finiteDifference.c:24-82).
+void staggered_coefficients(int N, double* c);
+
+// d = (-(3 v)/(2 L) * log(1e-6)) * (u/L) * (u/L)   (finiteDifference.c:253-280)
+double damp_c_order(double u, double v, double L);
+// d = d0 .* (u/L).^2                              (src/dampPml.m:16-18)
+double damp_m_order(double u, double v, double L);
+
+// Damping factors of the CPML bands of a 2D grid, C-gateway conventions
+// (fwdTimeCpmlFor2dAw_mex.c:100-145).  Bottom band: nB x nx (row r = i-(nz-nB)),
+// side bands: nz x 2nB (column c = j for the left band, nB + j-(nx-nB) for the right).
+struct Bands2D {
+    std::vector<double> zb, zbm1;  // nB x nx
+    std::vector<double> xb, xbm1;  // nz x 2nB
+};
+Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double dz, double dx, double dt);
+
+// Damping factors of the 3D MATLAB file (src/fwdTimeCpmlFor3dAw.m:45-70):
+// cell units (L = nB), x profiles from the y=0 slice, y profiles from the top row,
+// z profiles from the y=0 slice.  Bottom band: nB x nx (same for every y);
+// x bands: nz x 2nB (same for every y); y bands: nx x 2nB (same for every z).
+struct Bands3D {
+    std::vector<double> zb, zbm1;  // nB x nx
+    std::vector<double> xb, xbm1;  // nz x 2nB
+    std::vector<double> yb, ybm1;  // nx x 2nB
+};
+Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int nB, double dt);
+
+}  // namespace sssi

@@ -1,0 +1,137 @@
+"""Generates the committed golden vectors in tests/golden/ from the reference's
+own C gateways (src/fd_cmex/*_mex.c compiled unmodified against the project's
+mex.h shim by ``make -C oracle ref``).  Run where the reference tree exists:
+
+    python tests/golden/make_golden.py
+
+Outputs (all float64, MATLAB index order):
+  dcoef.npz     dCoef(N,'s') for N = 1..8 (reference dCoef through the shim's mldivide)
+  damppml.npz   reference dampPml on a 30 x 40 model, nB = 5, both bands
+  fwd2d_rvs2d.npz  15 cases (37 x 53, nt = 48, N = 1..5, nB in {0, 3, 8}):
+                inputs, reference data, two forward snapshots, reverse model
+                and two reverse snapshots
+  rtm2d.npz     one reference RTM shot (40 x 60, nt = 120): dataTrue, dataSmooth,
+                and image = M./s2 with the sums in ascending time order
+  fwd3d.npz     3D forward (24 x 20 x 18, nt = 32, N = 3, nB = 4) from the C
+                restatement (the reference has no C for 3D; its MATLAB file is
+                restated and cross-checked against the numpy restatement here)
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from oracle import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+CASES_2D = [(37, 53, 48, N, nB) for N in (1, 2, 3, 4, 5) for nB in (0, 3, 8)]
+
+
+def source_2d(rng, nz, nx, nt):
+    """Ricker at (2, nx//2) plus 12 random impulses (iz, ix, it, amplitude)."""
+    trace = O.ricker(25.0, nt, 1e-3)
+    imp = np.stack([rng.integers(0, nz, 12), rng.integers(0, nx, 12), rng.integers(0, nt, 12)], axis=1)
+    amp = rng.standard_normal(12)
+    return trace, imp.astype(np.int64), amp
+
+
+def dense_source(nz, nx, nt, trace, imp, amp):
+    src = np.zeros((nz, nx, nt), order="F")
+    src[2, nx // 2, :] = trace
+    for (iz, ix, it), a in zip(imp, amp):
+        src[iz, ix, it] += a
+    return src
+
+
+def main() -> None:
+    O.build(reference=True)
+    fwd = O.RefMex("fwdTimeCpmlFor2dAw_mex")
+    rvs = O.RefMex("rvsTimeCpmlFor2dAw_mex")
+    co = O.COracle()
+
+    np.savez_compressed(OUT / "dcoef.npz", **{f"N{N}": fwd.dcoef(N) for N in range(1, 9)})
+
+    # reference dampPml(pu, pv, m, n, L) on both band shapes
+    lib = fwd.lib
+    lib.dampPml.restype = ctypes.POINTER(ctypes.c_double)
+    lib.dampPml.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_double]
+    rng = np.random.default_rng(7)
+    v = rng.uniform(1500.0, 4000.0, (30, 40))
+    nB, dx = 5, 10.0
+    u_left = np.asfortranarray(np.tile((nB - np.arange(nB)) * dx, (30, 1)))
+    v_left = np.asfortranarray(v[:, :nB])
+    p = lib.dampPml(u_left.ctypes.data, v_left.ctypes.data, 30, nB, nB * dx)
+    d_left = np.ctypeslib.as_array(p, shape=(nB * 30,)).copy().reshape((30, nB), order="F")
+    u_bot = np.asfortranarray(np.tile(((np.arange(nB) + 1) * dx)[:, None], (1, 40)))
+    v_bot = np.asfortranarray(v[30 - nB:, :])
+    p = lib.dampPml(u_bot.ctypes.data, v_bot.ctypes.data, nB, 40, nB * dx)
+    d_bot = np.ctypeslib.as_array(p, shape=(nB * 40,)).copy().reshape((nB, 40), order="F")
+    np.savez_compressed(OUT / "damppml.npz", v=v, nB=nB, dx=dx, u_left=u_left, d_left=d_left, u_bot=u_bot,
+                        d_bot=d_bot)
+
+    rec = {}
+    for k, (nz, nx, nt, N, nB) in enumerate(CASES_2D):
+        rng = np.random.default_rng(1000 + k)
+        v = rng.uniform(1500.0, 4000.0, (nz, nx))
+        trace, imp, amp = source_2d(rng, nz, nx, nt)
+        src = dense_source(nz, nx, nt, trace, imp, amp)
+        data, snap = fwd.call(2, v, src, N, nB, 10.0, 10.0, 1e-3)
+        model, rsnap = rvs.call(2, v, data, N, nB, 10.0, 10.0, 1e-3)
+        # the restatement must agree bit for bit before anything is stored
+        d2, s2 = co.fwd2d(v, src, N, nB, 10.0, 10.0, 1e-3)
+        m2, r2 = co.rvs2d(v, data, N, nB, 10.0, 10.0, 1e-3)
+        assert np.array_equal(d2, data) and np.array_equal(s2, snap)
+        assert np.array_equal(m2, model) and np.array_equal(r2, rsnap)
+        pre = f"c{k}_"
+        rec.update({pre + "params": np.array([nz, nx, nt, N, nB]), pre + "v": v, pre + "trace": trace,
+                    pre + "imp": imp, pre + "amp": amp, pre + "data": data,
+                    pre + "snap_mid": snap[:, :, nt // 2], pre + "snap_last": snap[:, :, -1], pre + "model": model,
+                    pre + "rsnap_first": rsnap[:, :, 0], pre + "rsnap_mid": rsnap[:, :, nt // 2]})
+    rec["ncases"] = np.array(len(CASES_2D))
+    np.savez_compressed(OUT / "fwd2d_rvs2d.npz", **rec)
+
+    # one RTM shot of the reference application, at small size
+    nz, nx, nt, N, nB = 40, 60, 120, 4, 8
+    rng = np.random.default_rng(2024)
+    v = np.full((nz, nx), 2000.0)
+    v[18:, :] = 2600.0
+    v[30:, :] = 3300.0
+    v += rng.uniform(-50, 50, (nz, nx))
+    vs = v.copy()
+    for _ in range(4):  # a light smoothing; the exact filter does not matter to parity
+        vs[1:-1, 1:-1] = 0.2 * (vs[1:-1, 1:-1] + vs[:-2, 1:-1] + vs[2:, 1:-1] + vs[1:-1, :-2] + vs[1:-1, 2:])
+    trace = O.ricker(30.0, nt, 1e-3)
+    src = np.zeros((nz, nx, nt), order="F")
+    src[0, nx // 2, :] = trace
+    d_true, _ = fwd.call(2, v, src, N, nB, 10.0, 10.0, 1e-3)
+    d_smooth, f_snap = fwd.call(2, vs, src, N, nB, 10.0, 10.0, 1e-3)
+    _, r_snap = rvs.call(2, v, d_true - d_smooth, N, nB, 10.0, 10.0, 1e-3)
+    image = O.image_np(f_snap, r_snap, 1e-3)
+    img_c, dt_c, ds_c = co.rtm2d(v, vs, trace, 0, nx // 2, N, nB, 10.0, 10.0, 1e-3, 1e-3)
+    assert np.array_equal(img_c, image) and np.array_equal(dt_c, d_true) and np.array_equal(ds_c, d_smooth)
+    np.savez_compressed(OUT / "rtm2d.npz", params=np.array([nz, nx, nt, N, nB]), v=v, vs=vs, trace=trace,
+                        src_ix=nx // 2, epsilon=1e-3, data_true=d_true, data_smooth=d_smooth, image=image)
+
+    # 3D forward from the C restatement, cross-checked with the numpy restatement
+    nz, nx, ny, nt, N, nB = 24, 20, 18, 32, 3, 4
+    rng = np.random.default_rng(33)
+    v = rng.uniform(1500.0, 4000.0, (nz, nx, ny))
+    trace = O.ricker(30.0, nt, 1e-3)
+    src = np.zeros((nz, nx, ny, nt), order="F")
+    src[1, nx // 2, ny // 2, :] = trace
+    d3, s3 = co.fwd3d(v, src, N, nB, 10.0, 10.0, 10.0, 1e-3)
+    d3n, s3n = O.fwd3d_np(v, src, N, nB, 10.0, 10.0, 10.0, 1e-3)
+    assert np.array_equal(d3, d3n) and np.array_equal(s3, s3n)
+    np.savez_compressed(OUT / "fwd3d.npz", params=np.array([nz, nx, ny, nt, N, nB]), v=v, trace=trace, data=d3,
+                        snap_last=s3[:, :, :, -1], snap_mid=s3[:, :, :, nt // 2])
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

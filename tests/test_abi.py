@@ -1,0 +1,116 @@
+"""The C ABI without a GPU: the library loads, exports every symbol the header
+declares, computes the host-side building blocks exactly like the oracle, and
+turns bad arguments (and a missing GPU) into status codes, not crashes."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "sssi_gb300.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sssi_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sssi_gb300 import _native
+    from sssi_gb300.build import LIB, build_library
+
+    if not LIB.exists():
+        build_library()
+    return _native.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    from sssi_gb300._native import SIGNATURES
+
+    missing = [s for s in declared_symbols() if s not in SIGNATURES]
+    assert not missing, missing
+
+
+def test_dcoef_matches_oracle(lib, co):
+    import sssi_gb300 as S
+
+    for N in range(1, 9):
+        assert np.array_equal(S.dCoef(N), co.dcoef(N)), N
+    from sssi_gb300._native import SSSIError
+
+    with pytest.raises(SSSIError, match="order"):
+        S.dCoef(9)
+
+
+def test_damppml_matches_reference_golden(lib, golden):
+    import sssi_gb300 as S
+
+    g = golden("damppml.npz")
+    nB, dx = int(g["nB"]), float(g["dx"])
+    assert np.array_equal(S.dampPml(g["u_left"], g["v"][:, :nB], nB * dx), g["d_left"])
+    assert np.array_equal(S.dampPml(g["u_bot"], g["v"][30 - nB:, :], nB * dx), g["d_bot"])
+
+
+def test_bad_arguments_are_status_codes(lib):
+    v = np.full((20, 30), 2000.0, order="F")
+    src = np.zeros((20, 30, 5), order="F")
+    out = np.zeros((30, 5), order="F")
+    p = lambda a: a.ctypes.data  # noqa: E731
+    # nDiffOrder out of range
+    rc = lib.sssi_fwdTimeCpmlFor2dAw(p(v), p(src), 20, 30, 5, 0, 3, 10.0, 10.0, 1e-3, p(out), None, 0)
+    assert rc == 1 and b"nDiffOrder" in lib.sssi_last_error()
+    # negative spacing
+    rc = lib.sssi_rvsTimeCpmlFor2dAw(p(v), p(out), 20, 30, 5, 4, 3, -10.0, 10.0, 1e-3, None, None, 0)
+    assert rc == 1
+    # unknown mode
+    rc = lib.sssi_fwdTimeCpmlFor2dAw(p(v), p(src), 20, 30, 5, 4, 3, 10.0, 10.0, 1e-3, p(out), None, 9)
+    assert rc == 1 and b"mode" in lib.sssi_last_error()
+    # a source outside the model
+    img = np.zeros((20, 30), order="F")
+    w = np.zeros(5)
+    rc = lib.sssi_rtmTimeCpmlFor2dAw(p(v), p(v), 20, 30, 5, 4, 3, 10.0, 10.0, 1e-3, p(w), 25, 3, 1e-3, 2, 4,
+                                     p(img), None, None)
+    assert rc == 1 and b"outside" in lib.sssi_last_error()
+
+
+def test_no_gpu_is_a_status_code(lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    v = np.full((20, 30), 2000.0, order="F")
+    src = np.zeros((20, 30, 5), order="F")
+    out = np.zeros((30, 5), order="F")
+    rc = lib.sssi_fwdTimeCpmlFor2dAw(v.ctypes.data, src.ctypes.data, 20, 30, 5, 4, 3, 10.0, 10.0, 1e-3,
+                                     out.ctypes.data, None, 0)
+    assert rc == 2, lib.sssi_last_error()
+
+
+def test_mex_gateways_export_mexfunction():
+    """This project's gateways, built on the test shim, export the MEX entry point."""
+    import subprocess
+
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "mexgw"], check=True)
+    for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex"):
+        gw = ctypes.CDLL(str(ROOT / "oracle" / "_build" / f"mexgw_{name}.so"), mode=ctypes.RTLD_LOCAL)
+        assert hasattr(gw, "mexFunction")
+
+
+def test_mex_gateway_error_message():
+    """Too few arguments: the reference's message, raised through mexErrMsgTxt."""
+    from oracle import oracle as O
+
+    gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeCpmlFor2dAw_mex.so")
+    with pytest.raises(O.MexError, match="All 7 input arguments shall be provided!"):
+        O.shim_call(gw, 2, np.ones((3, 3)), np.zeros((3, 3, 2)))
