@@ -1,0 +1,372 @@
+#!/usr/bin/env python3
+"""Benchmark of the SSSI acoustic CPML hot path on GB300.
+
+Workload (one "step" = one reverse-time-migration shot): 2D single-shot RTM
+on a 600 x 1200 physical grid (620 x 1240 after extBoundary with a 20-cell
+CPML on the bottom/left/right, no top layer), dx = dz = 10 m, dt = 0.8 ms,
+nt = 4000, 8th-order staggered space (nDiffOrder = 4), 15 Hz Ricker source at
+the surface centre, seeded 6-layer velocity model (1500-4000 m/s increasing
+with depth) and its Gaussian-smoothed copy (sigma = 15 cells) as migration
+model.  One shot = forward modelling in both models + reverse propagation of
+dataTrue - dataSmooth + zero-lag imaging: 3 * 620 * 1240 * 4000 = 9.23e9
+cell-updates.
+
+Headline arm (default): FP32 wavefield, compensated/FP64 CPML memory, FP16
+forward snapshots with one power-of-two scale each, stored and imaged every
+4th step, FP64 image sums.  The FP64 drop-in (fused FP64) is measured beside
+it.  ``value`` times the shot with every input already in HBM; ``e2e`` calls
+the same C ABI with host buffers (models and wavelet copied in, image copied
+out inside the timed region).
+
+``--impl reference`` times the CPU implementation of the same shot (the C
+restatement of the reference's algorithm, OpenMP over every host core) on a
+bounded number of time steps and reports the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-updates/s (2D RTM shot, 620x1240 padded, nt=4000)"
+UNIT = "Gcell-updates/s"
+
+# ---------------------------------------------------------------- workload
+NZ0, NX0, NB, N_ORDER = 600, 1200, 20, 4
+NT, DT, DX, DZ, FREQ, EPS = 4000, 8e-4, 10.0, 10.0, 15.0, 1e-3
+STRIDE = 4
+
+
+def ext_boundary(V, nB):
+    W = np.concatenate([np.repeat(V[:, :1], nB, 1), V, np.repeat(V[:, -1:], nB, 1)], axis=1)
+    return np.concatenate([W, np.repeat(W[-1:, :], nB, 0)], axis=0)
+
+
+def ricker(f, n, dt):
+    t = np.arange(n) * dt
+    tau = t - 1.0 / f
+    return (1 - 2 * tau * tau * f ** 2 * np.pi ** 2) * np.exp(-(tau ** 2) * np.pi ** 2 * f ** 2)
+
+
+def make_models(seed=20240601):
+    """Seeded 6-layer model (flat interfaces at sorted random depths, velocities
+    sorted uniform in [1500, 4000]) and its Gaussian-smoothed copy."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    depths = np.sort(rng.choice(np.arange(40, NZ0 - 20), 5, replace=False))
+    vel = np.sort(rng.uniform(1500.0, 4000.0, 6))
+    v = np.empty((NZ0, NX0))
+    edges = [0, *depths, NZ0]
+    for k in range(6):
+        v[edges[k]:edges[k + 1], :] = vel[k]
+    vs = gaussian_filter(v, sigma=15, mode="nearest")
+    V = np.asfortranarray(ext_boundary(v, NB))
+    VS = np.asfortranarray(ext_boundary(vs, NB))
+    return V, VS
+
+
+def workload():
+    V, VS = make_models()
+    nz, nx = V.shape
+    w = ricker(FREQ, NT, DT)
+    return V, VS, w, 0, NB + NX0 // 2, nz, nx
+
+
+def cell_updates(nz, nx, nt):
+    return 3 * nz * nx * nt
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.rows = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=5)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 7 for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+
+    import sssi_gb300 as S
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    S.set_stream(stream)
+
+    V, VS, w, siz, six, nz, nx = workload()
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a.T)).cuda().T
+
+    dV, dVS, dw = dev(V), dev(VS), torch.from_numpy(w).cuda()
+    dimg = dev(np.zeros((nz, nx)))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def shot(mode, stride, vv, vvs, ww, img):
+        return S.api.lib().sssi_rtmTimeCpmlFor2dAw(
+            S.api._addr(vv), S.api._addr(vvs), nz, nx, NT, N_ORDER, NB, DZ, DX, DT, S.api._addr(ww), siz, six, EPS,
+            S.api._mode(mode), stride, S.api._addr(img), None, None)
+
+    def timed_shots(mode, stride, steps, warmup, host=False):
+        if host:
+            hV = torch.from_numpy(np.ascontiguousarray(V.T)).pin_memory().T
+            hVS = torch.from_numpy(np.ascontiguousarray(VS.T)).pin_memory().T
+            hw = torch.from_numpy(w).pin_memory()
+            himg = torch.zeros((nx, nz), dtype=torch.float64).pin_memory().T
+            operands = (hV, hVS, hw, himg)
+        else:
+            operands = (dV, dVS, dw, dimg)
+        for _ in range(warmup):
+            S.api.check(shot(mode, stride, *operands))
+        total = 0.0
+        phases = []
+        launches0 = S.launch_count()
+        for _ in range(steps):
+            flush.zero_()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            S.api.check(shot(mode, stride, *operands))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+            phases.append(S.last_timing())
+        launches = S.launch_count() - launches0
+        ms = total / steps
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, phases, launches // max(steps, 1)
+
+    S.enable_timing(True)
+    clocks = ClockSampler()
+    clocks.start()
+    ms32, ph32, launches32 = timed_shots("fp32", STRIDE, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms32_e2e, _, _ = timed_shots("fp32", STRIDE, max(1, args.steps // 2), 1, host=True)
+    fp64_steps = max(1, min(args.steps, args.fp64_steps))
+    ms64, ph64, _ = timed_shots("fp64", 1, fp64_steps, 1)
+
+    cells = cell_updates(nz, nx, NT)
+    value = world * cells / (ms32 * 1e-3) / 1e9
+    e2e = world * cells / (ms32_e2e * 1e-3) / 1e9
+
+    # roofline of the dominant kernel: the fused step, timed over the forward phase
+    fwd_ms = float(np.mean([p[0][0] for p in ph32]))
+    fwd_launch = ph32[0][0][1]
+    per_launch_ms = fwd_ms / fwd_launch
+    f_z = NB / nz
+    f_x = 2 * NB / nx
+    band_bytes = 6 * 8  # phi in/out, psi read/write, b, b-1 per damped cell per axis (8-byte words)
+    bytes_cell = 16 + band_bytes * (f_z + f_x)
+    alg_bytes = bytes_cell * nz * nx
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms32, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded layered model, Ricker source)",
+        "config": {"workload": "rtm2d-single-shot", "nz": nz, "nx": nx, "nt": NT, "nDiffOrder": N_ORDER,
+                   "nBoundary": NB, "dt": DT, "dx": DX, "snapshot": f"fp16 every {STRIDE} steps",
+                   "cell_updates_per_step": cells, "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single-gpu"},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(2 * nz * nx * 8 + NT * 8),
+                "d2h_bytes_per_step": int(nz * nx * 8), "ms_per_step": round(ms32_e2e, 3),
+                "api": "sssi_rtmTimeCpmlFor2dAw (host buffers)"},
+        "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms64, 3),
+                 "mode": "fp64 (fused multiply-add)", "steps": fp64_steps},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "cpml2d step (fp32, forward phase)", "bytes_per_cell": round(bytes_cell, 2),
+                     "launch_ms": round(per_launch_ms, 5)},
+        "gpu_launches": int(launches32),
+        "clocks": clk,
+        "phases_ms": {"forward": round(fwd_ms, 2), "reverse+imaging": round(float(np.mean([p[1][0] for p in ph32])), 2),
+                      "finish": round(float(np.mean([p[2][0] for p in ph32])), 3)},
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------- CPU arm
+def cpu_rtm_rate(nt_sample, threads=None):
+    """Gcell-updates/s of the CPU RTM shot (C restatement, OpenMP) on nt_sample steps."""
+    from oracle import oracle as O
+
+    co = O.COracle()
+    if threads:
+        co.set_threads(threads)
+    V, VS, w, siz, six, nz, nx = workload()
+    t0 = time.perf_counter()
+    co.rtm2d(V, VS, w[:nt_sample], siz, six, N_ORDER, NB, DZ, DX, DT, EPS)
+    el = time.perf_counter() - t0
+    return cell_updates(nz, nx, nt_sample) / el / 1e9, co.threads(), el
+
+
+def cpu_baseline(args):
+    from oracle import oracle as O
+
+    O.build(reference=False)
+    rate, cores, el = cpu_rtm_rate(args.cpu_nt)
+    return {"value": round(rate, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one RTM shot on the same 620x1240 grid for nt={args.cpu_nt} of 4000 steps "
+                      f"({el:.1f} s); C restatement of the reference algorithm, OpenMP"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build(reference=False)
+    for _ in range(args.warmup):
+        cpu_rtm_rate(max(2, args.cpu_nt // 10))
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, cores, el = cpu_rtm_rate(args.cpu_nt)
+        rates.append(r)
+        times.append(el)
+    value = float(np.mean(rates))
+    nz, nx = NZ0 + NB, NX0 + 2 * NB
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(times)), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded layered model, Ricker source)", "impl": "reference",
+            "config": {"workload": "rtm2d-single-shot", "nz": nz, "nx": nx, "nt": NT,
+                       "sample_nt": args.cpu_nt, "nDiffOrder": N_ORDER, "nBoundary": NB},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"each step: one RTM shot on the 620x1240 grid for nt={args.cpu_nt} "
+                                       "(rate extrapolates linearly in nt)"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- profiling cases
+CASES = {
+    # name: (nz, nx, nt, mode) -- a grid larger than L2 so DRAM counters mean something
+    "step2d-fp32-large": (4096, 4096, 6, "fp32"),
+    "step2d-fp64-large": (4096, 4096, 4, "fp64"),
+    "step2d-strict-large": (4096, 4096, 3, "fp64-strict"),
+}
+
+
+def run_case(name):
+    """Runs one small fixed workload (for ncu captures); prints a short status line."""
+    import torch
+
+    import sssi_gb300 as S
+
+    torch.cuda.set_device(0)
+    if name == "rtm-short":
+        V, VS, w, siz, six, nz, nx = workload()
+        img = S.rtmTimeCpmlFor2dAw(V, VS, w[:64], siz, six, N_ORDER, NB, DZ, DX, DT, epsilon=EPS, mode="fp32",
+                                   snap_stride=STRIDE)
+        print(f"case {name}: image max {np.abs(img).max():.3e}")
+        return
+    nz, nx, nt, mode = CASES[name]
+    rng = np.random.default_rng(1)
+    v = rng.uniform(1500.0, 4000.0, (nz, nx))
+    d, _ = S.fwdTimeCpmlFor2dAwPoint(v, nt, [2], [nx // 2], ricker(FREQ, nt, DT)[None, :], N_ORDER, NB, DZ, DX, DT,
+                                     mode=mode)
+    torch.cuda.synchronize()
+    print(f"case {name}: {nz}x{nx} nt={nt} {mode} ok, data max {np.abs(d).max():.3e}")
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short"],
+                    help="run one small fixed workload for a profiler capture and exit")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-nt", type=int, default=200, help="time steps of the bounded CPU sample")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("note: fewer than 3 warm-up steps requested", file=sys.stderr)
+    if args.case:
+        run_case(args.case)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,15 @@ int sssi_release_cache(void);
 /* Stream the library launches on (a cudaStream_t; NULL = legacy default). */
 int sssi_set_stream(void *stream);
 
+/* Phase timing with CUDA events on the launching stream.  When enabled, each
+ * propagation call records an event at every phase boundary (RTM shot:
+ * forward modelling of both models, reverse propagation with imaging, image
+ * finish; forward/reverse calls: one propagation phase).  After the call,
+ * sssi_last_timing reports each phase's device time in milliseconds and the
+ * number of kernels launched in it. */
+int sssi_enable_timing(int on);
+int sssi_last_timing(double *phase_ms, int64_t *phase_launches, int max_phases, int *n_phases);
+
 /* ---- host-side building blocks ---- */
 
 /* Staggered-grid first-derivative coefficients of half-order `order`

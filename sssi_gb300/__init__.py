@@ -9,6 +9,8 @@ from .api import (  # noqa: F401
     MODES,
     dampPml,
     dCoef,
+    enable_timing,
+    last_timing,
     fwdTimeCpmlFor2dAw,
     fwdTimeCpmlFor2dAwPoint,
     fwdTimeCpmlFor3dAw,

@@ -194,6 +194,20 @@ def set_stream(stream) -> None:
     check(lib().sssi_set_stream(ctypes.c_void_p(handle)))
 
 
+def enable_timing(on: bool = True) -> None:
+    """Record CUDA events at phase boundaries of each propagation call."""
+    check(lib().sssi_enable_timing(1 if on else 0))
+
+
+def last_timing():
+    """[(device ms, kernels launched)] per phase of the last timed call."""
+    ms = np.zeros(16)
+    nl = np.zeros(16, dtype=np.int64)
+    n = ctypes.c_int(0)
+    check(lib().sssi_last_timing(ms.ctypes.data, nl.ctypes.data, 16, ctypes.addressof(n)))
+    return [(float(ms[k]), int(nl[k])) for k in range(min(n.value, 16))]
+
+
 def release_cache() -> None:
     check(lib().sssi_release_cache())
 

@@ -196,6 +196,7 @@ void fwd2d_point(const double* v, int64_t nz, int64_t nx, int64_t nt, int N, int
     const int64_t K = std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * n))));
     DeviceBuffer snapbuf;
     if (snapshot && !snap_dev) snapbuf.allocate(sizeof(double) * n * K);
+    timing_begin(s);
     for (int64_t t0 = 0; t0 < nt; t0 += K) {
         const int64_t kk = std::min(K, nt - t0);
         for (int64_t t = t0; t < t0 + kk; ++t) {
@@ -211,6 +212,7 @@ void fwd2d_point(const double* v, int64_t nz, int64_t nx, int64_t nt, int N, int
             SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
         }
     }
+    timing_end(s);
     ddata.download(data, (size_t)(nx * nt), s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
@@ -310,6 +312,7 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
     }
 
     // forward modelling in the true and the migration model
+    timing_begin(s);
     for (int64_t t = 0; t < nt; ++t) {
         StepIO io;
         io.t = (int)t;
@@ -337,8 +340,10 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
                         amax.as<unsigned>() + k, fsnap.as<__half>() + k * n, inv.as<float>() + k, s);
     }
 
+    timing_mark(s);
     // reverse propagation of dataTrue - dataSmooth in the true model, imaging
     A.reset();
+    A.set_point_sources(0, nullptr, nullptr, nullptr, (int)nt);
     for (int64_t t = nt - 1; t >= 0; --t) {
         StepIO io;
         io.t = (int)t;
@@ -356,10 +361,9 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
             io.img_m = M.as<double>();
             io.img_s2 = S2.as<double>();
         }
-        // the reverse pass uses point sources of its own: none
-        A.set_point_sources(0, nullptr, nullptr, nullptr, (int)nt);
         A.step(io);
     }
+    timing_mark(s);
 
     DeviceView dimg(image, (size_t)n, false, s);
     if (strict) {
@@ -370,6 +374,7 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
     }
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
+    timing_end(s);
     dimg.download(image, (size_t)n, s);
     dtrue.download(data_true, (size_t)(nx * nt), s);
     dsmooth.download(data_smooth, (size_t)(nx * nt), s);

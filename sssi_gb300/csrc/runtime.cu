@@ -21,7 +21,48 @@ cudaStream_t g_stream = nullptr;
 std::mutex g_pool_mu;
 std::multimap<size_t, void*> g_pool;
 size_t g_pool_bytes = 0;
+
+// phase timing
+bool g_timing = false;
+std::vector<cudaEvent_t> g_events;
+std::vector<int64_t> g_marks;
+int g_nmarks = 0;
+std::vector<double> g_phase_ms;
+std::vector<int64_t> g_phase_launches;
 }  // namespace
+
+void timing_begin(cudaStream_t s) {
+    g_nmarks = 0;
+    g_marks.clear();
+    g_phase_ms.clear();
+    g_phase_launches.clear();
+    if (!g_timing) return;
+    timing_mark(s);
+}
+
+void timing_mark(cudaStream_t s) {
+    if (!g_timing) return;
+    if ((int)g_events.size() <= g_nmarks) {
+        cudaEvent_t e;
+        SSSI_CHECK_CUDA(cudaEventCreate(&e));
+        g_events.push_back(e);
+    }
+    SSSI_CHECK_CUDA(cudaEventRecord(g_events[g_nmarks], s));
+    g_marks.push_back(g_launches.load());
+    ++g_nmarks;
+}
+
+void timing_end(cudaStream_t s) {
+    if (!g_timing) return;
+    timing_mark(s);
+    SSSI_CHECK_CUDA(cudaEventSynchronize(g_events[g_nmarks - 1]));
+    for (int k = 1; k < g_nmarks; ++k) {
+        float ms = 0.f;
+        SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms, g_events[k - 1], g_events[k]));
+        g_phase_ms.push_back(ms);
+        g_phase_launches.push_back(g_marks[k] - g_marks[k - 1]);
+    }
+}
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -133,6 +174,21 @@ extern "C" int64_t sssi_launch_count(void) { return sssi::g_launches.load(); }
 
 extern "C" int sssi_release_cache(void) {
     return sssi::guarded([] { sssi::pool_trim(); });
+}
+
+extern "C" int sssi_enable_timing(int on) {
+    return sssi::guarded([&] { sssi::g_timing = on != 0; });
+}
+
+extern "C" int sssi_last_timing(double* phase_ms, int64_t* phase_launches, int max_phases, int* n_phases) {
+    return sssi::guarded([&] {
+        const int n = (int)sssi::g_phase_ms.size();
+        if (n_phases) *n_phases = n;
+        for (int k = 0; k < n && k < max_phases; ++k) {
+            if (phase_ms) phase_ms[k] = sssi::g_phase_ms[k];
+            if (phase_launches) phase_launches[k] = sssi::g_phase_launches[k];
+        }
+    });
 }
 
 extern "C" int sssi_set_stream(void* stream) {

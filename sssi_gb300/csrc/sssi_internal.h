@@ -102,6 +102,11 @@ class DeviceBuffer {
     size_t bytes_ = 0;
 };
 
+// Phase boundaries of the current call (no-ops unless timing is enabled).
+void timing_begin(cudaStream_t s);
+void timing_mark(cudaStream_t s);
+void timing_end(cudaStream_t s);
+
 // Releases every cached buffer (sssi_release_cache).
 void pool_trim();
 size_t pool_cached_bytes();
