@@ -130,6 +130,34 @@ int sssi_rtmTimeCpmlFor2dAw(const double *v, const double *vs, int64_t nz, int64
                             const double *wavelet, int64_t src_iz, int64_t src_ix, double epsilon, int mode,
                             int snap_stride, double *image, double *data_true, double *data_smooth);
 
+/* ---- forward modelling without any allocation ---- */
+
+/* Size of the fixed working array behind sssi_fwdTimeCpmlFor2dAwNoAlloc. */
+#define SSSI_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* No counterpart in the reference: an addition for callers that must not
+ * allocate memory while they run, such as a service whose GPU memory already
+ * belongs to its own pool (an extra cudaMalloc would fail), a latency-bound
+ * loop that cannot pay for the device-wide synchronisation of cudaMalloc and
+ * cudaFree, or a host program that forbids heap use after start-up.
+ *
+ * Same inputs, outputs and results as sssi_fwdTimeCpmlFor2dAw in the FP64
+ * modes, but every pointer must be device memory owned by the caller, and all
+ * working state lives in one array of SSSI_NOALLOC_SCRATCH_BYTES compiled
+ * into the library, which every GPU that uses this function keeps until the
+ * process exits.  The function calls no allocating routine.  Grids whose
+ * state does not fit (beyond about 620 x 1240 at nDiffOrder 4) are refused
+ * with SSSI_ERR_ARG and a message giving the size needed.
+ *
+ * All calls share that one array: calls whose work overlaps on the GPU (from
+ * two threads or two streams) corrupt each other and must be serialised by
+ * the caller.  Each call clears the state that has to start at zero.  The
+ * first call on each device looks up the array's device address with that
+ * device current; make that first call before any stream capture begins. */
+int sssi_fwdTimeCpmlFor2dAwNoAlloc(const double *v, const double *source, int64_t nz, int64_t nx, int64_t nt,
+                                   int nDiffOrder, int nBoundary, double dz, double dx, double dt, double *data,
+                                   double *snapshot, int mode);
+
 #ifdef __cplusplus
 }
 #endif

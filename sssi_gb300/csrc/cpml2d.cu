@@ -327,6 +327,39 @@ void launch_cpml2d_step(const Step2D<T, TA>& p, int N, bool strict, int bz, cuda
     }
 }
 
+template <typename T, typename TA>
+cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool strict, int bz, cudaStream_t stream) {
+    if (N < 1 || N > kMaxOrder) return cudaErrorInvalidValue;
+    if constexpr (std::is_same<T, double>::value && std::is_same<TA, double>::value) {
+        if (strict) {
+            switch (N) {
+                case 1: launch_n<T, TA, true, 1>(p, bz, stream); break;
+                case 2: launch_n<T, TA, true, 2>(p, bz, stream); break;
+                case 3: launch_n<T, TA, true, 3>(p, bz, stream); break;
+                case 4: launch_n<T, TA, true, 4>(p, bz, stream); break;
+                case 5: launch_n<T, TA, true, 5>(p, bz, stream); break;
+                case 6: launch_n<T, TA, true, 6>(p, bz, stream); break;
+                case 7: launch_n<T, TA, true, 7>(p, bz, stream); break;
+                default: launch_n<T, TA, true, 8>(p, bz, stream); break;
+            }
+            return cudaGetLastError();
+        }
+    } else {
+        if (strict) return cudaErrorInvalidValue;
+    }
+    switch (N) {
+        case 1: launch_n<T, TA, false, 1>(p, bz, stream); break;
+        case 2: launch_n<T, TA, false, 2>(p, bz, stream); break;
+        case 3: launch_n<T, TA, false, 3>(p, bz, stream); break;
+        case 4: launch_n<T, TA, false, 4>(p, bz, stream); break;
+        case 5: launch_n<T, TA, false, 5>(p, bz, stream); break;
+        case 6: launch_n<T, TA, false, 6>(p, bz, stream); break;
+        case 7: launch_n<T, TA, false, 7>(p, bz, stream); break;
+        default: launch_n<T, TA, false, 8>(p, bz, stream); break;
+    }
+    return cudaGetLastError();
+}
+
 void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
                      float* inv_scale_out, cudaStream_t stream) {
     pack_f16_kernel<<<152 * 4, 256, 0, stream>>>(P, ldp, nz, nx, amax, out, inv_scale_out);
@@ -474,5 +507,7 @@ template class Cpml2d<double, double>;
 template class Cpml2d<float, double>;
 template void launch_cpml2d_step<double, double>(const Step2D<double, double>&, int, bool, int, cudaStream_t);
 template void launch_cpml2d_step<float, double>(const Step2D<float, double>&, int, bool, int, cudaStream_t);
+template cudaError_t launch_cpml2d_step_nothrow<double, double>(const Step2D<double, double>&, int, bool, int,
+                                                                cudaStream_t);
 
 }  // namespace sssi

@@ -160,6 +160,10 @@ class Cpml2d {
 template <typename T, typename TA>
 void launch_cpml2d_step(const Step2D<T, TA>& p, int N, bool strict, int bz, cudaStream_t stream);
 
+// Same launch, reporting failure as a return value instead of an exception.
+template <typename T, typename TA>
+cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool strict, int bz, cudaStream_t stream);
+
 // Packs field P (padded, interior origin) into FP16 with the scale from *amax.
 void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
                      float* inv_scale_out, cudaStream_t stream);
