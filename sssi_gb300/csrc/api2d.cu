@@ -1,9 +1,11 @@
 // C-ABI entry points of the 2D propagators and the RTM shot.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "cpml2d.cuh"
+#include "tile2d.cuh"
 
 namespace sssi {
 
@@ -63,6 +65,16 @@ void pick_launch(int64_t nz, int64_t nx, int& bz, int& w) {
     }
 }
 
+// SSSI_ENGINE=xmarch routes the fused FP64 mode to the row-marching kernel
+// (the one strict FP64 always uses) instead of the tiled kernel.
+bool xmarch_engine() {
+    static const bool x = [] {
+        const char* e = std::getenv("SSSI_ENGINE");
+        return e && std::strcmp(e, "xmarch") == 0;
+    }();
+    return x;
+}
+
 void check_common(int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx, double dt, int mode) {
     SSSI_REQUIRE(nz > 0 && nx > 0 && nt >= 0, SSSI_ERR_ARG, "bad sizes nz=%lld nx=%lld nt=%lld", (long long)nz,
                  (long long)nx, (long long)nt);
@@ -107,6 +119,15 @@ __global__ void image_finish_kernel(const double* m, const double* s2, int64_t n
         image[q] = (scale * m[q]) / (eps + scale * s2[q]);
 }
 
+// Same from compensated FP32 sums (hi + lo).
+__global__ void image_finish_comp_kernel(const float2* m, const float2* s2, int64_t n, double scale, double eps,
+                                         double* image) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double mm = (double)m[q].x + (double)m[q].y, ss = (double)s2[q].x + (double)s2[q].y;
+        image[q] = (scale * mm) / (eps + scale * ss);
+    }
+}
+
 __global__ void fill_kernel(double* p, int64_t n, double v) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
         p[q] = v;
@@ -118,177 +139,296 @@ void fill(double* p, int64_t n, double v, cudaStream_t s) {
     SSSI_CHECK_CUDA(cudaGetLastError());
 }
 
+// Elementwise conversion between the API's double arrays and a propagator's
+// element type (a no-op copy is never launched: callers skip T == double).
+template <typename From, typename To>
+__global__ void convert_kernel(const From* in, To* out, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = static_cast<To>(in[q]);
+}
+
+template <typename From, typename To>
+void convert(const From* in, To* out, int64_t n, cudaStream_t s) {
+    if (n <= 0) return;
+    convert_kernel<From, To><<<152 * 4, 256, 0, s>>>(in, out, n);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+}
+
+// out = a - b in T
 template <typename T>
-void download_padded(const Cpml2d<T, double>& st, bool previous, double* model, cudaStream_t s) {
+__global__ void diff_kernel(const T* a, const T* b, T* out, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = a[q] - b[q];
+}
+
+// A device array of T holding (or receiving) a caller array of doubles.
+// When T is double and the caller's memory is on the device, it is used in
+// place; otherwise a cached device buffer stages it (and converts).
+template <typename T>
+struct Staged {
+    T* ptr = nullptr;
+    const double* caller = nullptr;
+    bool in_place = false;
+    size_t n = 0;
+    DeviceBuffer buf, tmp;
+
+    Staged(const double* p, size_t count, bool upload, cudaStream_t s) : caller(p), n(count) {
+        if (!p) return;
+        const bool dev = is_device_pointer(p);
+        if (std::is_same<T, double>::value && dev) {
+            ptr = reinterpret_cast<T*>(const_cast<double*>(p));
+            in_place = true;
+            return;
+        }
+        buf.allocate(std::max<size_t>(n, 1) * sizeof(T));
+        ptr = buf.as<T>();
+        if (!upload || n == 0) return;
+        if (std::is_same<T, double>::value) {
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(ptr, p, n * sizeof(double), cudaMemcpyHostToDevice, s));
+        } else {
+            const double* src = p;
+            if (!dev) {
+                tmp.allocate(n * sizeof(double));
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(tmp.get(), p, n * sizeof(double), cudaMemcpyHostToDevice, s));
+                src = tmp.as<double>();
+            }
+            convert(src, ptr, (int64_t)n, s);
+        }
+    }
+    // Copies the device contents back into the caller's array (host or device).
+    void download(double* out, cudaStream_t s) {
+        if (!out || in_place || n == 0) return;
+        const bool dev = is_device_pointer(out);
+        if (std::is_same<T, double>::value) {
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(out, ptr, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice
+                                                                               : cudaMemcpyDeviceToHost, s));
+            return;
+        }
+        if (dev) {
+            convert(ptr, out, (int64_t)n, s);
+            return;
+        }
+        tmp.allocate(n * sizeof(double));
+        convert(ptr, tmp.as<double>(), (int64_t)n, s);
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(out, tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+};
+
+// A chunk of K time slices of nz x nx streamed between the caller's array
+// (host or device, double) and a device array of T.
+template <typename T>
+struct SliceStream {
+    double* caller;
+    bool caller_dev = false;
+    int64_t n, K;
+    DeviceBuffer tbuf, dbuf;
+    T* base = nullptr;  // device slices of the current chunk (or the caller's when usable in place)
+
+    SliceStream(double* p, int64_t cells, int64_t k) : caller(p), n(cells), K(k) {
+        if (!p) return;
+        caller_dev = is_device_pointer(p);
+        if (!(std::is_same<T, double>::value && caller_dev)) tbuf.allocate(sizeof(T) * n * K);
+        if (!std::is_same<T, double>::value && !caller_dev) dbuf.allocate(sizeof(double) * n * K);
+    }
+    bool in_place() const { return std::is_same<T, double>::value && caller_dev; }
+    // device pointer of slice t (chunk starting at t0)
+    T* slice(int64_t t, int64_t t0) {
+        if (in_place()) return reinterpret_cast<T*>(caller) + t * n;
+        return tbuf.as<T>() + (t - t0) * n;
+    }
+    // input: bring slices [t0, t0+kk) to the device
+    void load(int64_t t0, int64_t kk, cudaStream_t s) {
+        if (!caller || in_place()) return;
+        const size_t bytes = sizeof(double) * n * kk;
+        if (std::is_same<T, double>::value) {
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(tbuf.get(), caller + t0 * n, bytes, cudaMemcpyHostToDevice, s));
+        } else if (caller_dev) {
+            convert(caller + t0 * n, tbuf.as<T>(), n * kk, s);
+        } else {
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(dbuf.get(), caller + t0 * n, bytes, cudaMemcpyHostToDevice, s));
+            convert(dbuf.as<double>(), tbuf.as<T>(), n * kk, s);
+        }
+    }
+    // output: send slices [t0, t0+kk) to the caller
+    void store(int64_t t0, int64_t kk, cudaStream_t s) {
+        if (!caller || in_place()) return;
+        const size_t bytes = sizeof(double) * n * kk;
+        if (std::is_same<T, double>::value) {
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(caller + t0 * n, tbuf.get(), bytes, cudaMemcpyDeviceToHost, s));
+        } else if (caller_dev) {
+            convert(tbuf.as<T>(), caller + t0 * n, n * kk, s);
+        } else {
+            convert(tbuf.as<T>(), dbuf.as<double>(), n * kk, s);
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(caller + t0 * n, dbuf.get(), bytes, cudaMemcpyDeviceToHost, s));
+        }
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+    }
+};
+
+template <class Prop>
+void download_padded(const Prop& st, bool previous, double* model, cudaStream_t s) {
+    using T = typename Prop::value_type;
     const int L = st.L();
     const int64_t rows = st.nz() + 2 * L, cols = st.padded_cols();
     DeviceView out(model, (size_t)(rows * cols), false, s);
-    const int k = previous ? 1 : 0;
-    // field(k) is relative to the current index; base() indexes the raw buffers
     const T* f = previous ? st.previous() : st.current();
     const T* base = f - st.origin();
     const int64_t row0 = (st.origin() % st.ldp()) - L;
-    (void)k;
     padded_to_dense_kernel<T><<<152 * 4, 256, 0, s>>>(base, st.ldp(), row0, rows, cols, out.ptr);
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     out.download(model, (size_t)(rows * cols), s);
 }
 
+int64_t chunk_steps(int64_t nt, int64_t cells) {
+    return std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * cells))));
+}
+
 // ---------------------------------------------------------------- forward
-template <typename T>
+template <class Prop>
 void fwd2d_dense(const double* v, const double* source, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
                  double dx, double dt, double* data, double* snapshot, bool strict) {
+    using T = typename Prop::value_type;
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
     std::vector<double> vh = host_copy(v, (size_t)n, s);
-    Cpml2d<T, double> st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
     int bz, w;
     pick_launch(nz, nx, bz, w);
     st.set_launch(bz, w);
-
-    DeviceView ddata(data, (size_t)(nx * nt), false, s);
-    const bool src_dev = source && is_device_pointer(source);
-    const bool snap_dev = snapshot && is_device_pointer(snapshot);
-    const int64_t K = std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * n))));
-    DeviceBuffer srcbuf, snapbuf;
-    if (source && !src_dev) srcbuf.allocate(sizeof(double) * n * K);
-    if (snapshot && !snap_dev) snapbuf.allocate(sizeof(double) * n * K);
-
+    Staged<T> rec(data, (size_t)(nx * nt), false, s);
+    const int64_t K = chunk_steps(nt, n);
+    SliceStream<T> src(const_cast<double*>(source), n, K), snap(snapshot, n, K);
+    timing_begin(s);
     for (int64_t t0 = 0; t0 < nt; t0 += K) {
         const int64_t kk = std::min(K, nt - t0);
-        if (source && !src_dev)
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(srcbuf.get(), source + t0 * n, sizeof(double) * n * kk,
-                                            cudaMemcpyHostToDevice, s));
+        src.load(t0, kk, s);
         for (int64_t t = t0; t < t0 + kk; ++t) {
-            StepIO io;
+            StepIO<T> io;
             io.t = (int)t;
-            if (source) io.src_dense = src_dev ? source + t * n : srcbuf.as<double>() + (t - t0) * n;
-            if (data) io.rec = ddata.ptr + t * nx;
-            if (snapshot) io.snap = snap_dev ? snapshot + t * n : snapbuf.as<double>() + (t - t0) * n;
+            if (source) io.src_dense = src.slice(t, t0);
+            if (data) io.rec = rec.ptr + t * nx;
+            if (snapshot) io.snap = snap.slice(t, t0);
             st.step(io);
         }
-        if (snapshot && !snap_dev) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(snapshot + t0 * n, snapbuf.get(), sizeof(double) * n * kk,
-                                            cudaMemcpyDeviceToHost, s));
-            SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
-        }
+        snap.store(t0, kk, s);
     }
-    ddata.download(data, (size_t)(nx * nt), s);
+    timing_end(s);
+    st.check_errors();
+    rec.download(data, s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
-template <typename T>
+template <class Prop>
 void fwd2d_point(const double* v, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx, double dt,
                  int nsrc, const int64_t* iz, const int64_t* ix, const double* wavelets, double* data,
                  double* snapshot, bool strict) {
+    using T = typename Prop::value_type;
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
     std::vector<double> vh = host_copy(v, (size_t)n, s);
-    Cpml2d<T, double> st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
     int bz, w;
     pick_launch(nz, nx, bz, w);
     st.set_launch(bz, w);
-    DeviceView dwav(wavelets, (size_t)(nsrc * nt), true, s);
-    st.set_point_sources(nsrc, iz, ix, dwav.ptr, (int)nt);
-    DeviceView ddata(data, (size_t)(nx * nt), false, s);
-    const bool snap_dev = snapshot && is_device_pointer(snapshot);
-    const int64_t K = std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * n))));
-    DeviceBuffer snapbuf;
-    if (snapshot && !snap_dev) snapbuf.allocate(sizeof(double) * n * K);
+    Staged<T> wav(wavelets, (size_t)(nsrc * nt), true, s);
+    st.set_point_sources(nsrc, iz, ix, wav.ptr, (int)nt);
+    Staged<T> rec(data, (size_t)(nx * nt), false, s);
+    const int64_t K = chunk_steps(nt, n);
+    SliceStream<T> snap(snapshot, n, K);
     timing_begin(s);
     for (int64_t t0 = 0; t0 < nt; t0 += K) {
         const int64_t kk = std::min(K, nt - t0);
         for (int64_t t = t0; t < t0 + kk; ++t) {
-            StepIO io;
+            StepIO<T> io;
             io.t = (int)t;
-            if (data) io.rec = ddata.ptr + t * nx;
-            if (snapshot) io.snap = snap_dev ? snapshot + t * n : snapbuf.as<double>() + (t - t0) * n;
+            if (data) io.rec = rec.ptr + t * nx;
+            if (snapshot) io.snap = snap.slice(t, t0);
             st.step(io);
         }
-        if (snapshot && !snap_dev) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(snapshot + t0 * n, snapbuf.get(), sizeof(double) * n * kk,
-                                            cudaMemcpyDeviceToHost, s));
-            SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
-        }
+        snap.store(t0, kk, s);
     }
     timing_end(s);
-    ddata.download(data, (size_t)(nx * nt), s);
+    st.check_errors();
+    rec.download(data, s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
 // ---------------------------------------------------------------- reverse
-template <typename T>
+template <class Prop>
 void rvs2d_dense(const double* v, const double* data, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
                  double dx, double dt, double* model, double* snapshot, bool strict) {
+    using T = typename Prop::value_type;
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
     std::vector<double> vh = host_copy(v, (size_t)n, s);
-    Cpml2d<T, double> st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop st(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
     int bz, w;
     pick_launch(nz, nx, bz, w);
     st.set_launch(bz, w);
-    DeviceView ddata(data, (size_t)(nx * nt), true, s);
-    const bool snap_dev = snapshot && is_device_pointer(snapshot);
-    const int64_t K = std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * n))));
-    DeviceBuffer snapbuf;
-    if (snapshot && !snap_dev) snapbuf.allocate(sizeof(double) * n * K);
-    // chunks [t0, t0+kk) visited from the end of time to the start
+    Staged<T> rows(data, (size_t)(nx * nt), true, s);
+    const int64_t K = chunk_steps(nt, n);
+    SliceStream<T> snap(snapshot, n, K);
+    timing_begin(s);
+    // chunks [t0, t_hi) visited from the end of time to the start
     for (int64_t t_hi = nt; t_hi > 0; t_hi -= K) {
         const int64_t t0 = std::max<int64_t>(0, t_hi - K);
         for (int64_t t = t_hi - 1; t >= t0; --t) {
-            StepIO io;
+            StepIO<T> io;
             io.t = (int)t;
-            if (data) io.src_row = ddata.ptr + t * nx;
-            if (snapshot) io.snap = snap_dev ? snapshot + t * n : snapbuf.as<double>() + (t - t0) * n;
+            if (data) io.src_row = rows.ptr + t * nx;
+            if (snapshot) io.snap = snap.slice(t, t0);
             st.step(io);
         }
-        if (snapshot && !snap_dev) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(snapshot + t0 * n, snapbuf.get(), sizeof(double) * n * (t_hi - t0),
-                                            cudaMemcpyDeviceToHost, s));
-            SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
-        }
+        snap.store(t0, t_hi - t0, s);
     }
+    timing_end(s);
+    st.check_errors();
     // the reference returns the field held as "old" after its final rotation
-    if (model) download_padded<T>(st, nt > 0, model, s);
+    if (model) download_padded(st, nt > 0, model, s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
 // ---------------------------------------------------------------- RTM shot
-template <typename T>
+template <class Prop>
 void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx,
            double dt, const double* wavelet, int64_t src_iz, int64_t src_ix, double eps, int mode, int stride,
            double* image, double* data_true, double* data_smooth) {
+    using T = typename Prop::value_type;
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
     const bool strict = mode == SSSI_MODE_FP64_STRICT;
     const bool f16 = mode == SSSI_MODE_FP32;
     if (!f16) stride = 1;
     SSSI_REQUIRE(stride >= 1, SSSI_ERR_ARG, "snap_stride must be >= 1");
+    constexpr bool kDouble = std::is_same<T, double>::value;
+    SSSI_REQUIRE(f16 || kDouble, SSSI_ERR_INTERNAL, "FP64 RTM needs an FP64 propagator");
     std::vector<double> vh = host_copy(v, (size_t)n, s);
     std::vector<double> vsh = host_copy(vs, (size_t)n, s);
-    Cpml2d<T, double> A(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
-    Cpml2d<T, double> B(vsh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop A(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop B(vsh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
     int bz, w;
     pick_launch(nz, nx, bz, w);
     A.set_launch(bz, w);
     B.set_launch(bz, w);
-    DeviceView dwav(wavelet, (size_t)nt, true, s);
-    A.set_point_sources(1, &src_iz, &src_ix, dwav.ptr, (int)nt);
-    B.set_point_sources(1, &src_iz, &src_ix, dwav.ptr, (int)nt);
-    DeviceView dtrue(data_true, (size_t)(nx * nt), false, s);
-    DeviceView dsmooth(data_smooth, (size_t)(nx * nt), false, s);
-    DeviceBuffer dtrue_own, dsmooth_own;
-    double* d_true = dtrue.ptr;
-    double* d_smooth = dsmooth.ptr;
+    Staged<T> wav(wavelet, (size_t)nt, true, s);
+    A.set_point_sources(1, &src_iz, &src_ix, wav.ptr, (int)nt);
+    B.set_point_sources(1, &src_iz, &src_ix, wav.ptr, (int)nt);
+    const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
+    Staged<T> dtrue(data_true, ndata, false, s), dsmooth(data_smooth, ndata, false, s);
+    DeviceBuffer dtrue_own, dsmooth_own, delta;
+    T* d_true = dtrue.ptr;
+    T* d_smooth = dsmooth.ptr;
     if (!d_true) {
-        dtrue_own.allocate(sizeof(double) * nx * std::max<int64_t>(nt, 1));
-        d_true = dtrue_own.as<double>();
+        dtrue_own.allocate(sizeof(T) * ndata);
+        d_true = dtrue_own.as<T>();
     }
     if (!d_smooth) {
-        dsmooth_own.allocate(sizeof(double) * nx * std::max<int64_t>(nt, 1));
-        d_smooth = dsmooth_own.as<double>();
+        dsmooth_own.allocate(sizeof(T) * ndata);
+        d_smooth = dsmooth_own.as<T>();
     }
+    delta.allocate(sizeof(T) * ndata);
 
     const int64_t nsnap = f16 ? (nt + stride - 1) / stride : nt;
     DeviceBuffer fsnap, rsnap, amax, inv, M, S2;
@@ -302,7 +442,7 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
         if (strict) rsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
     }
     if (!strict) {
-        M.allocate(sizeof(double) * n);
+        M.allocate(sizeof(double) * n);  // FP64 sums, or compensated FP32 (hi, lo) pairs of the same size
         S2.allocate(sizeof(double) * n);
         M.zero(s);
         if (f16)
@@ -314,15 +454,15 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
     // forward modelling in the true and the migration model
     timing_begin(s);
     for (int64_t t = 0; t < nt; ++t) {
-        StepIO io;
+        StepIO<T> io;
         io.t = (int)t;
         io.rec = d_true + t * nx;
         A.step(io);
-        StepIO jo;
+        StepIO<T> jo;
         jo.t = (int)t;
         jo.rec = d_smooth + t * nx;
         if (!f16) {
-            jo.snap = fsnap.as<double>() + t * n;
+            jo.snap = reinterpret_cast<T*>(fsnap.as<double>()) + t * n;
         } else {
             if (t % stride == 0) jo.amax = amax.as<unsigned>() + t / stride;
             if (t >= 1 && (t - 1) % stride == 0) {
@@ -339,18 +479,21 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
         launch_pack_f16(reinterpret_cast<const float*>(B.current()), B.ldp(), (int)nz, (int)nx,
                         amax.as<unsigned>() + k, fsnap.as<__half>() + k * n, inv.as<float>() + k, s);
     }
-
+    // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse time
+    diff_kernel<T><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<T>(), nx * nt);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
     timing_mark(s);
-    // reverse propagation of dataTrue - dataSmooth in the true model, imaging
+
+    // reverse propagation in the true model, imaging
     A.reset();
     A.set_point_sources(0, nullptr, nullptr, nullptr, (int)nt);
     for (int64_t t = nt - 1; t >= 0; --t) {
-        StepIO io;
+        StepIO<T> io;
         io.t = (int)t;
-        io.src_row = d_true + t * nx;
-        io.src_row_sub = d_smooth + t * nx;
+        io.src_row = delta.as<T>() + t * nx;
         if (strict) {
-            io.snap = rsnap.as<double>() + t * n;
+            io.snap = reinterpret_cast<T*>(rsnap.as<double>()) + t * n;
         } else if (!f16) {
             io.img_f64 = fsnap.as<double>() + t * n;
             io.img_m = M.as<double>();
@@ -358,8 +501,8 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
         } else if (t % stride == 0) {
             io.img_f16 = fsnap.as<__half>() + (t / stride) * n;
             io.img_inv_scale = inv.as<float>() + t / stride;
-            io.img_m = M.as<double>();
-            io.img_s2 = S2.as<double>();
+            io.img_m2 = M.as<float2>();
+            io.img_s22 = S2.as<float2>();
         }
         A.step(io);
     }
@@ -369,15 +512,20 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
     if (strict) {
         image_ascending_kernel<<<152 * 4, 256, 0, s>>>(fsnap.as<double>(), rsnap.as<double>(), n, nt, eps, dimg.ptr);
     } else {
-        image_finish_kernel<<<152 * 4, 256, 0, s>>>(M.as<double>(), S2.as<double>(), n, f16 ? (double)stride : 1.0,
-                                                     f16 ? eps : 0.0, dimg.ptr);
+        if (f16)
+            image_finish_comp_kernel<<<152 * 4, 256, 0, s>>>(M.as<float2>(), S2.as<float2>(), n, (double)stride, eps,
+                                                              dimg.ptr);
+        else
+            image_finish_kernel<<<152 * 4, 256, 0, s>>>(M.as<double>(), S2.as<double>(), n, 1.0, 0.0, dimg.ptr);
     }
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_end(s);
+    A.check_errors();
+    B.check_errors();
     dimg.download(image, (size_t)n, s);
-    dtrue.download(data_true, (size_t)(nx * nt), s);
-    dsmooth.download(data_smooth, (size_t)(nx * nt), s);
+    if (dtrue.ptr) dtrue.download(data_true, s);
+    if (dsmooth.ptr) dsmooth.download(data_smooth, s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -393,11 +541,18 @@ extern "C" int sssi_fwdTimeCpmlFor2dAw(const double* v, const double* source, in
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP32)
-            fwd2d_dense<float>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot, false);
+        if (mode == SSSI_MODE_FP64_STRICT)
+            fwd2d_dense<Cpml2d<double, double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data,
+                                                snapshot, true);
+        else if (xmarch_engine())
+            fwd2d_dense<Cpml2d<double, double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data,
+                                                snapshot, false);
+        else if (mode == SSSI_MODE_FP32)
+            fwd2d_dense<Tile2d<float>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot,
+                                       false);
         else
-            fwd2d_dense<double>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot,
-                                mode == SSSI_MODE_FP64_STRICT);
+            fwd2d_dense<Tile2d<double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot,
+                                        false);
     });
 }
 
@@ -411,12 +566,18 @@ extern "C" int sssi_fwdTimeCpmlFor2dAwPoint(const double* v, int64_t nz, int64_t
         SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "nsrc must be in 0..%d", kMaxPointSources);
         SSSI_REQUIRE(nsrc == 0 || (src_iz && src_ix && wavelets), SSSI_ERR_ARG, "point-source arrays are NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP32)
-            fwd2d_point<float>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix, wavelets, data,
-                               snapshot, false);
+        if (mode == SSSI_MODE_FP64_STRICT)
+            fwd2d_point<Cpml2d<double, double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
+                                                wavelets, data, snapshot, true);
+        else if (xmarch_engine())
+            fwd2d_point<Cpml2d<double, double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
+                                                wavelets, data, snapshot, false);
+        else if (mode == SSSI_MODE_FP32)
+            fwd2d_point<Tile2d<float>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
+                                       wavelets, data, snapshot, false);
         else
-            fwd2d_point<double>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix, wavelets,
-                                data, snapshot, mode == SSSI_MODE_FP64_STRICT);
+            fwd2d_point<Tile2d<double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
+                                        wavelets, data, snapshot, false);
     });
 }
 
@@ -427,11 +588,17 @@ extern "C" int sssi_rvsTimeCpmlFor2dAw(const double* v, const double* data, int6
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP32)
-            rvs2d_dense<float>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot, false);
+        if (mode == SSSI_MODE_FP64_STRICT)
+            rvs2d_dense<Cpml2d<double, double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
+                                                true);
+        else if (xmarch_engine())
+            rvs2d_dense<Cpml2d<double, double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
+                                                false);
+        else if (mode == SSSI_MODE_FP32)
+            rvs2d_dense<Tile2d<float>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot, false);
         else
-            rvs2d_dense<double>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
-                                mode == SSSI_MODE_FP64_STRICT);
+            rvs2d_dense<Tile2d<double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
+                                        false);
     });
 }
 
@@ -448,10 +615,13 @@ extern "C" int sssi_rtmTimeCpmlFor2dAw(const double* v, const double* vs, int64_
         SSSI_REQUIRE(epsilon >= 0, SSSI_ERR_ARG, "epsilon must be >= 0");
         ensure_device();
         if (mode == SSSI_MODE_FP32)
-            rtm2d<float>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon, mode,
-                         snap_stride, image, data_true, data_smooth);
+            rtm2d<Tile2d<float>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix,
+                                 epsilon, mode, snap_stride, image, data_true, data_smooth);
+        else if (mode == SSSI_MODE_FP64 && !xmarch_engine())
+            rtm2d<Tile2d<double>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix,
+                                  epsilon, mode, snap_stride, image, data_true, data_smooth);
         else
-            rtm2d<double>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon,
-                          mode, snap_stride, image, data_true, data_smooth);
+            rtm2d<Cpml2d<double, double>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz,
+                                          src_ix, epsilon, mode, snap_stride, image, data_true, data_smooth);
     });
 }

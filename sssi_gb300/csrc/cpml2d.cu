@@ -456,8 +456,7 @@ void Cpml2d<T, TA>::reset() {
 }
 
 template <typename T, typename TA>
-void Cpml2d<T, TA>::set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const double* d_wavelet,
-                                      int nt) {
+void Cpml2d<T, TA>::set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet, int nt) {
     SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "at most %d point sources (got %d)",
                  kMaxPointSources, nsrc);
     tmpl_.nsrc = nsrc;
@@ -473,7 +472,7 @@ void Cpml2d<T, TA>::set_point_sources(int nsrc, const int64_t* iz, const int64_t
 }
 
 template <typename T, typename TA>
-void Cpml2d<T, TA>::step(const StepIO& io) {
+void Cpml2d<T, TA>::step(const StepIO<T>& io) {
     Step2D<T, TA> p = tmpl_;
     p.W = w_;
     p.t = io.t;
@@ -485,7 +484,7 @@ void Cpml2d<T, TA>::step(const StepIO& io) {
     p.xphi_out = xphi_[1 - phase_].template as<TA>();
     p.src_dense = io.src_dense;
     p.src_row = io.src_row;
-    p.src_row_sub = io.src_row_sub;
+    p.src_row_sub = nullptr;
     p.rec = io.rec;
     p.snap = io.snap;
     p.pack = io.pack;
@@ -504,9 +503,7 @@ void Cpml2d<T, TA>::step(const StepIO& io) {
 }
 
 template class Cpml2d<double, double>;
-template class Cpml2d<float, double>;
 template void launch_cpml2d_step<double, double>(const Step2D<double, double>&, int, bool, int, cudaStream_t);
-template void launch_cpml2d_step<float, double>(const Step2D<float, double>&, int, bool, int, cudaStream_t);
 template cudaError_t launch_cpml2d_step_nothrow<double, double>(const Step2D<double, double>&, int, bool, int,
                                                                 cudaStream_t);
 

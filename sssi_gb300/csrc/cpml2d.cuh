@@ -95,13 +95,14 @@ struct Scalar<float> {
     static constexpr int kAlign = 32;
 };
 
-// Per-step inputs/outputs chosen by the caller.
+// Per-step inputs/outputs chosen by the caller, in the propagator's element
+// type (conversions to and from double happen outside the step kernels).
+template <typename T>
 struct StepIO {
-    const double* src_dense = nullptr;
-    const double* src_row = nullptr;
-    const double* src_row_sub = nullptr;
-    double* rec = nullptr;
-    double* snap = nullptr;
+    const T* src_dense = nullptr;  // nz x nx source slice of this step
+    const T* src_row = nullptr;    // nx values injected on row 0
+    T* rec = nullptr;              // nx: new field on row 0
+    T* snap = nullptr;             // nz x nx: new field
     __half* pack = nullptr;
     const unsigned* pack_amax = nullptr;
     float* pack_inv_scale_out = nullptr;
@@ -111,6 +112,8 @@ struct StepIO {
     const float* img_inv_scale = nullptr;
     double* img_m = nullptr;
     double* img_s2 = nullptr;
+    float2* img_m2 = nullptr;  // compensated FP32 sums used with img_f16 by the tiled kernel
+    float2* img_s22 = nullptr;
     int t = 0;
 };
 
@@ -119,13 +122,14 @@ struct StepIO {
 template <typename T, typename TA>
 class Cpml2d {
   public:
+    using value_type = T;
     // v: nz x nx host array (column-major).
     Cpml2d(const double* v, int64_t nz, int64_t nx, int N, int nB, double dz, double dx, double dt, bool strict,
            cudaStream_t stream);
 
     void reset();  // zero fields and memory variables
-    void set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const double* d_wavelet, int nt);
-    void step(const StepIO& io);
+    void set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet, int nt);
+    void step(const StepIO<T>& io);
 
     // Field after the last step (padded storage; interior (0,0) at offset).
     const T* current() const { return field(cur_); }
@@ -143,6 +147,7 @@ class Cpml2d {
         bz_ = bz;
         w_ = w;
     }
+    void check_errors() {}
 
   private:
     int64_t nz_, nx_;

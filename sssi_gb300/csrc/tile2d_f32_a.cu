@@ -1,0 +1,9 @@
+// Tiled 2D CPML step, float, orders 1-4.
+#include "tile2d_kernel.cuh"
+
+namespace sssi {
+SSSI_TILE2D_INSTANCE(float, 1)
+SSSI_TILE2D_INSTANCE(float, 2)
+SSSI_TILE2D_INSTANCE(float, 3)
+SSSI_TILE2D_INSTANCE(float, 4)
+}  // namespace sssi

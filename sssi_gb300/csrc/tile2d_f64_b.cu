@@ -1,0 +1,9 @@
+// Tiled 2D CPML step, double, orders 5-8.
+#include "tile2d_kernel.cuh"
+
+namespace sssi {
+SSSI_TILE2D_INSTANCE(double, 5)
+SSSI_TILE2D_INSTANCE(double, 6)
+SSSI_TILE2D_INSTANCE(double, 7)
+SSSI_TILE2D_INSTANCE(double, 8)
+}  // namespace sssi
