@@ -4,8 +4,8 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "batch2d.cuh"
 #include "cpml2d.cuh"
-#include "tile2d.cuh"
 
 namespace sssi {
 
@@ -529,6 +529,204 @@ void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
+// ================================================================ batched engine
+// Dense copy of a padded field (device) for the reverse pass's model output.
+template <typename T>
+void download_field(const T* field, int64_t ldp, int L, int64_t nz, int64_t nx, double* model, cudaStream_t s) {
+    const int64_t rows = nz + 2 * L, cols = nx + 2 * L;
+    DeviceView out(model, (size_t)(rows * cols), false, s);
+    // field points at interior (0,0); padded (0,0) is L rows up and L columns left
+    const T* base = field - L - (int64_t)L * ldp;
+    padded_to_dense_kernel<T><<<152 * 4, 256, 0, s>>>(base, ldp, 0, rows, cols, out.ptr);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+    out.download(model, (size_t)(rows * cols), s);
+}
+
+template <typename T>
+void bfwd2d(const double* v, const double* source, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
+            double dx, double dt, int nsrc, const int64_t* iz, const int64_t* ix, const double* wavelets, double* data,
+            double* snapshot) {
+    cudaStream_t s = current_stream();
+    const int64_t n = nz * nx;
+    std::vector<double> vh = host_copy(v, (size_t)n, s);
+    Batch2d<T> B(N, dz, dx, s);
+    const int k = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, false);
+    Staged<T> wav(wavelets, (size_t)(nsrc * nt), true, s);
+    if (nsrc) B.set_point_sources(k, nsrc, iz, ix, wav.ptr);
+    Staged<T> rec(data, (size_t)(nx * nt), false, s);
+    B.shot(k).rec = rec.ptr;
+    const int64_t K = chunk_steps(nt, n);
+    SliceStream<T> src(const_cast<double*>(source), n, K), snap(snapshot, n, K);
+    B.finalize();
+    B.set_step(0);
+    timing_begin(s);
+    for (int64_t t0 = 0; t0 < nt; t0 += K) {
+        const int64_t kk = std::min(K, nt - t0);
+        src.load(t0, kk, s);
+        ShotTail<T>& d = B.shot(k);
+        d.src_dense = source ? src.slice(t0, t0) : nullptr;
+        d.dense_t0 = (int)t0;
+        d.snap = snapshot ? snap.slice(t0, t0) : nullptr;
+        d.snap_t0 = (int)t0;
+        B.sync_desc(k);
+        B.run((int)kk);
+        snap.store(t0, kk, s);
+    }
+    timing_end(s);
+    B.check_errors();
+    rec.download(data, s);
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void brvs2d(const double* v, const double* data, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
+            double dx, double dt, double* model, double* snapshot) {
+    cudaStream_t s = current_stream();
+    const int64_t n = nz * nx;
+    std::vector<double> vh = host_copy(v, (size_t)n, s);
+    Batch2d<T> B(N, dz, dx, s);
+    const int k = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, true);
+    Staged<T> rows(data, (size_t)(nx * nt), true, s);
+    B.shot(k).src_row = data ? rows.ptr : nullptr;
+    const int64_t K = chunk_steps(nt, n);
+    SliceStream<T> snap(snapshot, n, K);
+    B.finalize();
+    B.set_step(0);
+    timing_begin(s);
+    // chunks [t0, t_hi) visited from the end of time to the start
+    for (int64_t t_hi = nt; t_hi > 0; t_hi -= K) {
+        const int64_t t0 = std::max<int64_t>(0, t_hi - K);
+        ShotTail<T>& d = B.shot(k);
+        d.snap = snapshot ? snap.slice(t0, t0) : nullptr;
+        d.snap_t0 = (int)t0;
+        B.sync_desc(k);
+        B.run((int)(t_hi - t0));
+        snap.store(t0, t_hi - t0, s);
+    }
+    timing_end(s);
+    B.check_errors();
+    // the reference returns the field held as "old" after its final rotation:
+    // the result of the step before the last one
+    if (model) {
+        const ShotTail<T>& d = B.shot(k);
+        const T* prev = d.field[(nt + 1) & 1];
+        download_field(prev, d.ldp, B.L(), nz, nx, model, s);
+    }
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
+            double dx, double dt, const double* wavelet, int64_t src_iz, int64_t src_ix, double eps, int stride,
+            double* image, double* data_true, double* data_smooth) {
+    constexpr bool kF16 = std::is_same<T, float>::value;
+    cudaStream_t s = current_stream();
+    const int64_t n = nz * nx;
+    if (!kF16) stride = 1;
+    SSSI_REQUIRE(stride >= 1, SSSI_ERR_ARG, "snap_stride must be >= 1");
+    std::vector<double> vh = host_copy(v, (size_t)n, s);
+    std::vector<double> vsh = host_copy(vs, (size_t)n, s);
+    Batch2d<T> B(N, dz, dx, s);
+    // forward in v and in vs over batch steps [0, nt); reverse in v over [nt, 2nt)
+    const int kA = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, false);
+    const int kB = B.add_shot(vsh.data(), nz, nx, nB, dt, (int)nt, 0, false);
+    const int kR = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, (int)nt, true);
+    Staged<T> wav(wavelet, (size_t)nt, true, s);
+    B.set_point_sources(kA, 1, &src_iz, &src_ix, wav.ptr);
+    B.set_point_sources(kB, 1, &src_iz, &src_ix, wav.ptr);
+    const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
+    Staged<T> dtrue(data_true, ndata, false, s), dsmooth(data_smooth, ndata, false, s);
+    DeviceBuffer dtrue_own, dsmooth_own, delta;
+    T* d_true = dtrue.ptr;
+    T* d_smooth = dsmooth.ptr;
+    if (!d_true) {
+        dtrue_own.allocate(sizeof(T) * ndata);
+        d_true = dtrue_own.as<T>();
+    }
+    if (!d_smooth) {
+        dsmooth_own.allocate(sizeof(T) * ndata);
+        d_smooth = dsmooth_own.as<T>();
+    }
+    delta.allocate(sizeof(T) * ndata);
+    const int64_t nsnap = (nt + stride - 1) / stride;
+    DeviceBuffer fsnap, amax, inv, M, S2;
+    if (kF16) {
+        fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
+        amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
+        amax.zero(s);
+        inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
+    } else {
+        fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
+    }
+    M.allocate(sizeof(double) * n);  // FP64 sums, or compensated FP32 (hi, lo) pairs of the same size
+    S2.allocate(sizeof(double) * n);
+    M.zero(s);
+    if (kF16)
+        S2.zero(s);
+    else
+        fill(S2.as<double>(), n, eps, s);
+
+    ShotTail<T>& a = B.shot(kA);
+    a.rec = d_true;
+    ShotTail<T>& b = B.shot(kB);
+    b.rec = d_smooth;
+    if (kF16) {
+        b.stride = stride;
+        b.amax = amax.as<unsigned>();
+        b.pack = fsnap.as<__half>();
+        b.inv_scale = inv.as<float>();
+    } else {
+        b.snap = reinterpret_cast<T*>(fsnap.as<double>());
+        b.snap_t0 = 0;
+    }
+    ShotTail<T>& r = B.shot(kR);
+    r.src_row = delta.as<T>();
+    if (kF16) {
+        r.stride = stride;
+        r.img_f16 = fsnap.as<__half>();
+        r.img_inv = inv.as<float>();
+        r.img_m2 = M.as<float2>();
+        r.img_s22 = S2.as<float2>();
+    } else {
+        r.img_f64 = fsnap.as<double>();
+        r.img_m = M.as<double>();
+        r.img_s2 = S2.as<double>();
+    }
+    B.finalize();
+    B.set_step(0);
+
+    timing_begin(s);
+    B.run((int)nt);
+    if (kF16 && nt >= 1 && (nt - 1) % stride == 0) {
+        const int64_t k = (nt - 1) / stride;
+        launch_pack_f16(reinterpret_cast<const float*>(B.current_field(kB)), B.ldp(kB), (int)nz, (int)nx,
+                        amax.as<unsigned>() + k, fsnap.as<__half>() + k * n, inv.as<float>() + k, s);
+    }
+    // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse time
+    diff_kernel<T><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<T>(), nx * nt);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+    timing_mark(s);
+    B.run((int)nt);
+    timing_mark(s);
+
+    DeviceView dimg(image, (size_t)n, false, s);
+    if (kF16)
+        image_finish_comp_kernel<<<152 * 4, 256, 0, s>>>(M.as<float2>(), S2.as<float2>(), n, (double)stride, eps,
+                                                          dimg.ptr);
+    else
+        image_finish_kernel<<<152 * 4, 256, 0, s>>>(M.as<double>(), S2.as<double>(), n, 1.0, 0.0, dimg.ptr);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+    timing_end(s);
+    B.check_errors();
+    dimg.download(image, (size_t)n, s);
+    if (dtrue.ptr) dtrue.download(data_true, s);
+    if (dsmooth.ptr) dsmooth.download(data_smooth, s);
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+}
+
 }  // namespace
 }  // namespace sssi
 
@@ -541,18 +739,15 @@ extern "C" int sssi_fwdTimeCpmlFor2dAw(const double* v, const double* source, in
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT)
+        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
             fwd2d_dense<Cpml2d<double, double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data,
-                                                snapshot, true);
-        else if (xmarch_engine())
-            fwd2d_dense<Cpml2d<double, double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data,
-                                                snapshot, false);
+                                                snapshot, mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
-            fwd2d_dense<Tile2d<float>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot,
-                                       false);
+            bfwd2d<float>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, 0, nullptr, nullptr, nullptr, data,
+                          snapshot);
         else
-            fwd2d_dense<Tile2d<double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data, snapshot,
-                                        false);
+            bfwd2d<double>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, 0, nullptr, nullptr, nullptr,
+                           data, snapshot);
     });
 }
 
@@ -566,18 +761,15 @@ extern "C" int sssi_fwdTimeCpmlFor2dAwPoint(const double* v, int64_t nz, int64_t
         SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "nsrc must be in 0..%d", kMaxPointSources);
         SSSI_REQUIRE(nsrc == 0 || (src_iz && src_ix && wavelets), SSSI_ERR_ARG, "point-source arrays are NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT)
+        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
             fwd2d_point<Cpml2d<double, double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
-                                                wavelets, data, snapshot, true);
-        else if (xmarch_engine())
-            fwd2d_point<Cpml2d<double, double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
-                                                wavelets, data, snapshot, false);
+                                                wavelets, data, snapshot, mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
-            fwd2d_point<Tile2d<float>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
-                                       wavelets, data, snapshot, false);
+            bfwd2d<float>(v, nullptr, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix, wavelets,
+                          data, snapshot);
         else
-            fwd2d_point<Tile2d<double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
-                                        wavelets, data, snapshot, false);
+            bfwd2d<double>(v, nullptr, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix, wavelets,
+                           data, snapshot);
     });
 }
 
@@ -588,17 +780,13 @@ extern "C" int sssi_rvsTimeCpmlFor2dAw(const double* v, const double* data, int6
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT)
+        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
             rvs2d_dense<Cpml2d<double, double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
-                                                true);
-        else if (xmarch_engine())
-            rvs2d_dense<Cpml2d<double, double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
-                                                false);
+                                                mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
-            rvs2d_dense<Tile2d<float>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot, false);
+            brvs2d<float>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot);
         else
-            rvs2d_dense<Tile2d<double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
-                                        false);
+            brvs2d<double>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot);
     });
 }
 
@@ -615,11 +803,11 @@ extern "C" int sssi_rtmTimeCpmlFor2dAw(const double* v, const double* vs, int64_
         SSSI_REQUIRE(epsilon >= 0, SSSI_ERR_ARG, "epsilon must be >= 0");
         ensure_device();
         if (mode == SSSI_MODE_FP32)
-            rtm2d<Tile2d<float>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix,
-                                 epsilon, mode, snap_stride, image, data_true, data_smooth);
+            brtm2d<float>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon,
+                          snap_stride, image, data_true, data_smooth);
         else if (mode == SSSI_MODE_FP64 && !xmarch_engine())
-            rtm2d<Tile2d<double>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix,
-                                  epsilon, mode, snap_stride, image, data_true, data_smooth);
+            brtm2d<double>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon, 1,
+                           image, data_true, data_smooth);
         else
             rtm2d<Cpml2d<double, double>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz,
                                           src_ix, epsilon, mode, snap_stride, image, data_true, data_smooth);

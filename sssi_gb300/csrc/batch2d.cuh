@@ -1,0 +1,141 @@
+// Batched 2D CPML step: many independent propagations ("shots"), each with
+// its own grid, model, start step and length, advanced by one persistent
+// launch per time step.  The tiled kernel of tile2d.cuh generalised so that a
+// CTA's tiles may belong to different shots.
+//
+// Per-shot state and per-step hooks live in a device-resident array of
+// ShotDesc.  The batch step counter also lives in device memory: every launch
+// reads it, and the last CTA to finish increments it, so a run of steps is a
+// sequence of identical launches (which a CUDA graph can replay).
+#pragma once
+
+#include "tile2d.cuh"
+
+namespace sssi {
+
+// Per-shot fields the tile code reads; copied to shared memory once per tile.
+template <typename T>
+struct alignas(16) ShotTail {
+    using M = typename MemVar<T>::type;
+    T* field[2];  // interior origin of field k; field (t_local & 1) is current at local step t_local
+    const T* zb;
+    const T* zbm1;
+    M* zphi[2];
+    M* zpsi;
+    const T* xb;
+    const T* xbm1;
+    M* xphi[2];
+    M* xpsi;
+    int64_t ldp;
+    int nz, nx, nB, ntz, ntx, oz;
+    int t_start;  // batch step of the shot's first step
+    int nt;       // steps of the shot
+    int reverse;  // time index tau = nt-1-t_local when set, else t_local
+    int nsrc;
+    int src_iz[kMaxPointSources];
+    int src_ix[kMaxPointSources];
+    const T* src_wavelet;  // nsrc x nt, indexed by tau
+    const T* src_row;      // nx x nt: injected on row 0 at tau
+    const T* src_dense;    // slices of nz x nx for tau = dense_t0, dense_t0+1, ...
+    T* rec;                // nx x nt: row 0 after the step at tau
+    T* snap;               // slices of nz x nx for tau = snap_t0, ...
+    int dense_t0;
+    int snap_t0;
+    // RTM, forward shot: at tau % stride == 0 the max |field| goes to amax[tau/stride];
+    // at (tau-1) % stride == 0 the current field (the result of step tau-1) is
+    // stored in FP16 at pack + ((tau-1)/stride) * nz*nx, its 1/scale in inv_scale.
+    int stride;
+    int pad_;
+    unsigned* amax;
+    __half* pack;
+    float* inv_scale;
+    // RTM, reverse shot: at tau % stride == 0 image against the stored forward field
+    const __half* img_f16;  // stored forward fields (as written by pack)
+    const float* img_inv;   // their 1/scale
+    float2* img_m2;         // compensated FP32 sums
+    float2* img_s22;
+    const double* img_f64;  // FP64: forward field of every step, nz x nx x nt
+    double* img_m;
+    double* img_s2;
+};
+
+template <typename T>
+struct alignas(128) ShotDesc {
+    CUtensorMap tm_box[2];   // halo box of field k
+    CUtensorMap tm_tile[2];  // tile box of field k
+    CUtensorMap tm_v;        // tile box of (v dt)^2
+    ShotTail<T> s;
+};
+
+template <typename T>
+struct BatchConst {
+    T az[16], ax[16];  // composed second-derivative coefficients a_0 .. a_l
+    T wz[8], wx[8];    // first-derivative weights c_k / d
+    int nshots;
+    int ntiles;
+    const int* cta_begin;  // gridDim.x + 1: each CTA's range in `work`
+    const int2* work;      // (shot, tile within the shot), grouped by CTA
+    int* step;             // batch step counter
+    int* done;             // CTAs finished in this launch
+    int* err;              // set when a TMA copy does not arrive in time
+};
+
+// Device state of a batch of shots sharing the order and the grid spacing.
+template <typename T>
+class Batch2d {
+  public:
+    using value_type = T;
+    using M = typename MemVar<T>::type;
+    Batch2d(int N, double dz, double dx, cudaStream_t stream);
+
+    // Adds a shot: v is the host nz x nx model.  Returns the shot index.
+    int add_shot(const double* v, int64_t nz, int64_t nx, int nB, double dt, int nt, int t_start, bool reverse);
+    ShotTail<T>& shot(int k) { return shots_[k].desc.s; }
+    void set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet);
+    void enable(int k, bool on) { shots_[k].enabled = on; }
+    // Zeroes the fields and memory variables of shot k.
+    void reset_shot(int k);
+    // Assigns the tiles of the enabled shots to CTAs (longest-processing-time
+    // first, tiles next to a damped band weighted heavier) and uploads every
+    // descriptor.  Call again whenever the set of active shots changes.
+    void finalize();
+    // Re-uploads the descriptor of shot k (after its hooks changed).
+    void sync_desc(int k);
+    void set_step(int step);
+    // Launches `nsteps` batch steps.
+    void run(int nsteps);
+    void check_errors();
+
+    const T* current_field(int k) const;  // field after the last completed step of shot k
+    int64_t ldp(int k) const { return shots_[k].desc.s.ldp; }
+    int L() const { return L_; }
+    int grid() const { return grid_; }
+    int step_host() const { return step_; }
+
+  private:
+    struct Shot {
+        ShotDesc<T> desc{};
+        bool enabled = true;
+        int64_t origin = 0;
+        DeviceBuffer P[2], vdt2, zb, zbm1, zphi[2], zpsi, xb, xbm1, xphi[2], xpsi;
+    };
+    int N_, L_;
+    double dz_, dx_;
+    cudaStream_t stream_;
+    BatchConst<T> bc_{};
+    std::vector<Shot> shots_;
+    DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;
+    int grid_ = 0, ntiles_ = 0, step_ = 0;
+    int ctas_per_sm_ = 1, sms_ = 1;
+};
+
+template <typename T, int N>
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream);
+template <typename T, int N>
+int batch2d_occupancy_n();
+template <typename T>
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream);
+template <typename T>
+int batch2d_ctas_per_sm(int N);
+
+}  // namespace sssi

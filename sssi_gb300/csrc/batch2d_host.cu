@@ -1,0 +1,365 @@
+// Host side of the batched 2D CPML step: shot state, descriptors, launches.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
+#include <cmath>
+#include <mutex>
+#include <queue>
+
+#include "batch2d.cuh"
+
+namespace sssi {
+
+bool encode_tensor_map_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, size_t elem_bytes,
+                          uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    });
+    if (!encode) return false;
+    const cuuint64_t dims[2] = {rows, cols};
+    const cuuint64_t strides[1] = {ld * elem_bytes};
+    const cuuint32_t box[2] = {box_rows, box_cols};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+namespace {
+
+template <typename T>
+struct TmaType;
+template <>
+struct TmaType<float> {
+    static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+};
+template <>
+struct TmaType<double> {
+    static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+};
+
+// Band coefficients in T.  In FP32, b - 1 comes from expm1 so it keeps full
+// relative precision where b is close to 1.
+template <typename T>
+void band_coefficients(const std::vector<double>& b, const std::vector<double>& bm1, std::vector<T>& ob,
+                       std::vector<T>& obm1) {
+    ob.resize(b.size());
+    obm1.resize(b.size());
+    for (size_t k = 0; k < b.size(); ++k) {
+        ob[k] = static_cast<T>(b[k]);
+        if constexpr (std::is_same<T, float>::value)
+            obm1[k] = static_cast<float>(std::expm1(std::log(b[k])));
+        else
+            obm1[k] = bm1[k];
+    }
+}
+
+// Composed second-derivative coefficients a_0..a_l of D-(D+ .) for weights w:
+// coefficient of P(i+m) (= that of P(i-m)).
+void composed(const double* w, int N, double* a) {
+    const int L = 2 * N - 1;
+    for (int m = 0; m <= L; ++m) a[m] = 0.0;
+    for (int k = 0; k < N; ++k)
+        for (int n = 0; n < N; ++n) {
+            const double ww = w[k] * w[n];
+            a[k + n + 1] += ww;  // +P(i+k+n+1) and its mirror +P(i-1-k-n)
+            // -P(i+k-n) and -P(i-k+n): over ordered pairs each |k-n| > 0 is met
+            // twice (once per sign), while k = n puts both terms on P(i)
+            const int d = k - n;
+            a[d < 0 ? -d : d] -= (d == 0 ? 2.0 : 1.0) * ww;
+        }
+}
+
+}  // namespace
+
+template <typename T>
+Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
+    : N_(N), L_(2 * N - 1), dz_(dz), dx_(dx), stream_(stream) {
+    SSSI_REQUIRE(N >= 1 && N <= kMaxOrder, SSSI_ERR_ARG, "nDiffOrder must be in 1..%d (got %d)", kMaxOrder, N);
+    SSSI_REQUIRE(dz > 0 && dx > 0, SSSI_ERR_ARG, "dz and dx must be positive");
+    double c[kMaxOrder], wz[kMaxOrder], wx[kMaxOrder], az[16], ax[16];
+    staggered_coefficients(N, c);
+    for (int k = 0; k < N; ++k) {
+        wz[k] = c[k] / dz;
+        wx[k] = c[k] / dx;
+    }
+    composed(wz, N, az);
+    composed(wx, N, ax);
+    for (int k = 0; k < 8; ++k) {
+        bc_.wz[k] = k < N ? static_cast<T>(wz[k]) : T(0);
+        bc_.wx[k] = k < N ? static_cast<T>(wx[k]) : T(0);
+    }
+    for (int m = 0; m < 16; ++m) {
+        bc_.az[m] = m <= L_ ? static_cast<T>(az[m]) : T(0);
+        bc_.ax[m] = m <= L_ ? static_cast<T>(ax[m]) : T(0);
+    }
+    d_ctr_.allocate(4 * sizeof(int));  // step, done, err, spare
+    d_ctr_.zero(stream);
+    bc_.step = d_ctr_.template as<int>();
+    bc_.done = d_ctr_.template as<int>() + 1;
+    bc_.err = d_ctr_.template as<int>() + 2;
+    int dev = 0;
+    SSSI_CHECK_CUDA(cudaGetDevice(&dev));
+    SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+    ctas_per_sm_ = batch2d_ctas_per_sm<T>(N);
+}
+
+template <typename T>
+int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double dt, int nt, int t_start,
+                         bool reverse) {
+    SSSI_REQUIRE(nz >= 1 && nx >= 1, SSSI_ERR_ARG, "empty model (%lld x %lld)", (long long)nz, (long long)nx);
+    SSSI_REQUIRE(nB >= 0 && nB <= nz && 2 * (int64_t)nB <= nx, SSSI_ERR_ARG,
+                 "nBoundary %d does not fit the model (%lld x %lld): need nBoundary <= nz and 2*nBoundary <= nx", nB,
+                 (long long)nz, (long long)nx);
+    SSSI_REQUIRE(nz < (1LL << 30) && nx < (1LL << 30), SSSI_ERR_ARG, "model too large");
+    SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
+    using Sh = TileShape<T>;
+    shots_.emplace_back();
+    Shot& S = shots_.back();
+    ShotTail<T>& d = S.desc.s;
+    const int HZ = tile_halo_rows(N_);
+    constexpr int al = Scalar<T>::kAlign;
+    const int64_t oz = (std::max(L_, HZ) + al - 1) / al * al;
+    const int64_t nz_alloc = (nz + Sh::TZ - 1) / Sh::TZ * Sh::TZ;
+    const int64_t ldp = (oz + nz_alloc + HZ + al - 1) / al * al;
+    S.origin = oz + (int64_t)L_ * ldp;
+    const int64_t cols = nx + 2 * L_;
+    const size_t pbytes = sizeof(T) * (size_t)ldp * (size_t)cols;
+    for (auto& b : S.P) b.allocate(pbytes);
+    S.vdt2.allocate(pbytes);
+    {
+        const int64_t n = nz * nx;
+        std::vector<T> h(n);
+        for (int64_t q = 0; q < n; ++q) h[q] = static_cast<T>((v[q] * dt) * (v[q] * dt));
+        S.vdt2.zero(stream_);
+        SSSI_CHECK_CUDA(cudaMemcpy2DAsync(S.vdt2.template as<T>() + S.origin, sizeof(T) * ldp, h.data(), sizeof(T) * nz,
+                                          sizeof(T) * nz, nx, cudaMemcpyHostToDevice, stream_));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    }
+    Bands2D bands = damping_bands_2d(v, nz, nx, nB, dz_, dx_, dt);
+    auto upload = [&](DeviceBuffer& buf, const std::vector<T>& h) {
+        buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
+        if (!h.empty())
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
+                                            stream_));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    };
+    std::vector<T> b, bm1;
+    band_coefficients<T>(bands.zb, bands.zbm1, b, bm1);
+    upload(S.zb, b);
+    upload(S.zbm1, bm1);
+    band_coefficients<T>(bands.xb, bands.xbm1, b, bm1);
+    upload(S.xb, b);
+    upload(S.xbm1, bm1);
+    const size_t zbytes = sizeof(M) * std::max<size_t>((size_t)nB * nx, 1);
+    const size_t xbytes = sizeof(M) * std::max<size_t>((size_t)nz * 2 * nB, 1);
+    for (auto* bf : {&S.zphi[0], &S.zphi[1], &S.zpsi}) bf->allocate(zbytes);
+    for (auto* bf : {&S.xphi[0], &S.xphi[1], &S.xpsi}) bf->allocate(xbytes);
+
+    const uint32_t box_rows = Sh::TZ + 2 * HZ, box_cols = Sh::TX + 2 * L_;
+    for (int k = 0; k < 2; ++k) {
+        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_box[k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp, cols,
+                                          ldp, box_rows, box_cols),
+                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field halo box");
+        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_tile[k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp, cols,
+                                          ldp, Sh::TZ, Sh::TX),
+                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field tile box");
+    }
+    SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_v, S.vdt2.get(), TmaType<T>::kType, sizeof(T), ldp, cols, ldp,
+                                      Sh::TZ, Sh::TX),
+                 SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for (v dt)^2");
+    d.field[0] = S.P[0].template as<T>() + S.origin;
+    d.field[1] = S.P[1].template as<T>() + S.origin;
+    d.zb = S.zb.template as<T>();
+    d.zbm1 = S.zbm1.template as<T>();
+    d.zphi[0] = S.zphi[0].template as<M>();
+    d.zphi[1] = S.zphi[1].template as<M>();
+    d.zpsi = S.zpsi.template as<M>();
+    d.xb = S.xb.template as<T>();
+    d.xbm1 = S.xbm1.template as<T>();
+    d.xphi[0] = S.xphi[0].template as<M>();
+    d.xphi[1] = S.xphi[1].template as<M>();
+    d.xpsi = S.xpsi.template as<M>();
+    d.ldp = ldp;
+    d.nz = (int)nz;
+    d.nx = (int)nx;
+    d.nB = nB;
+    d.ntz = (int)((nz + Sh::TZ - 1) / Sh::TZ);
+    d.ntx = (int)((nx + Sh::TX - 1) / Sh::TX);
+    d.oz = (int)oz;
+    d.t_start = t_start;
+    d.nt = nt;
+    d.reverse = reverse ? 1 : 0;
+    d.stride = 1;
+    const int k = (int)shots_.size() - 1;
+    reset_shot(k);
+    return k;
+}
+
+template <typename T>
+void Batch2d<T>::set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet) {
+    SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "at most %d point sources (got %d)",
+                 kMaxPointSources, nsrc);
+    ShotTail<T>& d = shots_[k].desc.s;
+    d.nsrc = nsrc;
+    for (int s = 0; s < nsrc; ++s) {
+        SSSI_REQUIRE(iz[s] >= 0 && iz[s] < d.nz && ix[s] >= 0 && ix[s] < d.nx, SSSI_ERR_ARG,
+                     "point source %d at (%lld, %lld) outside the %d x %d model", s, (long long)iz[s],
+                     (long long)ix[s], d.nz, d.nx);
+        d.src_iz[s] = (int)iz[s];
+        d.src_ix[s] = (int)ix[s];
+    }
+    d.src_wavelet = nsrc ? d_wavelet : nullptr;
+}
+
+template <typename T>
+void Batch2d<T>::reset_shot(int k) {
+    Shot& S = shots_[k];
+    for (auto& b : S.P) b.zero(stream_);
+    for (auto* b : {&S.zphi[0], &S.zphi[1], &S.zpsi, &S.xphi[0], &S.xphi[1], &S.xpsi}) b->zero(stream_);
+}
+
+template <typename T>
+void Batch2d<T>::finalize() {
+    using Sh = TileShape<T>;
+    // tiles of the enabled shots with an estimated cost: tiles whose stencil
+    // reaches a damped band run the two-stage form in part of their threads
+    struct Item {
+        int shot, local;
+        float cost;
+    };
+    std::vector<Item> items;
+    for (int k = 0; k < (int)shots_.size(); ++k) {
+        if (!shots_[k].enabled) continue;
+        const ShotTail<T>& d = shots_[k].desc.s;
+        for (int q = 0; q < d.ntz * d.ntx; ++q) {
+            const int z0 = (q % d.ntz) * Sh::TZ, x0 = (q / d.ntz) * Sh::TX;
+            const bool interior = d.nB == 0 || (z0 + Sh::TZ + N_ - 1 <= d.nz - d.nB && x0 - N_ >= d.nB &&
+                                                x0 + Sh::TX + N_ - 1 <= d.nx - d.nB);
+            items.push_back({k, q, interior ? 1.0f : 2.5f});
+        }
+    }
+    ntiles_ = (int)items.size();
+    grid_ = std::max(1, std::min(ntiles_, sms_ * ctas_per_sm_));
+    // longest processing time first onto the least loaded CTA
+    std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
+    std::vector<float> load(grid_, 0.0f);
+    std::vector<std::vector<int2>> lists(grid_);
+    {
+        using P = std::pair<float, int>;
+        std::priority_queue<P, std::vector<P>, std::greater<P>> heap;
+        for (int c = 0; c < grid_; ++c) heap.push({0.0f, c});
+        for (const Item& it : items) {
+            P top = heap.top();
+            heap.pop();
+            lists[top.second].push_back(make_int2(it.shot, it.local));
+            top.first += it.cost;
+            heap.push(top);
+        }
+    }
+    std::vector<int> begin(grid_ + 1, 0);
+    std::vector<int2> work;
+    work.reserve(items.size());
+    for (int c = 0; c < grid_; ++c) {
+        begin[c] = (int)work.size();
+        work.insert(work.end(), lists[c].begin(), lists[c].end());
+    }
+    begin[grid_] = (int)work.size();
+
+    const size_t nd = std::max<size_t>(shots_.size(), 1);
+    if (d_desc_.bytes() < nd * sizeof(ShotDesc<T>)) d_desc_.allocate(nd * sizeof(ShotDesc<T>));
+    for (int k = 0; k < (int)shots_.size(); ++k) sync_desc(k);
+    if (d_cta_begin_.bytes() < sizeof(int) * begin.size()) d_cta_begin_.allocate(sizeof(int) * begin.size());
+    if (d_work_.bytes() < sizeof(int2) * std::max<size_t>(work.size(), 1))
+        d_work_.allocate(sizeof(int2) * std::max<size_t>(work.size(), 1));
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(d_cta_begin_.get(), begin.data(), sizeof(int) * begin.size(),
+                                    cudaMemcpyHostToDevice, stream_));
+    if (!work.empty())
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_work_.get(), work.data(), sizeof(int2) * work.size(),
+                                        cudaMemcpyHostToDevice, stream_));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    bc_.nshots = (int)shots_.size();
+    bc_.ntiles = ntiles_;
+    bc_.cta_begin = d_cta_begin_.template as<int>();
+    bc_.work = d_work_.template as<int2>();
+}
+
+template <typename T>
+void Batch2d<T>::sync_desc(int k) {
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.template as<ShotDesc<T>>() + k, &shots_[k].desc, sizeof(ShotDesc<T>),
+                                    cudaMemcpyHostToDevice, stream_));
+}
+
+template <typename T>
+void Batch2d<T>::set_step(int step) {
+    step_ = step;
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(bc_.step, &step_, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+}
+
+template <typename T>
+void Batch2d<T>::run(int nsteps) {
+    for (int q = 0; q < nsteps; ++q) launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc_, grid_, stream_);
+    step_ += nsteps;
+}
+
+template <typename T>
+const T* Batch2d<T>::current_field(int k) const {
+    const ShotTail<T>& d = shots_[k].desc.s;
+    int done = step_ - d.t_start;
+    done = std::max(0, std::min(done, d.nt));
+    return d.field[done & 1];
+}
+
+template <typename T>
+void Batch2d<T>::check_errors() {
+    int h = 0;
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(&h, bc_.err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    SSSI_REQUIRE(h == 0, SSSI_ERR_INTERNAL, "a tile copy did not arrive within the wait limit (kernel aborted)");
+}
+
+template <typename T>
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
+    switch (N) {
+        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, stream); break;
+        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, stream); break;
+        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, stream); break;
+        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, stream); break;
+        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, stream); break;
+        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, stream); break;
+        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, stream); break;
+        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, stream); break;
+        default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
+    }
+}
+
+template <typename T>
+int batch2d_ctas_per_sm(int N) {
+    switch (N) {
+        case 1: return batch2d_occupancy_n<T, 1>();
+        case 2: return batch2d_occupancy_n<T, 2>();
+        case 3: return batch2d_occupancy_n<T, 3>();
+        case 4: return batch2d_occupancy_n<T, 4>();
+        case 5: return batch2d_occupancy_n<T, 5>();
+        case 6: return batch2d_occupancy_n<T, 6>();
+        case 7: return batch2d_occupancy_n<T, 7>();
+        default: return batch2d_occupancy_n<T, 8>();
+    }
+}
+
+template class Batch2d<float>;
+template class Batch2d<double>;
+
+}  // namespace sssi

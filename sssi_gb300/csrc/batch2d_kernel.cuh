@@ -1,0 +1,593 @@
+// Kernel body of the batched 2D CPML step (included by the per-type,
+// per-order translation units batch2d_{f32,f64}_{a,b}.cu).
+//
+// Tile loop of one persistent CTA (see tile2d.cuh for the numerics):
+//   iteration k computes the CTA's k-th work item from pipeline stage k&1
+//   while the TMA copies of item k+1 land in the other stage.  Warp 0 prepares
+//   an item: it stores the shot's ShotTail (prefetched into registers one
+//   iteration earlier) in the stage's shared slot, works out the shot's local
+//   step and time index, and (lane 0) issues the three box copies.  Items of
+//   shots that are not active at this batch step are skipped without copies.
+#pragma once
+
+#include "batch2d.cuh"
+
+namespace sssi {
+namespace batch {
+
+template <typename T>
+struct V4 {
+    T v[4];
+};
+
+__device__ __forceinline__ V4<float> ld4(const float* p) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    return {{q.x, q.y, q.z, q.w}};
+}
+__device__ __forceinline__ V4<double> ld4(const double* p) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    return {{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void st4(float* p, const float* v) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double* v) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+// ---- CPML memory variables ----
+// FP64: phi <- b phi + (b-1) d.
+__device__ __forceinline__ double mem_new(double b, double bm1, double m, double d) { return fma(b, m, bm1 * d); }
+__device__ __forceinline__ double mem_add(double d, double m) { return d + m; }
+// FP32, compensated: phi = hi + lo carried through the update with error-free
+// products (fma residuals) and a two-sum; rounded operations use intrinsics so
+// the compiler cannot fuse them.
+__device__ __forceinline__ float2 mem_new(float b, float bm1, float2 m, float d) {
+    const float p1 = __fmul_rn(b, m.x);
+    const float e1 = fmaf(b, m.x, -p1);
+    const float p2 = __fmul_rn(bm1, d);
+    const float e2 = fmaf(bm1, d, -p2);
+    const float s = __fadd_rn(p1, p2);
+    const float bb = __fsub_rn(s, p1);
+    const float e3 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, bb)), __fsub_rn(p2, bb));
+    float lo = fmaf(b, m.y, __fadd_rn(__fadd_rn(e1, e2), e3));
+    const float hi = __fadd_rn(s, lo);
+    lo = __fsub_rn(lo, __fsub_rn(hi, s));
+    return make_float2(hi, lo);
+}
+__device__ __forceinline__ float mem_add(float d, float2 m) { return (d + m.x) + m.y; }
+
+// Compensated running sum (hi, lo) += x: two-sum of hi and x, error kept in lo.
+__device__ __forceinline__ float2 comp_add(float2 acc, float x) {
+    const float s = __fadd_rn(acc.x, x);
+    const float bb = __fsub_rn(s, acc.x);
+    const float e = __fadd_rn(__fsub_rn(acc.x, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    return make_float2(s, __fadd_rn(acc.y, e));
+}
+
+__device__ __forceinline__ float f32(float x) { return x; }
+__device__ __forceinline__ float f32(double x) { return static_cast<float>(x); }
+
+// Per-tile facts shared by the block (written by warp 0 with the ShotTail).
+struct TileInfo {
+    int tile;   // batch tile index (>= ntiles: the CTA has no more tiles)
+    int shot;   // -1: nothing to do (no tile, or the shot is inactive)
+    int local;  // tile index within the shot
+    int tloc;   // local step of the shot
+    int tau;    // time index of the step
+    int pad[3];
+};
+
+template <typename T, int RX>
+struct Blk {
+    T v[RX][4];
+};
+
+// ---- band paths (two-stage form with the CPML memory variables) ----
+// Out of line: only threads whose stencil reaches a damped band call them, and
+// keeping them out of the hot path keeps the kernel's code in the instruction
+// cache.
+
+// z: 4 rows i0..i0+3 of column j from the window col[0 .. 4+2HZ) (rows i0-HZ ..).
+template <typename T, int N>
+__device__ __noinline__ V4<T> z_band(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, int i0, int j,
+                                     const T* col) {
+    using M = typename MemVar<T>::type;
+    constexpr int L = 2 * N - 1;
+    constexpr int HZ = tile_halo_rows(N);
+    const int nz = sh.nz, nB = sh.nB, zb0 = nz - nB;
+    const bool jok = j < sh.nx;
+    const M* phi_in = sh.zphi[ph];
+    M* phi_out = sh.zphi[ph ^ 1];
+    T za[4 + L];  // zA at rows i0-N .. i0+3+N-1
+#pragma unroll 1
+    for (int e = 0; e < 4 + L; ++e) {
+        const int op = e - N;
+        T d = bc.wz[0] * (col[HZ + op + 1] - col[HZ + op]);
+#pragma unroll
+        for (int n = 1; n < N; ++n) d = fma(bc.wz[n], col[HZ + op + 1 + n] - col[HZ + op - n], d);
+        const int ip = i0 + op;
+        T a = d;
+        if (jok && ip >= zb0 && ip < nz && ip >= 0) {
+            const int64_t q = (ip - zb0) + (int64_t)j * nB;
+            const M phi = mem_new(sh.zb[q], sh.zbm1[q], phi_in[q], d);
+            if (op >= 0 && op < 4) phi_out[q] = phi;
+            a = mem_add(d, phi);
+        }
+        za[e] = a;
+    }
+    V4<T> out;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        T d = bc.wz[0] * (za[o + N] - za[o + N - 1]);
+#pragma unroll
+        for (int k = 1; k < N; ++k) d = fma(bc.wz[k], za[o + N + k] - za[o + N - 1 - k], d);
+        const int i = i0 + o;
+        if (jok && i >= zb0 && i < nz) {
+            const int64_t q = (i - zb0) + (int64_t)j * nB;
+            const M psi = mem_new(sh.zb[q], sh.zbm1[q], sh.zpsi[q], d);
+            sh.zpsi[q] = psi;
+            d = mem_add(d, psi);
+        }
+        out.v[o] = d;
+    }
+    return out;
+}
+
+// x: rows i0..i0+3, columns j0..j0+RX-1, from the row vectors at rowp + c*SP.
+template <typename T, int N, int RX, int SP>
+__device__ __noinline__ Blk<T, RX> x_band(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, int i0, int j0,
+                                          const T* rowp) {
+    using M = typename MemVar<T>::type;
+    constexpr int L = 2 * N - 1;
+    const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
+    const M* phi_in = sh.xphi[ph];
+    M* phi_out = sh.xphi[ph ^ 1];
+    Blk<T, RX> lx;
+#pragma unroll
+    for (int c = 0; c < RX; ++c)
+#pragma unroll
+        for (int o = 0; o < 4; ++o) lx.v[c][o] = T(0);
+    // xA columns e = -N .. RX+N-2 (relative to j0), each from P columns e-N+1 .. e+N
+#pragma unroll 1
+    for (int e = -N; e <= RX + N - 2; ++e) {
+        const int jc = j0 + e;
+        T xa[4];
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            // P column e+1+n sits at smem column index (e + 1 + n) + L relative to rowp
+            T d = bc.wx[0] * (rowp[(e + 1 + L) * SP + o] - rowp[(e + L) * SP + o]);
+#pragma unroll
+            for (int n = 1; n < N; ++n)
+                d = fma(bc.wx[n], rowp[(e + 1 + n + L) * SP + o] - rowp[(e - n + L) * SP + o], d);
+            xa[o] = d;
+        }
+        if (jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB)) {
+            const int cb = jc < nB ? jc : nB + jc - (nx - nB);
+            const bool own = e >= 0 && e < RX;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int i = i0 + o;
+                if (i < nz) {
+                    const int64_t qq = i + (int64_t)cb * nz;
+                    const M phi = mem_new(sh.xb[qq], sh.xbm1[qq], phi_in[qq], xa[o]);
+                    if (own) phi_out[qq] = phi;
+                    xa[o] = mem_add(xa[o], phi);
+                }
+            }
+        }
+        // D- at output c: sum_k w_k (xA(c+k) - xA(c-1-k))
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const int cp = e - k, cm = e + 1 + k;
+#pragma unroll
+            for (int c = 0; c < RX; ++c) {
+                if (c == cp) {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(bc.wx[k], xa[o], lx.v[c][o]);
+                }
+                if (c == cm) {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(-bc.wx[k], xa[o], lx.v[c][o]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < RX; ++c) {
+        const int j = j0 + c;
+        if (j < nx && (j < nB || j >= nx - nB)) {
+            const int cb = j < nB ? j : nB + j - (nx - nB);
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int i = i0 + o;
+                if (i < nz) {
+                    const int64_t qq = i + (int64_t)cb * nz;
+                    const M psi = mem_new(sh.xb[qq], sh.xbm1[qq], sh.xpsi[qq], lx.v[c][o]);
+                    sh.xpsi[qq] = psi;
+                    lx.v[c][o] = mem_add(lx.v[c][o], psi);
+                }
+            }
+        }
+    }
+    return lx;
+}
+
+// Optional per-step outputs other than the receiver row (dense snapshots, the
+// RTM FP16 pack and max, the imaging sums).  Out of line for the same reason.
+template <typename T, int RX>
+__device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileInfo& ti, int i0, int j0,
+                                              Blk<T, RX> pn, Blk<T, RX> pc) {
+    const int nz = sh.nz, nx = sh.nx, tau = ti.tau;
+    const int64_t ncell = (int64_t)nz * nx;
+    const int nrow = min(4, nz - i0);
+    const int ncol = min(RX, nx - j0);
+    unsigned amax_bits = 0u;
+    if (sh.snap) {
+        T* snap = sh.snap + (int64_t)(tau - sh.snap_t0) * ncell;
+        for (int c = 0; c < ncol; ++c)
+            for (int o = 0; o < nrow; ++o) snap[(i0 + o) + (int64_t)(j0 + c) * nz] = pn.v[c][o];
+    }
+    const int stride = sh.stride > 0 ? sh.stride : 1;
+    if (sh.pack && tau >= 1 && (tau - 1) % stride == 0) {
+        const int k = (tau - 1) / stride;
+        const float scale = fp16_scale_from_amax(sh.amax[k]);
+        __half* pack = sh.pack + (int64_t)k * ncell;
+        for (int c = 0; c < ncol; ++c)
+            for (int o = 0; o < nrow; ++o)
+                pack[(i0 + o) + (int64_t)(j0 + c) * nz] = __float2half_rn(f32(pc.v[c][o]) * scale);
+        if (ti.local == 0 && i0 == 0 && j0 == 0) sh.inv_scale[k] = 1.0f / scale;
+    }
+    if (sh.amax && tau % stride == 0) {
+        for (int c = 0; c < ncol; ++c)
+            for (int o = 0; o < nrow; ++o) amax_bits = max(amax_bits, __float_as_uint(fabsf(f32(pn.v[c][o]))));
+    }
+    if constexpr (std::is_same<T, double>::value) {
+        if (sh.img_f64) {
+            const double* f64 = sh.img_f64 + (int64_t)tau * ncell;
+            for (int c = 0; c < ncol; ++c)
+                for (int o = 0; o < nrow; ++o) {
+                    const int64_t q = (i0 + o) + (int64_t)(j0 + c) * nz;
+                    const double f = f64[q];
+                    sh.img_m[q] = fma(f, pn.v[c][o], sh.img_m[q]);
+                    sh.img_s2[q] = fma(f, f, sh.img_s2[q]);
+                }
+        }
+    }
+    if (sh.img_f16 && tau % stride == 0) {
+        const int k = tau / stride;
+        const __half* f16 = sh.img_f16 + (int64_t)k * ncell;
+        const float inv = sh.img_inv[k];
+        for (int c = 0; c < ncol; ++c)
+            for (int o = 0; o < nrow; ++o) {
+                const int64_t q = (i0 + o) + (int64_t)(j0 + c) * nz;
+                const float f = __half2float(f16[q]) * inv;
+                const float r = f32(pn.v[c][o]);
+                sh.img_m2[q] = comp_add(sh.img_m2[q], __fmul_rn(f, r));
+                sh.img_s22[q] = comp_add(sh.img_s22[q], __fmul_rn(f, f));
+            }
+    }
+    return amax_bits;
+}
+
+// All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  zc / xc: the
+// thread's z / x stencil stays clear of the damped bands (composed form).
+template <typename T, int N>
+__device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
+                                           const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
+                                           bool zc, bool xc, unsigned& amax_bits) {
+    using S = TileShape<T>;
+    constexpr int TZ = S::TZ, RX = S::RX;
+    constexpr int L = 2 * N - 1;
+    constexpr int HZ = tile_halo_rows(N);
+    constexpr int SP = TZ + 2 * HZ;  // pitch of a P-box column
+    constexpr int WIN = 4 + 2 * HZ;  // z window of one column
+    const int nz = sh.nz, nx = sh.nx;
+    const int i0 = z0 + r0, j0 = x0 + c0;
+    const int ph = ti.tloc & 1;
+
+    Blk<T, RX> lz, lx, pc;
+
+    // ---------------- z ----------------
+#pragma unroll
+    for (int c = 0; c < RX; ++c) {
+        const T* col = Pb + (c0 + c + L) * SP + r0;
+        if (zc) {
+            T w[WIN];
+#pragma unroll
+            for (int q = 0; q < WIN / 4; ++q) {
+                const V4<T> v = ld4(col + 4 * q);
+                w[4 * q] = v.v[0];
+                w[4 * q + 1] = v.v[1];
+                w[4 * q + 2] = v.v[2];
+                w[4 * q + 3] = v.v[3];
+            }
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                pc.v[c][o] = w[HZ + o];
+                T acc = bc.az[0] * w[HZ + o];
+#pragma unroll
+                for (int m = 1; m <= L; ++m) acc = fma(bc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
+                lz.v[c][o] = acc;
+            }
+        } else {
+            const V4<T> cen = ld4(col + HZ);
+            const V4<T> z = z_band<T, N>(bc, sh, ph, i0, j0 + c, col);
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                pc.v[c][o] = cen.v[o];
+                lz.v[c][o] = z.v[o];
+            }
+        }
+    }
+
+    // ---------------- x ----------------
+    const T* rowp = Pb + r0 + HZ;  // the thread's 4 rows; column offset added below
+    if (xc) {
+#pragma unroll
+        for (int c = 0; c < RX; ++c)
+#pragma unroll
+            for (int o = 0; o < 4; ++o) lx.v[c][o] = T(0);
+#pragma unroll
+        for (int q = 0; q < RX + 2 * L; ++q) {
+            const V4<T> v = ld4(rowp + (c0 + q) * SP);
+#pragma unroll
+            for (int c = 0; c < RX; ++c) {
+                const int m = q - L - c;  // offset of column q from output column c
+                if (m >= -L && m <= L) {
+                    const T a = bc.ax[m < 0 ? -m : m];
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(a, v.v[o], lx.v[c][o]);
+                }
+            }
+        }
+    } else {
+        lx = x_band<T, N, RX, SP>(bc, sh, ph, i0, j0, rowp + c0 * SP);
+    }
+
+    // ---------------- update ----------------
+    const int tau = ti.tau;
+    const int64_t ncell = (int64_t)nz * nx;
+    const T* src_dense = sh.src_dense ? sh.src_dense + (int64_t)(tau - sh.dense_t0) * ncell : nullptr;
+    const T* src_row = (sh.src_row && i0 == 0) ? sh.src_row + (int64_t)tau * nx : nullptr;
+    bool has_point = false;
+    for (int s = 0; s < sh.nsrc; ++s)
+        has_point |= sh.src_iz[s] >= i0 && sh.src_iz[s] < i0 + 4 && sh.src_ix[s] >= j0 && sh.src_ix[s] < j0 + RX;
+    const bool full_rows = i0 + 3 < nz;
+    T* const Pnew = sh.field[ph ^ 1];
+    Blk<T, RX> pn;
+#pragma unroll
+    for (int c = 0; c < RX; ++c) {
+        const int j = j0 + c;
+        if (j >= nx) continue;
+        const V4<T> po = ld4(Ob + (c0 + c) * TZ + r0);
+        const V4<T> vv = ld4(Vb + (c0 + c) * TZ + r0);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            const int i = i0 + o;
+            T sv = T(0);
+            if (src_dense && i < nz) sv = src_dense[i + (int64_t)j * nz];
+            if (src_row && o == 0) sv = src_row[j];
+            if (has_point) {
+                for (int s = 0; s < sh.nsrc; ++s)
+                    if (i == sh.src_iz[s] && j == sh.src_ix[s]) sv += sh.src_wavelet[(int64_t)s * sh.nt + tau];
+            }
+            const T lap = lz.v[c][o] + lx.v[c][o] + sv;
+            pn.v[c][o] = fma(vv.v[o], lap, fma(T(2), pc.v[c][o], -po.v[o]));
+        }
+        T* dst = Pnew + i0 + (int64_t)j * sh.ldp;
+        if (full_rows) {
+            st4(dst, pn.v[c]);
+        } else {
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (i0 + o < nz) dst[o] = pn.v[c][o];
+        }
+    }
+    if (sh.rec && i0 == 0) {
+        T* rec = sh.rec + (int64_t)tau * nx;
+        const int ncol = min(RX, nx - j0);
+        for (int c = 0; c < ncol; ++c) rec[j0 + c] = pn.v[c][0];
+    }
+    if (sh.snap || sh.pack || sh.amax || sh.img_f16 || (std::is_same<T, double>::value && sh.img_f64))
+        amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
+}
+
+// Shared-memory layout of one pipeline stage (byte offsets, 128-aligned).
+template <typename T, int N>
+struct StageLayout {
+    using S = TileShape<T>;
+    static constexpr int L = 2 * N - 1;
+    static constexpr int HZ = tile_halo_rows(N);
+    static constexpr int SP = S::TZ + 2 * HZ;
+    static constexpr unsigned kPBoxBytes = sizeof(T) * SP * (S::TX + 2 * L);
+    static constexpr unsigned kTileBytes = sizeof(T) * S::TZ * S::TX;
+    static constexpr unsigned kP = 0;
+    static constexpr unsigned kO = (kPBoxBytes + 127) / 128 * 128;
+    static constexpr unsigned kV = kO + (kTileBytes + 127) / 128 * 128;
+    static constexpr unsigned kTail = kV + (kTileBytes + 127) / 128 * 128;
+    static constexpr unsigned kInfo = kTail + (sizeof(ShotTail<T>) + 127) / 128 * 128;
+    static constexpr unsigned kStage = kInfo + 128;  // TileInfo (32 bytes) rounded up
+    static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;  // bytes the TMA copies deliver
+    static constexpr unsigned kSmem = 2 * kStage + 64;            // two stages + barriers
+};
+
+constexpr unsigned kWaitLimit = 1u << 24;
+
+template <typename T, int N>
+__global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBlocks)
+    batch2d_kernel(const ShotDesc<T>* __restrict__ shots, const __grid_constant__ BatchConst<T> bc) {
+    using S = TileShape<T>;
+    using G = StageLayout<T, N>;
+    constexpr int TZ = S::TZ, TX = S::TX, RX = S::RX;
+    constexpr int HZ = G::HZ, L = G::L;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * G::kStage);
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int step = *reinterpret_cast<volatile const int*>(bc.step);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    // Each CTA walks its own list of work items.  Warp 0 keeps the next item
+    // and its shot's ShotTail in registers (loaded one iteration ahead), so
+    // preparing a stage costs shared-memory stores and three TMA issues.
+    const int wbeg = bc.cta_begin[blockIdx.x], wend = bc.cta_begin[blockIdx.x + 1];
+    constexpr int kTailVec = (int)(sizeof(ShotTail<T>) / 16);
+    static_assert(kTailVec <= 32, "ShotTail must fit one 16-byte load per lane");
+    int2 item = make_int2(-1, 0);  // prefetched work item
+    uint4 tail_reg = make_uint4(0, 0, 0, 0);
+    auto fetch = [&](int w) {  // warp 0: load item w and its shot's tail into registers
+        item = w < wend ? bc.work[w] : make_int2(-1, 0);
+        if (item.x >= 0 && lane < kTailVec) tail_reg = reinterpret_cast<const uint4*>(&shots[item.x].s)[lane];
+    };
+    // warp 0: put the prefetched item into stage s (tile = its position in the list)
+    auto prepare = [&](int w, int s) {
+        unsigned char* st = smem + s * G::kStage;
+        TileInfo* info = reinterpret_cast<TileInfo*>(st + G::kInfo);
+        const int k = item.x;
+        if (k >= 0 && lane < kTailVec) reinterpret_cast<uint4*>(st + G::kTail)[lane] = tail_reg;
+        __syncwarp();
+        if (lane == 0) {
+            int shot = -1, tloc = 0, tau = 0;
+            const ShotTail<T>& g = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
+            if (k >= 0) {
+                tloc = step - g.t_start;
+                if (tloc >= 0 && tloc < g.nt) {
+                    shot = k;
+                    tau = g.reverse ? g.nt - 1 - tloc : tloc;
+                }
+            }
+            info->tile = w < wend ? w : bc.ntiles;
+            info->shot = shot;
+            info->local = item.y;
+            info->tloc = tloc;
+            info->tau = tau;
+            if (shot >= 0) {
+                const int z0 = (item.y % g.ntz) * TZ, x0 = (item.y / g.ntz) * TX;
+                const int cur = tloc & 1;
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(&bar[s], G::kTx);
+                tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], g.oz + z0 - HZ, x0);
+                tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], g.oz + z0, x0 + L);
+                tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], g.oz + z0, x0 + L);
+            }
+        }
+    };
+
+    const int r0 = 4 * (tid % (TZ / 4));
+    const int c0 = RX * (tid / (TZ / 4));
+    unsigned phase_bits = 0;  // completed uses of each stage's barrier (bit s = parity)
+
+    if (tid < 32) {
+        fetch(wbeg);
+        prepare(wbeg, 0);
+        fetch(wbeg + 1);
+    }
+    __syncthreads();
+    bool failed = false;
+    for (int k = 0;; ++k) {
+        const int s = k & 1;
+        const unsigned char* st = smem + s * G::kStage;
+        const TileInfo ti = *reinterpret_cast<const TileInfo*>(st + G::kInfo);
+        if (ti.tile >= bc.ntiles) break;
+        if (tid < 32) {
+            prepare(wbeg + k + 1, s ^ 1);
+            fetch(wbeg + k + 2);
+        }
+        if (ti.shot >= 0) {
+            const bool ok = mbar_wait_bounded(&bar[s], (phase_bits >> s) & 1u, kWaitLimit);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            phase_bits ^= 1u << s;
+            const ShotTail<T>& sh = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
+            const T* Pb = reinterpret_cast<const T*>(st + G::kP);
+            const T* Ob = reinterpret_cast<const T*>(st + G::kO);
+            const T* Vb = reinterpret_cast<const T*>(st + G::kV);
+            const int z0 = (ti.local % sh.ntz) * TZ, x0 = (ti.local / sh.ntz) * TX;
+            unsigned amax_bits = 0u;
+            const int i0 = z0 + r0, j0 = x0 + c0;
+            if (i0 < sh.nz && j0 < sh.nx) {
+                // composed stencil wherever this thread's stencil stays clear of
+                // the damped bands (decided per thread: only threads next to a
+                // band pay for the two-stage form)
+                const int nB = sh.nB;
+                const bool zc = nB == 0 || i0 + N + 3 <= sh.nz - nB;
+                const bool xc = nB == 0 || (j0 - N >= nB && j0 + RX + N - 2 < sh.nx - nB);
+                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, zc, xc, amax_bits);
+            }
+            if (sh.amax && ti.tau % (sh.stride > 0 ? sh.stride : 1) == 0) {
+                const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
+                if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
+            }
+        }
+        __syncthreads();  // stage s is refilled by the next iteration's prepare
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicExch(bc.err, 1);
+            // copies issued for either stage may still be in flight: wait for them (bounded)
+            for (int q = 0; q < 2; ++q) {
+                const TileInfo* info = reinterpret_cast<const TileInfo*>(smem + q * G::kStage + G::kInfo);
+                if (info->shot >= 0) mbar_wait_bounded(&bar[q], (phase_bits >> q) & 1u, kWaitLimit);
+            }
+        }
+        __syncthreads();
+    }
+    // The last CTA to finish advances the batch step and resets the schedule.
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(bc.done, 1) == (int)gridDim.x - 1) {
+            *bc.done = 0;
+            atomicAdd(bc.step, 1);
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace batch
+
+template <typename T, int N>
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
+    using G = batch::StageLayout<T, N>;
+    static bool configured = false;
+    if (!configured) {
+        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)G::kSmem));
+        configured = true;
+    }
+    batch::batch2d_kernel<T, N><<<grid, TileShape<T>::kThreads, G::kSmem, stream>>>(shots, bc);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+}
+
+template <typename T, int N>
+int batch2d_occupancy_n() {
+    const size_t smem = batch::StageLayout<T, N>::kSmem;
+    int n = 0;
+    cudaError_t e =
+        cudaFuncSetAttribute(batch::batch2d_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N>, TileShape<T>::kThreads,
+                                                          smem);
+    if (e != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n;
+}
+
+#define SSSI_BATCH2D_INSTANCE(T, N)                                                                           \
+    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, cudaStream_t);      \
+    template int batch2d_occupancy_n<T, N>();
+
+}  // namespace sssi
