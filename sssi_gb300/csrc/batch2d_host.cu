@@ -234,7 +234,8 @@ template <typename T>
 void Batch2d<T>::finalize() {
     using Sh = TileShape<T>;
     // tiles of the enabled shots with an estimated cost: tiles whose stencil
-    // reaches a damped band run the two-stage form in part of their threads
+    // reaches a damped band add a cooperative first-derivative pass and the
+    // memory-variable traffic
     struct Item {
         int shot, local;
         float cost;
@@ -247,7 +248,7 @@ void Batch2d<T>::finalize() {
             const int z0 = (q % d.ntz) * Sh::TZ, x0 = (q / d.ntz) * Sh::TX;
             const bool interior = d.nB == 0 || (z0 + Sh::TZ + N_ - 1 <= d.nz - d.nB && x0 - N_ >= d.nB &&
                                                 x0 + Sh::TX + N_ - 1 <= d.nx - d.nB);
-            items.push_back({k, q, interior ? 1.0f : 2.5f});
+            items.push_back({k, q, interior ? 1.0f : 2.0f});
         }
     }
     ntiles_ = (int)items.size();

@@ -85,134 +85,142 @@ struct Blk {
     T v[RX][4];
 };
 
-// ---- band paths (two-stage form with the CPML memory variables) ----
-// Out of line: only threads whose stencil reaches a damped band call them, and
-// keeping them out of the hot path keeps the kernel's code in the instruction
-// cache.
+template <typename T>
+__device__ __forceinline__ T ldg_t(const T* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ldg_t(const float2* p) { return __ldg(p); }
 
-// z: 4 rows i0..i0+3 of column j from the window col[0 .. 4+2HZ) (rows i0-HZ ..).
+// ---- band tiles (two-stage form with the CPML memory variables) ----
+// A tile whose stencil reaches a damped band in z (bz) or in x (bx) first
+// computes that direction's first derivative A = D+ P (+ phi inside the band)
+// once per cell, cooperatively, into shared memory: zA at rows z0-N ..
+// z0+TZ+N-2 of the tile's columns, xA at columns x0-N .. x0+TX+N-2 of its
+// rows.  The second derivative D- A (+ psi) then reads them back.  All global
+// operands of a batch are loaded before any memory variable is stored, so a
+// batch costs one round trip to L2.
 template <typename T, int N>
-__device__ __noinline__ V4<T> z_band(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, int i0, int j,
-                                     const T* col) {
+struct BandScratch {
+    static constexpr int TZ = TileShape<T>::TZ, TX = TileShape<T>::TX;
+    static constexpr int RZ = TZ + 2 * N - 1;    // zA rows
+    static constexpr int ZP = (RZ + 3) / 4 * 4;  // pitch of a zA column
+    static constexpr int CX = TX + 2 * N - 1;    // xA columns (pitch TZ)
+    static constexpr unsigned kX = (sizeof(T) * ZP * TX + 127) / 128 * 128;  // byte offset of xA
+    static constexpr unsigned kBytes = kX + (sizeof(T) * TZ * CX + 127) / 128 * 128;
+};
+
+// Stage one of a band tile, run by every thread of the block; the caller
+// synchronises the block before the scratch is read.
+template <typename T, int N>
+__device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
+                                         int x0, bool bz, bool bx, T* scratch) {
+    using S = TileShape<T>;
+    using B = BandScratch<T, N>;
     using M = typename MemVar<T>::type;
+    constexpr int TZ = S::TZ, TX = S::TX, NT = S::kThreads;
     constexpr int L = 2 * N - 1;
     constexpr int HZ = tile_halo_rows(N);
-    const int nz = sh.nz, nB = sh.nB, zb0 = nz - nB;
-    const bool jok = j < sh.nx;
-    const M* phi_in = sh.zphi[ph];
-    M* phi_out = sh.zphi[ph ^ 1];
-    T za[4 + L];  // zA at rows i0-N .. i0+3+N-1
-#pragma unroll 1
-    for (int e = 0; e < 4 + L; ++e) {
-        const int op = e - N;
-        T d = bc.wz[0] * (col[HZ + op + 1] - col[HZ + op]);
-#pragma unroll
-        for (int n = 1; n < N; ++n) d = fma(bc.wz[n], col[HZ + op + 1 + n] - col[HZ + op - n], d);
-        const int ip = i0 + op;
-        T a = d;
-        if (jok && ip >= zb0 && ip < nz && ip >= 0) {
-            const int64_t q = (ip - zb0) + (int64_t)j * nB;
-            const M phi = mem_new(sh.zb[q], sh.zbm1[q], phi_in[q], d);
-            if (op >= 0 && op < 4) phi_out[q] = phi;
-            a = mem_add(d, phi);
-        }
-        za[e] = a;
-    }
-    V4<T> out;
-#pragma unroll
-    for (int o = 0; o < 4; ++o) {
-        T d = bc.wz[0] * (za[o + N] - za[o + N - 1]);
-#pragma unroll
-        for (int k = 1; k < N; ++k) d = fma(bc.wz[k], za[o + N + k] - za[o + N - 1 - k], d);
-        const int i = i0 + o;
-        if (jok && i >= zb0 && i < nz) {
-            const int64_t q = (i - zb0) + (int64_t)j * nB;
-            const M psi = mem_new(sh.zb[q], sh.zbm1[q], sh.zpsi[q], d);
-            sh.zpsi[q] = psi;
-            d = mem_add(d, psi);
-        }
-        out.v[o] = d;
-    }
-    return out;
-}
-
-// x: rows i0..i0+3, columns j0..j0+RX-1, from the row vectors at rowp + c*SP.
-template <typename T, int N, int RX, int SP>
-__device__ __noinline__ Blk<T, RX> x_band(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, int i0, int j0,
-                                          const T* rowp) {
-    using M = typename MemVar<T>::type;
-    constexpr int L = 2 * N - 1;
+    constexpr int SP = TZ + 2 * HZ;
+    const int tid = threadIdx.x;
     const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
-    const M* phi_in = sh.xphi[ph];
-    M* phi_out = sh.xphi[ph ^ 1];
-    Blk<T, RX> lx;
+    if (bz) {
+        constexpr int CELLS = B::RZ * TX;
+        constexpr int MU = (CELLS + NT - 1) / NT;
+        const int zb0 = nz - nB;
+        const T* zb = sh.zb;
+        const T* zbm1 = sh.zbm1;
+        const M* phi_in = sh.zphi[ph];
+        M* phi_out = sh.zphi[ph ^ 1];
+        bool in[MU];
+        T b[MU], bm[MU];
+        M m[MU];
 #pragma unroll
-    for (int c = 0; c < RX; ++c)
-#pragma unroll
-        for (int o = 0; o < 4; ++o) lx.v[c][o] = T(0);
-    // xA columns e = -N .. RX+N-2 (relative to j0), each from P columns e-N+1 .. e+N
-#pragma unroll 1
-    for (int e = -N; e <= RX + N - 2; ++e) {
-        const int jc = j0 + e;
-        T xa[4];
-#pragma unroll
-        for (int o = 0; o < 4; ++o) {
-            // P column e+1+n sits at smem column index (e + 1 + n) + L relative to rowp
-            T d = bc.wx[0] * (rowp[(e + 1 + L) * SP + o] - rowp[(e + L) * SP + o]);
-#pragma unroll
-            for (int n = 1; n < N; ++n)
-                d = fma(bc.wx[n], rowp[(e + 1 + n + L) * SP + o] - rowp[(e - n + L) * SP + o], d);
-            xa[o] = d;
-        }
-        if (jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB)) {
-            const int cb = jc < nB ? jc : nB + jc - (nx - nB);
-            const bool own = e >= 0 && e < RX;
-#pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                const int i = i0 + o;
-                if (i < nz) {
-                    const int64_t qq = i + (int64_t)cb * nz;
-                    const M phi = mem_new(sh.xb[qq], sh.xbm1[qq], phi_in[qq], xa[o]);
-                    if (own) phi_out[qq] = phi;
-                    xa[o] = mem_add(xa[o], phi);
-                }
+        for (int u = 0; u < MU; ++u) {
+            const int idx = tid + u * NT;
+            const int r = idx % B::RZ, c = idx / B::RZ;
+            const int ip = z0 - N + r, j = x0 + c;
+            in[u] = idx < CELLS && j < nx && ip >= zb0 && ip < nz;
+            b[u] = T(0);
+            bm[u] = T(0);
+            m[u] = M{};
+            if (in[u]) {
+                const int64_t q = (ip - zb0) + (int64_t)j * nB;
+                b[u] = ldg_t(zb + q);
+                bm[u] = ldg_t(zbm1 + q);
+                m[u] = ldg_t(phi_in + q);
             }
         }
-        // D- at output c: sum_k w_k (xA(c+k) - xA(c-1-k))
+        T* zA = scratch;
 #pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const int cp = e - k, cm = e + 1 + k;
+        for (int u = 0; u < MU; ++u) {
+            const int idx = tid + u * NT;
+            if (idx < CELLS) {
+                const int r = idx % B::RZ, c = idx / B::RZ;
+                const T* col = Pb + (c + L) * SP + (r - N + HZ);  // P at row z0-N+r
+                T d = bc.wz[0] * (col[1] - col[0]);
 #pragma unroll
-            for (int c = 0; c < RX; ++c) {
-                if (c == cp) {
-#pragma unroll
-                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(bc.wx[k], xa[o], lx.v[c][o]);
+                for (int n = 1; n < N; ++n) d = fma(bc.wz[n], col[1 + n] - col[-n], d);
+                if (in[u]) {
+                    m[u] = mem_new(b[u], bm[u], m[u], d);
+                    d = mem_add(d, m[u]);
                 }
-                if (c == cm) {
-#pragma unroll
-                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(-bc.wx[k], xa[o], lx.v[c][o]);
-                }
+                zA[c * B::ZP + r] = d;
             }
+        }
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int idx = tid + u * NT;
+            const int r = idx % B::RZ, c = idx / B::RZ;
+            if (in[u] && r >= N && r < N + TZ) phi_out[(z0 - N + r - zb0) + (int64_t)(x0 + c) * nB] = m[u];
         }
     }
+    if (bx) {
+        constexpr int CELLS = TZ * B::CX;
+        constexpr int MU = (CELLS + NT - 1) / NT;
+        const T* xb = sh.xb;
+        const T* xbm1 = sh.xbm1;
+        const M* phi_in = sh.xphi[ph];
+        M* phi_out = sh.xphi[ph ^ 1];
+        int64_t qc[MU];
+        T b[MU], bm[MU];
+        M m[MU];
 #pragma unroll
-    for (int c = 0; c < RX; ++c) {
-        const int j = j0 + c;
-        if (j < nx && (j < nB || j >= nx - nB)) {
-            const int cb = j < nB ? j : nB + j - (nx - nB);
-#pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                const int i = i0 + o;
-                if (i < nz) {
-                    const int64_t qq = i + (int64_t)cb * nz;
-                    const M psi = mem_new(sh.xb[qq], sh.xbm1[qq], sh.xpsi[qq], lx.v[c][o]);
-                    sh.xpsi[qq] = psi;
-                    lx.v[c][o] = mem_add(lx.v[c][o], psi);
-                }
+        for (int u = 0; u < MU; ++u) {
+            const int idx = tid + u * NT;
+            const int r = idx % TZ, cx = idx / TZ;
+            const int i = z0 + r, jc = x0 - N + cx;
+            const bool band = jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+            qc[u] = (idx < CELLS && i < nz && band) ? i + (int64_t)(jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
+            b[u] = T(0);
+            bm[u] = T(0);
+            m[u] = M{};
+            if (qc[u] >= 0) {
+                b[u] = ldg_t(xb + qc[u]);
+                bm[u] = ldg_t(xbm1 + qc[u]);
+                m[u] = ldg_t(phi_in + qc[u]);
             }
         }
+        T* xA = scratch + B::kX / sizeof(T);
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int idx = tid + u * NT;
+            if (idx < CELLS) {
+                const int r = idx % TZ, cx = idx / TZ;
+                const T* row = Pb + (r + HZ) + (cx - N + L) * SP;  // P at column x0-N+cx
+                T d = bc.wx[0] * (row[SP] - row[0]);
+#pragma unroll
+                for (int n = 1; n < N; ++n) d = fma(bc.wx[n], row[(1 + n) * SP] - row[-n * SP], d);
+                if (qc[u] >= 0) {
+                    m[u] = mem_new(b[u], bm[u], m[u], d);
+                    d = mem_add(d, m[u]);
+                }
+                xA[cx * TZ + r] = d;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int cx = (tid + u * NT) / TZ;
+            if (qc[u] >= 0 && cx >= N && cx < N + TX) phi_out[qc[u]] = m[u];
+        }
     }
-    return lx;
 }
 
 // Optional per-step outputs other than the receiver row (dense snapshots, the
@@ -272,29 +280,32 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
     return amax_bits;
 }
 
-// All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  zc / xc: the
-// thread's z / x stencil stays clear of the damped bands (composed form).
+// All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  bz / bx: the
+// tile is a band tile in z / x, its first derivatives are in `scratch`;
+// otherwise the composed stencil is used in that direction.
 template <typename T, int N>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
-                                           bool zc, bool xc, unsigned& amax_bits) {
+                                           bool bz, bool bx, const T* scratch, unsigned& amax_bits) {
     using S = TileShape<T>;
+    using B = BandScratch<T, N>;
+    using M = typename MemVar<T>::type;
     constexpr int TZ = S::TZ, RX = S::RX;
     constexpr int L = 2 * N - 1;
     constexpr int HZ = tile_halo_rows(N);
     constexpr int SP = TZ + 2 * HZ;  // pitch of a P-box column
     constexpr int WIN = 4 + 2 * HZ;  // z window of one column
-    const int nz = sh.nz, nx = sh.nx;
+    const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
     const int i0 = z0 + r0, j0 = x0 + c0;
     const int ph = ti.tloc & 1;
 
     Blk<T, RX> lz, lx, pc;
 
     // ---------------- z ----------------
+    if (!bz) {
 #pragma unroll
-    for (int c = 0; c < RX; ++c) {
-        const T* col = Pb + (c0 + c + L) * SP + r0;
-        if (zc) {
+        for (int c = 0; c < RX; ++c) {
+            const T* col = Pb + (c0 + c + L) * SP + r0;
             T w[WIN];
 #pragma unroll
             for (int q = 0; q < WIN / 4; ++q) {
@@ -312,20 +323,69 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 for (int m = 1; m <= L; ++m) acc = fma(bc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
                 lz.v[c][o] = acc;
             }
-        } else {
-            const V4<T> cen = ld4(col + HZ);
-            const V4<T> z = z_band<T, N>(bc, sh, ph, i0, j0 + c, col);
+        }
+    } else {
+        // D- zA (+ psi): zA row r0+t of the scratch is global row i0-N+t
+        constexpr int ZW = (2 * N + 3 + 3) / 4;  // 4-vectors covering the 2N+3 rows used
+        const int zb0 = nz - nB;
+        const T* zb = sh.zb;
+        const T* zbm1 = sh.zbm1;
+        M* zpsi = sh.zpsi;
+        bool in[RX][4];
+        T pb[RX][4], pbm[RX][4];
+        M ps[RX][4];
+#pragma unroll
+        for (int c = 0; c < RX; ++c)
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int i = i0 + o, j = j0 + c;
+                in[c][o] = j < nx && i >= zb0 && i < nz;
+                pb[c][o] = T(0);
+                pbm[c][o] = T(0);
+                ps[c][o] = M{};
+                if (in[c][o]) {
+                    const int64_t q = (i - zb0) + (int64_t)j * nB;
+                    pb[c][o] = ldg_t(zb + q);
+                    pbm[c][o] = ldg_t(zbm1 + q);
+                    ps[c][o] = zpsi[q];
+                }
+            }
+#pragma unroll
+        for (int c = 0; c < RX; ++c) {
+            const V4<T> cen = ld4(Pb + (c0 + c + L) * SP + r0 + HZ);
+            const T* za = scratch + (c0 + c) * B::ZP + r0;
+            T w[4 * ZW];
+#pragma unroll
+            for (int q = 0; q < ZW; ++q) {
+                const V4<T> v = ld4(za + 4 * q);
+                w[4 * q] = v.v[0];
+                w[4 * q + 1] = v.v[1];
+                w[4 * q + 2] = v.v[2];
+                w[4 * q + 3] = v.v[3];
+            }
 #pragma unroll
             for (int o = 0; o < 4; ++o) {
                 pc.v[c][o] = cen.v[o];
-                lz.v[c][o] = z.v[o];
+                T d = bc.wz[0] * (w[o + N] - w[o + N - 1]);
+#pragma unroll
+                for (int k = 1; k < N; ++k) d = fma(bc.wz[k], w[o + N + k] - w[o + N - 1 - k], d);
+                if (in[c][o]) {
+                    ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
+                    d = mem_add(d, ps[c][o]);
+                }
+                lz.v[c][o] = d;
             }
         }
+#pragma unroll
+        for (int c = 0; c < RX; ++c)
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (in[c][o]) zpsi[(i0 + o - zb0) + (int64_t)(j0 + c) * nB] = ps[c][o];
     }
 
     // ---------------- x ----------------
-    const T* rowp = Pb + r0 + HZ;  // the thread's 4 rows; column offset added below
-    if (xc) {
+    if (!bx) {
+        const T* rowp = Pb + r0 + HZ;  // the thread's 4 rows; column offset added below
 #pragma unroll
         for (int c = 0; c < RX; ++c)
 #pragma unroll
@@ -344,7 +404,52 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
             }
         }
     } else {
-        lx = x_band<T, N, RX, SP>(bc, sh, ph, i0, j0, rowp + c0 * SP);
+        // D- xA (+ psi): xA column c0+t of the scratch is global column j0-N+t
+        const T* xb = sh.xb;
+        const T* xbm1 = sh.xbm1;
+        M* xpsi = sh.xpsi;
+        int64_t qo[RX];
+        T pb[RX][4], pbm[RX][4];
+        M ps[RX][4];
+#pragma unroll
+        for (int c = 0; c < RX; ++c) {
+            const int j = j0 + c;
+            qo[c] = (j < nx && (j < nB || j >= nx - nB)) ? (int64_t)(j < nB ? j : nB + j - (nx - nB)) * nz : -1;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                pb[c][o] = T(0);
+                pbm[c][o] = T(0);
+                ps[c][o] = M{};
+                if (qo[c] >= 0 && i0 + o < nz) {
+                    const int64_t q = qo[c] + i0 + o;
+                    pb[c][o] = ldg_t(xb + q);
+                    pbm[c][o] = ldg_t(xbm1 + q);
+                    ps[c][o] = xpsi[q];
+                }
+            }
+        }
+        const T* xa = scratch + B::kX / sizeof(T) + r0;
+        V4<T> a[RX + 2 * N - 1];
+#pragma unroll
+        for (int t = 0; t < RX + 2 * N - 1; ++t) a[t] = ld4(xa + (c0 + t) * TZ);
+#pragma unroll
+        for (int c = 0; c < RX; ++c)
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                T d = bc.wx[0] * (a[c + N].v[o] - a[c + N - 1].v[o]);
+#pragma unroll
+                for (int k = 1; k < N; ++k) d = fma(bc.wx[k], a[c + N + k].v[o] - a[c + N - 1 - k].v[o], d);
+                if (qo[c] >= 0 && i0 + o < nz) {
+                    ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
+                    d = mem_add(d, ps[c][o]);
+                }
+                lx.v[c][o] = d;
+            }
+#pragma unroll
+        for (int c = 0; c < RX; ++c)
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (qo[c] >= 0 && i0 + o < nz) xpsi[qo[c] + i0 + o] = ps[c][o];
     }
 
     // ---------------- update ----------------
@@ -411,7 +516,8 @@ struct StageLayout {
     static constexpr unsigned kInfo = kTail + (sizeof(ShotTail<T>) + 127) / 128 * 128;
     static constexpr unsigned kStage = kInfo + 128;  // TileInfo (32 bytes) rounded up
     static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;  // bytes the TMA copies deliver
-    static constexpr unsigned kSmem = 2 * kStage + 64;            // two stages + barriers
+    static constexpr unsigned kScratch = 2 * kStage + 128;         // two stages, barriers, band scratch
+    static constexpr unsigned kSmem = kScratch + BandScratch<T, N>::kBytes;
 };
 
 constexpr unsigned kWaitLimit = 1u << 24;
@@ -516,15 +622,16 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             const int z0 = (ti.local % sh.ntz) * TZ, x0 = (ti.local / sh.ntz) * TX;
             unsigned amax_bits = 0u;
             const int i0 = z0 + r0, j0 = x0 + c0;
-            if (i0 < sh.nz && j0 < sh.nx) {
-                // composed stencil wherever this thread's stencil stays clear of
-                // the damped bands (decided per thread: only threads next to a
-                // band pay for the two-stage form)
-                const int nB = sh.nB;
-                const bool zc = nB == 0 || i0 + N + 3 <= sh.nz - nB;
-                const bool xc = nB == 0 || (j0 - N >= nB && j0 + RX + N - 2 < sh.nx - nB);
-                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, zc, xc, amax_bits);
+            const int nB = sh.nB;
+            const bool bz = nB > 0 && z0 + TZ + N - 1 > sh.nz - nB;
+            const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= sh.nx - nB);
+            T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
+            if (bz || bx) {
+                band_stage1<T, N>(bc, sh, ti.tloc & 1, Pb, z0, x0, bz, bx, scratch);
+                __syncthreads();
             }
+            if (i0 < sh.nz && j0 < sh.nx)
+                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, bz, bx, scratch, amax_bits);
             if (sh.amax && ti.tau % (sh.stride > 0 ? sh.stride : 1) == 0) {
                 const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
                 if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
