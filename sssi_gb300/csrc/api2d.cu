@@ -693,6 +693,8 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
         r.img_m = M.as<double>();
         r.img_s2 = S2.as<double>();
     }
+    // only the shots active in a phase take part in its schedule
+    B.enable(kR, false);
     B.finalize();
     B.set_step(0);
 
@@ -708,6 +710,10 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_mark(s);
+    B.enable(kA, false);
+    B.enable(kB, false);
+    B.enable(kR, true);
+    B.finalize();
     B.run((int)nt);
     timing_mark(s);
 

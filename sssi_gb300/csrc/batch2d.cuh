@@ -4,9 +4,11 @@
 // CTA's tiles may belong to different shots.
 //
 // Per-shot state and per-step hooks live in a device-resident array of
-// ShotDesc.  The batch step counter also lives in device memory: every launch
-// reads it, and the last CTA to finish increments it, so a run of steps is a
-// sequence of identical launches (which a CUDA graph can replay).
+// ShotDesc.  A launch advances every active shot by one step; its batch step is
+// a device-resident base plus a per-launch offset, so a captured run of K steps
+// (offsets 0..K-1, then base += K) replays as a CUDA graph.  Consecutive steps
+// are launched with programmatic stream serialization: the next step's blocks
+// set up and fetch their work lists while the previous step drains.
 #pragma once
 
 #include "tile2d.cuh"
@@ -75,8 +77,8 @@ struct BatchConst {
     int ntiles;
     const int* cta_begin;  // gridDim.x + 1: each CTA's range in `work`
     const int2* work;      // (shot, tile within the shot), grouped by CTA
-    int* step;             // batch step counter
-    int* done;             // CTAs finished in this launch
+    const int* step_base;  // the launch computes batch step *step_base + step_offset
+    int step_offset;
     int* err;              // set when a TMA copy does not arrive in time
 };
 
@@ -102,9 +104,13 @@ class Batch2d {
     // Re-uploads the descriptor of shot k (after its hooks changed).
     void sync_desc(int k);
     void set_step(int step);
-    // Launches `nsteps` batch steps.
+    // Launches `nsteps` batch steps (whole runs of kGraphSteps as graph replays).
     void run(int nsteps);
     void check_errors();
+    ~Batch2d();
+    Batch2d(const Batch2d&) = delete;
+    Batch2d& operator=(const Batch2d&) = delete;
+    static constexpr int kGraphSteps = 32;
 
     const T* current_field(int k) const;  // field after the last completed step of shot k
     int64_t ldp(int k) const { return shots_[k].desc.s.ldp; }
@@ -124,11 +130,15 @@ class Batch2d {
     cudaStream_t stream_;
     BatchConst<T> bc_{};
     std::vector<Shot> shots_;
-    DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;
+    void launch_step(const int* base, int offset, cudaStream_t stream);
+    void drop_graph();
+    DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;  // d_ctr_: graph step base, zero, error flag
     int grid_ = 0, ntiles_ = 0, step_ = 0;
     int ctas_per_sm_ = 1, sms_ = 1;
+    cudaGraphExec_t graph_ = nullptr;
 };
 
+// Launches one batch step with the programmatic-serialization attribute.
 template <typename T, int N>
 void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream);
 template <typename T, int N>

@@ -81,6 +81,18 @@ void composed(const double* w, int N, double* a) {
         }
 }
 
+__global__ void store_int_kernel(int* p, int v) { *p = v; }
+__global__ void add_int_kernel(int* p, int v) { *p += v; }
+
+// A stream used only to record graphs (capture does not run anything); the
+// legacy default stream cannot be captured.
+cudaStream_t capture_stream() {
+    static cudaStream_t cs = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] { SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)); });
+    return cs;
+}
+
 }  // namespace
 
 template <typename T>
@@ -104,10 +116,10 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
         bc_.az[m] = m <= L_ ? static_cast<T>(az[m]) : T(0);
         bc_.ax[m] = m <= L_ ? static_cast<T>(ax[m]) : T(0);
     }
-    d_ctr_.allocate(4 * sizeof(int));  // step, done, err, spare
+    d_ctr_.allocate(4 * sizeof(int));  // graph step base, zero, error flag, spare
     d_ctr_.zero(stream);
-    bc_.step = d_ctr_.template as<int>();
-    bc_.done = d_ctr_.template as<int>() + 1;
+    bc_.step_base = d_ctr_.template as<int>() + 1;
+    bc_.step_offset = 0;
     bc_.err = d_ctr_.template as<int>() + 2;
     int dev = 0;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
@@ -231,7 +243,19 @@ void Batch2d<T>::reset_shot(int k) {
 }
 
 template <typename T>
+Batch2d<T>::~Batch2d() {
+    drop_graph();
+}
+
+template <typename T>
+void Batch2d<T>::drop_graph() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+}
+
+template <typename T>
 void Batch2d<T>::finalize() {
+    drop_graph();  // launch parameters change
     using Sh = TileShape<T>;
     // tiles of the enabled shots with an estimated cost: tiles whose stencil
     // reaches a damped band add a cooperative first-derivative pass and the
@@ -305,13 +329,56 @@ void Batch2d<T>::sync_desc(int k) {
 template <typename T>
 void Batch2d<T>::set_step(int step) {
     step_ = step;
-    SSSI_CHECK_CUDA(cudaMemcpyAsync(bc_.step, &step_, sizeof(int), cudaMemcpyHostToDevice, stream_));
-    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+}
+
+template <typename T>
+void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
+    BatchConst<T> bc = bc_;
+    bc.step_base = base;
+    bc.step_offset = offset;
+    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, stream);
 }
 
 template <typename T>
 void Batch2d<T>::run(int nsteps) {
-    for (int q = 0; q < nsteps; ++q) launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc_, grid_, stream_);
+    SSSI_REQUIRE(grid_ > 0, SSSI_ERR_INTERNAL, "Batch2d::run before finalize");
+    int q = 0;
+    if (nsteps >= kGraphSteps) {
+        int* base = d_ctr_.template as<int>();
+        if (!graph_) {
+            // steps base .. base+K-1, then base += K
+            static std::mutex capture_mutex;
+            std::lock_guard<std::mutex> lock(capture_mutex);
+            cudaStream_t cs = capture_stream();
+            cudaGraph_t g = nullptr;
+            SSSI_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            try {
+                for (int k = 0; k < kGraphSteps; ++k) launch_step(base, k, cs);
+                add_int_kernel<<<1, 1, 0, cs>>>(base, kGraphSteps);
+                e = cudaGetLastError();
+            } catch (...) {
+                cudaStreamEndCapture(cs, &g);  // leave the capture stream usable
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            count_launch(-kGraphSteps);  // recorded, not run
+            const cudaError_t ee = cudaStreamEndCapture(cs, &g);
+            if (e == cudaSuccess) e = ee;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&graph_, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) graph_ = nullptr;
+            SSSI_CHECK_CUDA(e);
+        }
+        store_int_kernel<<<1, 1, 0, stream_>>>(base, step_);
+        SSSI_CHECK_CUDA(cudaGetLastError());
+        count_launch();
+        for (; q + kGraphSteps <= nsteps; q += kGraphSteps) {
+            SSSI_CHECK_CUDA(cudaGraphLaunch(graph_, stream_));
+            count_launch(kGraphSteps + 1);
+        }
+    }
+    for (; q < nsteps; ++q) launch_step(bc_.step_base, step_ + q, stream_);
     step_ += nsteps;
 }
 

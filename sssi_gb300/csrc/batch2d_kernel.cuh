@@ -534,13 +534,16 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const int step = *reinterpret_cast<volatile const int*>(bc.step);
+    // The next step's grid may be scheduled once every block of this one runs;
+    // its blocks then wait (griddepcontrol.wait) for this grid to complete.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_barrier_init();
     }
     __syncthreads();
+    int step = 0;  // set once the previous step's grid has completed
 
     // Each CTA walks its own list of work items.  Warp 0 keeps the next item
     // and its shot's ShotTail in registers (loaded one iteration ahead), so
@@ -592,8 +595,11 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     const int c0 = RX * (tid / (TZ / 4));
     unsigned phase_bits = 0;  // completed uses of each stage's barrier (bit s = parity)
 
+    if (tid < 32) fetch(wbeg);  // work lists and descriptors are not written by kernels
+    // fields, memory variables and the step base are: wait for the previous grid
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    step = *reinterpret_cast<volatile const int*>(bc.step_base) + bc.step_offset;
     if (tid < 32) {
-        fetch(wbeg);
         prepare(wbeg, 0);
         fetch(wbeg + 1);
     }
@@ -650,15 +656,6 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
         }
         __syncthreads();
     }
-    // The last CTA to finish advances the batch step and resets the schedule.
-    if (tid == 0) {
-        __threadfence();
-        if (atomicAdd(bc.done, 1) == (int)gridDim.x - 1) {
-            *bc.done = 0;
-            atomicAdd(bc.step, 1);
-            __threadfence();
-        }
-    }
 }
 
 }  // namespace batch
@@ -672,9 +669,18 @@ void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int gri
                                              (int)G::kSmem));
         configured = true;
     }
-    batch::batch2d_kernel<T, N><<<grid, TileShape<T>::kThreads, G::kSmem, stream>>>(shots, bc);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(TileShape<T>::kThreads);
+    cfg.dynamicSmemBytes = G::kSmem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N>, shots, bc));
     count_launch();
-    SSSI_CHECK_CUDA(cudaGetLastError());
 }
 
 template <typename T, int N>
