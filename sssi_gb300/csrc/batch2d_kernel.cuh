@@ -516,7 +516,9 @@ struct StageLayout {
     static constexpr unsigned kInfo = kTail + (sizeof(ShotTail<T>) + 127) / 128 * 128;
     static constexpr unsigned kStage = kInfo + 128;  // TileInfo (32 bytes) rounded up
     static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;  // bytes the TMA copies deliver
-    static constexpr unsigned kScratch = 2 * kStage + 128;         // two stages, barriers, band scratch
+    static constexpr int kStages = 2;                             // tiles in the copy pipeline
+    static constexpr unsigned kBar = kStages * kStage;            // one mbarrier per stage
+    static constexpr unsigned kScratch = kBar + 128;              // band scratch
     static constexpr unsigned kSmem = kScratch + BandScratch<T, N>::kBytes;
 };
 
@@ -530,7 +532,8 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     constexpr int TZ = S::TZ, TX = S::TX, RX = S::RX;
     constexpr int HZ = G::HZ, L = G::L;
     extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * G::kStage);
+    constexpr int NS = G::kStages;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + G::kBar);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -538,8 +541,8 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     // its blocks then wait (griddepcontrol.wait) for this grid to complete.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+#pragma unroll
+        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -552,6 +555,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     constexpr int kTailVec = (int)(sizeof(ShotTail<T>) / 16);
     static_assert(kTailVec <= 32, "ShotTail must fit one 16-byte load per lane");
     int2 item = make_int2(-1, 0);  // prefetched work item
+    unsigned inflight = 0;          // lane 0 of warp 0: stages with copies not yet consumed
     uint4 tail_reg = make_uint4(0, 0, 0, 0);
     auto fetch = [&](int w) {  // warp 0: load item w and its shot's tail into registers
         item = w < wend ? bc.work[w] : make_int2(-1, 0);
@@ -582,6 +586,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             if (shot >= 0) {
                 const int z0 = (item.y % g.ntz) * TZ, x0 = (item.y / g.ntz) * TX;
                 const int cur = tloc & 1;
+                inflight |= 1u << s;
                 fence_proxy_async_shared();
                 mbar_arrive_expect_tx(&bar[s], G::kTx);
                 tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], g.oz + z0 - HZ, x0);
@@ -600,19 +605,22 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     asm volatile("griddepcontrol.wait;" ::: "memory");
     step = *reinterpret_cast<volatile const int*>(bc.step_base) + bc.step_offset;
     if (tid < 32) {
-        prepare(wbeg, 0);
-        fetch(wbeg + 1);
+        for (int q = 0; q < NS - 1; ++q) {  // the first NS-1 items go into stages 0 .. NS-2
+            prepare(wbeg + q, q);
+            fetch(wbeg + q + 1);
+        }
     }
     __syncthreads();
     bool failed = false;
     for (int k = 0;; ++k) {
-        const int s = k & 1;
+        const int s = k % NS;
         const unsigned char* st = smem + s * G::kStage;
         const TileInfo ti = *reinterpret_cast<const TileInfo*>(st + G::kInfo);
         if (ti.tile >= bc.ntiles) break;
         if (tid < 32) {
-            prepare(wbeg + k + 1, s ^ 1);
-            fetch(wbeg + k + 2);
+            // stage (k-1) % NS was released by the barrier that ended iteration k-1
+            prepare(wbeg + k + NS - 1, (k + NS - 1) % NS);
+            fetch(wbeg + k + NS);
         }
         if (ti.shot >= 0) {
             const bool ok = mbar_wait_bounded(&bar[s], (phase_bits >> s) & 1u, kWaitLimit);
@@ -621,6 +629,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 break;
             }
             phase_bits ^= 1u << s;
+            inflight &= ~(1u << s);
             const ShotTail<T>& sh = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
             const T* Pb = reinterpret_cast<const T*>(st + G::kP);
             const T* Ob = reinterpret_cast<const T*>(st + G::kO);
@@ -648,11 +657,9 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     if (failed) {
         if (tid == 0) {
             atomicExch(bc.err, 1);
-            // copies issued for either stage may still be in flight: wait for them (bounded)
-            for (int q = 0; q < 2; ++q) {
-                const TileInfo* info = reinterpret_cast<const TileInfo*>(smem + q * G::kStage + G::kInfo);
-                if (info->shot >= 0) mbar_wait_bounded(&bar[q], (phase_bits >> q) & 1u, kWaitLimit);
-            }
+            // copies issued for stages not yet consumed may still be in flight: wait for them (bounded)
+            for (int q = 0; q < NS; ++q)
+                if ((inflight >> q) & 1u) mbar_wait_bounded(&bar[q], (phase_bits >> q) & 1u, kWaitLimit);
         }
         __syncthreads();
     }
