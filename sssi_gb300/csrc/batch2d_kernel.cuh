@@ -72,13 +72,19 @@ __device__ __forceinline__ float f32(double x) { return static_cast<float>(x); }
 
 // Per-tile facts shared by the block (written by warp 0 with the ShotTail).
 struct TileInfo {
-    int tile;   // batch tile index (>= ntiles: the CTA has no more tiles)
-    int shot;   // -1: nothing to do (no tile, or the shot is inactive)
-    int local;  // tile index within the shot
-    int tloc;   // local step of the shot
-    int tau;    // time index of the step
-    int pad[3];
+    int tile;        // batch tile index (>= ntiles: the CTA has no more tiles)
+    int shot;        // -1: nothing to do (no tile, or the shot is inactive)
+    int local;       // tile index within the shot
+    int tloc;        // local step of the shot
+    int tau;         // time index of the step
+    int z0, x0;      // tile origin within the shot
+    unsigned flags;  // kBandZ | kBandX | kSource | kRare | kAmax
 };
+constexpr unsigned kBandZ = 1u;   // the z stencil of some cell reaches the damped band
+constexpr unsigned kBandX = 2u;   // the x stencil of some cell reaches a damped band
+constexpr unsigned kSource = 4u;  // something is injected into the tile at this step
+constexpr unsigned kRare = 8u;    // snapshot / FP16 pack / max / imaging output at this step
+constexpr unsigned kAmax = 16u;   // the step's max |field| is wanted
 
 template <typename T, int RX>
 struct Blk {
@@ -280,13 +286,32 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
     return amax_bits;
 }
 
-// All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  bz / bx: the
-// tile is a band tile in z / x, its first derivatives are in `scratch`;
+// Injected terms of column j, rows i0..i0+3, added to lap: a dense source
+// slice, the surface row (row 0), point sources.  Only tiles flagged kSource.
+template <typename T>
+__device__ __forceinline__ void add_sources(const ShotTail<T>& sh, int tau, int i0, int j, T* lap) {
+    const int nz = sh.nz, nx = sh.nx;
+    const T* src_dense = sh.src_dense ? sh.src_dense + (int64_t)(tau - sh.dense_t0) * ((int64_t)nz * nx) : nullptr;
+    const T* src_row = (sh.src_row && i0 == 0) ? sh.src_row + (int64_t)tau * nx : nullptr;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int i = i0 + o;
+        T sv = T(0);
+        if (src_dense && i < nz) sv = src_dense[i + (int64_t)j * nz];
+        if (src_row && o == 0) sv = src_row[j];
+        for (int s = 0; s < sh.nsrc; ++s)
+            if (i == sh.src_iz[s] && j == sh.src_ix[s]) sv += sh.src_wavelet[(int64_t)s * sh.nt + tau];
+        lap[o] += sv;
+    }
+}
+
+// All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  kBandZ / kBandX:
+// the tile is a band tile in z / x, its first derivatives are in `scratch`;
 // otherwise the composed stencil is used in that direction.
 template <typename T, int N>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
-                                           bool bz, bool bx, const T* scratch, unsigned& amax_bits) {
+                                           unsigned flags, const T* scratch, unsigned& amax_bits) {
     using S = TileShape<T>;
     using B = BandScratch<T, N>;
     using M = typename MemVar<T>::type;
@@ -298,6 +323,7 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
     const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
     const int i0 = z0 + r0, j0 = x0 + c0;
     const int ph = ti.tloc & 1;
+    const bool bz = flags & kBandZ, bx = flags & kBandX;
 
     Blk<T, RX> lz, lx, pc;
 
@@ -454,12 +480,6 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 
     // ---------------- update ----------------
     const int tau = ti.tau;
-    const int64_t ncell = (int64_t)nz * nx;
-    const T* src_dense = sh.src_dense ? sh.src_dense + (int64_t)(tau - sh.dense_t0) * ncell : nullptr;
-    const T* src_row = (sh.src_row && i0 == 0) ? sh.src_row + (int64_t)tau * nx : nullptr;
-    bool has_point = false;
-    for (int s = 0; s < sh.nsrc; ++s)
-        has_point |= sh.src_iz[s] >= i0 && sh.src_iz[s] < i0 + 4 && sh.src_ix[s] >= j0 && sh.src_ix[s] < j0 + RX;
     const bool full_rows = i0 + 3 < nz;
     T* const Pnew = sh.field[ph ^ 1];
     Blk<T, RX> pn;
@@ -469,19 +489,12 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         if (j >= nx) continue;
         const V4<T> po = ld4(Ob + (c0 + c) * TZ + r0);
         const V4<T> vv = ld4(Vb + (c0 + c) * TZ + r0);
+        T lap[4];
 #pragma unroll
-        for (int o = 0; o < 4; ++o) {
-            const int i = i0 + o;
-            T sv = T(0);
-            if (src_dense && i < nz) sv = src_dense[i + (int64_t)j * nz];
-            if (src_row && o == 0) sv = src_row[j];
-            if (has_point) {
-                for (int s = 0; s < sh.nsrc; ++s)
-                    if (i == sh.src_iz[s] && j == sh.src_ix[s]) sv += sh.src_wavelet[(int64_t)s * sh.nt + tau];
-            }
-            const T lap = lz.v[c][o] + lx.v[c][o] + sv;
-            pn.v[c][o] = fma(vv.v[o], lap, fma(T(2), pc.v[c][o], -po.v[o]));
-        }
+        for (int o = 0; o < 4; ++o) lap[o] = lz.v[c][o] + lx.v[c][o];
+        if (flags & kSource) add_sources<T>(sh, tau, i0, j, lap);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) pn.v[c][o] = fma(vv.v[o], lap[o], fma(T(2), pc.v[c][o], -po.v[o]));
         T* dst = Pnew + i0 + (int64_t)j * sh.ldp;
         if (full_rows) {
             st4(dst, pn.v[c]);
@@ -496,8 +509,29 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         const int ncol = min(RX, nx - j0);
         for (int c = 0; c < ncol; ++c) rec[j0 + c] = pn.v[c][0];
     }
-    if (sh.snap || sh.pack || sh.amax || sh.img_f16 || (std::is_same<T, double>::value && sh.img_f64))
-        amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
+    if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
+}
+
+// Per-tile work flags, worked out once by the preparing thread.
+template <typename T, int N>
+__device__ __forceinline__ unsigned tile_flags(const ShotTail<T>& g, int z0, int x0, int tau) {
+    constexpr int TZ = TileShape<T>::TZ, TX = TileShape<T>::TX;
+    unsigned f = 0u;
+    const int nB = g.nB;
+    if (nB > 0 && z0 + TZ + N - 1 > g.nz - nB) f |= kBandZ;
+    if (nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= g.nx - nB)) f |= kBandX;
+    bool src = g.src_dense != nullptr || (g.src_row != nullptr && z0 == 0);
+    for (int s = 0; s < g.nsrc; ++s)
+        src |= g.src_iz[s] >= z0 && g.src_iz[s] < z0 + TZ && g.src_ix[s] >= x0 && g.src_ix[s] < x0 + TX;
+    if (src) f |= kSource;
+    const int stride = g.stride > 0 ? g.stride : 1;
+    const bool on_stride = tau % stride == 0;
+    if (g.amax && on_stride) f |= kAmax;
+    bool rare = g.snap != nullptr || (g.pack != nullptr && tau >= 1 && (tau - 1) % stride == 0) ||
+                (g.amax != nullptr && on_stride) || (g.img_f16 != nullptr && on_stride);
+    if constexpr (std::is_same<T, double>::value) rare |= g.img_f64 != nullptr;
+    if (rare) f |= kRare;
+    return f;
 }
 
 // Shared-memory layout of one pipeline stage (byte offsets, 128-aligned).
@@ -585,6 +619,9 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             info->tau = tau;
             if (shot >= 0) {
                 const int z0 = (item.y % g.ntz) * TZ, x0 = (item.y / g.ntz) * TX;
+                info->z0 = z0;
+                info->x0 = x0;
+                info->flags = tile_flags<T, N>(g, z0, x0, tau);
                 const int cur = tloc & 1;
                 inflight |= 1u << s;
                 fence_proxy_async_shared();
@@ -634,20 +671,17 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             const T* Pb = reinterpret_cast<const T*>(st + G::kP);
             const T* Ob = reinterpret_cast<const T*>(st + G::kO);
             const T* Vb = reinterpret_cast<const T*>(st + G::kV);
-            const int z0 = (ti.local % sh.ntz) * TZ, x0 = (ti.local / sh.ntz) * TX;
+            const int z0 = ti.z0, x0 = ti.x0;
             unsigned amax_bits = 0u;
             const int i0 = z0 + r0, j0 = x0 + c0;
-            const int nB = sh.nB;
-            const bool bz = nB > 0 && z0 + TZ + N - 1 > sh.nz - nB;
-            const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= sh.nx - nB);
             T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
-            if (bz || bx) {
-                band_stage1<T, N>(bc, sh, ti.tloc & 1, Pb, z0, x0, bz, bx, scratch);
+            if (ti.flags & (kBandZ | kBandX)) {
+                band_stage1<T, N>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX, scratch);
                 __syncthreads();
             }
             if (i0 < sh.nz && j0 < sh.nx)
-                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, bz, bx, scratch, amax_bits);
-            if (sh.amax && ti.tau % (sh.stride > 0 ? sh.stride : 1) == 0) {
+                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+            if (ti.flags & kAmax) {
                 const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
                 if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
             }
