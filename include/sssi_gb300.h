@@ -113,6 +113,28 @@ int sssi_fwdTimeCpmlFor2dAwPoint(const double *v, int64_t nz, int64_t nx, int64_
                                   const int64_t *src_iz, const int64_t *src_ix, const double *wavelets,
                                   double *data, double *snapshot, int mode);
 
+/* 3D forward modelling: [data, snapshot] = fwdTimeCpmlFor3dAw(v, source,
+ * nDiffOrder, nBoundary, dz, dx, dy, dt) of src/fwdTimeCpmlFor3dAw.m:1-163
+ * (MATLAB only in the reference; this is the MEX it would call).
+ * v: nz x nx x ny; source: nz x nx x ny x nt (may be NULL: no source);
+ * data: nx x ny x nt, the top interior face after each step (NULL: not
+ * returned); snapshot: nz x nx x ny x nt (NULL: not returned).  Damping as
+ * that file computes it: profiles in cell units, x and z profiles from the
+ * y = 0 slice of v, y profiles from its top row (src/fwdTimeCpmlFor3dAw.m:45-70).
+ * SSSI_MODE_FP64_STRICT runs as SSSI_MODE_FP64 (there is no C reference to
+ * reproduce bit for bit). */
+int sssi_fwdTimeCpmlFor3dAw(const double *v, const double *source, int64_t nz, int64_t nx, int64_t ny,
+                            int64_t nt, int nDiffOrder, int nBoundary, double dz, double dx, double dy,
+                            double dt, double *data, double *snapshot, int mode);
+
+/* The same with nsrc (<= 8) point sources instead of the dense source volume:
+ * wavelets is nsrc x nt (row s at wavelets + s * nt); source s adds
+ * wavelets[s * nt + t] at interior cell (src_iz[s], src_ix[s], src_iy[s]) in step t. */
+int sssi_fwdTimeCpmlFor3dAwPoint(const double *v, int64_t nz, int64_t nx, int64_t ny, int64_t nt,
+                                 int nDiffOrder, int nBoundary, double dz, double dx, double dy, double dt,
+                                 int nsrc, const int64_t *src_iz, const int64_t *src_ix, const int64_t *src_iy,
+                                 const double *wavelets, double *data, double *snapshot, int mode);
+
 /* One reverse-time-migration shot, the work of
  * applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:156-166,252-275,315
  * done on the device: forward modelling of the point source in v (true

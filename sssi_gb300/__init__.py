@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     fwdTimeCpmlFor2dAw,
     fwdTimeCpmlFor2dAwPoint,
     fwdTimeCpmlFor3dAw,
+    fwdTimeCpmlFor3dAwPoint,
     launch_count,
     release_cache,
     rtmTimeCpmlFor2dAw,

@@ -38,6 +38,10 @@ SIGNATURES = {
     "sssi_fwdTimeCpmlFor3dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                 c_dp, c_dp, ctypes.c_int]),
+    "sssi_fwdTimeCpmlFor3dAwPoint": (ctypes.c_int, [c_dp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_int, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp,
+                                                     ctypes.c_int]),
     "sssi_fwdTimeCpmlFor2dAwPoint": (ctypes.c_int, [c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                      ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                      ctypes.c_int, c_dp, c_dp, c_dp, c_dp, c_dp, ctypes.c_int]),

@@ -165,6 +165,29 @@ def fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt, *, mode
     return data, snap
 
 
+def fwdTimeCpmlFor3dAwPoint(v, nt, src_iz, src_ix, src_iy, wavelets, nDiffOrder, nBoundary, dz, dx, dy, dt, *,
+                            mode="fp64", want_snapshot=False):
+    """3D forward modelling with point sources: source s at interior
+    (src_iz[s], src_ix[s], src_iy[s]) with amplitude wavelets[s, t].  Returns
+    (data nx x ny x nt, snapshot or None)."""
+    pv, kv, vshape = _in(v, "v")
+    if vshape is None or len(vshape) != 3:
+        raise ValueError("v must be nz x nx x ny")
+    nz, nx, ny = vshape
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    iy = np.ascontiguousarray(np.atleast_1d(src_iy), dtype=np.int64)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or len(ix) != len(iz) or len(iy) != len(iz):
+        raise ValueError("wavelets must be nsrc x nt and src_iz/src_ix/src_iy of length nsrc")
+    data, _ = _out_like(v, (nx, ny, nt))
+    snap, _ = _out_like(v, (nz, nx, ny, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeCpmlFor3dAwPoint(pv, nz, nx, ny, int(nt), int(nDiffOrder), int(nBoundary), float(dz),
+                                             float(dx), float(dy), float(dt), len(iz), iz.ctypes.data, ix.ctypes.data,
+                                             iy.ctypes.data, w.ctypes.data, _addr(data), _addr(snap), _mode(mode)))
+    return data, snap
+
+
 def rtmTimeCpmlFor2dAw(v, vs, wavelet, src_iz, src_ix, nDiffOrder, nBoundary, dz, dx, dt, *, epsilon=1e-3,
                        mode="fp64-strict", snap_stride=4, want_data=False):
     """One RTM shot: image = M./s2 of mainRtmTimeCpmlFor2dAw.m:268-275,315 for a

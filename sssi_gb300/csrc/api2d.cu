@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "api_util.cuh"
 #include "batch2d.cuh"
 #include "cpml2d.cuh"
 
@@ -11,43 +12,7 @@ namespace sssi {
 
 namespace {
 
-constexpr size_t kChunkBytes = size_t(256) << 20;  // host<->device streaming granularity
-
-std::vector<double> host_copy(const double* p, size_t n, cudaStream_t s) {
-    std::vector<double> h(n);
-    if (n == 0) return h;
-    if (is_device_pointer(p)) {
-        SSSI_CHECK_CUDA(cudaMemcpyAsync(h.data(), p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
-    } else {
-        std::memcpy(h.data(), p, n * sizeof(double));
-    }
-    return h;
-}
-
-// A device view of a caller array: the caller's pointer if it is device memory,
-// otherwise a cached device buffer (filled from the host when `upload`).
-struct DeviceView {
-    double* ptr = nullptr;
-    bool caller_device = false;
-    DeviceBuffer buf;
-    DeviceView(const double* p, size_t n, bool upload, cudaStream_t s) {
-        if (!p) return;
-        if (is_device_pointer(p)) {
-            ptr = const_cast<double*>(p);
-            caller_device = true;
-            return;
-        }
-        buf.allocate(std::max<size_t>(n, 1) * sizeof(double));
-        ptr = buf.as<double>();
-        if (upload && n)
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(ptr, p, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    }
-    void download(double* host, size_t n, cudaStream_t s) const {
-        if (!host || caller_device || n == 0) return;
-        SSSI_CHECK_CUDA(cudaMemcpyAsync(host, ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    }
-};
+using namespace api;
 
 // Launch shape for a grid: rows per block (a power of two <= 256) and the
 // number of columns each block marches over.
@@ -128,143 +93,12 @@ __global__ void image_finish_comp_kernel(const float2* m, const float2* s2, int6
     }
 }
 
-__global__ void fill_kernel(double* p, int64_t n, double v) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        p[q] = v;
-}
-
-void fill(double* p, int64_t n, double v, cudaStream_t s) {
-    fill_kernel<<<152 * 4, 256, 0, s>>>(p, n, v);
-    count_launch();
-    SSSI_CHECK_CUDA(cudaGetLastError());
-}
-
-// Elementwise conversion between the API's double arrays and a propagator's
-// element type (a no-op copy is never launched: callers skip T == double).
-template <typename From, typename To>
-__global__ void convert_kernel(const From* in, To* out, int64_t n) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        out[q] = static_cast<To>(in[q]);
-}
-
-template <typename From, typename To>
-void convert(const From* in, To* out, int64_t n, cudaStream_t s) {
-    if (n <= 0) return;
-    convert_kernel<From, To><<<152 * 4, 256, 0, s>>>(in, out, n);
-    count_launch();
-    SSSI_CHECK_CUDA(cudaGetLastError());
-}
-
 // out = a - b in T
 template <typename T>
 __global__ void diff_kernel(const T* a, const T* b, T* out, int64_t n) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
         out[q] = a[q] - b[q];
 }
-
-// A device array of T holding (or receiving) a caller array of doubles.
-// When T is double and the caller's memory is on the device, it is used in
-// place; otherwise a cached device buffer stages it (and converts).
-template <typename T>
-struct Staged {
-    T* ptr = nullptr;
-    const double* caller = nullptr;
-    bool in_place = false;
-    size_t n = 0;
-    DeviceBuffer buf, tmp;
-
-    Staged(const double* p, size_t count, bool upload, cudaStream_t s) : caller(p), n(count) {
-        if (!p) return;
-        const bool dev = is_device_pointer(p);
-        if (std::is_same<T, double>::value && dev) {
-            ptr = reinterpret_cast<T*>(const_cast<double*>(p));
-            in_place = true;
-            return;
-        }
-        buf.allocate(std::max<size_t>(n, 1) * sizeof(T));
-        ptr = buf.as<T>();
-        if (!upload || n == 0) return;
-        if (std::is_same<T, double>::value) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(ptr, p, n * sizeof(double), cudaMemcpyHostToDevice, s));
-        } else {
-            const double* src = p;
-            if (!dev) {
-                tmp.allocate(n * sizeof(double));
-                SSSI_CHECK_CUDA(cudaMemcpyAsync(tmp.get(), p, n * sizeof(double), cudaMemcpyHostToDevice, s));
-                src = tmp.as<double>();
-            }
-            convert(src, ptr, (int64_t)n, s);
-        }
-    }
-    // Copies the device contents back into the caller's array (host or device).
-    void download(double* out, cudaStream_t s) {
-        if (!out || in_place || n == 0) return;
-        const bool dev = is_device_pointer(out);
-        if (std::is_same<T, double>::value) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(out, ptr, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice
-                                                                               : cudaMemcpyDeviceToHost, s));
-            return;
-        }
-        if (dev) {
-            convert(ptr, out, (int64_t)n, s);
-            return;
-        }
-        tmp.allocate(n * sizeof(double));
-        convert(ptr, tmp.as<double>(), (int64_t)n, s);
-        SSSI_CHECK_CUDA(cudaMemcpyAsync(out, tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    }
-};
-
-// A chunk of K time slices of nz x nx streamed between the caller's array
-// (host or device, double) and a device array of T.
-template <typename T>
-struct SliceStream {
-    double* caller;
-    bool caller_dev = false;
-    int64_t n, K;
-    DeviceBuffer tbuf, dbuf;
-    T* base = nullptr;  // device slices of the current chunk (or the caller's when usable in place)
-
-    SliceStream(double* p, int64_t cells, int64_t k) : caller(p), n(cells), K(k) {
-        if (!p) return;
-        caller_dev = is_device_pointer(p);
-        if (!(std::is_same<T, double>::value && caller_dev)) tbuf.allocate(sizeof(T) * n * K);
-        if (!std::is_same<T, double>::value && !caller_dev) dbuf.allocate(sizeof(double) * n * K);
-    }
-    bool in_place() const { return std::is_same<T, double>::value && caller_dev; }
-    // device pointer of slice t (chunk starting at t0)
-    T* slice(int64_t t, int64_t t0) {
-        if (in_place()) return reinterpret_cast<T*>(caller) + t * n;
-        return tbuf.as<T>() + (t - t0) * n;
-    }
-    // input: bring slices [t0, t0+kk) to the device
-    void load(int64_t t0, int64_t kk, cudaStream_t s) {
-        if (!caller || in_place()) return;
-        const size_t bytes = sizeof(double) * n * kk;
-        if (std::is_same<T, double>::value) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(tbuf.get(), caller + t0 * n, bytes, cudaMemcpyHostToDevice, s));
-        } else if (caller_dev) {
-            convert(caller + t0 * n, tbuf.as<T>(), n * kk, s);
-        } else {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(dbuf.get(), caller + t0 * n, bytes, cudaMemcpyHostToDevice, s));
-            convert(dbuf.as<double>(), tbuf.as<T>(), n * kk, s);
-        }
-    }
-    // output: send slices [t0, t0+kk) to the caller
-    void store(int64_t t0, int64_t kk, cudaStream_t s) {
-        if (!caller || in_place()) return;
-        const size_t bytes = sizeof(double) * n * kk;
-        if (std::is_same<T, double>::value) {
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(caller + t0 * n, tbuf.get(), bytes, cudaMemcpyDeviceToHost, s));
-        } else if (caller_dev) {
-            convert(tbuf.as<T>(), caller + t0 * n, n * kk, s);
-        } else {
-            convert(tbuf.as<T>(), dbuf.as<double>(), n * kk, s);
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(caller + t0 * n, dbuf.get(), bytes, cudaMemcpyDeviceToHost, s));
-        }
-        SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
-    }
-};
 
 template <class Prop>
 void download_padded(const Prop& st, bool previous, double* model, cudaStream_t s) {
@@ -279,10 +113,6 @@ void download_padded(const Prop& st, bool previous, double* model, cudaStream_t 
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     out.download(model, (size_t)(rows * cols), s);
-}
-
-int64_t chunk_steps(int64_t nt, int64_t cells) {
-    return std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)(kChunkBytes / (sizeof(double) * cells))));
 }
 
 // ---------------------------------------------------------------- forward
@@ -556,7 +386,8 @@ void bfwd2d(const double* v, const double* source, int64_t nz, int64_t nx, int64
     if (nsrc) B.set_point_sources(k, nsrc, iz, ix, wav.ptr);
     Staged<T> rec(data, (size_t)(nx * nt), false, s);
     B.shot(k).rec = rec.ptr;
-    const int64_t K = chunk_steps(nt, n);
+    // dense sources and snapshots stream through the device in chunks of steps
+    const int64_t K = (source || snapshot) ? chunk_steps(nt, n) : std::max<int64_t>(nt, 1);
     SliceStream<T> src(const_cast<double*>(source), n, K), snap(snapshot, n, K);
     B.finalize();
     B.set_step(0);
@@ -589,7 +420,7 @@ void brvs2d(const double* v, const double* data, int64_t nz, int64_t nx, int64_t
     const int k = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, true);
     Staged<T> rows(data, (size_t)(nx * nt), true, s);
     B.shot(k).src_row = data ? rows.ptr : nullptr;
-    const int64_t K = chunk_steps(nt, n);
+    const int64_t K = snapshot ? chunk_steps(nt, n) : std::max<int64_t>(nt, 1);
     SliceStream<T> snap(snapshot, n, K);
     B.finalize();
     B.set_step(0);

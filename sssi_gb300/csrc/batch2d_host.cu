@@ -49,50 +49,6 @@ struct TmaType<double> {
     static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
 };
 
-// Band coefficients in T.  In FP32, b - 1 comes from expm1 so it keeps full
-// relative precision where b is close to 1.
-template <typename T>
-void band_coefficients(const std::vector<double>& b, const std::vector<double>& bm1, std::vector<T>& ob,
-                       std::vector<T>& obm1) {
-    ob.resize(b.size());
-    obm1.resize(b.size());
-    for (size_t k = 0; k < b.size(); ++k) {
-        ob[k] = static_cast<T>(b[k]);
-        if constexpr (std::is_same<T, float>::value)
-            obm1[k] = static_cast<float>(std::expm1(std::log(b[k])));
-        else
-            obm1[k] = bm1[k];
-    }
-}
-
-// Composed second-derivative coefficients a_0..a_l of D-(D+ .) for weights w:
-// coefficient of P(i+m) (= that of P(i-m)).
-void composed(const double* w, int N, double* a) {
-    const int L = 2 * N - 1;
-    for (int m = 0; m <= L; ++m) a[m] = 0.0;
-    for (int k = 0; k < N; ++k)
-        for (int n = 0; n < N; ++n) {
-            const double ww = w[k] * w[n];
-            a[k + n + 1] += ww;  // +P(i+k+n+1) and its mirror +P(i-1-k-n)
-            // -P(i+k-n) and -P(i-k+n): over ordered pairs each |k-n| > 0 is met
-            // twice (once per sign), while k = n puts both terms on P(i)
-            const int d = k - n;
-            a[d < 0 ? -d : d] -= (d == 0 ? 2.0 : 1.0) * ww;
-        }
-}
-
-__global__ void store_int_kernel(int* p, int v) { *p = v; }
-__global__ void add_int_kernel(int* p, int v) { *p += v; }
-
-// A stream used only to record graphs (capture does not run anything); the
-// legacy default stream cannot be captured.
-cudaStream_t capture_stream() {
-    static cudaStream_t cs = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] { SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)); });
-    return cs;
-}
-
 }  // namespace
 
 template <typename T>
@@ -106,8 +62,8 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
         wz[k] = c[k] / dz;
         wx[k] = c[k] / dx;
     }
-    composed(wz, N, az);
-    composed(wx, N, ax);
+    composed_coefficients(wz, N, az);
+    composed_coefficients(wx, N, ax);
     for (int k = 0; k < 8; ++k) {
         bc_.wz[k] = k < N ? static_cast<T>(wz[k]) : T(0);
         bc_.wx[k] = k < N ? static_cast<T>(wx[k]) : T(0);
@@ -347,16 +303,14 @@ void Batch2d<T>::run(int nsteps) {
         int* base = d_ctr_.template as<int>();
         if (!graph_) {
             // steps base .. base+K-1, then base += K
-            static std::mutex capture_mutex;
-            std::lock_guard<std::mutex> lock(capture_mutex);
+            std::lock_guard<std::mutex> lock(capture_mutex());
             cudaStream_t cs = capture_stream();
             cudaGraph_t g = nullptr;
             SSSI_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = cudaSuccess;
             try {
                 for (int k = 0; k < kGraphSteps; ++k) launch_step(base, k, cs);
-                add_int_kernel<<<1, 1, 0, cs>>>(base, kGraphSteps);
-                e = cudaGetLastError();
+                launch_add_int(base, kGraphSteps, cs);
             } catch (...) {
                 cudaStreamEndCapture(cs, &g);  // leave the capture stream usable
                 if (g) cudaGraphDestroy(g);
@@ -370,8 +324,7 @@ void Batch2d<T>::run(int nsteps) {
             if (e != cudaSuccess) graph_ = nullptr;
             SSSI_CHECK_CUDA(e);
         }
-        store_int_kernel<<<1, 1, 0, stream_>>>(base, step_);
-        SSSI_CHECK_CUDA(cudaGetLastError());
+        launch_store_int(base, step_, stream_);
         count_launch();
         for (; q + kGraphSteps <= nsteps; q += kGraphSteps) {
             SSSI_CHECK_CUDA(cudaGraphLaunch(graph_, stream_));

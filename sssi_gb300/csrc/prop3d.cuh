@@ -1,0 +1,123 @@
+// 3D CPML propagation (fwdTimeCpmlFor3dAw.m): one launch per time step over
+// the whole volume, persistent blocks marching along y.
+//
+// Work item: a TZ x TX tile of the (z, x) plane and a chunk of YC planes along
+// y.  For each output plane the block copies that plane's P tile with its z
+// and x halo, and its P_old and (v dt)^2 tiles, into shared memory (TMA, ring
+// of kStages planes); the z and x
+// second derivatives come from it (composed stencil, or the two-stage form
+// with the memory variables in tiles that reach a damped band).  The y
+// derivatives always use the two-stage form out of per-thread register
+// queues: P at planes y .. y+2N-1 and A_y = D+_y P (+ phi_y) at planes
+// y-N .. y+N-1, so each plane of the chunk is read once per thread.
+//
+// Layout in HBM:
+//   fields P (two buffers), (v dt)^2: padded Nzp x Nxp x Nyp, column-major
+//   (z fastest), interior origin at (HZ, L, L); HZ is a multiple of 4, so
+//   rows stay 16-byte aligned for vector loads and TMA coordinates;
+//   band coefficients b, b-1 (2D): z: nB x nx, x: nz x 2nB, y: nx x 2nB
+//   (the MATLAB profiles vary in two dimensions only);
+//   memory variables phi (two buffers: halo cells are read by neighbouring
+//   items while their owners update them) and psi: z: nB x nx x ny,
+//   x: nz x 2nB x ny, y: nz x nx x 2nB.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include "sssi_internal.h"
+#include "tile2d.cuh"
+
+namespace sssi {
+
+template <typename T>
+struct Shape3D;
+template <>
+struct Shape3D<float> {
+    static constexpr int TZ = 32, TX = 32, RZ = 4;  // tile, rows per thread
+    static constexpr int kThreads = (TZ / RZ) * TX;
+    static constexpr int kMinBlocks = 2;
+    static constexpr int YC = 32;  // planes per work item
+};
+template <>
+struct Shape3D<double> {
+    static constexpr int TZ = 16, TX = 32, RZ = 2;
+    static constexpr int kThreads = (TZ / RZ) * TX;
+    static constexpr int kMinBlocks = 1;
+    static constexpr int YC = 32;
+};
+
+template <typename T>
+struct Desc3 {
+    using M = typename MemVar<T>::type;
+    CUtensorMap tm_plane[2];  // plane tile of field k with its z/x halo
+    CUtensorMap tm_tile[2];   // plane tile of field k without halo (P_old)
+    CUtensorMap tm_v;         // plane tile of (v dt)^2
+    T* field[2];              // interior origin of field k; field (t & 1) is current at step t
+    const T* vdt2;            // interior origin of (v dt)^2
+    int64_t ldz;              // Nzp: stride of x
+    int64_t ldxy;             // Nzp * Nxp: stride of y
+    int nz, nx, ny, nB, nt;
+    int ntz, ntx, nchunk;  // tiles along z and x, chunks along y
+    // band coefficients (2D) and memory variables (3D), see the file header
+    const T *zb, *zbm1, *xb, *xbm1, *yb, *ybm1;
+    M *zphi[2], *zpsi, *xphi[2], *xpsi, *yphi[2], *ypsi;
+    // sources: dense slices (nz x nx x ny per step, from dense_t0 on), points
+    const T* src_dense;
+    int dense_t0;
+    int nsrc;
+    int src_iz[kMaxPointSources], src_ix[kMaxPointSources], src_iy[kMaxPointSources];
+    const T* src_wavelet;    // nsrc x nt
+    T* rec;                  // nx x ny per step: the top interior face after the step
+    T* snap;                 // nz x nx x ny per step from snap_t0 on
+    int snap_t0;
+};
+
+template <typename T>
+struct Const3 {
+    T az[16], ax[16];  // composed second-derivative coefficients (z, x)
+    T wz[8], wx[8], wy[8];
+    int nitems;
+    const int* step_base;  // the launch computes step *step_base + step_offset
+    int step_offset;
+    int* err;
+};
+
+// Host driver of one 3D propagation.
+template <typename T>
+class Prop3d {
+  public:
+    using M = typename MemVar<T>::type;
+    Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, int nB, double dz, double dx, double dy,
+           double dt, int nt, cudaStream_t stream);
+    ~Prop3d();
+    Prop3d(const Prop3d&) = delete;
+    Prop3d& operator=(const Prop3d&) = delete;
+
+    Desc3<T>& desc() { return desc_; }
+    void set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const int64_t* iy, const T* d_wavelet);
+    void sync_desc();
+    void run(int nsteps);  // whole runs of kGraphSteps go through a CUDA graph
+    void check_errors();
+    const T* current_field() const { return desc_.field[step_ & 1]; }
+    int step() const { return step_; }
+    static constexpr int kGraphSteps = 16;
+
+  private:
+    void launch_step(const int* base, int offset, cudaStream_t s);
+    int N_;
+    cudaStream_t stream_;
+    Desc3<T> desc_{};
+    Const3<T> cc_{};
+    DeviceBuffer P_[2], vdt2_, zb_, zbm1_, xb_, xbm1_, yb_, ybm1_, zphi_[2], zpsi_, xphi_[2], xpsi_, yphi_[2], ypsi_;
+    DeviceBuffer d_desc_, d_ctr_;
+    int grid_ = 0, step_ = 0;
+    cudaGraphExec_t graph_ = nullptr;
+};
+
+template <typename T, int N>
+void launch_prop3d_n(const Desc3<T>* d, const Const3<T>& c, int grid, cudaStream_t stream);
+template <typename T, int N>
+int prop3d_occupancy_n();
+
+}  // namespace sssi

@@ -1,0 +1,328 @@
+// Host side of the 3D CPML propagation: grids, damping, descriptors, launches.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
+#include "prop3d.cuh"
+
+namespace sssi {
+
+bool encode_tensor_map_3d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, size_t elem_bytes,
+                          uint64_t d0, uint64_t d1, uint64_t d2, uint64_t ld0, uint64_t ld1, uint32_t b0, uint32_t b1,
+                          uint32_t b2) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    });
+    if (!encode) return false;
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {ld0 * elem_bytes, ld1 * elem_bytes};
+    const cuuint32_t box[3] = {b0, b1, b2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = encode(map, dtype, 3, const_cast<void*>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+namespace {
+
+template <typename T>
+constexpr CUtensorMapDataType tma_type() {
+    return std::is_same<T, float>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+}
+
+// (v dt)^2 into the padded layout (interior origin `org`, strides ldz, ldxy).
+template <typename T>
+__global__ void vdt2_kernel(const double* v, int64_t nz, int64_t nx, int64_t ny, double dt, T* out, int64_t ldz,
+                            int64_t ldxy) {
+    const int64_t n = nz * nx * ny;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = q % nz, j = (q / nz) % nx, k = q / (nz * nx);
+        const double a = v[q] * dt;
+        out[i + j * ldz + k * ldxy] = static_cast<T>(a * a);
+    }
+}
+
+template <typename T>
+void launch_prop3d(int N, const Desc3<T>* d, const Const3<T>& c, int grid, cudaStream_t s) {
+    switch (N) {
+        case 1: launch_prop3d_n<T, 1>(d, c, grid, s); break;
+        case 2: launch_prop3d_n<T, 2>(d, c, grid, s); break;
+        case 3: launch_prop3d_n<T, 3>(d, c, grid, s); break;
+        case 4: launch_prop3d_n<T, 4>(d, c, grid, s); break;
+        case 5: launch_prop3d_n<T, 5>(d, c, grid, s); break;
+        case 6: launch_prop3d_n<T, 6>(d, c, grid, s); break;
+        case 7: launch_prop3d_n<T, 7>(d, c, grid, s); break;
+        case 8: launch_prop3d_n<T, 8>(d, c, grid, s); break;
+        default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
+    }
+}
+
+template <typename T>
+int prop3d_occupancy(int N) {
+    switch (N) {
+        case 1: return prop3d_occupancy_n<T, 1>();
+        case 2: return prop3d_occupancy_n<T, 2>();
+        case 3: return prop3d_occupancy_n<T, 3>();
+        case 4: return prop3d_occupancy_n<T, 4>();
+        case 5: return prop3d_occupancy_n<T, 5>();
+        case 6: return prop3d_occupancy_n<T, 6>();
+        case 7: return prop3d_occupancy_n<T, 7>();
+        default: return prop3d_occupancy_n<T, 8>();
+    }
+}
+
+}  // namespace
+
+template <typename T>
+Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, int nB, double dz, double dx,
+                  double dy, double dt, int nt, cudaStream_t stream)
+    : N_(N), stream_(stream) {
+    using S = Shape3D<T>;
+    SSSI_REQUIRE(N >= 1 && N <= kMaxOrder, SSSI_ERR_ARG, "nDiffOrder must be in 1..%d (got %d)", kMaxOrder, N);
+    SSSI_REQUIRE(nz > 0 && nx > 0 && ny > 0, SSSI_ERR_ARG, "bad 3D sizes");
+    SSSI_REQUIRE(nB >= 0 && 2 * (int64_t)nB <= std::min(nx, ny) && nB <= nz, SSSI_ERR_ARG,
+                 "nBoundary %d does not fit the grid", nB);
+    SSSI_REQUIRE(dz > 0 && dx > 0 && dy > 0 && dt > 0, SSSI_ERR_ARG, "dz, dx, dy, dt must be positive");
+    SSSI_REQUIRE(nz * nx * ny < (int64_t(1) << 40), SSSI_ERR_ARG, "grid too large");
+    const int L = 2 * N - 1, HZ = tile_halo_rows(N);
+    const int64_t Nzp = (nz + 2 * HZ + 3) / 4 * 4, Nxp = nx + 2 * L, Nyp = ny + 2 * L;
+    const int64_t np = Nzp * Nxp * Nyp, org = HZ + L * Nzp + L * Nzp * Nxp;
+    SSSI_REQUIRE(np < (int64_t(1) << 40), SSSI_ERR_ARG, "grid too large");
+
+    // coefficients
+    double c[kMaxOrder], wz[kMaxOrder], wx[kMaxOrder], az[16], ax[16];
+    staggered_coefficients(N, c);
+    for (int k = 0; k < N; ++k) {
+        wz[k] = c[k] / dz;
+        wx[k] = c[k] / dx;
+    }
+    composed_coefficients(wz, N, az);
+    composed_coefficients(wx, N, ax);
+    for (int k = 0; k < 8; ++k) {
+        cc_.wz[k] = k < N ? static_cast<T>(wz[k]) : T(0);
+        cc_.wx[k] = k < N ? static_cast<T>(wx[k]) : T(0);
+        cc_.wy[k] = k < N ? static_cast<T>(c[k] / dy) : T(0);
+    }
+    for (int m = 0; m < 16; ++m) {
+        cc_.az[m] = m <= L ? static_cast<T>(az[m]) : T(0);
+        cc_.ax[m] = m <= L ? static_cast<T>(ax[m]) : T(0);
+    }
+
+    // fields and (v dt)^2 in the padded layout (the padding stays zero)
+    for (auto& b : P_) {
+        b.allocate(sizeof(T) * np);
+        b.zero(stream_);
+    }
+    vdt2_.allocate(sizeof(T) * np);
+    vdt2_.zero(stream_);
+    const int64_t n = nz * nx * ny;
+    {
+        DeviceBuffer vd;
+        const double* vdev = v;
+        if (!is_device_pointer(v)) {
+            vd.allocate(sizeof(double) * n);
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(vd.get(), v, sizeof(double) * n, cudaMemcpyHostToDevice, stream_));
+            vdev = vd.template as<double>();
+        }
+        vdt2_kernel<T><<<152 * 4, 256, 0, stream_>>>(vdev, nz, nx, ny, dt, vdt2_.template as<T>() + org, Nzp,
+                                                      Nzp * Nxp);
+        count_launch();
+        SSSI_CHECK_CUDA(cudaGetLastError());
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));  // vd is released at the end of this scope
+    }
+
+    // damping: the profiles read v on the y = 0 slice and the top row only
+    std::vector<double> vslice((size_t)(nz * nx)), vtop((size_t)(nx * ny));
+    if (is_device_pointer(v)) {
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(vslice.data(), v, sizeof(double) * nz * nx, cudaMemcpyDeviceToHost, stream_));
+        SSSI_CHECK_CUDA(cudaMemcpy2DAsync(vtop.data(), sizeof(double), v, sizeof(double) * nz, sizeof(double),
+                                          (size_t)(nx * ny), cudaMemcpyDeviceToHost, stream_));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    } else {
+        std::copy(v, v + nz * nx, vslice.begin());
+        for (int64_t q = 0; q < nx * ny; ++q) vtop[q] = v[q * nz];
+    }
+    const Bands3D bands = damping_bands_3d(vslice.data(), vtop.data(), nz, nx, ny, nB, dt);
+    auto upload = [&](DeviceBuffer& buf, const std::vector<T>& h) {
+        buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
+        if (!h.empty())
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, stream_));
+    };
+    std::vector<T> b, bm1;
+    band_coefficients<T>(bands.zb, bands.zbm1, b, bm1);
+    upload(zb_, b);
+    upload(zbm1_, bm1);
+    band_coefficients<T>(bands.xb, bands.xbm1, b, bm1);
+    upload(xb_, b);
+    upload(xbm1_, bm1);
+    band_coefficients<T>(bands.yb, bands.ybm1, b, bm1);
+    upload(yb_, b);
+    upload(ybm1_, bm1);
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));  // host staging vectors go out of scope
+    auto mem = [&](DeviceBuffer& buf, int64_t count) {
+        buf.allocate(sizeof(M) * std::max<int64_t>(count, 1));
+        buf.zero(stream_);
+    };
+    const int64_t mz = (int64_t)nB * nx * ny, mx = nz * 2 * (int64_t)nB * ny, my = nz * nx * 2 * (int64_t)nB;
+    mem(zphi_[0], mz);
+    mem(zphi_[1], mz);
+    mem(zpsi_, mz);
+    mem(xphi_[0], mx);
+    mem(xphi_[1], mx);
+    mem(xpsi_, mx);
+    mem(yphi_[0], my);
+    mem(yphi_[1], my);
+    mem(ypsi_, my);
+
+    // descriptor
+    Desc3<T>& d = desc_;
+    const uint32_t box_rows = S::TZ + 2 * HZ, box_cols = S::TX + 2 * L;
+    for (int k = 0; k < 2; ++k) {
+        SSSI_REQUIRE(encode_tensor_map_3d(&d.tm_plane[k], P_[k].get(), tma_type<T>(), sizeof(T), Nzp, Nxp, Nyp, Nzp,
+                                          Nzp * Nxp, box_rows, box_cols, 1),
+                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the 3D field");
+        SSSI_REQUIRE(encode_tensor_map_3d(&d.tm_tile[k], P_[k].get(), tma_type<T>(), sizeof(T), Nzp, Nxp, Nyp, Nzp,
+                                          Nzp * Nxp, S::TZ, S::TX, 1),
+                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the 3D field");
+        d.field[k] = P_[k].template as<T>() + org;
+    }
+    SSSI_REQUIRE(encode_tensor_map_3d(&d.tm_v, vdt2_.get(), tma_type<T>(), sizeof(T), Nzp, Nxp, Nyp, Nzp, Nzp * Nxp,
+                                      S::TZ, S::TX, 1),
+                 SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for (v dt)^2");
+    d.vdt2 = vdt2_.template as<T>() + org;
+    d.ldz = Nzp;
+    d.ldxy = Nzp * Nxp;
+    d.nz = (int)nz;
+    d.nx = (int)nx;
+    d.ny = (int)ny;
+    d.nB = nB;
+    d.nt = nt;
+    d.ntz = (int)((nz + S::TZ - 1) / S::TZ);
+    d.ntx = (int)((nx + S::TX - 1) / S::TX);
+    d.nchunk = (int)((ny + S::YC - 1) / S::YC);
+    d.zb = zb_.template as<T>();
+    d.zbm1 = zbm1_.template as<T>();
+    d.xb = xb_.template as<T>();
+    d.xbm1 = xbm1_.template as<T>();
+    d.yb = yb_.template as<T>();
+    d.ybm1 = ybm1_.template as<T>();
+    for (int k = 0; k < 2; ++k) {
+        d.zphi[k] = zphi_[k].template as<M>();
+        d.xphi[k] = xphi_[k].template as<M>();
+        d.yphi[k] = yphi_[k].template as<M>();
+    }
+    d.zpsi = zpsi_.template as<M>();
+    d.xpsi = xpsi_.template as<M>();
+    d.ypsi = ypsi_.template as<M>();
+    d_desc_.allocate(sizeof(Desc3<T>));
+
+    d_ctr_.allocate(4 * sizeof(int));  // graph step base, zero, error flag, spare
+    d_ctr_.zero(stream_);
+    cc_.step_base = d_ctr_.template as<int>() + 1;
+    cc_.step_offset = 0;
+    cc_.err = d_ctr_.template as<int>() + 2;
+    cc_.nitems = d.ntz * d.ntx * d.nchunk;
+    int dev = 0, sms = 1;
+    SSSI_CHECK_CUDA(cudaGetDevice(&dev));
+    SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    grid_ = std::max(1, std::min(cc_.nitems, sms * prop3d_occupancy<T>(N)));
+    sync_desc();
+}
+
+template <typename T>
+Prop3d<T>::~Prop3d() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+}
+
+template <typename T>
+void Prop3d<T>::set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const int64_t* iy,
+                                  const T* d_wavelet) {
+    SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "at most %d point sources (got %d)",
+                 kMaxPointSources, nsrc);
+    for (int s = 0; s < nsrc; ++s)
+        SSSI_REQUIRE(iz[s] >= 0 && iz[s] < desc_.nz && ix[s] >= 0 && ix[s] < desc_.nx && iy[s] >= 0 &&
+                         iy[s] < desc_.ny,
+                     SSSI_ERR_ARG, "point source %d outside the grid", s);
+    desc_.nsrc = nsrc;
+    for (int s = 0; s < nsrc; ++s) {
+        desc_.src_iz[s] = (int)iz[s];
+        desc_.src_ix[s] = (int)ix[s];
+        desc_.src_iy[s] = (int)iy[s];
+    }
+    desc_.src_wavelet = d_wavelet;
+}
+
+template <typename T>
+void Prop3d<T>::sync_desc() {
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.get(), &desc_, sizeof(Desc3<T>), cudaMemcpyHostToDevice, stream_));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));  // desc_ may change on the host next
+}
+
+template <typename T>
+void Prop3d<T>::launch_step(const int* base, int offset, cudaStream_t s) {
+    Const3<T> c = cc_;
+    c.step_base = base;
+    c.step_offset = offset;
+    launch_prop3d<T>(N_, d_desc_.template as<Desc3<T>>(), c, grid_, s);
+}
+
+template <typename T>
+void Prop3d<T>::run(int nsteps) {
+    int q = 0;
+    if (nsteps >= kGraphSteps) {
+        int* base = d_ctr_.template as<int>();
+        if (!graph_) {
+            std::lock_guard<std::mutex> lock(capture_mutex());
+            cudaStream_t cs = capture_stream();
+            cudaGraph_t g = nullptr;
+            SSSI_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            try {
+                for (int k = 0; k < kGraphSteps; ++k) launch_step(base, k, cs);
+                launch_add_int(base, kGraphSteps, cs);
+            } catch (...) {
+                cudaStreamEndCapture(cs, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            count_launch(-kGraphSteps);  // recorded, not run
+            cudaError_t e = cudaStreamEndCapture(cs, &g);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&graph_, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) graph_ = nullptr;
+            SSSI_CHECK_CUDA(e);
+        }
+        launch_store_int(base, step_, stream_);
+        count_launch();
+        for (; q + kGraphSteps <= nsteps; q += kGraphSteps) {
+            SSSI_CHECK_CUDA(cudaGraphLaunch(graph_, stream_));
+            count_launch(kGraphSteps + 1);
+        }
+    }
+    for (; q < nsteps; ++q) launch_step(cc_.step_base, step_ + q, stream_);
+    step_ += nsteps;
+}
+
+template <typename T>
+void Prop3d<T>::check_errors() {
+    int h = 0;
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(&h, cc_.err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    SSSI_REQUIRE(h == 0, SSSI_ERR_INTERNAL, "a plane copy did not arrive within the wait limit (kernel aborted)");
+}
+
+template class Prop3d<float>;
+template class Prop3d<double>;
+
+}  // namespace sssi

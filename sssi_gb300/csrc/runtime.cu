@@ -77,6 +77,34 @@ void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 cudaStream_t current_stream() { return g_stream; }
 
+namespace {
+__global__ void store_int_kernel(int* p, int v) { *p = v; }
+__global__ void add_int_kernel(int* p, int v) { *p += v; }
+}  // namespace
+
+void launch_store_int(int* p, int v, cudaStream_t s) {
+    store_int_kernel<<<1, 1, 0, s>>>(p, v);
+    SSSI_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_add_int(int* p, int v, cudaStream_t s) {
+    add_int_kernel<<<1, 1, 0, s>>>(p, v);
+    SSSI_CHECK_CUDA(cudaGetLastError());
+}
+
+cudaStream_t capture_stream() {
+    static cudaStream_t cs = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] { SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)); });
+    return cs;
+}
+
+std::mutex& capture_mutex() {
+    static std::mutex m;
+    return m;
+}
+
+
 void ensure_device() {
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);

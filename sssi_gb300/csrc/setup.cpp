@@ -96,8 +96,8 @@ Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double
     return b;
 }
 
-Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int nB, double dt) {
-    (void)ny;
+Bands3D damping_bands_3d(const double* vslice, const double* vtop, int64_t nz, int64_t nx, int64_t ny, int nB,
+                         double dt) {
     Bands3D b;
     const double L = static_cast<double>(nB);
     b.zb.resize(static_cast<size_t>(nB) * nx);
@@ -106,10 +106,9 @@ Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, in
     b.xbm1.resize(b.xb.size());
     b.yb.resize(static_cast<size_t>(nx) * 2 * nB);
     b.ybm1.resize(b.yb.size());
-    const int64_t sxy = nz * nx;
     for (int64_t j = 0; j < nx; ++j)
         for (int r = 0; r < nB; ++r) {
-            const double d = damp_m_order(static_cast<double>(r + 1), v[(nz - nB + r) + j * nz], L);
+            const double d = damp_m_order(static_cast<double>(r + 1), vslice[(nz - nB + r) + j * nz], L);
             const double e = std::exp(-d * dt);
             b.zb[r + j * nB] = e;
             b.zbm1[r + j * nB] = e - 1;
@@ -118,7 +117,7 @@ Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, in
         const int64_t j = c < nB ? c : nx - nB + (c - nB);
         const double u = c < nB ? static_cast<double>(nB - c) : static_cast<double>(c - nB + 1);
         for (int64_t i = 0; i < nz; ++i) {
-            const double d = damp_m_order(u, v[i + j * nz], L);
+            const double d = damp_m_order(u, vslice[i + j * nz], L);
             const double e = std::exp(-d * dt);
             b.xb[i + c * nz] = e;
             b.xbm1[i + c * nz] = e - 1;
@@ -128,7 +127,7 @@ Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, in
         const int64_t k = c < nB ? c : ny - nB + (c - nB);
         const double u = c < nB ? static_cast<double>(nB - c) : static_cast<double>(c - nB + 1);
         for (int64_t j = 0; j < nx; ++j) {
-            const double d = damp_m_order(u, v[j * nz + k * sxy], L);
+            const double d = damp_m_order(u, vtop[j + k * nx], L);
             const double e = std::exp(-d * dt);
             b.yb[j + c * nx] = e;
             b.ybm1[j + c * nx] = e - 1;
@@ -136,6 +135,24 @@ Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, in
     }
     return b;
 }
+
+// Composed second-derivative coefficients a_0..a_l of D-(D+ .) for weights w:
+// coefficient of P(i+m) (= that of P(i-m)).
+void composed_coefficients(const double* w, int N, double* a) {
+    const int L = 2 * N - 1;
+    for (int m = 0; m <= L; ++m) a[m] = 0.0;
+    for (int k = 0; k < N; ++k)
+        for (int n = 0; n < N; ++n) {
+            const double ww = w[k] * w[n];
+            a[k + n + 1] += ww;  // +P(i+k+n+1) and its mirror +P(i-1-k-n)
+            // -P(i+k-n) and -P(i-k+n): over ordered pairs each |k-n| > 0 is met
+            // twice (once per sign), while k = n puts both terms on P(i)
+            const int d = k - n;
+            a[d < 0 ? -d : d] -= (d == 0 ? 2.0 : 1.0) * ww;
+        }
+}
+
+
 
 }  // namespace sssi
 

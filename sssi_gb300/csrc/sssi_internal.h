@@ -5,7 +5,10 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <cmath>
+#include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "sssi_gb300.h"
@@ -60,6 +63,14 @@ int guarded(F&& f) {
 
 // ---------------------------------------------------------------- runtime
 void count_launch(int n = 1);
+// One-thread kernels that set / advance a device int (graph step bases).
+void launch_store_int(int* p, int v, cudaStream_t s);
+void launch_add_int(int* p, int v, cudaStream_t s);
+// A non-blocking stream used only to record CUDA graphs (capture runs nothing;
+// the legacy default stream cannot be captured), and the lock held while
+// recording on it.
+cudaStream_t capture_stream();
+std::mutex& capture_mutex();
 cudaStream_t current_stream();
 bool is_device_pointer(const void* p);
 void ensure_device();
@@ -152,6 +163,30 @@ struct Bands3D {
     std::vector<double> xb, xbm1;  // nz x 2nB
     std::vector<double> yb, ybm1;  // nx x 2nB
 };
-Bands3D damping_bands_3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int nB, double dt);
+// vslice: v on the y = 0 slice (nz x nx); vtop: v on row 0 of every column
+// (nx x ny) -- the only velocities the profiles read.
+Bands3D damping_bands_3d(const double* vslice, const double* vtop, int64_t nz, int64_t nx, int64_t ny, int nB,
+                         double dt);
+
+// Composed second-derivative coefficients a_0..a_l (l = 2N-1) of D-(D+ .) for
+// the first-derivative weights w_0..w_{N-1}: coefficient of P(i+m) (= of P(i-m)).
+void composed_coefficients(const double* w, int N, double* a);
+
+// Band coefficients in T.  In FP32, b - 1 comes from expm1 so it keeps full
+// relative precision where b is close to 1.
+template <typename T>
+inline void band_coefficients(const std::vector<double>& b, const std::vector<double>& bm1, std::vector<T>& ob,
+                       std::vector<T>& obm1) {
+    ob.resize(b.size());
+    obm1.resize(b.size());
+    for (size_t k = 0; k < b.size(); ++k) {
+        ob[k] = static_cast<T>(b[k]);
+        if constexpr (std::is_same<T, float>::value)
+            obm1[k] = static_cast<float>(std::expm1(std::log(b[k])));
+        else
+            obm1[k] = bm1[k];
+    }
+}
+
 
 }  // namespace sssi

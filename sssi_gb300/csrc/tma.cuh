@@ -65,6 +65,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// 3D tiled copy global -> shared (x innermost, same alignment rule as 2D).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // Host: a 2D tensor map over a column-major array of `rows` x `cols` elements
 // with column pitch `ld` elements, copied in boxes of box_rows x box_cols.
 bool encode_tensor_map_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, size_t elem_bytes,
