@@ -1,10 +1,11 @@
 // 3D CPML propagation (fwdTimeCpmlFor3dAw.m): one launch per time step over
 // the whole volume, persistent blocks marching along y.
 //
-// Work item: a TZ x TX tile of the (z, x) plane and a chunk of YC planes along
-// y.  For each output plane the block copies that plane's P tile with its z
+// Work item: a TZ x TX tile of the (z, x) plane and a chunk of planes along
+// y (chunk length chosen per grid so that the items fill the GPU).  For each output plane the block copies that plane's P tile with its z
 // and x halo, and its P_old and (v dt)^2 tiles, into shared memory (TMA, ring
-// of kStages planes); the z and x
+// of kStages planes), together with the tile's own cells of P at plane
+// y+2N-1, which enter the y queue; the z and x
 // second derivatives come from it (composed stencil, or the two-stage form
 // with the memory variables in tiles that reach a damped band).  The y
 // derivatives always use the two-stage form out of per-thread register
@@ -37,14 +38,12 @@ struct Shape3D<float> {
     static constexpr int TZ = 32, TX = 32, RZ = 4;  // tile, rows per thread
     static constexpr int kThreads = (TZ / RZ) * TX;
     static constexpr int kMinBlocks = 2;
-    static constexpr int YC = 32;  // planes per work item
 };
 template <>
 struct Shape3D<double> {
     static constexpr int TZ = 16, TX = 32, RZ = 2;
     static constexpr int kThreads = (TZ / RZ) * TX;
     static constexpr int kMinBlocks = 1;
-    static constexpr int YC = 32;
 };
 
 template <typename T>
@@ -59,6 +58,9 @@ struct Desc3 {
     int64_t ldxy;             // Nzp * Nxp: stride of y
     int nz, nx, ny, nB, nt;
     int ntz, ntx, nchunk;  // tiles along z and x, chunks along y
+    int ychunk;            // planes per chunk
+    const int* order;      // work items (tile + ntz*ntx*chunk), most expensive first
+    int* next;             // two counters: items taken at steps of parity 0 / 1
     // band coefficients (2D) and memory variables (3D), see the file header
     const T *zb, *zbm1, *xb, *xbm1, *yb, *ybm1;
     M *zphi[2], *zpsi, *xphi[2], *xpsi, *yphi[2], *ypsi;
@@ -110,7 +112,7 @@ class Prop3d {
     Desc3<T> desc_{};
     Const3<T> cc_{};
     DeviceBuffer P_[2], vdt2_, zb_, zbm1_, xb_, xbm1_, yb_, ybm1_, zphi_[2], zpsi_, xphi_[2], xpsi_, yphi_[2], ypsi_;
-    DeviceBuffer d_desc_, d_ctr_;
+    DeviceBuffer d_desc_, d_ctr_, d_order_, d_next_;
     int grid_ = 0, step_ = 0;
     cudaGraphExec_t graph_ = nullptr;
 };

@@ -211,7 +211,18 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     d.nt = nt;
     d.ntz = (int)((nz + S::TZ - 1) / S::TZ);
     d.ntx = (int)((nx + S::TX - 1) / S::TX);
-    d.nchunk = (int)((ny + S::YC - 1) / S::YC);
+    // chunks along y: enough work items for about three per resident block,
+    // each at least 8 planes (a chunk re-reads 4N-2 planes to fill its queues)
+    int dev = 0, sms = 1;
+    SSSI_CHECK_CUDA(cudaGetDevice(&dev));
+    SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int slots = sms * prop3d_occupancy<T>(N);
+    const int64_t tiles = (int64_t)d.ntz * d.ntx;
+    int64_t yc = std::max<int64_t>(8, (ny * tiles + 3 * slots - 1) / (3 * (int64_t)slots));
+    yc = std::min<int64_t>(yc, 64);
+    const int64_t nch = (ny + yc - 1) / yc;
+    d.ychunk = (int)((ny + nch - 1) / nch);             // even chunks
+    d.nchunk = (int)((ny + d.ychunk - 1) / d.ychunk);  // every chunk starts inside the grid
     d.zb = zb_.template as<T>();
     d.zbm1 = zbm1_.template as<T>();
     d.xb = xb_.template as<T>();
@@ -234,10 +245,38 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     cc_.step_offset = 0;
     cc_.err = d_ctr_.template as<int>() + 2;
     cc_.nitems = d.ntz * d.ntx * d.nchunk;
-    int dev = 0, sms = 1;
-    SSSI_CHECK_CUDA(cudaGetDevice(&dev));
-    SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    grid_ = std::max(1, std::min(cc_.nitems, sms * prop3d_occupancy<T>(N)));
+    grid_ = std::max(1, std::min(cc_.nitems, slots));
+    // item order for the dynamic schedule: estimated cost, highest first
+    // (tiles next to a z or x band add a cooperative pass per plane; y band
+    // planes add memory-variable traffic; every chunk fills its queues)
+    {
+        struct It {
+            int item;
+            float cost;
+        };
+        std::vector<It> its((size_t)cc_.nitems);
+        for (int it = 0; it < cc_.nitems; ++it) {
+            const int tile = it % (d.ntz * d.ntx), chunk = it / (d.ntz * d.ntx);
+            const int z0 = (tile % d.ntz) * S::TZ, x0 = (tile / d.ntz) * S::TX;
+            const int y0 = chunk * d.ychunk, y1 = (int)std::min<int64_t>(y0 + d.ychunk, ny);
+            const bool band_zx = nB > 0 && (z0 + S::TZ + N - 1 > nz - nB || x0 - N < nB ||
+                                            x0 + S::TX + N - 2 >= nx - nB);
+            int ybands = 0;
+            for (int y = y0; y < y1; ++y) ybands += (nB > 0 && (y < nB || y >= ny - nB)) ? 1 : 0;
+            its[it] = {it, (float)(y1 - y0) * (band_zx ? 1.6f : 1.0f) + 0.4f * ybands + 0.3f * (2 * N - 1)};
+        }
+        std::stable_sort(its.begin(), its.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
+        std::vector<int> order(its.size());
+        for (size_t q = 0; q < its.size(); ++q) order[q] = its[q].item;
+        d_order_.allocate(sizeof(int) * std::max<size_t>(order.size(), 1));
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_order_.get(), order.data(), sizeof(int) * order.size(),
+                                        cudaMemcpyHostToDevice, stream_));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+        d.order = d_order_.template as<int>();
+        d_next_.allocate(2 * sizeof(int));
+        d_next_.zero(stream_);
+        d.next = d_next_.template as<int>();
+    }
     sync_desc();
 }
 

@@ -63,8 +63,9 @@ struct Layout3 {
     static constexpr unsigned kTileBytes = sizeof(T) * TZ * TX;
     static constexpr unsigned kO = (kBoxBytes + 127) / 128 * 128;  // P_old tile within a stage
     static constexpr unsigned kV = kO + (kTileBytes + 127) / 128 * 128;
-    static constexpr unsigned kPlane = kV + (kTileBytes + 127) / 128 * 128;  // one stage
-    static constexpr unsigned kTx = kBoxBytes + 2 * kTileBytes;
+    static constexpr unsigned kQ = kV + (kTileBytes + 127) / 128 * 128;      // P tile of plane y+2N-1
+    static constexpr unsigned kPlane = kQ + (kTileBytes + 127) / 128 * 128;  // one stage
+    static constexpr unsigned kTx = kBoxBytes + 3 * kTileBytes;
     static constexpr unsigned kDesc = kStages * kPlane;
     static constexpr unsigned kBar = kDesc + (sizeof(Desc3<T>) + 127) / 128 * 128;
     static constexpr unsigned kScratch = kBar + 128;
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
     prop3d_kernel(const Desc3<T>* __restrict__ dp, const __grid_constant__ Const3<T> cc) {
     using G = Layout3<T, N>;
     using M = typename MemVar<T>::type;
-    constexpr int TZ = G::TZ, TX = G::TX, RZ = G::RZ, YC = Shape3D<T>::YC;
+    constexpr int TZ = G::TZ, TX = G::TX, RZ = G::RZ;
     constexpr int NS = G::kStages;
     constexpr int NQ = 2 * N;  // queue length
     extern __shared__ __align__(128) unsigned char smem[];
@@ -424,10 +425,17 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
     unsigned phase_bits = 0, inflight = 0;
     bool failed = false;
 
-    for (int item = blockIdx.x; item < cc.nitems && !failed; item += gridDim.x) {
+    // dynamic schedule: the first item of a block is its index, later ones come
+    // from the step's counter; this step clears the counter of the next one
+    // (the next step reads it only after this grid has completed)
+    int* next = d.next + (step & 1);
+    if (blockIdx.x == 0 && tid == 0) d.next[(step + 1) & 1] = 0;
+    __shared__ int s_item;
+    for (int k = blockIdx.x; k < cc.nitems && !failed;) {
+        const int item = d.order[k];
         const int tile = item % ntile, chunk = item / ntile;
         const int z0 = (tile % d.ntz) * TZ, x0 = (tile / d.ntz) * TX;
-        const int y0 = chunk * YC, y1 = min(y0 + YC, ny);
+        const int y0 = chunk * d.ychunk, y1 = min(y0 + d.ychunk, ny);
         const bool bz = nB > 0 && z0 + TZ + N - 1 > nz - nB;
         const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= nx - nB);
         const int i0 = z0 + r0, j = x0 + c0;
@@ -446,17 +454,19 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                 tma_load_3d(st, &dp->tm_plane[cur], &bar[s], z0, x0, y + G::L);
                 tma_load_3d(st + G::kO, &dp->tm_tile[cur ^ 1], &bar[s], z0 + G::HZ, x0 + G::L, y + G::L);
                 tma_load_3d(st + G::kV, &dp->tm_v, &bar[s], z0 + G::HZ, x0 + G::L, y + G::L);
+                tma_load_3d(st + G::kQ, &dp->tm_tile[cur], &bar[s], z0 + G::HZ, x0 + G::L, y + 2 * N - 1 + G::L);
             }
         };
+        __syncthreads();  // the previous item's last planes are no longer read
         for (int q = 0; q < NS - 1; ++q) issue(y0 + q);
 
-        // queues (static slots after the unroll below): Pq slot of plane p is
-        // (p - ys) mod NQ, Aq slot of plane p is (p - ys - N + 1) mod NQ
+        // y queues.  Registers: before the shift of step s, Pq[k] = P(s-1+k)
+        // (k = 0 .. 2N-1); after it Pq[k] = P(s+k).  Shared memory: A_y(p) in
+        // slot (p - ys - N + 1) mod NQ of this thread, at Aq[slot * NT].
         const int ys = y0 - 2 * N + 1;
-        T Pq[NQ][RZ];
-        // A_y queue in shared memory: slot k of this thread at Aq[k * NT + tid]
-        Col<T>* Aq = reinterpret_cast<Col<T>*>(smem + G::kAq) + tid;
         constexpr int NT = Shape3D<T>::kThreads;
+        T Pq[NQ][RZ];
+        Col<T>* Aq = reinterpret_cast<Col<T>*>(smem + G::kAq) + tid;
 #pragma unroll
         for (int k = 0; k < NQ; ++k)
 #pragma unroll
@@ -466,34 +476,53 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
         Col<T> pnext{};
         if (act) {
 #pragma unroll
-            for (int k = 0; k < NQ - 1; ++k) {
-                const Col<T> v = ldc_nc(P + own + (int64_t)(ys + k) * ldxy);
+            for (int k = 1; k < NQ; ++k) {
+                const Col<T> v = ldc_nc(P + own + (int64_t)(ys - 1 + k) * ldxy);
 #pragma unroll
                 for (int o = 0; o < RZ; ++o) Pq[k][o] = v.v[o];
             }
             pnext = ldc_nc(P + own + (int64_t)(ys + NQ - 1) * ldxy);  // P(s+2N-1) for the first step
         }
 
-        for (int sb = ys; sb < y1 && !failed; sb += NQ) {
-#pragma unroll
-            for (int u = 0; u < NQ; ++u) {
-                const int s = sb + u;
-                if (s >= y1) break;
-                // queue in: P(s+2N-1); prefetch P(s+2N)
-#pragma unroll
-                for (int o = 0; o < RZ; ++o) Pq[(u + NQ - 1) % NQ][o] = pnext.v[o];
-                if (act && s + 1 < y1) pnext = ldc_nc(P + own + (int64_t)(s + NQ) * ldxy);
+        int u = 0;  // (s - ys) mod NQ
+        for (int s = ys; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
+            {
                 const bool out = s >= y0;
+                const int st = out ? (s - y0) % NS : 0;
+                Col<T> pin = pnext;  // P(s+2N-1)
+                if (out) {
+                    // output plane y = s: its copies (plane box, P_old, (v dt)^2, and the
+                    // own tile of P at y+2N-1) have arrived once the barrier passes
+                    bool ok = true;
+                    if ((inflight >> st) & 1u) ok = mbar_wait_bounded(&bar[st], (phase_bits >> st) & 1u, kWaitLimit3);
+                    if (__syncthreads_or(!ok)) {
+                        failed = true;
+                        break;
+                    }
+                    phase_bits ^= 1u << st;
+                    inflight &= ~(1u << st);
+                    // every thread is past plane s-1: its stage takes plane s+NS-1
+                    issue(s + NS - 1);
+                    if (act) pin = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kQ) + c0 * TZ + r0);
+                } else if (act && s + 1 < y0) {
+                    pnext = ldc_nc(P + own + (int64_t)(s + NQ) * ldxy);  // the next warm-up step's plane
+                }
+                // queue in: P(s+2N-1)
+#pragma unroll
+                for (int k = 0; k < NQ - 1; ++k)
+#pragma unroll
+                    for (int o = 0; o < RZ; ++o) Pq[k][o] = Pq[k + 1][o];
+#pragma unroll
+                for (int o = 0; o < RZ; ++o) Pq[NQ - 1][o] = pin.v[o];
                 // A_y at plane pa = s+N-1: D+ from P(s .. s+2N-1), phi_y in the y bands
                 {
                     const int pa = s + N - 1;
                     T a[RZ];
 #pragma unroll
                     for (int o = 0; o < RZ; ++o) {
-                        T dd = cc.wy[0] * (Pq[(u + N) % NQ][o] - Pq[(u + N - 1) % NQ][o]);
+                        T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
 #pragma unroll
-                        for (int k = 1; k < N; ++k)
-                            dd = fma(cc.wy[k], Pq[(u + N + k) % NQ][o] - Pq[(u + N - 1 - k) % NQ][o], dd);
+                        for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
                         a[o] = dd;
                     }
                     if (nB > 0 && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
@@ -512,19 +541,7 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                     }
                 }
                 if (!out) continue;
-
-                // ---- output plane y = s ----
                 const int y = s;
-                const int st = (y - y0) % NS;
-                issue(y + NS - 1);
-                bool ok = true;
-                if ((inflight >> st) & 1u) ok = mbar_wait_bounded(&bar[st], (phase_bits >> st) & 1u, kWaitLimit3);
-                if (__syncthreads_or(!ok)) {
-                    failed = true;
-                    break;
-                }
-                phase_bits ^= 1u << st;
-                inflight &= ~(1u << st);
                 const T* Pb = reinterpret_cast<const T*>(smem + st * G::kPlane);
                 if (bz || bx) {
                     band_plane_stage1<T, N>(cc, d, cur, Pb, z0, x0, y, bz, bx, scratch);
@@ -539,8 +556,12 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                         Col<T> ap[N], am[N];
 #pragma unroll
                         for (int k = 0; k < N; ++k) {
-                            ap[k] = Aq[((u + N + 1 + k) % NQ) * NT];
-                            am[k] = Aq[((u + N - k) % NQ) * NT];
+                            int sp = u + N + 1 + k, sm = u + N - k;  // < 3 NQ
+                            sp -= sp >= NQ ? NQ : 0;
+                            sp -= sp >= NQ ? NQ : 0;
+                            sm -= sm >= NQ ? NQ : 0;
+                            ap[k] = Aq[sp * NT];
+                            am[k] = Aq[sm * NT];
                         }
 #pragma unroll
                         for (int o = 0; o < RZ; ++o) {
@@ -575,7 +596,7 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                             for (int o = 0; o < RZ; ++o)
                                 if (d.src_iz[q] == i0 + o) lap[o] += d.src_wavelet[(int64_t)q * d.nt + tau];
                         }
-                    const T* pc = Pq[u % NQ];
+                    const T* pc = Pq[0];
                     const Col<T> po = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kO) + c0 * TZ + r0);
                     const Col<T> vv = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kV) + c0 * TZ + r0);
 #pragma unroll
@@ -596,9 +617,12 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                             if (i0 + o < nz) sn[o] = pn[o];
                     }
                 }
-                __syncthreads();  // plane stage and scratch are reused
             }
         }
+        __syncthreads();  // every thread has read s_item
+        if (tid == 0) s_item = (int)gridDim.x + atomicAdd(next, 1);
+        __syncthreads();
+        k = s_item;
     }
     if (failed) {
         if (tid == 0) {
