@@ -215,6 +215,8 @@ def run_gpu(args):
     fp64_steps = max(1, min(args.steps, args.fp64_steps))
     ms64, ph64, _ = timed_shots("fp64", 1, fp64_steps, 1)
 
+    accuracy = rtm_accuracy(S, dV, dVS, dw, siz, six, nz, nx) if (rank == 0 and not args.no_accuracy) else None
+
     cells = cell_updates(nz, nx, NT)
     value = world * cells / (ms32 * 1e-3) / 1e9
     e2e = world * cells / (ms32_e2e * 1e-3) / 1e9
@@ -253,12 +255,108 @@ def run_gpu(args):
         "phases_ms": {"forward": round(fwd_ms, 2), "reverse+imaging": round(float(np.mean([p[1][0] for p in ph32])), 2),
                       "finish": round(float(np.mean([p[2][0] for p in ph32])), 3)},
     }
+    if accuracy is not None:
+        line["accuracy"] = accuracy
+    if rank == 0 and not args.no_3d:
+        line["fwd3d"] = bench_3d(S, args)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def rtm_accuracy(S, dV, dVS, dw, siz, six, nz, nx):
+    """FP32 (FP16 snapshots every STRIDE steps) against the FP64 drop-in on the
+    full shot: relative L2 of the image and of both seismograms."""
+    import torch
+
+    res = {}
+    for mode, stride in (("fp64", 1), ("fp32", STRIDE)):
+        img = torch.zeros((nx, nz), dtype=torch.float64, device="cuda").T
+        dtrue = torch.zeros((NT, nx), dtype=torch.float64, device="cuda").T
+        dsm = torch.zeros((NT, nx), dtype=torch.float64, device="cuda").T
+        S.api.check(S.api.lib().sssi_rtmTimeCpmlFor2dAw(
+            S.api._addr(dV), S.api._addr(dVS), nz, nx, NT, N_ORDER, NB, DZ, DX, DT, S.api._addr(dw), siz, six, EPS,
+            S.api._mode(mode), stride, S.api._addr(img), S.api._addr(dtrue), S.api._addr(dsm)))
+        res[mode] = (img, dtrue, dsm)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
+
+    return {"image_rel_l2": rel(res["fp32"][0], res["fp64"][0]),
+            "seismogram_rel_l2": rel(res["fp32"][1], res["fp64"][1]),
+            "seismogram_smooth_rel_l2": rel(res["fp32"][2], res["fp64"][2]),
+            "against": "fp64 drop-in on the same shot (the fp64 path matches the reference C-MEX to <= 1e-12)",
+            "bound": 1e-4}
+
+
+def dipping_model_3d(n, seed=20240617):
+    """Seeded 5-layer model with dipping planar interfaces (dip <= 15 degrees in
+    x and y), velocities sorted uniform in [1500, 4500] m/s."""
+    rng = np.random.default_rng(seed)
+    vel = np.sort(rng.uniform(1500.0, 4500.0, 5))
+    depth = np.sort(rng.uniform(0.15, 0.9, 4)) * n
+    dips = np.tan(np.radians(rng.uniform(-15.0, 15.0, (4, 2))))
+    z = np.arange(n)[:, None, None]
+    x = np.arange(n)[None, :, None] - n / 2
+    y = np.arange(n)[None, None, :] - n / 2
+    v = np.full((n, n, n), vel[0])
+    for k in range(4):
+        v = np.where(z >= depth[k] + dips[k, 0] * x + dips[k, 1] * y, vel[k + 1], v)
+    return np.asfortranarray(v)
+
+
+def bench_3d(S, args):
+    """3D forward modelling, 256^3, nt = 2000, N = 4, 16-cell CPML, point source
+    at the surface centre; FP32 timed, receivers (every 2 cells) compared with
+    the FP64 path."""
+    import torch
+
+    n, nt, nb, dt3 = 256, args.nt3d, 16, 8e-4
+    v = dipping_model_3d(n)
+    dv = torch.from_numpy(np.ascontiguousarray(v.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    w = np.ascontiguousarray(ricker(20.0, nt, dt3)[None, :])
+    iz = np.array([0], dtype=np.int64)
+    ix = np.array([n // 2], dtype=np.int64)
+    iy = np.array([n // 2], dtype=np.int64)
+
+    def run(mode, data):
+        S.api.check(S.api.lib().sssi_fwdTimeCpmlFor3dAwPoint(
+            S.api._addr(dv), n, n, n, nt, N_ORDER, nb, 10.0, 10.0, 10.0, dt3, 1, iz.ctypes.data, ix.ctypes.data,
+            iy.ctypes.data, w.ctypes.data, S.api._addr(data), None, S.api._mode(mode)))
+
+    d32 = torch.zeros((nt, n, n), dtype=torch.float64, device="cuda").permute(2, 1, 0)
+    run("fp32", d32)  # warm-up
+    times = []
+    for _ in range(max(1, args.steps3d)):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run("fp32", d32)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    d64 = torch.zeros((nt, n, n), dtype=torch.float64, device="cuda").permute(2, 1, 0)
+    t0 = time.perf_counter()
+    run("fp64", d64)
+    torch.cuda.synchronize()
+    ms64 = (time.perf_counter() - t0) * 1e3
+    a, b = d32[::2, ::2, :], d64[::2, ::2, :]
+    err = float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
+    cells = n ** 3 * nt
+    return {"metric": "Gcell-updates/s (3D forward shot, 256^3, nt=%d)" % nt,
+            "value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_shot": round(ms, 2),
+            "us_per_step": round(ms * 1e3 / nt, 2), "dtype": "fp32", "shots": len(times),
+            "achieved_gbs_alg": round(16.0 * n ** 3 / (ms * 1e-3 / nt) / 1e9, 1),
+            "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "ms_per_shot": round(ms64, 1)},
+            "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (128 x 128)",
+            "config": {"workload": "fwd3d-point-source", "n": n, "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
+                       "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",
+                       "source": "20 Hz Ricker at the surface centre"}}
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -321,6 +419,7 @@ CASES = {
     "step2d-fp32-large": (4096, 4096, 6, "fp32"),
     "step2d-fp64-large": (4096, 4096, 4, "fp64"),
     "step2d-strict-large": (4096, 4096, 3, "fp64-strict"),
+    "step3d-fp32": (256, 256, 6, "fp32"),  # n^3 grid
 }
 
 
@@ -338,6 +437,13 @@ def run_case(name):
         print(f"case {name}: image max {np.abs(img).max():.3e}")
         return
     nz, nx, nt, mode = CASES[name]
+    if name.startswith("step3d"):
+        v = dipping_model_3d(nz)
+        d, _ = S.fwdTimeCpmlFor3dAwPoint(v, nt, [0], [nz // 2], [nz // 2], ricker(20.0, nt, 8e-4)[None, :],
+                                         N_ORDER, 16, 10.0, 10.0, 10.0, 8e-4, mode=mode)
+        torch.cuda.synchronize()
+        print(f"case {name}: {nz}^3 nt={nt} {mode} ok, data max {np.abs(d).max():.3e}")
+        return
     rng = np.random.default_rng(1)
     v = rng.uniform(1500.0, 4000.0, (nz, nx))
     d, _ = S.fwdTimeCpmlFor2dAwPoint(v, nt, [2], [nx // 2], ricker(FREQ, nt, DT)[None, :], N_ORDER, NB, DZ, DX, DT,
@@ -357,6 +463,10 @@ def main():
     ap.add_argument("--cpu-nt", type=int, default=200, help="time steps of the bounded CPU sample")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the fp32-vs-fp64 error report")
+    ap.add_argument("--no-3d", action="store_true", help="skip the 3D forward-modelling line")
+    ap.add_argument("--nt3d", type=int, default=2000)
+    ap.add_argument("--steps3d", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps requested", file=sys.stderr)
