@@ -102,7 +102,7 @@ def test_mex_gateways_export_mexfunction():
     import subprocess
 
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "mexgw"], check=True)
-    for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex"):
+    for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex", "fwdTimeCpmlFor3dAw_mex"):
         gw = ctypes.CDLL(str(ROOT / "oracle" / "_build" / f"mexgw_{name}.so"), mode=ctypes.RTLD_LOCAL)
         assert hasattr(gw, "mexFunction")
 
@@ -114,3 +114,12 @@ def test_mex_gateway_error_message():
     gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeCpmlFor2dAw_mex.so")
     with pytest.raises(O.MexError, match="All 7 input arguments shall be provided!"):
         O.shim_call(gw, 2, np.ones((3, 3)), np.zeros((3, 3, 2)))
+
+
+def test_mex_gateway_3d_error_message():
+    """The 3D gateway: too few arguments is refused before any GPU work."""
+    from oracle import oracle as O
+
+    gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeCpmlFor3dAw_mex.so")
+    with pytest.raises(O.MexError, match="All 8 input arguments shall be provided!"):
+        O.shim_call(gw, 2, np.ones((3, 3, 3)), np.zeros((3, 3, 3, 2)), 2, 1, 10.0, 10.0, 10.0)

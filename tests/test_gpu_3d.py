@@ -99,3 +99,22 @@ def test_fwd3d_errors(gpu):
         S.fwdTimeCpmlFor3dAw(v, src, 2, 5, 10.0, 10.0, 10.0, 1e-3, mode="fp64")  # 2 nB > nx
     with pytest.raises(S.SSSIError):
         S.fwdTimeCpmlFor3dAwPoint(v, 4, [9], [0], [0], np.zeros((1, 4)), 2, 1, 10.0, 10.0, 10.0, 1e-3)
+
+
+def test_fwd3d_mex_gateway(gpu, golden, oracle_mod):
+    """fwdTimeCpmlFor3dAw_mex (built on the test shim) on the golden case: the
+    MATLAB call [data, snapshot] = fwdTimeCpmlFor3dAw(v, source, N, nB, dz, dx, dy, dt)."""
+    import subprocess
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    subprocess.run(["make", "-s", "-C", str(root / "oracle"), "mexgw"], check=True)
+    gw = oracle_mod.load_shim_library(root / "oracle" / "_build" / "mexgw_fwdTimeCpmlFor3dAw_mex.so")
+    g = golden("fwd3d.npz")
+    nz, nx, ny, nt, N, nB = (int(x) for x in g["params"])
+    src = np.zeros((nz, nx, ny, nt), order="F")
+    src[1, nx // 2, ny // 2, :] = g["trace"]
+    data, snap = oracle_mod.shim_call(gw, 2, g["v"], src, N, nB, 10.0, 10.0, 10.0, 1e-3)
+    assert data.shape == (nx, ny, nt) and snap.shape == (nz, nx, ny, nt)
+    assert oracle_mod.rel_l2(data, g["data"]) <= TOL_FP64
+    assert oracle_mod.rel_l2(snap[:, :, :, -1], g["snap_last"]) <= TOL_FP64
