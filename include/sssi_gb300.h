@@ -152,6 +152,89 @@ int sssi_rtmTimeCpmlFor2dAw(const double *v, const double *vs, int64_t nz, int64
                             const double *wavelet, int64_t src_iz, int64_t src_ix, double epsilon, int mode,
                             int snap_stride, double *image, double *data_true, double *data_smooth);
 
+/* ---- batched and served shots: the plan API ----
+ *
+ * The reference runs one shot per MEX call and loops over shots in MATLAB
+ * (applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:156-166,252-275) or
+ * over MPI ranks (applications/rtm_2d_acoustic_mpi/mainRtmTimeCpmlFor2dAwOpenMPI.m:94-113).
+ * A plan keeps many shots resident on one GPU and advances all of them with
+ * one launch per time step: 2D forward-modelling and RTM shots of any grid
+ * size share the batched step kernel, 3D forward shots run alongside.  Shots
+ * are admitted first come first served while their estimated device memory
+ * fits the plan's budget, join the running batch at the next step boundary
+ * (continuous batching) and leave it when they finish, so their memory serves
+ * the next ones.  A worker thread with its own CUDA stream does all GPU work;
+ * submit, poll and wait are safe to call from any host thread.
+ *
+ * Results are identical to the single-shot entry points of the same mode
+ * (the per-cell arithmetic does not depend on which shots share a launch). */
+typedef struct sssi_plan sssi_plan;
+
+#define SSSI_SHOT_FWD2D 0 /* forward modelling: data = top interior row, nx x nt */
+#define SSSI_SHOT_RTM2D 1 /* one RTM shot: image nz x nx (as sssi_rtmTimeCpmlFor2dAw) */
+#define SSSI_SHOT_FWD3D 2 /* 3D forward modelling: data = top interior face, nx x ny x nt */
+
+#define SSSI_SHOT_QUEUED 0
+#define SSSI_SHOT_RUNNING 1
+#define SSSI_SHOT_DONE 2
+#define SSSI_SHOT_FAILED 3
+
+typedef struct {
+    int mode;            /* SSSI_MODE_FP32 or SSSI_MODE_FP64 (FP64_STRICT runs as FP64) */
+    int nDiffOrder;      /* shared by every shot of the plan */
+    double dz, dx, dy;   /* grid spacing shared by every shot (dy: 3D shots) */
+    size_t device_bytes; /* device memory the plan may hold for admitted shots;
+                            0: three quarters of the memory free at creation */
+    int steps_per_round; /* time steps between admissions; 0: 64 */
+} sssi_plan_config;
+
+typedef struct {
+    int kind;              /* SSSI_SHOT_* */
+    const double *v;       /* velocity, nz x nx (x ny), host or device, padded by extBoundary */
+    const double *vs;      /* RTM: migration (smoothed) velocity, nz x nx */
+    int64_t nz, nx, ny, nt; /* ny: 3D only */
+    int nBoundary;
+    double dt;
+    int nsrc;              /* point sources (<= 8); RTM: exactly one */
+    const int64_t *src_iz, *src_ix, *src_iy; /* interior indices; src_iy: 3D only */
+    const double *wavelets; /* nsrc x nt, row s at wavelets + s * nt */
+    double epsilon;        /* RTM: imaging stabiliser */
+    int snap_stride;       /* RTM in FP32 plans: forward field stored every snap_stride steps (0: 4) */
+    double *data;          /* receivers (FWD2D, FWD3D), dataTrue (RTM, may be NULL); host or device */
+    double *image;         /* RTM image, nz x nx; host or device */
+} sssi_shot_desc;
+
+typedef struct {
+    int state;     /* SSSI_SHOT_* state */
+    int status;    /* SSSI_OK, or the SSSI_ERR_* code of a failed shot */
+    double submit_s, start_s, done_s; /* seconds since plan creation (start: admission) */
+    int64_t cell_updates; /* grid cells advanced by one step, summed over the shot's propagations */
+} sssi_shot_info;
+
+typedef struct {
+    int64_t queued, running, done, failed;
+    size_t device_bytes_in_use, device_bytes_budget;
+    int64_t batch_steps;      /* launches of the batched 2D step */
+    double cell_updates;      /* all shots, all propagations */
+} sssi_plan_stats;
+
+/* Creates a plan on the current device.  Native form of the submit/poll/wait
+ * API sketched for the batched and served workloads; no counterpart in the
+ * reference. */
+int sssi_plan_create(const sssi_plan_config *config, sssi_plan **plan);
+/* Shots still queued or running fail with SSSI_ERR_INTERNAL ("plan destroyed"). */
+int sssi_plan_destroy(sssi_plan *plan);
+/* Checks the shot, copies its inputs (v, vs, wavelets, source indices) and
+ * queues it; outputs are written when the shot completes, so data / image
+ * must stay valid until then.  *ticket identifies the shot. */
+int sssi_shot_submit(sssi_plan *plan, const sssi_shot_desc *shot, int64_t *ticket);
+/* Current state of a shot (never blocks). */
+int sssi_poll(sssi_plan *plan, int64_t ticket, sssi_shot_info *info);
+/* Blocks until the shot is done or failed; returns its status (message in
+ * sssi_last_error()).  info may be NULL. */
+int sssi_wait(sssi_plan *plan, int64_t ticket, sssi_shot_info *info);
+int sssi_plan_stats_get(sssi_plan *plan, sssi_plan_stats *stats);
+
 /* ---- forward modelling without any allocation ---- */
 
 /* Size of the fixed working array behind sssi_fwdTimeCpmlFor2dAwNoAlloc. */

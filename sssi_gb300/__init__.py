@@ -7,6 +7,7 @@ the first call loads the library and fails loudly if it is not built.
 """
 from .api import (  # noqa: F401
     MODES,
+    Plan,
     dampPml,
     dCoef,
     enable_timing,

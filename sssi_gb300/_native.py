@@ -18,8 +18,45 @@ _lib: ctypes.CDLL | None = None
 c_i64 = ctypes.c_int64
 c_dp = ctypes.c_void_p  # double* / int64_t* passed as raw addresses (host or device)
 
+
+
+class PlanConfig(ctypes.Structure):
+    """sssi_plan_config"""
+    _fields_ = [("mode", ctypes.c_int), ("nDiffOrder", ctypes.c_int), ("dz", ctypes.c_double),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("device_bytes", ctypes.c_size_t),
+                ("steps_per_round", ctypes.c_int)]
+
+
+class ShotDesc(ctypes.Structure):
+    """sssi_shot_desc"""
+    _fields_ = [("kind", ctypes.c_int), ("v", ctypes.c_void_p), ("vs", ctypes.c_void_p), ("nz", c_i64),
+                ("nx", c_i64), ("ny", c_i64), ("nt", c_i64), ("nBoundary", ctypes.c_int), ("dt", ctypes.c_double),
+                ("nsrc", ctypes.c_int), ("src_iz", ctypes.c_void_p), ("src_ix", ctypes.c_void_p),
+                ("src_iy", ctypes.c_void_p), ("wavelets", ctypes.c_void_p), ("epsilon", ctypes.c_double),
+                ("snap_stride", ctypes.c_int), ("data", ctypes.c_void_p), ("image", ctypes.c_void_p)]
+
+
+class ShotInfo(ctypes.Structure):
+    """sssi_shot_info"""
+    _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("done_s", ctypes.c_double), ("cell_updates", c_i64)]
+
+
+class PlanStats(ctypes.Structure):
+    """sssi_plan_stats"""
+    _fields_ = [("queued", c_i64), ("running", c_i64), ("done", c_i64), ("failed", c_i64),
+                ("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_budget", ctypes.c_size_t),
+                ("batch_steps", c_i64), ("cell_updates", ctypes.c_double)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
+    "sssi_plan_create": (ctypes.c_int, [ctypes.POINTER(PlanConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "sssi_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "sssi_shot_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ShotDesc), ctypes.POINTER(c_i64)]),
+    "sssi_poll": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
+    "sssi_wait": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
+    "sssi_plan_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlanStats)]),
     "sssi_last_error": (ctypes.c_char_p, []),
     "sssi_version": (ctypes.c_int, []),
     "sssi_launch_count": (c_i64, []),

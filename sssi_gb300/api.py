@@ -237,3 +237,143 @@ def release_cache() -> None:
 
 def launch_count() -> int:
     return _native.launch_count()
+
+
+# ---------------------------------------------------------------- plans (batched / served shots)
+SHOT_FWD2D, SHOT_RTM2D, SHOT_FWD3D = 0, 1, 2
+SHOT_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
+
+class Ticket:
+    """A submitted shot: ``id`` for the C ABI, ``outputs`` filled when it completes."""
+
+    def __init__(self, plan, tid, outputs, keep):
+        self.plan = plan
+        self.id = tid
+        self.outputs = outputs
+        self._keep = keep  # inputs and outputs must stay alive until the shot completes
+
+
+class Plan:
+    """Many shots resident on one GPU (``sssi_plan_*``): 2D forward-modelling and
+    RTM shots of any grid size advance together in the batched step kernel,
+    3D shots alongside; shots are admitted first come first served while their
+    device memory fits ``device_bytes`` and leave as they finish.
+
+    Results equal the single-shot functions of the same mode."""
+
+    def __init__(self, nDiffOrder, dz, dx, dy=None, *, mode="fp32", device_bytes=0, steps_per_round=0):
+        from ._native import PlanConfig
+
+        cfg = PlanConfig(_mode(mode), int(nDiffOrder), float(dz), float(dx), float(dy if dy is not None else dx),
+                         int(device_bytes), int(steps_per_round))
+        h = ctypes.c_void_p()
+        check(lib().sssi_plan_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            check(lib().sssi_plan_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _submit(self, desc, outputs, keep):
+        from ._native import c_i64
+
+        t = c_i64()
+        check(lib().sssi_shot_submit(self._h, ctypes.byref(desc), ctypes.byref(t)))
+        return Ticket(self, int(t.value), outputs, keep)
+
+    def submit_fwd2d(self, v, nt, src_iz, src_ix, wavelets, nBoundary, dt):
+        """Forward modelling with point sources; outputs: data (nx x nt)."""
+        from ._native import ShotDesc
+
+        pv, kv, vshape = _in(v, "v")
+        nz, nx = vshape
+        iz, ix, w = _points(src_iz, src_ix, None, wavelets, nt)
+        data, kd = _out_like(v, (nx, nt))
+        d = ShotDesc(kind=SHOT_FWD2D, v=pv, nz=nz, nx=nx, ny=1, nt=int(nt), nBoundary=int(nBoundary), dt=float(dt),
+                     nsrc=len(iz), src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, wavelets=w.ctypes.data,
+                     data=_addr(data))
+        return self._submit(d, {"data": data}, (kv, kd, iz, ix, w, v))
+
+    def submit_rtm2d(self, v, vs, wavelet, src_iz, src_ix, nBoundary, dt, *, epsilon=1e-3, snap_stride=4,
+                     want_data=False):
+        """One RTM shot (as :func:`rtmTimeCpmlFor2dAw`); outputs: image (nz x nx),
+        and dataTrue (nx x nt) with ``want_data``."""
+        from ._native import ShotDesc
+
+        pv, kv, vshape = _in(v, "v")
+        pvs, kvs, _ = _in(vs, "vs")
+        nz, nx = vshape
+        nt = len(np.asarray(wavelet)) if not _is_torch(wavelet) else wavelet.shape[0]
+        iz, ix, w = _points([src_iz], [src_ix], None, np.asarray(wavelet, dtype=np.float64)[None, :], nt)
+        image, ki = _out_like(v, (nz, nx))
+        data, kd = _out_like(v, (nx, nt)) if want_data else (None, None)
+        d = ShotDesc(kind=SHOT_RTM2D, v=pv, vs=pvs, nz=nz, nx=nx, ny=1, nt=int(nt), nBoundary=int(nBoundary),
+                     dt=float(dt), nsrc=1, src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, wavelets=w.ctypes.data,
+                     epsilon=float(epsilon), snap_stride=int(snap_stride), data=_addr(data), image=_addr(image))
+        return self._submit(d, {"image": image, "data": data}, (kv, kvs, ki, kd, iz, ix, w, v, vs))
+
+    def submit_fwd3d(self, v, nt, src_iz, src_ix, src_iy, wavelets, nBoundary, dt):
+        """3D forward modelling with point sources; outputs: data (nx x ny x nt)."""
+        from ._native import ShotDesc
+
+        pv, kv, vshape = _in(v, "v")
+        nz, nx, ny = vshape
+        iz, ix, w = _points(src_iz, src_ix, None, wavelets, nt)
+        iy = np.ascontiguousarray(np.atleast_1d(src_iy), dtype=np.int64)
+        data, kd = _out_like(v, (nx, ny, nt))
+        d = ShotDesc(kind=SHOT_FWD3D, v=pv, nz=nz, nx=nx, ny=ny, nt=int(nt), nBoundary=int(nBoundary), dt=float(dt),
+                     nsrc=len(iz), src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, src_iy=iy.ctypes.data,
+                     wavelets=w.ctypes.data, data=_addr(data))
+        return self._submit(d, {"data": data}, (kv, kd, iz, ix, iy, w, v))
+
+    @staticmethod
+    def _info(info):
+        return {"state": SHOT_STATES.get(info.state, info.state), "status": info.status,
+                "submit_s": info.submit_s, "start_s": info.start_s, "done_s": info.done_s,
+                "cell_updates": int(info.cell_updates)}
+
+    def poll(self, ticket):
+        from ._native import ShotInfo
+
+        info = ShotInfo()
+        check(lib().sssi_poll(self._h, ticket.id, ctypes.byref(info)))
+        return self._info(info)
+
+    def wait(self, ticket):
+        """Blocks until the shot completes; returns its outputs (raises on failure)."""
+        from ._native import ShotInfo
+
+        info = ShotInfo()
+        check(lib().sssi_wait(self._h, ticket.id, ctypes.byref(info)))
+        ticket.info = self._info(info)
+        return ticket.outputs
+
+    def stats(self):
+        from ._native import PlanStats
+
+        st = PlanStats()
+        check(lib().sssi_plan_stats_get(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in PlanStats._fields_}
+
+
+def _points(src_iz, src_ix, src_iy, wavelets, nt):
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or len(ix) != len(iz):
+        raise ValueError("wavelets must be nsrc x nt and the source index arrays of length nsrc")
+    return iz, ix, w

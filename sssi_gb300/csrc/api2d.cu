@@ -77,29 +77,6 @@ __global__ void image_ascending_kernel(const double* f, const double* r, int64_t
     }
 }
 
-// image = (scale*M) / (eps + scale*S2)
-__global__ void image_finish_kernel(const double* m, const double* s2, int64_t n, double scale, double eps,
-                                    double* image) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        image[q] = (scale * m[q]) / (eps + scale * s2[q]);
-}
-
-// Same from compensated FP32 sums (hi + lo).
-__global__ void image_finish_comp_kernel(const float2* m, const float2* s2, int64_t n, double scale, double eps,
-                                         double* image) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const double mm = (double)m[q].x + (double)m[q].y, ss = (double)s2[q].x + (double)s2[q].y;
-        image[q] = (scale * mm) / (eps + scale * ss);
-    }
-}
-
-// out = a - b in T
-template <typename T>
-__global__ void diff_kernel(const T* a, const T* b, T* out, int64_t n) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        out[q] = a[q] - b[q];
-}
-
 template <class Prop>
 void download_padded(const Prop& st, bool previous, double* model, cudaStream_t s) {
     using T = typename Prop::value_type;

@@ -186,5 +186,28 @@ inline int64_t chunk_steps(int64_t nt, int64_t cells) {
 }
 
 
+// image = (scale*M) / (eps + scale*S2)
+static __global__ void image_finish_kernel(const double* m, const double* s2, int64_t n, double scale, double eps,
+                                    double* image) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        image[q] = (scale * m[q]) / (eps + scale * s2[q]);
+}
+
+// Same from compensated FP32 sums (hi + lo).
+static __global__ void image_finish_comp_kernel(const float2* m, const float2* s2, int64_t n, double scale, double eps,
+                                         double* image) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double mm = (double)m[q].x + (double)m[q].y, ss = (double)s2[q].x + (double)s2[q].y;
+        image[q] = (scale * mm) / (eps + scale * ss);
+    }
+}
+
+// out = a - b in T
+template <typename T>
+__global__ void diff_kernel(const T* a, const T* b, T* out, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = a[q] - b[q];
+}
+
 }  // namespace api
 }  // namespace sssi

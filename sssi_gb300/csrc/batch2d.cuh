@@ -95,6 +95,10 @@ class Batch2d {
     ShotTail<T>& shot(int k) { return shots_[k].desc.s; }
     void set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet);
     void enable(int k, bool on) { shots_[k].enabled = on; }
+    // Releases the device state of shot k; its slot is reused by a later add_shot.
+    // The caller must have synchronised the stream past the shot's last step.
+    void remove_shot(int k);
+    int active_shots() const;
     // Zeroes the fields and memory variables of shot k.
     void reset_shot(int k);
     // Assigns the tiles of the enabled shots to CTAs (longest-processing-time
@@ -122,6 +126,7 @@ class Batch2d {
     struct Shot {
         ShotDesc<T> desc{};
         bool enabled = true;
+        bool free = false;  // slot released by remove_shot
         int64_t origin = 0;
         DeviceBuffer P[2], vdt2, zb, zbm1, zphi[2], zpsi, xb, xbm1, xphi[2], xpsi;
     };

@@ -93,8 +93,18 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
     SSSI_REQUIRE(nz < (1LL << 30) && nx < (1LL << 30), SSSI_ERR_ARG, "model too large");
     SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
     using Sh = TileShape<T>;
-    shots_.emplace_back();
-    Shot& S = shots_.back();
+    int slot = -1;
+    for (int q = 0; q < (int)shots_.size(); ++q)
+        if (shots_[q].free) {
+            slot = q;
+            break;
+        }
+    if (slot < 0) {
+        shots_.emplace_back();
+        slot = (int)shots_.size() - 1;
+    }
+    shots_[slot] = Shot{};
+    Shot& S = shots_[slot];
     ShotTail<T>& d = S.desc.s;
     const int HZ = tile_halo_rows(N_);
     constexpr int al = Scalar<T>::kAlign;
@@ -170,9 +180,23 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
     d.nt = nt;
     d.reverse = reverse ? 1 : 0;
     d.stride = 1;
-    const int k = (int)shots_.size() - 1;
-    reset_shot(k);
-    return k;
+    reset_shot(slot);
+    return slot;
+}
+
+template <typename T>
+void Batch2d<T>::remove_shot(int k) {
+    SSSI_REQUIRE(k >= 0 && k < (int)shots_.size() && !shots_[k].free, SSSI_ERR_ARG, "no shot %d", k);
+    shots_[k] = Shot{};  // buffers go back to the pool
+    shots_[k].enabled = false;
+    shots_[k].free = true;
+}
+
+template <typename T>
+int Batch2d<T>::active_shots() const {
+    int n = 0;
+    for (const Shot& S : shots_) n += (!S.free && S.enabled) ? 1 : 0;
+    return n;
 }
 
 template <typename T>

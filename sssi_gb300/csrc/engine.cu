@@ -1,0 +1,630 @@
+// Plans: many shots resident on one GPU, advanced together (continuous
+// batching), admitted by device-memory footprint.  See the plan API in
+// sssi_gb300.h.
+//
+// One worker thread per plan owns a CUDA stream and all device state:
+//   - 2D shots (forward modelling, RTM) live in one Batch2d: every launch of
+//     the batched step advances all of them by one step.  A shot joins at the
+//     batch step at which it is admitted (its t_start) and is removed when its
+//     last step has run, so the tiles of finished shots leave the schedule
+//     and their memory returns to the pool.
+//   - An RTM request is three batch shots, as in the single-shot RTM: forward
+//     in v and in vs over its first nt steps, reverse in v over the next nt
+//     (added at admission, enabled at the phase change, when the FP16 pack of
+//     the last forward step and dataTrue - dataSmooth are computed).
+//   - 3D shots each keep a Prop3d and advance by up to steps_per_round steps
+//     per round.
+// Rounds end at the next event of any 2D shot (a phase change or a shot's
+// end), so events always fall on round boundaries.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
+
+#include "api_util.cuh"
+#include "batch2d.cuh"
+#include "cpml2d.cuh"
+#include "prop3d.cuh"
+
+namespace sssi {
+
+namespace {
+
+using namespace api;
+using Clock = std::chrono::steady_clock;
+
+// Device array of T -> caller array of doubles (host or device).
+template <typename T>
+void deliver(const T* dev, size_t n, double* out, cudaStream_t s) {
+    if (!out || n == 0) return;
+    const bool out_dev = is_device_pointer(out);
+    if (std::is_same<T, double>::value) {
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(out, dev, n * sizeof(double),
+                                        out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    } else if (out_dev) {
+        convert(dev, out, (int64_t)n, s);
+    } else {
+        DeviceBuffer tmp(n * sizeof(double));
+        convert(dev, tmp.as<double>(), (int64_t)n, s);
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(out, tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(s));  // before tmp returns to the pool
+    }
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+}
+
+// Host doubles -> new device array of T.
+template <typename T>
+void upload(DeviceBuffer& buf, const std::vector<double>& h, cudaStream_t s) {
+    buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
+    if (h.empty()) return;
+    std::vector<T> t(h.begin(), h.end());
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), t.data(), sizeof(T) * t.size(), cudaMemcpyHostToDevice, s));
+    SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+struct PlanRequest {
+    int64_t ticket = 0;
+    sssi_shot_desc d{};
+    std::vector<double> v, vs, wav;
+    std::vector<int64_t> iz, ix, iy;
+    int state = SSSI_SHOT_QUEUED;
+    int status = SSSI_OK;
+    std::string msg;
+    double t_submit = 0, t_start = 0, t_done = 0;
+    size_t bytes = 0;
+    int64_t cells = 0;
+};
+using ReqPtr = std::shared_ptr<PlanRequest>;
+
+class EngineBase {
+  public:
+    virtual ~EngineBase() = default;
+    virtual size_t footprint(const PlanRequest& r) const = 0;
+    virtual void admit(const ReqPtr& r) = 0;
+    // Advances every admitted shot; finished requests (done or failed) are
+    // appended to `fin`.  Returns cell-updates performed.
+    virtual double round(std::vector<ReqPtr>& fin) = 0;
+    virtual bool busy() const = 0;
+    virtual void fail_all(std::vector<ReqPtr>& fin, const std::string& why) = 0;
+    virtual int64_t batch_steps() const = 0;
+};
+
+template <typename T>
+class Engine final : public EngineBase {
+    using M = typename MemVar<T>::type;
+    static constexpr bool kF16 = std::is_same<T, float>::value;
+
+    struct Run {
+        ReqPtr r;
+        int kA = -1, kB = -1, kR = -1;
+        int64_t s0 = 0;
+        int phase = 1;
+        DeviceBuffer wav, recA, recB, delta, fsnap, amax, inv, Mb, S2;
+        std::unique_ptr<Prop3d<T>> p3;
+        int64_t done3 = 0;
+    };
+
+  public:
+    Engine(const sssi_plan_config& c, cudaStream_t s)
+        : cfg_(c), s_(s), B_(c.nDiffOrder, c.dz, c.dx, s), rounds_(c.steps_per_round > 0 ? c.steps_per_round : 64) {}
+
+    size_t footprint(const PlanRequest& r) const override {
+        const int N = cfg_.nDiffOrder, L = 2 * N - 1, HZ = tile_halo_rows(N);
+        const size_t ts = sizeof(T), ms = sizeof(M);
+        const int64_t nz = r.d.nz, nx = r.d.nx, ny = r.d.ny, nt = r.d.nt, nB = r.d.nBoundary;
+        auto shot2d = [&]() -> size_t {
+            const int64_t ldp = nz + 2 * std::max(L, HZ) + 2 * TileShape<T>::TZ;
+            const size_t field = ts * (size_t)ldp * (size_t)(nx + 2 * L);
+            const size_t band = (size_t)(nB * nx + nz * 2 * nB);
+            return 3 * field + band * (2 * ts + 3 * ms);
+        };
+        const size_t wav = ts * (size_t)(std::max(r.d.nsrc, 1) * std::max<int64_t>(nt, 1));
+        if (r.d.kind == SSSI_SHOT_FWD2D) return shot2d() + ts * (size_t)(nx * nt) + wav;
+        if (r.d.kind == SSSI_SHOT_RTM2D) {
+            const size_t n = (size_t)(nz * nx);
+            const int stride = kF16 ? (r.d.snap_stride > 0 ? r.d.snap_stride : 4) : 1;
+            const size_t nsnap = (size_t)((nt + stride - 1) / stride);
+            const size_t snaps = kF16 ? 2 * n * nsnap + 8 * nsnap : 8 * n * (size_t)nt;
+            return 3 * shot2d() + 3 * ts * (size_t)(nx * nt) + snaps + 16 * n + wav;
+        }
+        const int64_t vol = (nz + 2 * HZ + 3) * (nx + 2 * L) * (ny + 2 * L);
+        const size_t band3 = (size_t)(nB * nx * ny + nz * 2 * nB * ny + nz * nx * 2 * nB);
+        return 3 * ts * (size_t)vol + 3 * ms * band3 + ts * (size_t)(nx * ny * nt) + wav + 8 * (size_t)(nz * nx * ny);
+    }
+
+    void admit(const ReqPtr& r) override {
+        auto u = std::make_unique<Run>();
+        u->r = r;
+        const sssi_shot_desc& d = r->d;
+        const int64_t nz = d.nz, nx = d.nx, nt = d.nt;
+        upload<T>(u->wav, r->wav, s_);
+        if (d.kind == SSSI_SHOT_FWD3D) {
+            u->p3 = std::make_unique<Prop3d<T>>(r->v.data(), nz, nx, d.ny, cfg_.nDiffOrder, d.nBoundary, cfg_.dz,
+                                                cfg_.dx, cfg_.dy, d.dt, (int)nt, s_);
+            if (d.nsrc)
+                u->p3->set_point_sources(d.nsrc, r->iz.data(), r->ix.data(), r->iy.data(), u->wav.template as<T>());
+            u->recA.allocate(sizeof(T) * std::max<int64_t>(nx * d.ny * nt, 1));
+            u->p3->desc().rec = u->recA.template as<T>();
+            u->p3->sync_desc();
+            r->cells = nz * nx * d.ny * nt;
+            runs3_.push_back(std::move(u));
+            return;
+        }
+        u->s0 = step_;
+        const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
+        if (d.kind == SSSI_SHOT_FWD2D) {
+            u->kA = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
+            B_.set_point_sources(u->kA, d.nsrc, r->iz.data(), r->ix.data(), u->wav.template as<T>());
+            u->recA.allocate(sizeof(T) * ndata);
+            B_.shot(u->kA).rec = u->recA.template as<T>();
+            r->cells = nz * nx * nt;
+        } else {
+            const int64_t n = nz * nx;
+            const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
+            const int64_t nsnap = (nt + stride - 1) / stride;
+            u->kA = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
+            u->kB = B_.add_shot(r->vs.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
+            u->kR = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)(step_ + nt), true);
+            B_.enable(u->kR, false);
+            B_.set_point_sources(u->kA, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
+            B_.set_point_sources(u->kB, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
+            u->recA.allocate(sizeof(T) * ndata);
+            u->recB.allocate(sizeof(T) * ndata);
+            u->delta.allocate(sizeof(T) * ndata);
+            u->Mb.allocate(sizeof(double) * n);
+            u->S2.allocate(sizeof(double) * n);
+            u->Mb.zero(s_);
+            if (kF16) {
+                u->fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
+                u->amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
+                u->amax.zero(s_);
+                u->inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
+                u->S2.zero(s_);
+            } else {
+                u->fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
+                fill(u->S2.template as<double>(), n, d.epsilon, s_);
+            }
+            ShotTail<T>& a = B_.shot(u->kA);
+            a.rec = u->recA.template as<T>();
+            ShotTail<T>& b = B_.shot(u->kB);
+            b.rec = u->recB.template as<T>();
+            if (kF16) {
+                b.stride = stride;
+                b.amax = u->amax.template as<unsigned>();
+                b.pack = u->fsnap.template as<__half>();
+                b.inv_scale = u->inv.template as<float>();
+            } else {
+                b.snap = reinterpret_cast<T*>(u->fsnap.template as<double>());
+                b.snap_t0 = 0;
+            }
+            ShotTail<T>& rr = B_.shot(u->kR);
+            rr.src_row = u->delta.template as<T>();
+            if (kF16) {
+                rr.stride = stride;
+                rr.img_f16 = u->fsnap.template as<__half>();
+                rr.img_inv = u->inv.template as<float>();
+                rr.img_m2 = u->Mb.template as<float2>();
+                rr.img_s22 = u->S2.template as<float2>();
+            } else {
+                rr.img_f64 = u->fsnap.template as<double>();
+                rr.img_m = u->Mb.template as<double>();
+                rr.img_s2 = u->S2.template as<double>();
+            }
+            r->cells = 3 * n * nt;
+        }
+        dirty_ = true;
+        runs2_.push_back(std::move(u));
+    }
+
+    bool busy() const override { return !runs2_.empty() || !runs3_.empty(); }
+    int64_t batch_steps() const override { return launches_; }
+
+    double round(std::vector<ReqPtr>& fin) override {
+        double cells = 0;
+        // ---- 2D batch: up to the next event of any shot
+        finish_2d_events(fin);  // zero-step shots and events due right at admission
+        if (!runs2_.empty()) {
+            int64_t K = rounds_;
+            for (auto& u : runs2_) K = std::min(K, next_event(*u) - step_);
+            K = std::max<int64_t>(K, 1);
+            if (dirty_) {
+                B_.finalize();
+                dirty_ = false;
+            }
+            B_.set_step((int)step_);
+            B_.run((int)K);
+            for (auto& u : runs2_) {
+                const int64_t n = (int64_t)u->r->d.nz * u->r->d.nx;
+                cells += (double)n * K * (u->r->d.kind == SSSI_SHOT_RTM2D && u->phase == 1 ? 2 : 1);
+            }
+            step_ += K;
+            launches_ += K;
+            SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
+            B_.check_errors();
+            finish_2d_events(fin);
+        }
+        // ---- 3D shots
+        for (size_t q = 0; q < runs3_.size();) {
+            Run& u = *runs3_[q];
+            const int64_t nt = u.r->d.nt;
+            const int64_t k = std::min<int64_t>(rounds_, nt - u.done3);
+            if (k > 0) {
+                u.p3->run((int)k);
+                u.done3 += k;
+                cells += (double)u.r->d.nz * u.r->d.nx * u.r->d.ny * k;
+            }
+            if (u.done3 >= nt) {
+                SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
+                u.p3->check_errors();
+                deliver<T>(u.recA.template as<T>(), (size_t)(u.r->d.nx * u.r->d.ny * nt), u.r->d.data, s_);
+                fin.push_back(u.r);
+                runs3_.erase(runs3_.begin() + q);
+                continue;
+            }
+            ++q;
+        }
+        return cells;
+    }
+
+    void fail_all(std::vector<ReqPtr>& fin, const std::string& why) override {
+        cudaStreamSynchronize(s_);
+        for (auto& u : runs2_) {
+            u->r->status = SSSI_ERR_INTERNAL;
+            u->r->msg = why;
+            fin.push_back(u->r);
+            const int ks[3] = {u->kA, u->kB, u->kR};
+            for (int k : ks)
+                if (k >= 0) B_.remove_shot(k);
+        }
+        for (auto& u : runs3_) {
+            u->r->status = SSSI_ERR_INTERNAL;
+            u->r->msg = why;
+            fin.push_back(u->r);
+        }
+        runs2_.clear();
+        runs3_.clear();
+        dirty_ = true;
+    }
+
+  private:
+    int64_t next_event(const Run& u) const {
+        const int64_t nt = u.r->d.nt;
+        if (u.r->d.kind == SSSI_SHOT_RTM2D) return u.s0 + (u.phase == 1 ? nt : 2 * nt);
+        return u.s0 + nt;
+    }
+
+    void finish_2d_events(std::vector<ReqPtr>& fin) {
+        for (size_t q = 0; q < runs2_.size();) {
+            Run& u = *runs2_[q];
+            if (step_ < next_event(u)) {
+                ++q;
+                continue;
+            }
+            const sssi_shot_desc& d = u.r->d;
+            const int64_t nz = d.nz, nx = d.nx, nt = d.nt, n = nz * nx;
+            if (d.kind == SSSI_SHOT_FWD2D) {
+                deliver<T>(u.recA.template as<T>(), (size_t)(nx * nt), d.data, s_);
+                B_.remove_shot(u.kA);
+            } else if (u.phase == 1) {
+                // forward phase done: FP16 pack of the last forward step, residual data
+                const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
+                if (kF16 && nt >= 1 && (nt - 1) % stride == 0) {
+                    const int64_t k = (nt - 1) / stride;
+                    launch_pack_f16(reinterpret_cast<const float*>(B_.current_field(u.kB)), B_.ldp(u.kB), (int)nz,
+                                    (int)nx, u.amax.template as<unsigned>() + k, u.fsnap.template as<__half>() + k * n,
+                                    u.inv.template as<float>() + k, s_);
+                }
+                if (nt > 0) {
+                    diff_kernel<T><<<152 * 4, 256, 0, s_>>>(u.recA.template as<T>(), u.recB.template as<T>(),
+                                                            u.delta.template as<T>(), nx * nt);
+                    count_launch();
+                    SSSI_CHECK_CUDA(cudaGetLastError());
+                }
+                SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
+                B_.remove_shot(u.kA);
+                B_.remove_shot(u.kB);
+                u.kA = u.kB = -1;
+                B_.enable(u.kR, true);
+                u.phase = 2;
+                dirty_ = true;
+                ++q;  // its reverse phase ends nt steps later
+                continue;
+            } else {
+                DeviceBuffer img(sizeof(double) * std::max<int64_t>(n, 1));
+                const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
+                if (kF16)
+                    image_finish_comp_kernel<<<152 * 4, 256, 0, s_>>>(u.Mb.template as<float2>(),
+                                                                       u.S2.template as<float2>(), n, (double)stride,
+                                                                       d.epsilon, img.as<double>());
+                else
+                    image_finish_kernel<<<152 * 4, 256, 0, s_>>>(u.Mb.template as<double>(), u.S2.template as<double>(),
+                                                                  n, 1.0, 0.0, img.as<double>());
+                count_launch();
+                SSSI_CHECK_CUDA(cudaGetLastError());
+                deliver<double>(img.as<double>(), (size_t)n, d.image, s_);
+                if (d.data) deliver<T>(u.recA.template as<T>(), (size_t)(nx * nt), d.data, s_);
+                B_.remove_shot(u.kR);
+            }
+            fin.push_back(u.r);
+            runs2_.erase(runs2_.begin() + q);
+            dirty_ = true;
+        }
+    }
+
+    sssi_plan_config cfg_;
+    cudaStream_t s_;
+    Batch2d<T> B_;
+    int64_t rounds_;
+    int64_t step_ = 0, launches_ = 0;
+    bool dirty_ = true;
+    std::vector<std::unique_ptr<Run>> runs2_, runs3_;
+};
+
+}  // namespace sssi
+
+struct sssi_plan {
+    sssi_plan_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    sssi::Clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<sssi::ReqPtr> queue;
+    std::map<int64_t, sssi::ReqPtr> tickets;
+    int64_t next_ticket = 1;
+    size_t budget = 0, in_use = 0;
+    int64_t n_running = 0, n_done = 0, n_failed = 0, batch_steps = 0;
+    double cells = 0;
+    bool stop = false;
+    int fatal = SSSI_OK;
+    std::string fatal_msg;
+    std::unique_ptr<sssi::EngineBase> engine;
+    std::thread worker;
+
+    double now() const { return std::chrono::duration<double>(sssi::Clock::now() - t0).count(); }
+
+    void finish(std::vector<sssi::ReqPtr>& fin) {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto& r : fin) {
+            r->t_done = now();
+            r->state = r->status == SSSI_OK ? SSSI_SHOT_DONE : SSSI_SHOT_FAILED;
+            in_use -= std::min(in_use, r->bytes);
+            --n_running;
+            (r->status == SSSI_OK ? n_done : n_failed) += 1;
+        }
+        fin.clear();
+        cv_done.notify_all();
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        std::vector<sssi::ReqPtr> fin;
+        while (true) {
+            std::vector<sssi::ReqPtr> admit;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_work.wait(lk, [&] { return stop || !queue.empty() || engine->busy(); });
+                if (stop) break;
+                // first come first served while the footprint fits; a shot larger than
+                // the whole budget runs alone
+                while (!queue.empty()) {
+                    sssi::ReqPtr& r = queue.front();
+                    const bool alone = in_use == 0 && admit.empty();
+                    if (!alone && in_use + r->bytes > budget) break;
+                    in_use += r->bytes;
+                    r->state = SSSI_SHOT_RUNNING;
+                    r->t_start = now();
+                    ++n_running;
+                    admit.push_back(r);
+                    queue.pop_front();
+                }
+            }
+            for (auto& r : admit) {
+                sssi::clear_error();
+                try {
+                    engine->admit(r);
+                } catch (const sssi::Error& e) {
+                    r->status = e.code;
+                    r->msg = sssi_last_error();
+                    fin.push_back(r);
+                } catch (const std::bad_alloc&) {
+                    r->status = SSSI_ERR_NOMEM;
+                    r->msg = "host allocation failed";
+                    fin.push_back(r);
+                } catch (...) {
+                    r->status = SSSI_ERR_INTERNAL;
+                    r->msg = "unexpected exception while admitting the shot";
+                    fin.push_back(r);
+                }
+            }
+            if (!fin.empty()) finish(fin);
+            try {
+                const double c = engine->round(fin);
+                std::lock_guard<std::mutex> lk(mu);
+                cells += c;
+                batch_steps = engine->batch_steps();
+            } catch (const sssi::Error&) {
+                // a kernel or copy failed: every admitted shot shares the failure
+                engine->fail_all(fin, std::string("batch step failed: ") + sssi_last_error());
+            } catch (...) {
+                engine->fail_all(fin, "batch step failed: unexpected exception");
+            }
+            if (!fin.empty()) finish(fin);
+        }
+        // plan destroyed: fail what is left
+        engine->fail_all(fin, "plan destroyed");
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (auto& r : queue) {
+                r->status = SSSI_ERR_INTERNAL;
+                r->msg = "plan destroyed";
+                r->state = SSSI_SHOT_FAILED;
+                ++n_failed;
+            }
+            queue.clear();
+        }
+        finish(fin);
+        engine.reset();
+        cudaStreamSynchronize(stream);
+    }
+};
+
+namespace {
+
+using namespace sssi;
+
+void fill_info(const PlanRequest& r, sssi_shot_info* info) {
+    if (!info) return;
+    info->state = r.state;
+    info->status = r.status;
+    info->submit_s = r.t_submit;
+    info->start_s = r.t_start;
+    info->done_s = r.t_done;
+    info->cell_updates = r.cells;
+}
+
+}  // namespace
+
+extern "C" int sssi_plan_create(const sssi_plan_config* config, sssi_plan** plan) {
+    return guarded([&] {
+        SSSI_REQUIRE(config && plan, SSSI_ERR_ARG, "config and plan must not be NULL");
+        const sssi_plan_config& c = *config;
+        SSSI_REQUIRE(c.mode == SSSI_MODE_FP32 || c.mode == SSSI_MODE_FP64 || c.mode == SSSI_MODE_FP64_STRICT,
+                     SSSI_ERR_ARG, "unknown mode %d", c.mode);
+        SSSI_REQUIRE(c.nDiffOrder >= 1 && c.nDiffOrder <= kMaxOrder, SSSI_ERR_ARG, "nDiffOrder must be in 1..%d",
+                     kMaxOrder);
+        SSSI_REQUIRE(c.dz > 0 && c.dx > 0 && c.dy >= 0, SSSI_ERR_ARG, "dz and dx must be positive, dy >= 0");
+        ensure_device();
+        auto p = std::make_unique<sssi_plan>();
+        p->cfg = c;
+        if (p->cfg.mode == SSSI_MODE_FP64_STRICT) p->cfg.mode = SSSI_MODE_FP64;
+        if (p->cfg.dy <= 0) p->cfg.dy = p->cfg.dx;
+        SSSI_CHECK_CUDA(cudaGetDevice(&p->device));
+        size_t free_b = 0, total_b = 0;
+        SSSI_CHECK_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        p->budget = c.device_bytes ? c.device_bytes : free_b / 4 * 3;
+        SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+        p->t0 = Clock::now();
+        if (p->cfg.mode == SSSI_MODE_FP32)
+            p->engine = std::make_unique<Engine<float>>(p->cfg, p->stream);
+        else
+            p->engine = std::make_unique<Engine<double>>(p->cfg, p->stream);
+        sssi_plan* raw = p.release();
+        raw->worker = std::thread([raw] { raw->run(); });
+        *plan = raw;
+    });
+}
+
+extern "C" int sssi_plan_destroy(sssi_plan* plan) {
+    return guarded([&] {
+        if (!plan) return;
+        {
+            std::lock_guard<std::mutex> lk(plan->mu);
+            plan->stop = true;
+        }
+        plan->cv_work.notify_all();
+        if (plan->worker.joinable()) plan->worker.join();
+        cudaStreamDestroy(plan->stream);
+        delete plan;
+    });
+}
+
+extern "C" int sssi_shot_submit(sssi_plan* plan, const sssi_shot_desc* shot, int64_t* ticket) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan && shot && ticket, SSSI_ERR_ARG, "plan, shot and ticket must not be NULL");
+        const sssi_shot_desc& d = *shot;
+        SSSI_REQUIRE(d.kind == SSSI_SHOT_FWD2D || d.kind == SSSI_SHOT_RTM2D || d.kind == SSSI_SHOT_FWD3D,
+                     SSSI_ERR_ARG, "unknown shot kind %d", d.kind);
+        const bool is3 = d.kind == SSSI_SHOT_FWD3D;
+        SSSI_REQUIRE(d.v && d.nz > 0 && d.nx > 0 && d.nt >= 0 && (!is3 || d.ny > 0), SSSI_ERR_ARG,
+                     "bad shot sizes nz=%lld nx=%lld ny=%lld nt=%lld", (long long)d.nz, (long long)d.nx,
+                     (long long)d.ny, (long long)d.nt);
+        SSSI_REQUIRE(d.nBoundary >= 0 && d.nBoundary <= d.nz && 2 * (int64_t)d.nBoundary <= d.nx &&
+                         (!is3 || 2 * (int64_t)d.nBoundary <= d.ny),
+                     SSSI_ERR_ARG, "nBoundary %d does not fit the grid", d.nBoundary);
+        SSSI_REQUIRE(d.dt > 0, SSSI_ERR_ARG, "dt must be positive");
+        SSSI_REQUIRE(d.nt < (1LL << 30), SSSI_ERR_ARG, "nt too large");
+        SSSI_REQUIRE(d.nsrc >= 0 && d.nsrc <= kMaxPointSources, SSSI_ERR_ARG, "nsrc must be in 0..%d", kMaxPointSources);
+        SSSI_REQUIRE(d.nsrc == 0 || (d.src_iz && d.src_ix && d.wavelets && (!is3 || d.src_iy)), SSSI_ERR_ARG,
+                     "point-source arrays are NULL");
+        for (int s = 0; s < d.nsrc; ++s)
+            SSSI_REQUIRE(d.src_iz[s] >= 0 && d.src_iz[s] < d.nz && d.src_ix[s] >= 0 && d.src_ix[s] < d.nx &&
+                             (!is3 || (d.src_iy[s] >= 0 && d.src_iy[s] < d.ny)),
+                         SSSI_ERR_ARG, "point source %d outside the grid", s);
+        if (d.kind == SSSI_SHOT_RTM2D) {
+            SSSI_REQUIRE(d.vs && d.image, SSSI_ERR_ARG, "RTM needs vs and image");
+            SSSI_REQUIRE(d.nsrc == 1, SSSI_ERR_ARG, "RTM takes exactly one point source");
+            SSSI_REQUIRE(d.snap_stride >= 0, SSSI_ERR_ARG, "snap_stride must be >= 0");
+        }
+        auto r = std::make_shared<PlanRequest>();
+        r->d = d;
+        const size_t n = (size_t)(d.nz * d.nx * (is3 ? d.ny : 1));
+        r->v = api::host_copy(d.v, n, cudaStreamLegacy);
+        if (d.kind == SSSI_SHOT_RTM2D) r->vs = api::host_copy(d.vs, n, cudaStreamLegacy);
+        if (d.nsrc) r->wav = api::host_copy(d.wavelets, (size_t)(d.nsrc * d.nt), cudaStreamLegacy);
+        r->iz.assign(d.src_iz, d.src_iz + d.nsrc);
+        r->ix.assign(d.src_ix, d.src_ix + d.nsrc);
+        if (is3) r->iy.assign(d.src_iy, d.src_iy + d.nsrc);
+        r->d.v = r->d.vs = r->d.wavelets = nullptr;  // the copies are used from here on
+        r->d.src_iz = r->d.src_ix = r->d.src_iy = nullptr;
+        r->bytes = plan->engine->footprint(*r);
+        {
+            std::lock_guard<std::mutex> lk(plan->mu);
+            SSSI_REQUIRE(!plan->stop, SSSI_ERR_ARG, "plan is being destroyed");
+            r->ticket = plan->next_ticket++;
+            r->t_submit = plan->now();
+            plan->tickets[r->ticket] = r;
+            plan->queue.push_back(r);
+            *ticket = r->ticket;
+        }
+        plan->cv_work.notify_all();
+    });
+}
+
+extern "C" int sssi_poll(sssi_plan* plan, int64_t ticket, sssi_shot_info* info) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan, SSSI_ERR_ARG, "plan is NULL");
+        std::lock_guard<std::mutex> lk(plan->mu);
+        auto it = plan->tickets.find(ticket);
+        SSSI_REQUIRE(it != plan->tickets.end(), SSSI_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+        fill_info(*it->second, info);
+    });
+}
+
+extern "C" int sssi_wait(sssi_plan* plan, int64_t ticket, sssi_shot_info* info) {
+    int status = SSSI_OK;
+    std::string msg;
+    const int rc = guarded([&] {
+        SSSI_REQUIRE(plan, SSSI_ERR_ARG, "plan is NULL");
+        std::unique_lock<std::mutex> lk(plan->mu);
+        auto it = plan->tickets.find(ticket);
+        SSSI_REQUIRE(it != plan->tickets.end(), SSSI_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+        ReqPtr r = it->second;
+        plan->cv_done.wait(lk, [&] { return r->state == SSSI_SHOT_DONE || r->state == SSSI_SHOT_FAILED; });
+        fill_info(*r, info);
+        status = r->status;
+        msg = r->msg;
+    });
+    if (rc != SSSI_OK) return rc;
+    if (status != SSSI_OK) set_error("shot %lld failed: %s", (long long)ticket, msg.c_str());
+    return status;
+}
+
+extern "C" int sssi_plan_stats_get(sssi_plan* plan, sssi_plan_stats* stats) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan && stats, SSSI_ERR_ARG, "plan and stats must not be NULL");
+        std::lock_guard<std::mutex> lk(plan->mu);
+        stats->queued = (int64_t)plan->queue.size();
+        stats->running = plan->n_running;
+        stats->done = plan->n_done;
+        stats->failed = plan->n_failed;
+        stats->device_bytes_in_use = plan->in_use;
+        stats->device_bytes_budget = plan->budget;
+        stats->batch_steps = plan->batch_steps;
+        stats->cell_updates = plan->cells;
+    });
+}
