@@ -259,6 +259,10 @@ def run_gpu(args):
         line["accuracy"] = accuracy
     if rank == 0 and not args.no_3d:
         line["fwd3d"] = bench_3d(S, args)
+    if rank == 0 and not args.no_batch:
+        line["batch2d"] = bench_batch(S, args)
+    if rank == 0 and not args.no_serve:
+        line["serve"] = bench_serve(S, args)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -357,6 +361,191 @@ def bench_3d(S, args):
             "config": {"workload": "fwd3d-point-source", "n": n, "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
                        "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",
                        "source": "20 Hz Ricker at the surface centre"}}
+
+
+# ---------------------------------------------------------------- batched and served shots (plan API)
+def model_2d_anomalies(nz, nx, seed):
+    """Seeded 6-layer model (flat interfaces, velocities sorted uniform) with 3
+    Gaussian anomalies of +-15 %, clipped to [1500, 4500] m/s."""
+    rng = np.random.default_rng(seed)
+    depths = np.sort(rng.choice(np.arange(30, nz - 20), 5, replace=False))
+    vel = np.sort(rng.uniform(1500.0, 4200.0, 6))
+    v = np.empty((nz, nx))
+    edges = [0, *depths, nz]
+    for k in range(6):
+        v[edges[k]:edges[k + 1], :] = vel[k]
+    z = np.arange(nz)[:, None]
+    x = np.arange(nx)[None, :]
+    for _ in range(3):
+        cz, cx = rng.uniform(0.2, 0.8) * nz, rng.uniform(0.1, 0.9) * nx
+        r = rng.uniform(0.05, 0.12) * min(nz, nx)
+        v = v * (1 + rng.choice([-0.15, 0.15]) * np.exp(-((z - cz) ** 2 + (x - cx) ** 2) / (2 * r * r)))
+    return np.clip(v, 1500.0, 4500.0)
+
+
+def batch_shots(seed=20240702):
+    """64 shots on an 800 x 2400 model: sources every 35 cells at the surface,
+    each shot on an aperture window of w ~ U[600, 2400] columns around its
+    source (clipped to the model), nt ~ U[2000, 4000]."""
+    nz0, nx0 = 800, 2400
+    v = model_2d_anomalies(nz0, nx0, seed)
+    rng = np.random.default_rng(seed + 1)
+    shots = []
+    for k in range(64):
+        xs = 20 + 35 * k
+        w = int(rng.integers(600, 2401))
+        a = max(0, xs - w // 2)
+        b = min(nx0, a + w)
+        a = max(0, b - w)
+        nt = int(rng.integers(2000, 4001))
+        shots.append((np.asfortranarray(ext_boundary(v[:, a:b], NB)), nt, 0, xs - a + NB))
+    return shots
+
+
+def bench_batch(S, args):
+    """The 64 shots submitted at once to a plan (FP32), timed end to end with
+    host models in and host seismograms out; beside it the same shots' rate
+    through the single-shot entry point, and the FP32 error against FP64."""
+    dt = 8e-4
+    shots = batch_shots()
+    waves = [ricker(20.0, nt, dt)[None, :] for (_, nt, _, _) in shots]
+    cells = float(sum(V.shape[0] * V.shape[1] * nt for (V, nt, _, _) in shots))
+    with S.Plan(N_ORDER, DZ, DX, mode="fp32") as plan:
+        V, nt, iz, ix = shots[0]
+        plan.wait(plan.submit_fwd2d(V, 200, [iz], [ix], waves[0][:, :200], NB, dt))  # warm-up
+        t0 = time.perf_counter()
+        tickets = [plan.submit_fwd2d(V, nt, [iz], [ix], w, NB, dt) for (V, nt, iz, ix), w in zip(shots, waves)]
+        outs = [plan.wait(t)["data"] for t in tickets]
+        el = time.perf_counter() - t0
+        st = plan.stats()
+    # the same kind of shots one call at a time
+    sample = list(range(0, 64, 8))
+    t0 = time.perf_counter()
+    for k in sample:
+        V, nt, iz, ix = shots[k]
+        S.fwdTimeCpmlFor2dAwPoint(V, nt, [iz], [ix], waves[k], N_ORDER, NB, DZ, DX, dt, mode="fp32")
+    el1 = time.perf_counter() - t0
+    cells1 = float(sum(shots[k][0].shape[0] * shots[k][0].shape[1] * shots[k][1] for k in sample))
+    errs = []
+    for k in sample[:2]:
+        V, nt, iz, ix = shots[k]
+        ref, _ = S.fwdTimeCpmlFor2dAwPoint(V, nt, [iz], [ix], waves[k], N_ORDER, NB, DZ, DX, dt, mode="fp64")
+        errs.append(float(np.linalg.norm(outs[k] - ref) / np.linalg.norm(ref)))
+    value = cells / el / 1e9
+    single = cells1 / el1 / 1e9
+    return {"metric": "Gcell-updates/s (64-shot batched forward modelling, 800x2400 model)",
+            "value": round(value, 2), "unit": UNIT, "wall_s": round(el, 3), "shots_per_s": round(64 / el, 2),
+            "cell_updates": cells, "dtype": "fp32", "batch_steps": int(st["batch_steps"]),
+            "single_shot_value": round(single, 2), "speedup_vs_single_shot": round(value / single, 2),
+            "single_shot_sample": "8 of the 64 shots, one sssi_fwdTimeCpmlFor2dAwPoint call each",
+            "data_rel_l2_vs_fp64_max": max(errs), "error_sample": "2 shots against the fp64 path",
+            "e2e": "host models in, host seismograms (double) out, inside the timed region",
+            "config": {"workload": "batched-fwd2d", "model": "800x2400, 6 layers + 3 Gaussian anomalies (+-15%)",
+                       "shots": 64, "aperture": "U[600, 2400] columns", "nt": "U[2000, 4000]", "dt": dt,
+                       "nDiffOrder": N_ORDER, "nBoundary": NB, "source": "20 Hz Ricker, every 35 cells"}}
+
+
+def bench_serve(S, args):
+    """A seeded Poisson stream of requests served by one FP32 plan: 2D forward
+    modelling (200x300 .. 1000x3000), 2D RTM with FP16 snapshots (400x800 ..
+    800x2400), 3D forward modelling (128^3 .. 256^3), nt in [1000, 4000]."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(20240801)
+    n_req, rate = args.serve_requests, args.serve_rate
+    big2d = model_2d_anomalies(1000, 3000, 7)
+    smooth2d = gaussian_filter(big2d, sigma=15, mode="nearest")
+    big3d = dipping_model_3d(256, seed=99)
+    reqs = []
+    t = 0.0
+    for k in range(n_req):
+        t += rng.exponential(1.0 / rate)
+        kind = rng.choice(["fwd2d", "rtm2d", "fwd3d"], p=[0.45, 0.35, 0.20])
+        nt = int(rng.integers(1000, 4001))
+        if kind == "fwd2d":
+            nz, nx = int(rng.integers(200, 1001)), int(rng.integers(300, 3001))
+        elif kind == "rtm2d":
+            nz, nx = int(rng.integers(400, 801)), int(rng.integers(800, 2401))
+        else:
+            nz = nx = int(rng.integers(128, 257))
+        z0 = int(rng.integers(0, (1000 if kind != "fwd3d" else 256) - nz + 1))
+        x0 = int(rng.integers(0, (3000 if kind != "fwd3d" else 256) - nx + 1))
+        reqs.append((t, kind, nz, nx, nt, z0, x0))
+    # outputs: a pinned sink per kind (requests overwrite it in turn), own arrays for the checked sample
+    check = set(int(k) for k in rng.choice(n_req, 8, replace=False))
+
+    def sink(n):
+        return torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+
+    sinks = {"fwd2d": sink(3000 * 4000), "rtm2d": sink(800 * 2400), "fwd3d": sink(256 * 256 * 4000)}
+
+    def view(kind, shape, own):
+        n = int(np.prod(shape))
+        return np.zeros(shape, order="F") if own else sinks[kind][:n].reshape(shape, order="F")
+
+    tickets, inputs = [], {}
+    dt = 8e-4
+    with S.Plan(N_ORDER, DZ, DX, DX, mode="fp32", device_bytes=64 << 30) as plan:
+        plan.wait(plan.submit_fwd2d(np.asfortranarray(big2d[:200, :300]), 100, [0], [150],
+                                    ricker(20.0, 100, dt)[None, :], NB, dt))  # warm-up
+        t_start = time.perf_counter()
+        for k, (ta, kind, nz, nx, nt, z0, x0) in enumerate(reqs):
+            delay = ta - (time.perf_counter() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            w = ricker(20.0 if kind != "rtm2d" else 15.0, nt, dt)
+            own = k in check
+            if kind == "fwd2d":
+                v = np.asfortranarray(big2d[z0:z0 + nz, x0:x0 + nx])
+                tk = plan.submit_fwd2d(v, nt, [0], [nx // 2], w[None, :], NB, dt, data=view(kind, (nx, nt), own))
+            elif kind == "rtm2d":
+                v = np.asfortranarray(big2d[z0:z0 + nz, x0:x0 + nx])
+                vs = np.asfortranarray(smooth2d[z0:z0 + nz, x0:x0 + nx])
+                tk = plan.submit_rtm2d(v, vs, w, 0, nx // 2, NB, dt, epsilon=EPS, snap_stride=STRIDE,
+                                       image=view(kind, (nz, nx), own))
+            else:
+                v = np.asfortranarray(big3d[z0:z0 + nz, x0:x0 + nx, :nx])
+                tk = plan.submit_fwd3d(v, nt, [0], [nx // 2], [nx // 2], w[None, :], 16, dt,
+                                       data=view(kind, (nx, nx, nt), own))
+            tickets.append(tk)
+            if own:
+                inputs[k] = (kind, v, vs if kind == "rtm2d" else None, w, nt)
+        for tk in tickets:
+            plan.wait(tk)
+        st = plan.stats()
+    infos = [tk.info for tk in tickets]
+    lat = np.array([i["done_s"] - i["submit_s"] for i in infos])
+    span = max(i["done_s"] for i in infos) - min(i["submit_s"] for i in infos)
+    cells = float(sum(i["cell_updates"] for i in infos))
+    errs = {}
+    for k, (kind, v, vs, w, nt) in sorted(inputs.items()):
+        if kind == "fwd2d":
+            ref, _ = S.fwdTimeCpmlFor2dAwPoint(v, nt, [0], [v.shape[1] // 2], w[None, :], N_ORDER, NB, DZ, DX, dt,
+                                               mode="fp64")
+            got = tickets[k].outputs["data"]
+        elif kind == "rtm2d":
+            ref = S.rtmTimeCpmlFor2dAw(v, vs, w, 0, v.shape[1] // 2, N_ORDER, NB, DZ, DX, dt, epsilon=EPS,
+                                       mode="fp64")
+            got = tickets[k].outputs["image"]
+        else:
+            n = v.shape[1]
+            ref, _ = S.fwdTimeCpmlFor3dAwPoint(v, nt, [0], [n // 2], [n // 2], w[None, :], N_ORDER, 16, DZ, DX, DX,
+                                               dt, mode="fp64")
+            got = tickets[k].outputs["data"]
+        errs[f"{k}:{kind}"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    kinds = [r[1] for r in reqs]
+    return {"metric": "served shots/s (Poisson stream of %d mixed requests)" % n_req,
+            "value": round(n_req / span, 3), "unit": "shots/s", "p50_latency_s": round(float(np.percentile(lat, 50)), 3),
+            "p99_latency_s": round(float(np.percentile(lat, 99)), 3), "mean_latency_s": round(float(lat.mean()), 3),
+            "gcell_updates_per_s": round(cells / span / 1e9, 2), "span_s": round(span, 2),
+            "offered_rate_per_s": rate, "requests": {k: kinds.count(k) for k in ("fwd2d", "rtm2d", "fwd3d")},
+            "rel_l2_vs_fp64": errs, "rel_l2_vs_fp64_max": max(errs.values()) if errs else None,
+            "admission_budget_bytes": int(st["device_bytes_budget"]), "failed": int(st["failed"]), "dtype": "fp32",
+            "config": {"workload": "serve-mixed", "fwd2d": "200x300 .. 1000x3000", "rtm2d": "400x800 .. 800x2400, "
+                       "fp16 snapshots every 4 steps", "fwd3d": "128^3 .. 256^3, nB 16", "nt": "U[1000, 4000]",
+                       "dt": dt, "arrivals": "Poisson, seeded", "models": "cut from a seeded layered+anomaly 2D "
+                       "model (1000x3000) and a seeded dipping-layer 3D model (256^3)"}}
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -467,6 +656,10 @@ def main():
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D forward-modelling line")
     ap.add_argument("--nt3d", type=int, default=2000)
     ap.add_argument("--steps3d", type=int, default=2)
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-shot batched line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-stream line")
+    ap.add_argument("--serve-requests", type=int, default=500)
+    ap.add_argument("--serve-rate", type=float, default=10.0, help="mean arrivals per second")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps requested", file=sys.stderr)

@@ -295,21 +295,22 @@ class Plan:
         check(lib().sssi_shot_submit(self._h, ctypes.byref(desc), ctypes.byref(t)))
         return Ticket(self, int(t.value), outputs, keep)
 
-    def submit_fwd2d(self, v, nt, src_iz, src_ix, wavelets, nBoundary, dt):
-        """Forward modelling with point sources; outputs: data (nx x nt)."""
+    def submit_fwd2d(self, v, nt, src_iz, src_ix, wavelets, nBoundary, dt, *, data=None):
+        """Forward modelling with point sources; outputs: data (nx x nt), into
+        ``data`` when given (a column-major float64 array, host or device)."""
         from ._native import ShotDesc
 
         pv, kv, vshape = _in(v, "v")
         nz, nx = vshape
         iz, ix, w = _points(src_iz, src_ix, None, wavelets, nt)
-        data, kd = _out_like(v, (nx, nt))
+        data, kd = _out_like(v, (nx, nt)) if data is None else (data, None)
         d = ShotDesc(kind=SHOT_FWD2D, v=pv, nz=nz, nx=nx, ny=1, nt=int(nt), nBoundary=int(nBoundary), dt=float(dt),
                      nsrc=len(iz), src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, wavelets=w.ctypes.data,
                      data=_addr(data))
         return self._submit(d, {"data": data}, (kv, kd, iz, ix, w, v))
 
     def submit_rtm2d(self, v, vs, wavelet, src_iz, src_ix, nBoundary, dt, *, epsilon=1e-3, snap_stride=4,
-                     want_data=False):
+                     want_data=False, image=None):
         """One RTM shot (as :func:`rtmTimeCpmlFor2dAw`); outputs: image (nz x nx),
         and dataTrue (nx x nt) with ``want_data``."""
         from ._native import ShotDesc
@@ -319,14 +320,14 @@ class Plan:
         nz, nx = vshape
         nt = len(np.asarray(wavelet)) if not _is_torch(wavelet) else wavelet.shape[0]
         iz, ix, w = _points([src_iz], [src_ix], None, np.asarray(wavelet, dtype=np.float64)[None, :], nt)
-        image, ki = _out_like(v, (nz, nx))
+        image, ki = _out_like(v, (nz, nx)) if image is None else (image, None)
         data, kd = _out_like(v, (nx, nt)) if want_data else (None, None)
         d = ShotDesc(kind=SHOT_RTM2D, v=pv, vs=pvs, nz=nz, nx=nx, ny=1, nt=int(nt), nBoundary=int(nBoundary),
                      dt=float(dt), nsrc=1, src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, wavelets=w.ctypes.data,
                      epsilon=float(epsilon), snap_stride=int(snap_stride), data=_addr(data), image=_addr(image))
         return self._submit(d, {"image": image, "data": data}, (kv, kvs, ki, kd, iz, ix, w, v, vs))
 
-    def submit_fwd3d(self, v, nt, src_iz, src_ix, src_iy, wavelets, nBoundary, dt):
+    def submit_fwd3d(self, v, nt, src_iz, src_ix, src_iy, wavelets, nBoundary, dt, *, data=None):
         """3D forward modelling with point sources; outputs: data (nx x ny x nt)."""
         from ._native import ShotDesc
 
@@ -334,7 +335,7 @@ class Plan:
         nz, nx, ny = vshape
         iz, ix, w = _points(src_iz, src_ix, None, wavelets, nt)
         iy = np.ascontiguousarray(np.atleast_1d(src_iy), dtype=np.int64)
-        data, kd = _out_like(v, (nx, ny, nt))
+        data, kd = _out_like(v, (nx, ny, nt)) if data is None else (data, None)
         d = ShotDesc(kind=SHOT_FWD3D, v=pv, nz=nz, nx=nx, ny=ny, nt=int(nt), nBoundary=int(nBoundary), dt=float(dt),
                      nsrc=len(iz), src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, src_iy=iy.ctypes.data,
                      wavelets=w.ctypes.data, data=_addr(data))
