@@ -258,30 +258,62 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
         for (int c = 0; c < ncol; ++c)
             for (int o = 0; o < nrow; ++o) amax_bits = max(amax_bits, __float_as_uint(fabsf(f32(pn.v[c][o]))));
     }
+    // Imaging: the operands of a column's cells are loaded before any of its
+    // sums is stored, so those cells share one round trip to memory.
     if constexpr (std::is_same<T, double>::value) {
         if (sh.img_f64) {
             const double* f64 = sh.img_f64 + (int64_t)tau * ncell;
-            for (int c = 0; c < ncol; ++c)
-                for (int o = 0; o < nrow; ++o) {
-                    const int64_t q = (i0 + o) + (int64_t)(j0 + c) * nz;
-                    const double f = f64[q];
-                    sh.img_m[q] = fma(f, pn.v[c][o], sh.img_m[q]);
-                    sh.img_s2[q] = fma(f, f, sh.img_s2[q]);
-                }
+            double* im = sh.img_m;
+            double* is2 = sh.img_s2;
+#pragma unroll
+            for (int c = 0; c < RX; ++c) {
+                if (c >= ncol) break;
+                const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
+                double f[4], m[4], s2[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o)
+                    if (o < nrow) {
+                        f[o] = f64[q0 + o];
+                        m[o] = im[q0 + o];
+                        s2[o] = is2[q0 + o];
+                    }
+#pragma unroll
+                for (int o = 0; o < 4; ++o)
+                    if (o < nrow) {
+                        im[q0 + o] = fma(f[o], pn.v[c][o], m[o]);
+                        is2[q0 + o] = fma(f[o], f[o], s2[o]);
+                    }
+            }
         }
     }
     if (sh.img_f16 && tau % stride == 0) {
         const int k = tau / stride;
         const __half* f16 = sh.img_f16 + (int64_t)k * ncell;
         const float inv = sh.img_inv[k];
-        for (int c = 0; c < ncol; ++c)
-            for (int o = 0; o < nrow; ++o) {
-                const int64_t q = (i0 + o) + (int64_t)(j0 + c) * nz;
-                const float f = __half2float(f16[q]) * inv;
-                const float r = f32(pn.v[c][o]);
-                sh.img_m2[q] = comp_add(sh.img_m2[q], __fmul_rn(f, r));
-                sh.img_s22[q] = comp_add(sh.img_s22[q], __fmul_rn(f, f));
-            }
+        float2* im = sh.img_m2;
+        float2* is2 = sh.img_s22;
+#pragma unroll
+        for (int c = 0; c < RX; ++c) {
+            if (c >= ncol) break;
+            const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
+            __half h[4];
+            float2 m[4], s2[4];
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (o < nrow) {
+                    h[o] = f16[q0 + o];
+                    m[o] = im[q0 + o];
+                    s2[o] = is2[q0 + o];
+                }
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (o < nrow) {
+                    const float f = __half2float(h[o]) * inv;
+                    const float r = f32(pn.v[c][o]);
+                    im[q0 + o] = comp_add(m[o], __fmul_rn(f, r));
+                    is2[q0 + o] = comp_add(s2[o], __fmul_rn(f, f));
+                }
+        }
     }
     return amax_bits;
 }
