@@ -608,7 +608,8 @@ CASES = {
     "step2d-fp32-large": (4096, 4096, 6, "fp32"),
     "step2d-fp64-large": (4096, 4096, 4, "fp64"),
     "step2d-strict-large": (4096, 4096, 3, "fp64-strict"),
-    "step3d-fp32": (256, 256, 6, "fp32"),  # n^3 grid
+    "step3d-fp32": (256, 256, 6, "fp32"),  # n^3 grid, 16-cell CPML
+    "step3d-fp32-nb0": (256, 256, 6, "fp32"),  # n^3 grid without damped bands
 }
 
 
@@ -628,8 +629,9 @@ def run_case(name):
     nz, nx, nt, mode = CASES[name]
     if name.startswith("step3d"):
         v = dipping_model_3d(nz)
+        nb = 0 if name.endswith("nb0") else 16
         d, _ = S.fwdTimeCpmlFor3dAwPoint(v, nt, [0], [nz // 2], [nz // 2], ricker(20.0, nt, 8e-4)[None, :],
-                                         N_ORDER, 16, 10.0, 10.0, 10.0, 8e-4, mode=mode)
+                                         N_ORDER, nb, 10.0, 10.0, 10.0, 8e-4, mode=mode)
         torch.cuda.synchronize()
         print(f"case {name}: {nz}^3 nt={nt} {mode} ok, data max {np.abs(d).max():.3e}")
         return

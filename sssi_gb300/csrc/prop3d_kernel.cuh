@@ -440,6 +440,15 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
         const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= nx - nB);
         const int i0 = z0 + r0, j = x0 + c0;
         const bool act = i0 < nz && j < nx;
+        // per-item facts (uniform over the block): what the planes of this item
+        // need beyond the stencil
+        bool item_src = d.src_dense != nullptr;
+        for (int q = 0; q < d.nsrc; ++q)
+            item_src |= d.src_iz[q] >= z0 && d.src_iz[q] < z0 + TZ && d.src_ix[q] >= x0 && d.src_ix[q] < x0 + TX &&
+                        d.src_iy[q] >= y0 && d.src_iy[q] < y1;
+        const bool rec_here = d.rec != nullptr && i0 == 0;
+        const bool item_snap = d.snap != nullptr;
+        const bool item_yband = nB > 0 && (y0 - 2 * N < nB || y1 + 2 * N > ny - nB);
         // plane y of a field: base + y * ldxy; own column segment at i0 + j * ldz
         const int64_t own = (int64_t)i0 + (int64_t)j * ldz;
 
@@ -484,11 +493,13 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
             pnext = ldc_nc(P + own + (int64_t)(ys + NQ - 1) * ldxy);  // P(s+2N-1) for the first step
         }
 
-        int u = 0;  // (s - ys) mod NQ
+        int u = 0;        // (s - ys) mod NQ
+        int st_next = 0;  // ring stage of the next output plane
         for (int s = ys; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
             {
                 const bool out = s >= y0;
-                const int st = out ? (s - y0) % NS : 0;
+                const int st = st_next;
+                if (out) st_next = st_next + 1 == NS ? 0 : st_next + 1;
                 Col<T> pin = pnext;  // P(s+2N-1)
                 if (out) {
                     // output plane y = s: its copies (plane box, P_old, (v dt)^2, and the
@@ -525,7 +536,7 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                         for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
                         a[o] = dd;
                     }
-                    if (nB > 0 && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
+                    if (item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
                         Col<T> av;
 #pragma unroll
                         for (int o = 0; o < RZ; ++o) av.v[o] = a[o];
@@ -571,7 +582,7 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                             ly[o] = dd;
                         }
                     }
-                    if (nB > 0 && (y < nB || y >= ny - nB)) {
+                    if (item_yband && (y < nB || y >= ny - nB)) {
                         Col<T> lv;
 #pragma unroll
                         for (int o = 0; o < RZ; ++o) lv.v[o] = ly[o];
@@ -584,18 +595,20 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                     T lap[RZ], pn[RZ];
 #pragma unroll
                     for (int o = 0; o < RZ; ++o) lap[o] = (lz[o] + lx[o]) + ly[o];
-                    if (d.src_dense) {
-                        const T* sd = d.src_dense + (int64_t)(tau - d.dense_t0) * ((int64_t)nz * nx * ny) + qi;
-#pragma unroll
-                        for (int o = 0; o < RZ; ++o)
-                            if (i0 + o < nz) lap[o] += sd[o];
-                    }
-                    for (int q = 0; q < d.nsrc; ++q)
-                        if (d.src_iy[q] == y && d.src_ix[q] == j && d.src_iz[q] >= i0 && d.src_iz[q] < i0 + RZ) {
+                    if (item_src) {
+                        if (d.src_dense) {
+                            const T* sd = d.src_dense + (int64_t)(tau - d.dense_t0) * ((int64_t)nz * nx * ny) + qi;
 #pragma unroll
                             for (int o = 0; o < RZ; ++o)
-                                if (d.src_iz[q] == i0 + o) lap[o] += d.src_wavelet[(int64_t)q * d.nt + tau];
+                                if (i0 + o < nz) lap[o] += sd[o];
                         }
+                        for (int q = 0; q < d.nsrc; ++q)
+                            if (d.src_iy[q] == y && d.src_ix[q] == j && d.src_iz[q] >= i0 && d.src_iz[q] < i0 + RZ) {
+#pragma unroll
+                                for (int o = 0; o < RZ; ++o)
+                                    if (d.src_iz[q] == i0 + o) lap[o] += d.src_wavelet[(int64_t)q * d.nt + tau];
+                            }
+                    }
                     const T* pc = Pq[0];
                     const Col<T> po = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kO) + c0 * TZ + r0);
                     const Col<T> vv = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kV) + c0 * TZ + r0);
@@ -609,8 +622,8 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                         for (int o = 0; o < RZ; ++o)
                             if (i0 + o < nz) dst[o] = pn[o];
                     }
-                    if (d.rec && i0 == 0) d.rec[j + (int64_t)y * nx + (int64_t)tau * nx * ny] = pn[0];
-                    if (d.snap) {
+                    if (rec_here) d.rec[j + (int64_t)y * nx + (int64_t)tau * nx * ny] = pn[0];
+                    if (item_snap) {
                         T* sn = d.snap + (int64_t)(tau - d.snap_t0) * ((int64_t)nz * nx * ny) + qi;
 #pragma unroll
                         for (int o = 0; o < RZ; ++o)
