@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
         fence_barrier_init();
     }
     __syncthreads();
-    int step = 0;  // set once the previous step's grid has completed
+    int step = 0;
 
     // Each CTA walks its own list of work items.  Warp 0 keeps the next item
     // and its shot's ShotTail in registers (loaded one iteration ahead), so
@@ -628,7 +628,22 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
         if (item.x >= 0 && lane < kTailVec) tail_reg = reinterpret_cast<const uint4*>(&shots[item.x].s)[lane];
     };
     // warp 0: put the prefetched item into stage s (tile = its position in the list)
-    auto prepare = [&](int w, int s) {
+    // lane 0 of warp 0: the three copies of stage s (after prepare_info recorded it)
+    auto issue = [&](int s) {
+        unsigned char* st = smem + s * G::kStage;
+        const TileInfo* info = reinterpret_cast<const TileInfo*>(st + G::kInfo);
+        if (lane == 0 && info->shot >= 0) {
+            const ShotTail<T>& g = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
+            const int k = info->shot, z0 = info->z0, x0 = info->x0, cur = info->tloc & 1;
+            inflight |= 1u << s;
+            fence_proxy_async_shared();
+            mbar_arrive_expect_tx(&bar[s], G::kTx);
+            tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], g.oz + z0 - HZ, x0);
+            tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], g.oz + z0, x0 + L);
+            tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], g.oz + z0, x0 + L);
+        }
+    };
+    auto prepare = [&](int w, int s, bool copy) {
         unsigned char* st = smem + s * G::kStage;
         TileInfo* info = reinterpret_cast<TileInfo*>(st + G::kInfo);
         const int k = item.x;
@@ -654,31 +669,33 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 info->z0 = z0;
                 info->x0 = x0;
                 info->flags = tile_flags<T, N>(g, z0, x0, tau);
-                const int cur = tloc & 1;
-                inflight |= 1u << s;
-                fence_proxy_async_shared();
-                mbar_arrive_expect_tx(&bar[s], G::kTx);
-                tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], g.oz + z0 - HZ, x0);
-                tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], g.oz + z0, x0 + L);
-                tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], g.oz + z0, x0 + L);
             }
         }
+        __syncwarp();
+        if (copy) issue(s);
     };
 
     const int r0 = 4 * (tid % (TZ / 4));
     const int c0 = RX * (tid / (TZ / 4));
     unsigned phase_bits = 0;  // completed uses of each stage's barrier (bit s = parity)
 
-    if (tid < 32) fetch(wbeg);  // work lists and descriptors are not written by kernels
-    // fields, memory variables and the step base are: wait for the previous grid
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // Work lists and descriptors are written by the host only.  The step base is
+    // written only by the one-thread kernels that run between graph replays and
+    // at the start of a run; those do not trigger their dependents early, so a
+    // step launched after one of them starts only once it has completed, and the
+    // base can be read before the wait.  Fields and memory variables are written
+    // by the previous step: the copies are issued after the wait.
     step = *reinterpret_cast<volatile const int*>(bc.step_base) + bc.step_offset;
     if (tid < 32) {
+        fetch(wbeg);
         for (int q = 0; q < NS - 1; ++q) {  // the first NS-1 items go into stages 0 .. NS-2
-            prepare(wbeg + q, q);
+            prepare(wbeg + q, q, false);
             fetch(wbeg + q + 1);
         }
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (tid < 32)
+        for (int q = 0; q < NS - 1; ++q) issue(q);
     __syncthreads();
     bool failed = false;
     for (int k = 0;; ++k) {
@@ -688,7 +705,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
         if (ti.tile >= bc.ntiles) break;
         if (tid < 32) {
             // stage (k-1) % NS was released by the barrier that ended iteration k-1
-            prepare(wbeg + k + NS - 1, (k + NS - 1) % NS);
+            prepare(wbeg + k + NS - 1, (k + NS - 1) % NS, true);
             fetch(wbeg + k + NS);
         }
         if (ti.shot >= 0) {
