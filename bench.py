@@ -87,6 +87,14 @@ def cell_updates(nz, nx, nt):
     return 3 * nz * nx * nt
 
 
+def step_bytes_per_cell(nz, nx, nb):
+    """Algorithmic HBM bytes of one FP32 step per cell: P(t), P(t-1), (v dt)^2
+    read and P(t+1) written (16 B), plus, per damped cell and axis, the
+    compensated memory variables phi (read, write) and psi (read, write) at
+    8 B each and the coefficients b, b-1 at 4 B each (40 B)."""
+    return 16 + 40 * (nb / nz + 2 * nb / nx)
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
@@ -225,11 +233,10 @@ def run_gpu(args):
     fwd_ms = float(np.mean([p[0][0] for p in ph32]))
     fwd_launch = ph32[0][0][1]
     per_launch_ms = fwd_ms / fwd_launch
-    f_z = NB / nz
-    f_x = 2 * NB / nx
-    band_bytes = 6 * 8  # phi in/out, psi read/write, b, b-1 per damped cell per axis (8-byte words)
-    bytes_cell = 16 + band_bytes * (f_z + f_x)
-    alg_bytes = bytes_cell * nz * nx
+    bytes_cell = step_bytes_per_cell(nz, nx, NB)
+    # a forward launch advances the shots in v and in vs, and packs the vs field
+    # to FP16 every STRIDE steps
+    alg_bytes = nz * nx * (2 * bytes_cell + 2.0 / STRIDE)
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
 
@@ -433,9 +440,22 @@ def bench_batch(S, args):
         errs.append(float(np.linalg.norm(outs[k] - ref) / np.linalg.norm(ref)))
     value = cells / el / 1e9
     single = cells1 / el1 / 1e9
+    # the batched step kernel alone: device time of the plan's 2D rounds
+    alg_bytes = sum(V.shape[0] * V.shape[1] * nt * step_bytes_per_cell(V.shape[0], V.shape[1], NB)
+                    for (V, nt, _, _) in shots)
+    peak, peak_kind = peaks()
+    kern_s = st["batch2d_gpu_s"]
+    kernel = {"value": round(st["batch2d_cell_updates"] / kern_s / 1e9, 2), "unit": UNIT,
+              "device_s": round(kern_s, 4),
+              "roofline": {"bound": "hbm", "achieved": round(alg_bytes / kern_s / 1e9, 1), "peak": peak,
+                           "unit": "GB/s", "frac": round(alg_bytes / kern_s / 1e9 / peak, 4), "peak_kind": peak_kind,
+                           "bytes_per_cell": round(alg_bytes / cells, 2)},
+              "timing": "CUDA events around each round of batched steps inside the plan (whole batch, all rounds)"}
     return {"metric": "Gcell-updates/s (64-shot batched forward modelling, 800x2400 model)",
             "value": round(value, 2), "unit": UNIT, "wall_s": round(el, 3), "shots_per_s": round(64 / el, 2),
             "cell_updates": cells, "dtype": "fp32", "batch_steps": int(st["batch_steps"]),
+            "plan_host_s": {k: round(st[k], 3) for k in ("admit_s", "round_s", "gpu_wait_s", "deliver_s")},
+            "step_kernel": kernel,
             "single_shot_value": round(single, 2), "speedup_vs_single_shot": round(value / single, 2),
             "single_shot_sample": "8 of the 64 shots, one sssi_fwdTimeCpmlFor2dAwPoint call each",
             "data_rel_l2_vs_fp64_max": max(errs), "error_sample": "2 shots against the fp64 path",
@@ -542,6 +562,7 @@ def bench_serve(S, args):
             "offered_rate_per_s": rate, "requests": {k: kinds.count(k) for k in ("fwd2d", "rtm2d", "fwd3d")},
             "rel_l2_vs_fp64": errs, "rel_l2_vs_fp64_max": max(errs.values()) if errs else None,
             "admission_budget_bytes": int(st["device_bytes_budget"]), "failed": int(st["failed"]), "dtype": "fp32",
+            "plan_host_s": {k: round(st[k], 3) for k in ("admit_s", "round_s", "gpu_wait_s", "deliver_s")},
             "config": {"workload": "serve-mixed", "fwd2d": "200x300 .. 1000x3000", "rtm2d": "400x800 .. 800x2400, "
                        "fp16 snapshots every 4 steps", "fwd3d": "128^3 .. 256^3, nB 16", "nt": "U[1000, 4000]",
                        "dt": dt, "arrivals": "Poisson, seeded", "models": "cut from a seeded layered+anomaly 2D "

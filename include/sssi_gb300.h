@@ -216,6 +216,13 @@ typedef struct {
     size_t device_bytes_in_use, device_bytes_budget;
     int64_t batch_steps;      /* launches of the batched 2D step */
     double cell_updates;      /* all shots, all propagations */
+    /* host time of the plan's threads, seconds: admitting shots (allocation,
+     * model conversion, uploads), rounds (launches, schedules, events), of
+     * which waiting for the GPU, and copying outputs out */
+    double admit_s, round_s, gpu_wait_s, deliver_s;
+    /* device time of the batched 2D steps (events around each round's
+     * launches) and the cell-updates made in it */
+    double batch2d_gpu_s, batch2d_cell_updates;
 } sssi_plan_stats;
 
 /* Creates a plan on the current device.  Native form of the submit/poll/wait

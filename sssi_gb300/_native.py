@@ -46,7 +46,9 @@ class PlanStats(ctypes.Structure):
     """sssi_plan_stats"""
     _fields_ = [("queued", c_i64), ("running", c_i64), ("done", c_i64), ("failed", c_i64),
                 ("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_budget", ctypes.c_size_t),
-                ("batch_steps", c_i64), ("cell_updates", ctypes.c_double)]
+                ("batch_steps", c_i64), ("cell_updates", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("round_s", ctypes.c_double), ("gpu_wait_s", ctypes.c_double), ("deliver_s", ctypes.c_double),
+                ("batch2d_gpu_s", ctypes.c_double), ("batch2d_cell_updates", ctypes.c_double)]
 
 
 # name -> (restype, argtypes)

@@ -356,9 +356,8 @@ void bfwd2d(const double* v, const double* source, int64_t nz, int64_t nx, int64
             double* snapshot) {
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    std::vector<double> vh = host_copy(v, (size_t)n, s);
     Batch2d<T> B(N, dz, dx, s);
-    const int k = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, false);
+    const int k = B.add_shot(v, nz, nx, nB, dt, (int)nt, 0, false);
     Staged<T> wav(wavelets, (size_t)(nsrc * nt), true, s);
     if (nsrc) B.set_point_sources(k, nsrc, iz, ix, wav.ptr);
     Staged<T> rec(data, (size_t)(nx * nt), false, s);
@@ -392,9 +391,8 @@ void brvs2d(const double* v, const double* data, int64_t nz, int64_t nx, int64_t
             double dx, double dt, double* model, double* snapshot) {
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    std::vector<double> vh = host_copy(v, (size_t)n, s);
     Batch2d<T> B(N, dz, dx, s);
-    const int k = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, true);
+    const int k = B.add_shot(v, nz, nx, nB, dt, (int)nt, 0, true);
     Staged<T> rows(data, (size_t)(nx * nt), true, s);
     B.shot(k).src_row = data ? rows.ptr : nullptr;
     const int64_t K = snapshot ? chunk_steps(nt, n) : std::max<int64_t>(nt, 1);
@@ -433,13 +431,11 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     const int64_t n = nz * nx;
     if (!kF16) stride = 1;
     SSSI_REQUIRE(stride >= 1, SSSI_ERR_ARG, "snap_stride must be >= 1");
-    std::vector<double> vh = host_copy(v, (size_t)n, s);
-    std::vector<double> vsh = host_copy(vs, (size_t)n, s);
     Batch2d<T> B(N, dz, dx, s);
     // forward in v and in vs over batch steps [0, nt); reverse in v over [nt, 2nt)
-    const int kA = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, 0, false);
-    const int kB = B.add_shot(vsh.data(), nz, nx, nB, dt, (int)nt, 0, false);
-    const int kR = B.add_shot(vh.data(), nz, nx, nB, dt, (int)nt, (int)nt, true);
+    const int kA = B.add_shot(v, nz, nx, nB, dt, (int)nt, 0, false);
+    const int kB = B.add_shot(vs, nz, nx, nB, dt, (int)nt, 0, false);
+    const int kR = B.add_shot_like(kA, (int)nt, (int)nt, true);
     Staged<T> wav(wavelet, (size_t)nt, true, s);
     B.set_point_sources(kA, 1, &src_iz, &src_ix, wav.ptr);
     B.set_point_sources(kB, 1, &src_iz, &src_ix, wav.ptr);

@@ -74,7 +74,7 @@ struct BatchConst {
     T az[16], ax[16];  // composed second-derivative coefficients a_0 .. a_l
     T wz[8], wx[8];    // first-derivative weights c_k / d
     int nshots;
-    int ntiles;
+    int ntiles;  // host bookkeeping only: the kernel ends at the end of its work list
     const int* cta_begin;  // gridDim.x + 1: each CTA's range in `work`
     const int2* work;      // (shot, tile within the shot), grouped by CTA
     const int* step_base;  // the launch computes batch step *step_base + step_offset
@@ -90,8 +90,15 @@ class Batch2d {
     using M = typename MemVar<T>::type;
     Batch2d(int N, double dz, double dx, cudaStream_t stream);
 
-    // Adds a shot: v is the host nz x nx model.  Returns the shot index.
+    // Adds a shot: v is the nz x nx model (host or device).  Returns the shot index.  The
+    // uploads and the zeroing of its state go to the upload stream (the batch
+    // stream unless set_upload_stream was called), where they can overlap
+    // batch steps in flight; the caller orders the batch stream after them.
+    // On failure the slot is released again.
     int add_shot(const double* v, int64_t nz, int64_t nx, int nB, double dt, int nt, int t_start, bool reverse);
+    // Adds a shot on the model of shot k (same grid, bands and dt) with its own
+    // state, length and start: the reverse propagation of an RTM shot.
+    int add_shot_like(int k, int nt, int t_start, bool reverse);
     ShotTail<T>& shot(int k) { return shots_[k].desc.s; }
     void set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet);
     void enable(int k, bool on) { shots_[k].enabled = on; }
@@ -99,8 +106,9 @@ class Batch2d {
     // The caller must have synchronised the stream past the shot's last step.
     void remove_shot(int k);
     int active_shots() const;
-    // Zeroes the fields and memory variables of shot k.
+    // Zeroes the fields and memory variables of shot k (upload stream).
     void reset_shot(int k);
+    void set_upload_stream(cudaStream_t s) { upload_ = s; }
     // Assigns the tiles of the enabled shots to CTAs (longest-processing-time
     // first, tiles next to a damped band weighted heavier) and uploads every
     // descriptor.  Call again whenever the set of active shots changes.
@@ -133,10 +141,27 @@ class Batch2d {
     int N_, L_;
     double dz_, dx_;
     cudaStream_t stream_;
+    cudaStream_t upload_ = nullptr;
+    cudaStream_t up() const { return upload_ ? upload_ : stream_; }
+    int take_slot();
+    int add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,
+                    int t_start, bool reverse);
     BatchConst<T> bc_{};
     std::vector<Shot> shots_;
     void launch_step(const int* base, int offset, cudaStream_t stream);
     void drop_graph();
+    // launch parameters the graph was captured with (the work list and the
+    // descriptors are read from device memory, so only these invalidate it)
+    struct GraphKey {
+        int grid = 0;
+        const void *desc = nullptr, *begin = nullptr, *work = nullptr;
+        bool operator==(const GraphKey& o) const {
+            return grid == o.grid && desc == o.desc && begin == o.begin && work == o.work;
+        }
+    } graph_key_;
+    GraphKey current_key() const {
+        return GraphKey{grid_, d_desc_.get(), d_cta_begin_.get(), d_work_.get()};
+    }
     DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;  // d_ctr_: graph step base, zero, error flag
     int grid_ = 0, ntiles_ = 0, step_ = 0;
     int ctas_per_sm_ = 1, sms_ = 1;

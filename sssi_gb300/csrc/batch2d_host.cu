@@ -92,17 +92,44 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
                  (long long)nz, (long long)nx);
     SSSI_REQUIRE(nz < (1LL << 30) && nx < (1LL << 30), SSSI_ERR_ARG, "model too large");
     SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
-    using Sh = TileShape<T>;
-    int slot = -1;
+    const int slot = take_slot();
+    try {
+        return add_shot_in(slot, v, -1, nz, nx, nB, dt, nt, t_start, reverse);
+    } catch (...) {
+        remove_shot(slot);
+        throw;
+    }
+}
+
+template <typename T>
+int Batch2d<T>::add_shot_like(int k, int nt, int t_start, bool reverse) {
+    SSSI_REQUIRE(k >= 0 && k < (int)shots_.size() && !shots_[k].free, SSSI_ERR_ARG, "no shot %d", k);
+    SSSI_REQUIRE(nt >= 0, SSSI_ERR_ARG, "nt must be >= 0");
+    const ShotTail<T> q = shots_[k].desc.s;
+    const int slot = take_slot();
+    try {
+        return add_shot_in(slot, nullptr, k, q.nz, q.nx, q.nB, 0.0, nt, t_start, reverse);
+    } catch (...) {
+        remove_shot(slot);
+        throw;
+    }
+}
+
+template <typename T>
+int Batch2d<T>::take_slot() {
     for (int q = 0; q < (int)shots_.size(); ++q)
         if (shots_[q].free) {
-            slot = q;
-            break;
+            shots_[q].free = false;
+            return q;
         }
-    if (slot < 0) {
-        shots_.emplace_back();
-        slot = (int)shots_.size() - 1;
-    }
+    shots_.emplace_back();
+    return (int)shots_.size() - 1;
+}
+
+template <typename T>
+int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,
+                            int t_start, bool reverse) {
+    using Sh = TileShape<T>;
     shots_[slot] = Shot{};
     Shot& S = shots_[slot];
     ShotTail<T>& d = S.desc.s;
@@ -115,31 +142,65 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
     const int64_t cols = nx + 2 * L_;
     const size_t pbytes = sizeof(T) * (size_t)ldp * (size_t)cols;
     for (auto& b : S.P) b.allocate(pbytes);
-    S.vdt2.allocate(pbytes);
-    {
+    if (like >= 0) {
+        // the same model as shot `like`: copy its (v dt)^2 and band coefficients
+        auto copy = [&](DeviceBuffer& dst, const DeviceBuffer& src) {
+            dst.allocate(src.bytes());
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(dst.get(), src.get(), src.bytes(), cudaMemcpyDeviceToDevice, up()));
+        };
+        const Shot& Q = shots_[like];
+        copy(S.vdt2, Q.vdt2);
+        copy(S.zb, Q.zb);
+        copy(S.zbm1, Q.zbm1);
+        copy(S.xb, Q.xb);
+        copy(S.xbm1, Q.xbm1);
+    } else {
+        // (v dt)^2 on the device, from v where it lies (host models go up once
+        // as doubles); the damping bands on the host, from the band strips of v
         const int64_t n = nz * nx;
-        std::vector<T> h(n);
-        for (int64_t q = 0; q < n; ++q) h[q] = static_cast<T>((v[q] * dt) * (v[q] * dt));
-        S.vdt2.zero(stream_);
-        SSSI_CHECK_CUDA(cudaMemcpy2DAsync(S.vdt2.template as<T>() + S.origin, sizeof(T) * ldp, h.data(), sizeof(T) * nz,
-                                          sizeof(T) * nz, nx, cudaMemcpyHostToDevice, stream_));
-        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+        const bool dev = is_device_pointer(v);
+        DeviceBuffer vd;
+        const double* vdev = v;
+        S.vdt2.allocate(pbytes);
+        S.vdt2.zero(up());
+        if (!dev) {
+            vd.allocate(sizeof(double) * n);
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(vd.get(), v, sizeof(double) * n, cudaMemcpyHostToDevice, up()));
+            vdev = vd.template as<double>();
+        }
+        launch_vdt2<T>(vdev, nz, nx, 1, dt, S.vdt2.template as<T>() + S.origin, ldp, ldp * cols, up());
+        Bands2D bands;
+        if (dev) {
+            std::vector<double> bottom((size_t)nB * nx), sides((size_t)nz * 2 * nB);
+            if (nB > 0) {
+                SSSI_CHECK_CUDA(cudaMemcpy2DAsync(bottom.data(), sizeof(double) * nB, v + (nz - nB),
+                                                  sizeof(double) * nz, sizeof(double) * nB, nx,
+                                                  cudaMemcpyDeviceToHost, up()));
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data(), v, sizeof(double) * nz * nB, cudaMemcpyDeviceToHost,
+                                                up()));
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data() + nz * nB, v + (nx - nB) * nz, sizeof(double) * nz * nB,
+                                                cudaMemcpyDeviceToHost, up()));
+            }
+            SSSI_CHECK_CUDA(cudaStreamSynchronize(up()));
+            bands = damping_bands_2d_strips(bottom.data(), sides.data(), nz, nx, nB, dz_, dx_, dt);
+        } else {
+            bands = damping_bands_2d(v, nz, nx, nB, dz_, dx_, dt);
+        }
+        auto upload = [&](DeviceBuffer& buf, const std::vector<T>& h) {
+            buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
+            if (!h.empty())
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
+                                                up()));
+        };
+        std::vector<T> zb, zbm1, xb, xbm1;
+        band_coefficients<T>(bands.zb, bands.zbm1, zb, zbm1);
+        band_coefficients<T>(bands.xb, bands.xbm1, xb, xbm1);
+        upload(S.zb, zb);
+        upload(S.zbm1, zbm1);
+        upload(S.xb, xb);
+        upload(S.xbm1, xbm1);
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(up()));  // vd and the host vectors go out of scope
     }
-    Bands2D bands = damping_bands_2d(v, nz, nx, nB, dz_, dx_, dt);
-    auto upload = [&](DeviceBuffer& buf, const std::vector<T>& h) {
-        buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
-        if (!h.empty())
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
-                                            stream_));
-        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
-    };
-    std::vector<T> b, bm1;
-    band_coefficients<T>(bands.zb, bands.zbm1, b, bm1);
-    upload(S.zb, b);
-    upload(S.zbm1, bm1);
-    band_coefficients<T>(bands.xb, bands.xbm1, b, bm1);
-    upload(S.xb, b);
-    upload(S.xbm1, bm1);
     const size_t zbytes = sizeof(M) * std::max<size_t>((size_t)nB * nx, 1);
     const size_t xbytes = sizeof(M) * std::max<size_t>((size_t)nz * 2 * nB, 1);
     for (auto* bf : {&S.zphi[0], &S.zphi[1], &S.zpsi}) bf->allocate(zbytes);
@@ -218,8 +279,8 @@ void Batch2d<T>::set_point_sources(int k, int nsrc, const int64_t* iz, const int
 template <typename T>
 void Batch2d<T>::reset_shot(int k) {
     Shot& S = shots_[k];
-    for (auto& b : S.P) b.zero(stream_);
-    for (auto* b : {&S.zphi[0], &S.zphi[1], &S.zpsi, &S.xphi[0], &S.xphi[1], &S.xpsi}) b->zero(stream_);
+    for (auto& b : S.P) b.zero(up());
+    for (auto* b : {&S.zphi[0], &S.zphi[1], &S.zpsi, &S.xphi[0], &S.xphi[1], &S.xpsi}) b->zero(up());
 }
 
 template <typename T>
@@ -235,7 +296,6 @@ void Batch2d<T>::drop_graph() {
 
 template <typename T>
 void Batch2d<T>::finalize() {
-    drop_graph();  // launch parameters change
     using Sh = TileShape<T>;
     // tiles of the enabled shots with an estimated cost: tiles whose stencil
     // reaches a damped band add a cooperative first-derivative pass and the
@@ -330,7 +390,9 @@ void Batch2d<T>::run(int nsteps) {
     int q = 0;
     if (nsteps >= kGraphSteps) {
         int* base = d_ctr_.template as<int>();
+        if (graph_ && !(graph_key_ == current_key())) drop_graph();
         if (!graph_) {
+            graph_key_ = current_key();
             // steps base .. base+K-1, then base += K
             std::lock_guard<std::mutex> lock(capture_mutex());
             cudaStream_t cs = capture_stream();

@@ -70,9 +70,11 @@ __device__ __forceinline__ float2 comp_add(float2 acc, float x) {
 __device__ __forceinline__ float f32(float x) { return x; }
 __device__ __forceinline__ float f32(double x) { return static_cast<float>(x); }
 
+constexpr int kNoTile = 0x7fffffff;
+
 // Per-tile facts shared by the block (written by warp 0 with the ShotTail).
 struct TileInfo {
-    int tile;        // batch tile index (>= ntiles: the CTA has no more tiles)
+    int tile;        // position in the work list (kNoTile: the CTA has no more tiles)
     int shot;        // -1: nothing to do (no tile, or the shot is inactive)
     int local;       // tile index within the shot
     int tloc;        // local step of the shot
@@ -659,7 +661,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                     tau = g.reverse ? g.nt - 1 - tloc : tloc;
                 }
             }
-            info->tile = w < wend ? w : bc.ntiles;
+            info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
             info->local = item.y;
             info->tloc = tloc;
@@ -702,7 +704,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
         const int s = k % NS;
         const unsigned char* st = smem + s * G::kStage;
         const TileInfo ti = *reinterpret_cast<const TileInfo*>(st + G::kInfo);
-        if (ti.tile >= bc.ntiles) break;
+        if (ti.tile == kNoTile) break;
         if (tid < 32) {
             // stage (k-1) % NS was released by the barrier that ended iteration k-1
             prepare(wbeg + k + NS - 1, (k + NS - 1) % NS, true);

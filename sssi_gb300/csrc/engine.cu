@@ -19,6 +19,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <thread>
@@ -80,17 +81,45 @@ struct PlanRequest {
 };
 using ReqPtr = std::shared_ptr<PlanRequest>;
 
+// The outputs of a finished shot, copied out by the plan's delivery thread on
+// its own stream (after `ready`, recorded on the batch stream once the shot's
+// last work is queued), so the batch keeps stepping meanwhile.
+struct Delivery {
+    ReqPtr r;
+    cudaEvent_t ready = nullptr;
+    std::function<void(cudaStream_t)> copy;
+    std::shared_ptr<void> keep;  // device buffers the copy reads
+};
+
 class EngineBase {
   public:
     virtual ~EngineBase() = default;
     virtual size_t footprint(const PlanRequest& r) const = 0;
     virtual void admit(const ReqPtr& r) = 0;
-    // Advances every admitted shot; finished requests (done or failed) are
-    // appended to `fin`.  Returns cell-updates performed.
-    virtual double round(std::vector<ReqPtr>& fin) = 0;
+    // A round in two halves, so that admitting new shots (host work and
+    // uploads on a side stream) overlaps the steps in flight:
+    // launch() queues the next steps of every admitted shot and returns the
+    // cell-updates queued; complete() waits for them, checks the kernels'
+    // error flags and handles the shots' events.  Finished shots are appended
+    // to `out` (their outputs still to be copied).
+    virtual double launch(std::vector<Delivery>& out) = 0;
+    virtual void complete(std::vector<Delivery>& out) = 0;
     virtual bool busy() const = 0;
     virtual void fail_all(std::vector<ReqPtr>& fin, const std::string& why) = 0;
     virtual int64_t batch_steps() const = 0;
+    double gpu_wait_s = 0;  // host time blocked on the batch stream
+    // device time of the batched 2D steps (CUDA events around each round's
+    // launches) and the cell-updates they made
+    double batch2d_gpu_s = 0, batch2d_cells = 0;
+
+  protected:
+    // Waits for the batch stream, counting the time.
+    void wait_stream(cudaStream_t s) {
+        const auto t = Clock::now();
+        const cudaError_t e = cudaStreamSynchronize(s);
+        gpu_wait_s += std::chrono::duration<double>(Clock::now() - t).count();
+        SSSI_CHECK_CUDA(e);
+    }
 };
 
 template <typename T>
@@ -103,14 +132,27 @@ class Engine final : public EngineBase {
         int kA = -1, kB = -1, kR = -1;
         int64_t s0 = 0;
         int phase = 1;
-        DeviceBuffer wav, recA, recB, delta, fsnap, amax, inv, Mb, S2;
+        DeviceBuffer wav, recA, recB, delta, fsnap, amax, inv, Mb, S2, img;
         std::unique_ptr<Prop3d<T>> p3;
         int64_t done3 = 0;
     };
 
   public:
     Engine(const sssi_plan_config& c, cudaStream_t s)
-        : cfg_(c), s_(s), B_(c.nDiffOrder, c.dz, c.dx, s), rounds_(c.steps_per_round > 0 ? c.steps_per_round : 64) {}
+        : cfg_(c), s_(s), B_(c.nDiffOrder, c.dz, c.dx, s), rounds_(c.steps_per_round > 0 ? c.steps_per_round : 64) {
+        SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&up_, cudaStreamNonBlocking));
+        SSSI_CHECK_CUDA(cudaEventCreateWithFlags(&up_done_, cudaEventDisableTiming));
+        SSSI_CHECK_CUDA(cudaEventCreate(&ev2_[0]));
+        SSSI_CHECK_CUDA(cudaEventCreate(&ev2_[1]));
+        B_.set_upload_stream(up_);
+    }
+    ~Engine() override {
+        cudaStreamSynchronize(up_);
+        cudaEventDestroy(up_done_);
+        cudaEventDestroy(ev2_[0]);
+        cudaEventDestroy(ev2_[1]);
+        cudaStreamDestroy(up_);
+    }
 
     size_t footprint(const PlanRequest& r) const override {
         const int N = cfg_.nDiffOrder, L = 2 * N - 1, HZ = tile_halo_rows(N);
@@ -141,19 +183,41 @@ class Engine final : public EngineBase {
         u->r = r;
         const sssi_shot_desc& d = r->d;
         const int64_t nz = d.nz, nx = d.nx, nt = d.nt;
-        upload<T>(u->wav, r->wav, s_);
+        upload<T>(u->wav, r->wav, up_);
         if (d.kind == SSSI_SHOT_FWD3D) {
+            // set up on the upload stream, stepped on the batch stream
             u->p3 = std::make_unique<Prop3d<T>>(r->v.data(), nz, nx, d.ny, cfg_.nDiffOrder, d.nBoundary, cfg_.dz,
-                                                cfg_.dx, cfg_.dy, d.dt, (int)nt, s_);
+                                                cfg_.dx, cfg_.dy, d.dt, (int)nt, up_);
             if (d.nsrc)
                 u->p3->set_point_sources(d.nsrc, r->iz.data(), r->ix.data(), r->iy.data(), u->wav.template as<T>());
             u->recA.allocate(sizeof(T) * std::max<int64_t>(nx * d.ny * nt, 1));
             u->p3->desc().rec = u->recA.template as<T>();
             u->p3->sync_desc();
+            u->p3->set_stream(s_);
+            SSSI_CHECK_CUDA(cudaEventRecord(up_done_, up_));
             r->cells = nz * nx * d.ny * nt;
             runs3_.push_back(std::move(u));
             return;
         }
+        try {
+            admit2d(*u);
+        } catch (...) {
+            const int ks[3] = {u->kA, u->kB, u->kR};
+            for (int k : ks)
+                if (k >= 0) B_.remove_shot(k);
+            throw;
+        }
+        SSSI_CHECK_CUDA(cudaEventRecord(up_done_, up_));
+        dirty_ = true;
+        runs2_.push_back(std::move(u));
+    }
+
+  private:
+    void admit2d(Run& ru) {
+        Run* u = &ru;
+        const ReqPtr& r = u->r;
+        const sssi_shot_desc& d = r->d;
+        const int64_t nz = d.nz, nx = d.nx, nt = d.nt;
         u->s0 = step_;
         const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
         if (d.kind == SSSI_SHOT_FWD2D) {
@@ -168,7 +232,7 @@ class Engine final : public EngineBase {
             const int64_t nsnap = (nt + stride - 1) / stride;
             u->kA = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
             u->kB = B_.add_shot(r->vs.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
-            u->kR = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)(step_ + nt), true);
+            u->kR = B_.add_shot_like(u->kA, (int)nt, (int)(step_ + nt), true);
             B_.enable(u->kR, false);
             B_.set_point_sources(u->kA, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
             B_.set_point_sources(u->kB, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
@@ -177,16 +241,16 @@ class Engine final : public EngineBase {
             u->delta.allocate(sizeof(T) * ndata);
             u->Mb.allocate(sizeof(double) * n);
             u->S2.allocate(sizeof(double) * n);
-            u->Mb.zero(s_);
+            u->Mb.zero(up_);
             if (kF16) {
                 u->fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
                 u->amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
-                u->amax.zero(s_);
+                u->amax.zero(up_);
                 u->inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
-                u->S2.zero(s_);
+                u->S2.zero(up_);
             } else {
                 u->fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
-                fill(u->S2.template as<double>(), n, d.epsilon, s_);
+                fill(u->S2.template as<double>(), n, d.epsilon, up_);
             }
             ShotTail<T>& a = B_.shot(u->kA);
             a.rec = u->recA.template as<T>();
@@ -216,17 +280,18 @@ class Engine final : public EngineBase {
             }
             r->cells = 3 * n * nt;
         }
-        dirty_ = true;
-        runs2_.push_back(std::move(u));
     }
 
+  public:
     bool busy() const override { return !runs2_.empty() || !runs3_.empty(); }
     int64_t batch_steps() const override { return launches_; }
 
-    double round(std::vector<ReqPtr>& fin) override {
+    double launch(std::vector<Delivery>& out) override {
         double cells = 0;
+        ran2_ = false;
+        finish_2d_events(out);  // zero-step shots and events due right at admission
+        SSSI_CHECK_CUDA(cudaStreamWaitEvent(s_, up_done_, 0));  // uploads of the shots admitted so far
         // ---- 2D batch: up to the next event of any shot
-        finish_2d_events(fin);  // zero-step shots and events due right at admission
         if (!runs2_.empty()) {
             int64_t K = rounds_;
             for (auto& u : runs2_) K = std::min(K, next_event(*u) - step_);
@@ -236,42 +301,63 @@ class Engine final : public EngineBase {
                 dirty_ = false;
             }
             B_.set_step((int)step_);
+            SSSI_CHECK_CUDA(cudaEventRecord(ev2_[0], s_));
             B_.run((int)K);
+            SSSI_CHECK_CUDA(cudaEventRecord(ev2_[1], s_));
+            cells2_ = 0;
             for (auto& u : runs2_) {
                 const int64_t n = (int64_t)u->r->d.nz * u->r->d.nx;
-                cells += (double)n * K * (u->r->d.kind == SSSI_SHOT_RTM2D && u->phase == 1 ? 2 : 1);
+                cells2_ += (double)n * K * (u->r->d.kind == SSSI_SHOT_RTM2D && u->phase == 1 ? 2 : 1);
             }
+            cells += cells2_;
             step_ += K;
             launches_ += K;
-            SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
-            B_.check_errors();
-            finish_2d_events(fin);
+            ran2_ = true;
         }
-        // ---- 3D shots
-        for (size_t q = 0; q < runs3_.size();) {
-            Run& u = *runs3_[q];
-            const int64_t nt = u.r->d.nt;
-            const int64_t k = std::min<int64_t>(rounds_, nt - u.done3);
+        // ---- 3D shots: up to steps_per_round steps each
+        for (auto& up : runs3_) {
+            Run& u = *up;
+            const int64_t k = std::min<int64_t>(rounds_, u.r->d.nt - u.done3);
             if (k > 0) {
                 u.p3->run((int)k);
                 u.done3 += k;
                 cells += (double)u.r->d.nz * u.r->d.nx * u.r->d.ny * k;
             }
+        }
+        return cells;
+    }
+
+    void complete(std::vector<Delivery>& out) override {
+        wait_stream(s_);
+        if (ran2_) {
+            float ms = 0;
+            SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms, ev2_[0], ev2_[1]));
+            batch2d_gpu_s += 1e-3 * ms;
+            batch2d_cells += cells2_;
+            B_.check_errors();
+            finish_2d_events(out);
+        }
+        ran2_ = false;
+        for (size_t q = 0; q < runs3_.size();) {
+            Run& u = *runs3_[q];
+            const int64_t nt = u.r->d.nt;
             if (u.done3 >= nt) {
-                SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
                 u.p3->check_errors();
-                deliver<T>(u.recA.template as<T>(), (size_t)(u.r->d.nx * u.r->d.ny * nt), u.r->d.data, s_);
-                fin.push_back(u.r);
+                const T* rec = u.recA.template as<T>();
+                const size_t n = (size_t)(u.r->d.nx * u.r->d.ny * nt);
+                double* dst = u.r->d.data;
+                hand_over(std::move(runs3_[q]), out, [=](cudaStream_t cs) { deliver<T>(rec, n, dst, cs); });
                 runs3_.erase(runs3_.begin() + q);
                 continue;
             }
             ++q;
         }
-        return cells;
     }
 
     void fail_all(std::vector<ReqPtr>& fin, const std::string& why) override {
         cudaStreamSynchronize(s_);
+        cudaStreamSynchronize(up_);
+        ran2_ = false;
         for (auto& u : runs2_) {
             u->r->status = SSSI_ERR_INTERNAL;
             u->r->msg = why;
@@ -297,7 +383,20 @@ class Engine final : public EngineBase {
         return u.s0 + nt;
     }
 
-    void finish_2d_events(std::vector<ReqPtr>& fin) {
+    // Queues the delivery of a finished run's outputs; the run (and its device
+    // buffers) lives until the copies are done.
+    template <class F>
+    void hand_over(std::unique_ptr<Run> u, std::vector<Delivery>& out, F&& copy) {
+        Delivery dl;
+        dl.r = u->r;
+        SSSI_CHECK_CUDA(cudaEventCreateWithFlags(&dl.ready, cudaEventDisableTiming));
+        SSSI_CHECK_CUDA(cudaEventRecord(dl.ready, s_));
+        dl.copy = std::forward<F>(copy);
+        dl.keep = std::shared_ptr<Run>(std::move(u));
+        out.push_back(std::move(dl));
+    }
+
+    void finish_2d_events(std::vector<Delivery>& out) {
         for (size_t q = 0; q < runs2_.size();) {
             Run& u = *runs2_[q];
             if (step_ < next_event(u)) {
@@ -307,8 +406,14 @@ class Engine final : public EngineBase {
             const sssi_shot_desc& d = u.r->d;
             const int64_t nz = d.nz, nx = d.nx, nt = d.nt, n = nz * nx;
             if (d.kind == SSSI_SHOT_FWD2D) {
-                deliver<T>(u.recA.template as<T>(), (size_t)(nx * nt), d.data, s_);
                 B_.remove_shot(u.kA);
+                const T* rec = u.recA.template as<T>();
+                double* dst = d.data;
+                const size_t cnt = (size_t)(nx * nt);
+                hand_over(std::move(runs2_[q]), out, [=](cudaStream_t cs) { deliver<T>(rec, cnt, dst, cs); });
+                runs2_.erase(runs2_.begin() + q);
+                dirty_ = true;
+                continue;
             } else if (u.phase == 1) {
                 // forward phase done: FP16 pack of the last forward step, residual data
                 const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
@@ -324,7 +429,7 @@ class Engine final : public EngineBase {
                     count_launch();
                     SSSI_CHECK_CUDA(cudaGetLastError());
                 }
-                SSSI_CHECK_CUDA(cudaStreamSynchronize(s_));
+                wait_stream(s_);
                 B_.remove_shot(u.kA);
                 B_.remove_shot(u.kB);
                 u.kA = u.kB = -1;
@@ -334,29 +439,39 @@ class Engine final : public EngineBase {
                 ++q;  // its reverse phase ends nt steps later
                 continue;
             } else {
-                DeviceBuffer img(sizeof(double) * std::max<int64_t>(n, 1));
+                u.img.allocate(sizeof(double) * std::max<int64_t>(n, 1));
                 const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
                 if (kF16)
                     image_finish_comp_kernel<<<152 * 4, 256, 0, s_>>>(u.Mb.template as<float2>(),
                                                                        u.S2.template as<float2>(), n, (double)stride,
-                                                                       d.epsilon, img.as<double>());
+                                                                       d.epsilon, u.img.template as<double>());
                 else
                     image_finish_kernel<<<152 * 4, 256, 0, s_>>>(u.Mb.template as<double>(), u.S2.template as<double>(),
-                                                                  n, 1.0, 0.0, img.as<double>());
+                                                                  n, 1.0, 0.0, u.img.template as<double>());
                 count_launch();
                 SSSI_CHECK_CUDA(cudaGetLastError());
-                deliver<double>(img.as<double>(), (size_t)n, d.image, s_);
-                if (d.data) deliver<T>(u.recA.template as<T>(), (size_t)(nx * nt), d.data, s_);
                 B_.remove_shot(u.kR);
+                const double* img = u.img.template as<double>();
+                const T* rec = u.recA.template as<T>();
+                double *dimg = d.image, *ddata = d.data;
+                const size_t cimg = (size_t)n, cdata = (size_t)(nx * nt);
+                hand_over(std::move(runs2_[q]), out, [=](cudaStream_t cs) {
+                    deliver<double>(img, cimg, dimg, cs);
+                    if (ddata) deliver<T>(rec, cdata, ddata, cs);
+                });
+                runs2_.erase(runs2_.begin() + q);
+                dirty_ = true;
             }
-            fin.push_back(u.r);
-            runs2_.erase(runs2_.begin() + q);
-            dirty_ = true;
         }
     }
 
     sssi_plan_config cfg_;
     cudaStream_t s_;
+    cudaStream_t up_ = nullptr;     // admission: uploads and zeroing of new shots
+    cudaEvent_t up_done_ = nullptr; // recorded after each admission; the batch stream waits on it
+    bool ran2_ = false;             // the round in flight has 2D steps
+    cudaEvent_t ev2_[2] = {nullptr, nullptr};  // around the 2D launches of the round in flight
+    double cells2_ = 0;                        // their cell-updates
     Batch2d<T> B_;
     int64_t rounds_;
     int64_t step_ = 0, launches_ = 0;
@@ -378,12 +493,19 @@ struct sssi_plan {
     int64_t next_ticket = 1;
     size_t budget = 0, in_use = 0;
     int64_t n_running = 0, n_done = 0, n_failed = 0, batch_steps = 0;
-    double cells = 0;
+    double cells = 0, admit_s = 0, round_s = 0, gpu_wait_s = 0, deliver_s = 0, batch2d_gpu_s = 0,
+           batch2d_cells = 0;
     bool stop = false;
     int fatal = SSSI_OK;
     std::string fatal_msg;
     std::unique_ptr<sssi::EngineBase> engine;
     std::thread worker;
+    // delivery thread: copies finished shots' outputs on its own stream
+    cudaStream_t dstream = nullptr;
+    std::deque<sssi::Delivery> deliveries;
+    std::condition_variable cv_deliver;
+    bool deliver_stop = false;
+    std::thread deliverer;
 
     double now() const { return std::chrono::duration<double>(sssi::Clock::now() - t0).count(); }
 
@@ -398,61 +520,142 @@ struct sssi_plan {
         }
         fin.clear();
         cv_done.notify_all();
+        cv_work.notify_all();  // memory came back: a queued shot may fit now
+    }
+
+    // The next queued shot fits the memory not held by admitted or delivering
+    // shots (a shot larger than the whole budget runs alone).
+    bool front_fits() const {
+        return !queue.empty() && (in_use == 0 || in_use + queue.front()->bytes <= budget);
+    }
+
+    void hand_over(std::vector<sssi::Delivery>& out) {
+        if (out.empty()) return;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (auto& d : out) deliveries.push_back(std::move(d));
+        }
+        out.clear();
+        cv_deliver.notify_one();
+    }
+
+    void deliver_loop() {
+        cudaSetDevice(device);
+        std::vector<sssi::ReqPtr> fin;
+        while (true) {
+            sssi::Delivery d;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_deliver.wait(lk, [&] { return deliver_stop || !deliveries.empty(); });
+                if (deliveries.empty()) break;  // stopped and drained
+                d = std::move(deliveries.front());
+                deliveries.pop_front();
+            }
+            sssi::clear_error();
+            const auto td = sssi::Clock::now();
+            try {
+                SSSI_CHECK_CUDA(cudaStreamWaitEvent(dstream, d.ready, 0));
+                d.copy(dstream);
+                SSSI_CHECK_CUDA(cudaStreamSynchronize(dstream));
+            } catch (const sssi::Error& e) {
+                d.r->status = e.code;
+                d.r->msg = std::string("output copy failed: ") + sssi_last_error();
+            } catch (...) {
+                d.r->status = SSSI_ERR_INTERNAL;
+                d.r->msg = "output copy failed: unexpected exception";
+            }
+            cudaStreamSynchronize(dstream);
+            cudaEventDestroy(d.ready);
+            d.keep.reset();
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                deliver_s += std::chrono::duration<double>(sssi::Clock::now() - td).count();
+            }
+            fin.push_back(d.r);
+            finish(fin);
+        }
+    }
+
+    // Admits the queued shots that fit, first come first served.
+    void admit_queued(std::vector<sssi::ReqPtr>& fin) {
+        std::vector<sssi::ReqPtr> admit;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            while (front_fits()) {
+                sssi::ReqPtr& r = queue.front();
+                in_use += r->bytes;
+                r->state = SSSI_SHOT_RUNNING;
+                r->t_start = now();
+                ++n_running;
+                admit.push_back(r);
+                queue.pop_front();
+            }
+        }
+        if (admit.empty()) return;
+        const auto ta = sssi::Clock::now();
+        for (auto& r : admit) {
+            sssi::clear_error();
+            try {
+                engine->admit(r);
+            } catch (const sssi::Error& e) {
+                r->status = e.code;
+                r->msg = sssi_last_error();
+                fin.push_back(r);
+            } catch (const std::bad_alloc&) {
+                r->status = SSSI_ERR_NOMEM;
+                r->msg = "host allocation failed";
+                fin.push_back(r);
+            } catch (...) {
+                r->status = SSSI_ERR_INTERNAL;
+                r->msg = "unexpected exception while admitting the shot";
+                fin.push_back(r);
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        admit_s += std::chrono::duration<double>(sssi::Clock::now() - ta).count();
+    }
+
+    // Runs one half of a round; a failure fails every admitted shot (they
+    // share the batch and its stream).
+    template <class F>
+    bool guarded_step(std::vector<sssi::ReqPtr>& fin, F&& f) {
+        try {
+            f();
+            return true;
+        } catch (const sssi::Error&) {
+            engine->fail_all(fin, std::string("batch step failed: ") + sssi_last_error());
+        } catch (...) {
+            engine->fail_all(fin, "batch step failed: unexpected exception");
+        }
+        return false;
     }
 
     void run() {
         cudaSetDevice(device);
         std::vector<sssi::ReqPtr> fin;
+        std::vector<sssi::Delivery> out;
         while (true) {
-            std::vector<sssi::ReqPtr> admit;
             {
                 std::unique_lock<std::mutex> lk(mu);
-                cv_work.wait(lk, [&] { return stop || !queue.empty() || engine->busy(); });
+                cv_work.wait(lk, [&] { return stop || front_fits() || engine->busy(); });
                 if (stop) break;
-                // first come first served while the footprint fits; a shot larger than
-                // the whole budget runs alone
-                while (!queue.empty()) {
-                    sssi::ReqPtr& r = queue.front();
-                    const bool alone = in_use == 0 && admit.empty();
-                    if (!alone && in_use + r->bytes > budget) break;
-                    in_use += r->bytes;
-                    r->state = SSSI_SHOT_RUNNING;
-                    r->t_start = now();
-                    ++n_running;
-                    admit.push_back(r);
-                    queue.pop_front();
-                }
             }
-            for (auto& r : admit) {
-                sssi::clear_error();
-                try {
-                    engine->admit(r);
-                } catch (const sssi::Error& e) {
-                    r->status = e.code;
-                    r->msg = sssi_last_error();
-                    fin.push_back(r);
-                } catch (const std::bad_alloc&) {
-                    r->status = SSSI_ERR_NOMEM;
-                    r->msg = "host allocation failed";
-                    fin.push_back(r);
-                } catch (...) {
-                    r->status = SSSI_ERR_INTERNAL;
-                    r->msg = "unexpected exception while admitting the shot";
-                    fin.push_back(r);
-                }
-            }
-            if (!fin.empty()) finish(fin);
-            try {
-                const double c = engine->round(fin);
+            const auto t0r = sssi::Clock::now();
+            const double admit0 = admit_s;
+            double c = 0;
+            bool ok = guarded_step(fin, [&] { c = engine->launch(out); });
+            admit_queued(fin);  // overlaps the steps just launched
+            if (ok) ok = guarded_step(fin, [&] { engine->complete(out); });
+            {
                 std::lock_guard<std::mutex> lk(mu);
-                cells += c;
+                if (ok) cells += c;
                 batch_steps = engine->batch_steps();
-            } catch (const sssi::Error&) {
-                // a kernel or copy failed: every admitted shot shares the failure
-                engine->fail_all(fin, std::string("batch step failed: ") + sssi_last_error());
-            } catch (...) {
-                engine->fail_all(fin, "batch step failed: unexpected exception");
+                round_s += std::chrono::duration<double>(sssi::Clock::now() - t0r).count() - (admit_s - admit0);
+                gpu_wait_s = engine->gpu_wait_s;
+                batch2d_gpu_s = engine->batch2d_gpu_s;
+                batch2d_cells = engine->batch2d_cells;
             }
+            hand_over(out);
             if (!fin.empty()) finish(fin);
         }
         // plan destroyed: fail what is left
@@ -508,12 +711,14 @@ extern "C" int sssi_plan_create(const sssi_plan_config* config, sssi_plan** plan
         SSSI_CHECK_CUDA(cudaMemGetInfo(&free_b, &total_b));
         p->budget = c.device_bytes ? c.device_bytes : free_b / 4 * 3;
         SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+        SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&p->dstream, cudaStreamNonBlocking));
         p->t0 = Clock::now();
         if (p->cfg.mode == SSSI_MODE_FP32)
             p->engine = std::make_unique<Engine<float>>(p->cfg, p->stream);
         else
             p->engine = std::make_unique<Engine<double>>(p->cfg, p->stream);
         sssi_plan* raw = p.release();
+        raw->deliverer = std::thread([raw] { raw->deliver_loop(); });
         raw->worker = std::thread([raw] { raw->run(); });
         *plan = raw;
     });
@@ -528,7 +733,14 @@ extern "C" int sssi_plan_destroy(sssi_plan* plan) {
         }
         plan->cv_work.notify_all();
         if (plan->worker.joinable()) plan->worker.join();
+        {
+            std::lock_guard<std::mutex> lk(plan->mu);
+            plan->deliver_stop = true;
+        }
+        plan->cv_deliver.notify_all();
+        if (plan->deliverer.joinable()) plan->deliverer.join();
         cudaStreamDestroy(plan->stream);
+        cudaStreamDestroy(plan->dstream);
         delete plan;
     });
 }
@@ -626,5 +838,11 @@ extern "C" int sssi_plan_stats_get(sssi_plan* plan, sssi_plan_stats* stats) {
         stats->device_bytes_budget = plan->budget;
         stats->batch_steps = plan->batch_steps;
         stats->cell_updates = plan->cells;
+        stats->admit_s = plan->admit_s;
+        stats->round_s = plan->round_s;
+        stats->gpu_wait_s = plan->gpu_wait_s;
+        stats->batch2d_gpu_s = plan->batch2d_gpu_s;
+        stats->batch2d_cell_updates = plan->batch2d_cells;
+        stats->deliver_s = plan->deliver_s;
     });
 }

@@ -98,6 +98,9 @@ class Prop3d {
 
     Desc3<T>& desc() { return desc_; }
     void set_point_sources(int nsrc, const int64_t* iz, const int64_t* ix, const int64_t* iy, const T* d_wavelet);
+    // Stream of the later launches and copies (set up on another stream, the
+    // caller orders this one after it).
+    void set_stream(cudaStream_t s) { stream_ = s; }
     void sync_desc();
     void run(int nsteps);  // whole runs of kGraphSteps go through a CUDA graph
     void check_errors();

@@ -86,6 +86,19 @@ int prop3d_occupancy(int N) {
 }  // namespace
 
 template <typename T>
+void launch_vdt2(const double* v, int64_t nz, int64_t nx, int64_t ny, double dt, T* out, int64_t ldz, int64_t ldxy,
+                 cudaStream_t s) {
+    if (nz * nx * ny == 0) return;
+    vdt2_kernel<T><<<152 * 4, 256, 0, s>>>(v, nz, nx, ny, dt, out, ldz, ldxy);
+    count_launch();
+    SSSI_CHECK_CUDA(cudaGetLastError());
+}
+template void launch_vdt2<float>(const double*, int64_t, int64_t, int64_t, double, float*, int64_t, int64_t,
+                                 cudaStream_t);
+template void launch_vdt2<double>(const double*, int64_t, int64_t, int64_t, double, double*, int64_t, int64_t,
+                                  cudaStream_t);
+
+template <typename T>
 Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, int nB, double dz, double dx,
                   double dy, double dt, int nt, cudaStream_t stream)
     : N_(N), stream_(stream) {
@@ -136,10 +149,7 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
             SSSI_CHECK_CUDA(cudaMemcpyAsync(vd.get(), v, sizeof(double) * n, cudaMemcpyHostToDevice, stream_));
             vdev = vd.template as<double>();
         }
-        vdt2_kernel<T><<<152 * 4, 256, 0, stream_>>>(vdev, nz, nx, ny, dt, vdt2_.template as<T>() + org, Nzp,
-                                                      Nzp * Nxp);
-        count_launch();
-        SSSI_CHECK_CUDA(cudaGetLastError());
+        launch_vdt2<T>(vdev, nz, nx, ny, dt, vdt2_.template as<T>() + org, Nzp, Nzp * Nxp, stream_);
         SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));  // vd is released at the end of this scope
     }
 

@@ -2,6 +2,7 @@
 // coefficients and damping profiles.  Compiled with -ffp-contract=off so every
 // expression rounds exactly as written (the reference C is built that way on
 // x86-64, where nothing is fused).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -67,7 +68,8 @@ double damp_m_order(double u, double v, double L) {
     return d0 * (q * q);
 }
 
-Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double dz, double dx, double dt) {
+Bands2D damping_bands_2d_strips(const double* bottom, const double* sides, int64_t nz, int64_t nx, int nB, double dz,
+                                double dx, double dt) {
     Bands2D b;
     b.zb.resize(static_cast<size_t>(nB) * nx);
     b.zbm1.resize(b.zb.size());
@@ -76,24 +78,33 @@ Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double
     // bottom band: u = (r+1)*dz, velocity of the damped cell (fwd...mex.c:127-145)
     for (int64_t j = 0; j < nx; ++j)
         for (int r = 0; r < nB; ++r) {
-            const int64_t i = nz - nB + r;
-            const double d = damp_c_order((r + 1) * dz, v[i + j * nz], nB * dz);
+            const double d = damp_c_order((r + 1) * dz, bottom[r + j * nB], nB * dz);
             const double e = std::exp(-d * dt);
             b.zb[r + j * nB] = e;
             b.zbm1[r + j * nB] = e - 1;
         }
     // left band u = (nB-j)*dx, right band u = (j-(nx-nB)+1)*dx (fwd...mex.c:100-124)
     for (int c = 0; c < 2 * nB; ++c) {
-        const int64_t j = c < nB ? c : nx - nB + (c - nB);
         const double u = c < nB ? (nB - c) * dx : (c - nB + 1) * dx;
         for (int64_t i = 0; i < nz; ++i) {
-            const double d = damp_c_order(u, v[i + j * nz], nB * dx);
+            const double d = damp_c_order(u, sides[i + c * nz], nB * dx);
             const double e = std::exp(-d * dt);
             b.xb[i + c * nz] = e;
             b.xbm1[i + c * nz] = e - 1;
         }
     }
     return b;
+}
+
+Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double dz, double dx, double dt) {
+    std::vector<double> bottom(static_cast<size_t>(nB) * nx), sides(static_cast<size_t>(nz) * 2 * nB);
+    for (int64_t j = 0; j < nx; ++j)
+        for (int r = 0; r < nB; ++r) bottom[r + j * nB] = v[nz - nB + r + j * nz];
+    for (int c = 0; c < 2 * nB; ++c) {
+        const int64_t j = c < nB ? c : nx - nB + (c - nB);
+        std::copy(v + j * nz, v + (j + 1) * nz, sides.begin() + c * nz);
+    }
+    return damping_bands_2d_strips(bottom.data(), sides.data(), nz, nx, nB, dz, dx, dt);
 }
 
 Bands3D damping_bands_3d(const double* vslice, const double* vtop, int64_t nz, int64_t nx, int64_t ny, int nB,

@@ -145,6 +145,12 @@ double damp_c_order(double u, double v, double L);
 // d = d0 .* (u/L).^2                              (src/dampPml.m:16-18)
 double damp_m_order(double u, double v, double L);
 
+// (v dt)^2 of the nz x nx x ny device model v into a padded layout (interior
+// origin `out`, strides ldz along x and ldxy along y), on stream s.
+template <typename T>
+void launch_vdt2(const double* v, int64_t nz, int64_t nx, int64_t ny, double dt, T* out, int64_t ldz, int64_t ldxy,
+                 cudaStream_t s);
+
 // Damping factors of the CPML bands of a 2D grid, C-gateway conventions
 // (fwdTimeCpmlFor2dAw_mex.c:100-145).  Bottom band: nB x nx (row r = i-(nz-nB)),
 // side bands: nz x 2nB (column c = j for the left band, nB + j-(nx-nB) for the right).
@@ -153,6 +159,10 @@ struct Bands2D {
     std::vector<double> xb, xbm1;  // nz x 2nB
 };
 Bands2D damping_bands_2d(const double* v, int64_t nz, int64_t nx, int nB, double dz, double dx, double dt);
+// The same from the velocities the bands read: bottom = rows nz-nB .. nz-1
+// (nB x nx), sides = columns 0 .. nB-1 then nx-nB .. nx-1 (nz x 2nB).
+Bands2D damping_bands_2d_strips(const double* bottom, const double* sides, int64_t nz, int64_t nx, int nB, double dz,
+                                double dx, double dt);
 
 // Damping factors of the 3D MATLAB file (src/fwdTimeCpmlFor3dAw.m:45-70):
 // cell units (L = nB), x profiles from the y=0 slice, y profiles from the top row,
