@@ -16,9 +16,15 @@
 namespace sssi {
 
 // Per-shot fields the tile code reads; copied to shared memory once per tile.
+// The first 16 bytes are what the thread that prepares a tile needs (it keeps
+// them in registers).
 template <typename T>
 struct alignas(16) ShotTail {
     using M = typename MemVar<T>::type;
+    int t_start;     // batch step of the shot's first step
+    int nt;          // steps of the shot
+    unsigned sched;  // derived on upload (sched_word): reverse, which hooks are set, stride
+    int oz;          // row offset of the interior in the padded fields
     T* field[2];  // interior origin of field k; field (t_local & 1) is current at local step t_local
     const T* zb;
     const T* zbm1;
@@ -29,9 +35,7 @@ struct alignas(16) ShotTail {
     M* xphi[2];
     M* xpsi;
     int64_t ldp;
-    int nz, nx, nB, ntz, ntx, oz;
-    int t_start;  // batch step of the shot's first step
-    int nt;       // steps of the shot
+    int nz, nx, nB, ntz, ntx;
     int reverse;  // time index tau = nt-1-t_local when set, else t_local
     int nsrc;
     int src_iz[kMaxPointSources];
@@ -47,7 +51,6 @@ struct alignas(16) ShotTail {
     // at (tau-1) % stride == 0 the current field (the result of step tau-1) is
     // stored in FP16 at pack + ((tau-1)/stride) * nz*nx, its 1/scale in inv_scale.
     int stride;
-    int pad_;
     unsigned* amax;
     __half* pack;
     float* inv_scale;
@@ -60,6 +63,46 @@ struct alignas(16) ShotTail {
     double* img_m;
     double* img_s2;
 };
+
+// Per-tile work flags.  kBandZ, kBandX and point sources inside the tile do
+// not change between steps and come with the work item; the rest are worked
+// out per step by the thread that prepares the tile.
+constexpr unsigned kBandZ = 1u;   // the z stencil of some cell reaches the damped band
+constexpr unsigned kBandX = 2u;   // the x stencil of some cell reaches a damped band
+constexpr unsigned kSource = 4u;  // something is injected into the tile at this step
+constexpr unsigned kRare = 8u;    // snapshot / FP16 pack / max / imaging output at this step
+constexpr unsigned kAmax = 16u;   // the step's max |field| is wanted
+
+// kBandZ / kBandX of the tile at (z0, x0) of an nz x nx grid with nB-cell bands
+// (bottom, left, right), stencil order N, tiles of TZ x TX cells.
+__host__ __device__ inline unsigned tile_band_flags(int N, int TZ, int TX, int nz, int nx, int nB, int z0, int x0) {
+    unsigned f = 0u;
+    if (nB > 0 && z0 + TZ + N - 1 > nz - nB) f |= kBandZ;
+    if (nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= nx - nB)) f |= kBandX;
+    return f;
+}
+
+// ShotTail::sched: bit 0 reverse, bits 1-7 the hooks that are set, stride above.
+constexpr unsigned kSchedReverse = 1u, kSchedDense = 2u, kSchedRow = 4u, kSchedSnap = 8u, kSchedImg64 = 16u,
+                   kSchedAmax = 32u, kSchedPack = 64u, kSchedImg16 = 128u;
+template <typename T>
+inline unsigned sched_word(const ShotTail<T>& d) {
+    unsigned w = d.reverse ? kSchedReverse : 0u;
+    if (d.src_dense) w |= kSchedDense;
+    if (d.src_row) w |= kSchedRow;
+    if (d.snap) w |= kSchedSnap;
+    if (d.img_f64) w |= kSchedImg64;
+    if (d.amax) w |= kSchedAmax;
+    if (d.pack) w |= kSchedPack;
+    if (d.img_f16) w |= kSchedImg16;
+    return w | ((unsigned)(d.stride > 0 ? d.stride : 1) << 8);
+}
+
+// A work item: shot k (< 2^24) with the tile's step-independent flags in the
+// top byte, and the tile's position (tz, tx) in tiles (each < 2^16).
+__host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int tz, int tx) {
+    return make_int2((int)((unsigned)k | (flags << 24)), (int)((unsigned)tz | ((unsigned)tx << 16)));
+}
 
 template <typename T>
 struct alignas(128) ShotDesc {
@@ -76,7 +119,7 @@ struct BatchConst {
     int nshots;
     int ntiles;  // host bookkeeping only: the kernel ends at the end of its work list
     const int* cta_begin;  // gridDim.x + 1: each CTA's range in `work`
-    const int2* work;      // (shot, tile within the shot), grouped by CTA
+    const int2* work;      // work items (pack_work_item), grouped by CTA
     const int* step_base;  // the launch computes batch step *step_base + step_offset
     int step_offset;
     int* err;              // set when a TMA copy does not arrive in time
@@ -101,7 +144,10 @@ class Batch2d {
     int add_shot_like(int k, int nt, int t_start, bool reverse);
     ShotTail<T>& shot(int k) { return shots_[k].desc.s; }
     void set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet);
-    void enable(int k, bool on) { shots_[k].enabled = on; }
+    void enable(int k, bool on) {
+        shots_[k].enabled = on;
+        stale_ = true;
+    }
     // Releases the device state of shot k; its slot is reused by a later add_shot.
     // The caller must have synchronised the stream past the shot's last step.
     void remove_shot(int k);
@@ -117,6 +163,8 @@ class Batch2d {
     void sync_desc(int k);
     void set_step(int step);
     // Launches `nsteps` batch steps (whole runs of kGraphSteps as graph replays).
+    // The schedule must be current: finalize() after any add, remove, enable
+    // or point-source change.
     void run(int nsteps);
     void check_errors();
     ~Batch2d();
@@ -142,6 +190,7 @@ class Batch2d {
     double dz_, dx_;
     cudaStream_t stream_;
     cudaStream_t upload_ = nullptr;
+    bool stale_ = true;  // shots or sources changed since the last finalize
     cudaStream_t up() const { return upload_ ? upload_ : stream_; }
     int take_slot();
     int add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,

@@ -90,9 +90,12 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
     SSSI_REQUIRE(nB >= 0 && nB <= nz && 2 * (int64_t)nB <= nx, SSSI_ERR_ARG,
                  "nBoundary %d does not fit the model (%lld x %lld): need nBoundary <= nz and 2*nBoundary <= nx", nB,
                  (long long)nz, (long long)nx);
-    SSSI_REQUIRE(nz < (1LL << 30) && nx < (1LL << 30), SSSI_ERR_ARG, "model too large");
+    SSSI_REQUIRE(nz <= 65535LL * TileShape<T>::TZ && nx <= 65535LL * TileShape<T>::TX, SSSI_ERR_ARG,
+                 "model too large (%lld x %lld): at most %lld x %lld", (long long)nz, (long long)nx,
+                 65535LL * TileShape<T>::TZ, 65535LL * TileShape<T>::TX);
     SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
     const int slot = take_slot();
+    stale_ = true;
     try {
         return add_shot_in(slot, v, -1, nz, nx, nB, dt, nt, t_start, reverse);
     } catch (...) {
@@ -107,6 +110,7 @@ int Batch2d<T>::add_shot_like(int k, int nt, int t_start, bool reverse) {
     SSSI_REQUIRE(nt >= 0, SSSI_ERR_ARG, "nt must be >= 0");
     const ShotTail<T> q = shots_[k].desc.s;
     const int slot = take_slot();
+    stale_ = true;
     try {
         return add_shot_in(slot, nullptr, k, q.nz, q.nx, q.nB, 0.0, nt, t_start, reverse);
     } catch (...) {
@@ -122,6 +126,7 @@ int Batch2d<T>::take_slot() {
             shots_[q].free = false;
             return q;
         }
+    SSSI_REQUIRE(shots_.size() < (1u << 24), SSSI_ERR_ARG, "too many shots in one batch");
     shots_.emplace_back();
     return (int)shots_.size() - 1;
 }
@@ -251,6 +256,7 @@ void Batch2d<T>::remove_shot(int k) {
     shots_[k] = Shot{};  // buffers go back to the pool
     shots_[k].enabled = false;
     shots_[k].free = true;
+    stale_ = true;
 }
 
 template <typename T>
@@ -266,6 +272,7 @@ void Batch2d<T>::set_point_sources(int k, int nsrc, const int64_t* iz, const int
                  kMaxPointSources, nsrc);
     ShotTail<T>& d = shots_[k].desc.s;
     d.nsrc = nsrc;
+    stale_ = true;  // point sources are part of the work items' flags
     for (int s = 0; s < nsrc; ++s) {
         SSSI_REQUIRE(iz[s] >= 0 && iz[s] < d.nz && ix[s] >= 0 && ix[s] < d.nx, SSSI_ERR_ARG,
                      "point source %d at (%lld, %lld) outside the %d x %d model", s, (long long)iz[s],
@@ -301,7 +308,8 @@ void Batch2d<T>::finalize() {
     // reaches a damped band add a cooperative first-derivative pass and the
     // memory-variable traffic
     struct Item {
-        int shot, local;
+        int shot, z0, x0;
+        unsigned flags;  // step-independent
         float cost;
     };
     std::vector<Item> items;
@@ -313,11 +321,14 @@ void Batch2d<T>::finalize() {
             // measured: a tile next to a band costs about 1.2 interior tiles more
             // per banded direction (the cooperative pass and the memory-variable
             // round trips); partial tiles cost in proportion to their cells
-            const bool bz = d.nB > 0 && z0 + Sh::TZ + N_ - 1 > d.nz - d.nB;
-            const bool bx = d.nB > 0 && (x0 - N_ < d.nB || x0 + Sh::TX + N_ - 2 >= d.nx - d.nB);
+            unsigned f = tile_band_flags(N_, Sh::TZ, Sh::TX, d.nz, d.nx, d.nB, z0, x0);
+            const bool bz = f & kBandZ, bx = f & kBandX;
+            for (int s = 0; s < d.nsrc; ++s)
+                if (d.src_iz[s] >= z0 && d.src_iz[s] < z0 + Sh::TZ && d.src_ix[s] >= x0 && d.src_ix[s] < x0 + Sh::TX)
+                    f |= kSource;
             const float fill = (float)(std::min(Sh::TZ, d.nz - z0) * std::min(Sh::TX, d.nx - x0)) /
                                (float)(Sh::TZ * Sh::TX);
-            items.push_back({k, q, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))});
+            items.push_back({k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))});
         }
     }
     ntiles_ = (int)items.size();
@@ -333,7 +344,7 @@ void Batch2d<T>::finalize() {
         for (const Item& it : items) {
             P top = heap.top();
             heap.pop();
-            lists[top.second].push_back(make_int2(it.shot, it.local));
+            lists[top.second].push_back(pack_work_item(it.shot, it.flags, it.z0 / Sh::TZ, it.x0 / Sh::TX));
             top.first += it.cost;
             heap.push(top);
         }
@@ -363,10 +374,14 @@ void Batch2d<T>::finalize() {
     bc_.ntiles = ntiles_;
     bc_.cta_begin = d_cta_begin_.template as<int>();
     bc_.work = d_work_.template as<int2>();
+    stale_ = false;
 }
 
 template <typename T>
 void Batch2d<T>::sync_desc(int k) {
+    ShotTail<T>& d = shots_[k].desc.s;
+    SSSI_REQUIRE(d.stride < (1 << 24), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
+    d.sched = sched_word(d);
     SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.template as<ShotDesc<T>>() + k, &shots_[k].desc, sizeof(ShotDesc<T>),
                                     cudaMemcpyHostToDevice, stream_));
 }
@@ -386,7 +401,7 @@ void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
 
 template <typename T>
 void Batch2d<T>::run(int nsteps) {
-    SSSI_REQUIRE(grid_ > 0, SSSI_ERR_INTERNAL, "Batch2d::run before finalize");
+    SSSI_REQUIRE(grid_ > 0 && !stale_, SSSI_ERR_INTERNAL, "Batch2d::run: the schedule is out of date (finalize)");
     int q = 0;
     if (nsteps >= kGraphSteps) {
         int* base = d_ctr_.template as<int>();

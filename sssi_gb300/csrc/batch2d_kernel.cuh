@@ -76,17 +76,11 @@ constexpr int kNoTile = 0x7fffffff;
 struct TileInfo {
     int tile;        // position in the work list (kNoTile: the CTA has no more tiles)
     int shot;        // -1: nothing to do (no tile, or the shot is inactive)
-    int local;       // tile index within the shot
     int tloc;        // local step of the shot
     int tau;         // time index of the step
     int z0, x0;      // tile origin within the shot
     unsigned flags;  // kBandZ | kBandX | kSource | kRare | kAmax
 };
-constexpr unsigned kBandZ = 1u;   // the z stencil of some cell reaches the damped band
-constexpr unsigned kBandX = 2u;   // the x stencil of some cell reaches a damped band
-constexpr unsigned kSource = 4u;  // something is injected into the tile at this step
-constexpr unsigned kRare = 8u;    // snapshot / FP16 pack / max / imaging output at this step
-constexpr unsigned kAmax = 16u;   // the step's max |field| is wanted
 
 template <typename T, int RX>
 struct Blk {
@@ -254,7 +248,7 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
         for (int c = 0; c < ncol; ++c)
             for (int o = 0; o < nrow; ++o)
                 pack[(i0 + o) + (int64_t)(j0 + c) * nz] = __float2half_rn(f32(pc.v[c][o]) * scale);
-        if (ti.local == 0 && i0 == 0 && j0 == 0) sh.inv_scale[k] = 1.0f / scale;
+        if (i0 == 0 && j0 == 0) sh.inv_scale[k] = 1.0f / scale;
     }
     if (sh.amax && tau % stride == 0) {
         for (int c = 0; c < ncol; ++c)
@@ -546,24 +540,19 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
     if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
 }
 
-// Per-tile work flags, worked out once by the preparing thread.
-template <typename T, int N>
-__device__ __forceinline__ unsigned tile_flags(const ShotTail<T>& g, int z0, int x0, int tau) {
-    constexpr int TZ = TileShape<T>::TZ, TX = TileShape<T>::TX;
-    unsigned f = 0u;
-    const int nB = g.nB;
-    if (nB > 0 && z0 + TZ + N - 1 > g.nz - nB) f |= kBandZ;
-    if (nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= g.nx - nB)) f |= kBandX;
-    bool src = g.src_dense != nullptr || (g.src_row != nullptr && z0 == 0);
-    for (int s = 0; s < g.nsrc; ++s)
-        src |= g.src_iz[s] >= z0 && g.src_iz[s] < z0 + TZ && g.src_ix[s] >= x0 && g.src_ix[s] < x0 + TX;
-    if (src) f |= kSource;
-    const int stride = g.stride > 0 ? g.stride : 1;
-    const bool on_stride = tau % stride == 0;
-    if (g.amax && on_stride) f |= kAmax;
-    bool rare = g.snap != nullptr || (g.pack != nullptr && tau >= 1 && (tau - 1) % stride == 0) ||
-                (g.amax != nullptr && on_stride) || (g.img_f16 != nullptr && on_stride);
-    if constexpr (std::is_same<T, double>::value) rare |= g.img_f64 != nullptr;
+// Per-tile work flags at step tau, worked out by the preparing thread from
+// the work item's step-independent flags (bands, point sources) and the
+// shot's sched word.
+__device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned f, int tau) {
+    if ((sched & kSchedDense) || ((sched & kSchedRow) && z0 == 0)) f |= kSource;
+    bool rare = (sched & (kSchedSnap | kSchedImg64)) != 0u;
+    if (sched & (kSchedAmax | kSchedPack | kSchedImg16)) {  // outputs every stride steps
+        const int stride = (int)(sched >> 8);
+        const bool on_stride = tau % stride == 0;
+        if ((sched & kSchedAmax) && on_stride) f |= kAmax;
+        rare |= ((sched & kSchedPack) && tau >= 1 && (tau - 1) % stride == 0) ||
+                ((sched & (kSchedAmax | kSchedImg16)) && on_stride);
+    }
     if (rare) f |= kRare;
     return f;
 }
@@ -622,15 +611,15 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
     const int wbeg = bc.cta_begin[blockIdx.x], wend = bc.cta_begin[blockIdx.x + 1];
     constexpr int kTailVec = (int)(sizeof(ShotTail<T>) / 16);
     static_assert(kTailVec <= 32, "ShotTail must fit one 16-byte load per lane");
-    int2 item = make_int2(-1, 0);  // prefetched work item
+    int2 item = make_int2(-1, 0);  // prefetched work item (pack_work_item; x = -1: none)
     unsigned inflight = 0;          // lane 0 of warp 0: stages with copies not yet consumed
     uint4 tail_reg = make_uint4(0, 0, 0, 0);
     auto fetch = [&](int w) {  // warp 0: load item w and its shot's tail into registers
         item = w < wend ? bc.work[w] : make_int2(-1, 0);
-        if (item.x >= 0 && lane < kTailVec) tail_reg = reinterpret_cast<const uint4*>(&shots[item.x].s)[lane];
+        if (item.x >= 0 && lane < kTailVec)
+            tail_reg = reinterpret_cast<const uint4*>(&shots[item.x & 0xffffff].s)[lane];
     };
-    // warp 0: put the prefetched item into stage s (tile = its position in the list)
-    // lane 0 of warp 0: the three copies of stage s (after prepare_info recorded it)
+    // lane 0 of warp 0: the three copies of a stage prepared earlier (first stages)
     auto issue = [&](int s) {
         unsigned char* st = smem + s * G::kStage;
         const TileInfo* info = reinterpret_cast<const TileInfo*>(st + G::kInfo);
@@ -645,36 +634,44 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], g.oz + z0, x0 + L);
         }
     };
+    // warp 0: put the prefetched item into stage s (tile = its position in the
+    // list); with `copy`, lane 0 also issues the stage's three copies.  Lane 0
+    // works from registers: the item and the head of the shot's tail.
     auto prepare = [&](int w, int s, bool copy) {
         unsigned char* st = smem + s * G::kStage;
         TileInfo* info = reinterpret_cast<TileInfo*>(st + G::kInfo);
-        const int k = item.x;
+        const int k = item.x >= 0 ? (item.x & 0xffffff) : -1;
         if (k >= 0 && lane < kTailVec) reinterpret_cast<uint4*>(st + G::kTail)[lane] = tail_reg;
-        __syncwarp();
         if (lane == 0) {
+            const int t_start = (int)tail_reg.x, nt = (int)tail_reg.y, oz = (int)tail_reg.w;
+            const unsigned sched = tail_reg.z;
             int shot = -1, tloc = 0, tau = 0;
-            const ShotTail<T>& g = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
             if (k >= 0) {
-                tloc = step - g.t_start;
-                if (tloc >= 0 && tloc < g.nt) {
+                tloc = step - t_start;
+                if (tloc >= 0 && tloc < nt) {
                     shot = k;
-                    tau = g.reverse ? g.nt - 1 - tloc : tloc;
+                    tau = (sched & kSchedReverse) ? nt - 1 - tloc : tloc;
                 }
             }
+            const int z0 = (item.y & 0xffff) * TZ, x0 = ((unsigned)item.y >> 16) * TX;
             info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
-            info->local = item.y;
             info->tloc = tloc;
             info->tau = tau;
-            if (shot >= 0) {
-                const int z0 = (item.y % g.ntz) * TZ, x0 = (item.y / g.ntz) * TX;
-                info->z0 = z0;
-                info->x0 = x0;
-                info->flags = tile_flags<T, N>(g, z0, x0, tau);
+            info->z0 = z0;
+            info->x0 = x0;
+            info->flags = shot >= 0 ? tile_flags(sched, z0, (unsigned)item.x >> 24, tau) : 0u;
+            if (copy && shot >= 0) {
+                const int cur = tloc & 1;
+                inflight |= 1u << s;
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(&bar[s], G::kTx);
+                tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], oz + z0 - HZ, x0);
+                tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], oz + z0, x0 + L);
+                tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], oz + z0, x0 + L);
             }
         }
         __syncwarp();
-        if (copy) issue(s);
     };
 
     const int r0 = 4 * (tid % (TZ / 4));
