@@ -87,6 +87,12 @@ def cell_updates(nz, nx, nt):
     return 3 * nz * nx * nt
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one forward step of the RTM
+# shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
+# python bench.py --case rtm-short`
+FWD_STEP_DRAM_BYTES = 22_955_008
+
+
 def step_bytes_per_cell(nz, nx, nb):
     """Algorithmic HBM bytes of one FP32 step per cell: P(t), P(t-1), (v dt)^2
     read and P(t+1) written (16 B), plus, per damped cell and axis, the
@@ -254,7 +260,10 @@ def run_gpu(args):
         "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms64, 3),
                  "mode": "fp64 (fused multiply-add)", "steps": fp64_steps},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": FWD_STEP_DRAM_BYTES,
+                     "traffic_note": "dram read+write of one forward step from an ncu capture of the same grid "
+                                     "(caches flushed per pass); the timed steps run from L2",
+                     "alg_bytes_per_launch": int(alg_bytes), "peak_kind": peak_kind,
                      "kernel": "cpml2d step (fp32, forward phase)", "bytes_per_cell": round(bytes_cell, 2),
                      "launch_ms": round(per_launch_ms, 5)},
         "gpu_launches": int(launches32),

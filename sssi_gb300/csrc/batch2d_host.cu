@@ -5,7 +5,7 @@
 
 #include <cmath>
 #include <mutex>
-#include <queue>
+#include <functional>
 
 #include "batch2d.cuh"
 
@@ -313,6 +313,12 @@ void Batch2d<T>::finalize() {
         float cost;
     };
     std::vector<Item> items;
+    {
+        size_t n = 0;
+        for (const Shot& S : shots_)
+            if (S.enabled) n += (size_t)S.desc.s.ntz * S.desc.s.ntx;
+        items.reserve(n);
+    }
     for (int k = 0; k < (int)shots_.size(); ++k) {
         if (!shots_[k].enabled) continue;
         const ShotTail<T>& d = shots_[k].desc.s;
@@ -335,32 +341,46 @@ void Batch2d<T>::finalize() {
     grid_ = std::max(1, std::min(ntiles_, sms_ * ctas_per_sm_));
     // longest processing time first onto the least loaded CTA
     std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
-    std::vector<float> load(grid_, 0.0f);
-    std::vector<std::vector<int2>> lists(grid_);
+    std::vector<int> owner(items.size());
+    std::vector<int> begin(grid_ + 1, 0);
     {
         using P = std::pair<float, int>;
-        std::priority_queue<P, std::vector<P>, std::greater<P>> heap;
-        for (int c = 0; c < grid_; ++c) heap.push({0.0f, c});
-        for (const Item& it : items) {
-            P top = heap.top();
-            heap.pop();
-            lists[top.second].push_back(pack_work_item(it.shot, it.flags, it.z0 / Sh::TZ, it.x0 / Sh::TX));
-            top.first += it.cost;
-            heap.push(top);
+        std::vector<P> heap;  // min-heap on load
+        heap.reserve(grid_);
+        for (int c = 0; c < grid_; ++c) heap.push_back({0.0f, c});
+        const auto cmp = std::greater<P>();
+        for (size_t q = 0; q < items.size(); ++q) {
+            std::pop_heap(heap.begin(), heap.end(), cmp);
+            P& top = heap.back();
+            owner[q] = top.second;
+            ++begin[top.second + 1];
+            top.first += items[q].cost;
+            std::push_heap(heap.begin(), heap.end(), cmp);
         }
     }
-    std::vector<int> begin(grid_ + 1, 0);
-    std::vector<int2> work;
-    work.reserve(items.size());
-    for (int c = 0; c < grid_; ++c) {
-        begin[c] = (int)work.size();
-        work.insert(work.end(), lists[c].begin(), lists[c].end());
+    for (int c = 0; c < grid_; ++c) begin[c + 1] += begin[c];
+    std::vector<int2> work(items.size());
+    {
+        std::vector<int> fill(begin.begin(), begin.end() - 1);
+        for (size_t q = 0; q < items.size(); ++q) {
+            const Item& it = items[q];
+            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0 / Sh::TZ, it.x0 / Sh::TX);
+        }
     }
-    begin[grid_] = (int)work.size();
 
+    // descriptors of every slot in one copy
     const size_t nd = std::max<size_t>(shots_.size(), 1);
     if (d_desc_.bytes() < nd * sizeof(ShotDesc<T>)) d_desc_.allocate(nd * sizeof(ShotDesc<T>));
-    for (int k = 0; k < (int)shots_.size(); ++k) sync_desc(k);
+    std::vector<ShotDesc<T>> hdesc(shots_.size());
+    for (int k = 0; k < (int)shots_.size(); ++k) {
+        ShotTail<T>& d = shots_[k].desc.s;
+        SSSI_REQUIRE(d.stride < (1 << 24), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
+        d.sched = sched_word(d);
+        hdesc[k] = shots_[k].desc;
+    }
+    if (!hdesc.empty())
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.get(), hdesc.data(), sizeof(ShotDesc<T>) * hdesc.size(),
+                                        cudaMemcpyHostToDevice, stream_));
     if (d_cta_begin_.bytes() < sizeof(int) * begin.size()) d_cta_begin_.allocate(sizeof(int) * begin.size());
     if (d_work_.bytes() < sizeof(int2) * std::max<size_t>(work.size(), 1))
         d_work_.allocate(sizeof(int2) * std::max<size_t>(work.size(), 1));
