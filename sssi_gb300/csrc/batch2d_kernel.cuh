@@ -71,6 +71,7 @@ __device__ __forceinline__ float f32(float x) { return x; }
 __device__ __forceinline__ float f32(double x) { return static_cast<float>(x); }
 
 constexpr int kNoTile = 0x7fffffff;
+constexpr unsigned kHalf = 32u;  // TileInfo flag: half of a tile (its TX/2 columns at x0)
 
 // Per-tile facts shared by the block (written by warp 0 with the ShotTail).
 struct TileInfo {
@@ -111,13 +112,14 @@ struct BandScratch {
 
 // Stage one of a band tile, run by every thread of the block; the caller
 // synchronises the block before the scratch is read.
-template <typename T, int N>
+template <typename T, int N, int TX>
 __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
                                          int x0, bool bz, bool bx, T* scratch) {
     using S = TileShape<T>;
     using B = BandScratch<T, N>;
     using M = typename MemVar<T>::type;
-    constexpr int TZ = S::TZ, TX = S::TX, NT = S::kThreads;
+    constexpr int TZ = S::TZ, NT = S::kThreads;
+    constexpr int CXW = TX + 2 * N - 1;  // xA columns used (pitch TZ)
     constexpr int L = 2 * N - 1;
     constexpr int HZ = tile_halo_rows(N);
     constexpr int SP = TZ + 2 * HZ;
@@ -175,7 +177,7 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
         }
     }
     if (bx) {
-        constexpr int CELLS = TZ * B::CX;
+        constexpr int CELLS = TZ * CXW;
         constexpr int MU = (CELLS + NT - 1) / NT;
         const T* xb = sh.xb;
         const T* xbm1 = sh.xbm1;
@@ -336,14 +338,14 @@ __device__ __forceinline__ void add_sources(const ShotTail<T>& sh, int tau, int 
 // All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  kBandZ / kBandX:
 // the tile is a band tile in z / x, its first derivatives are in `scratch`;
 // otherwise the composed stencil is used in that direction.
-template <typename T, int N>
+template <typename T, int N, int RX>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
                                            unsigned flags, const T* scratch, unsigned& amax_bits) {
     using S = TileShape<T>;
     using B = BandScratch<T, N>;
     using M = typename MemVar<T>::type;
-    constexpr int TZ = S::TZ, RX = S::RX;
+    constexpr int TZ = S::TZ;
     constexpr int L = 2 * N - 1;
     constexpr int HZ = tile_halo_rows(N);
     constexpr int SP = TZ + 2 * HZ;  // pitch of a P-box column
@@ -653,14 +655,16 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                     tau = (sched & kSchedReverse) ? nt - 1 - tloc : tloc;
                 }
             }
-            const int z0 = (item.y & 0xffff) * TZ, x0 = ((unsigned)item.y >> 16) * TX;
+            const unsigned top = (unsigned)item.x >> 24;  // static flags | half << 3
+            const unsigned half = (top >> 3) & 3u;         // 0 whole tile, 1 / 2 left / right half
+            const int z0 = (item.y & 0xffff) * TZ, x0 = ((unsigned)item.y >> 16) * TX + (half == 2u ? TX / 2 : 0);
             info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
             info->tloc = tloc;
             info->tau = tau;
             info->z0 = z0;
             info->x0 = x0;
-            info->flags = shot >= 0 ? tile_flags(sched, z0, (unsigned)item.x >> 24, tau) : 0u;
+            info->flags = shot >= 0 ? tile_flags(sched, z0, top & 7u, tau) | (half ? kHalf : 0u) : 0u;
             if (copy && shot >= 0) {
                 const int cur = tloc & 1;
                 inflight |= 1u << s;
@@ -723,12 +727,20 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             unsigned amax_bits = 0u;
             const int i0 = z0 + r0, j0 = x0 + c0;
             T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
+            // a half tile (band tiles of small grids, split so that they do not set the
+            // length of the step) has TX/2 columns: the first half of the threads
+            const bool half = ti.flags & kHalf;
             if (ti.flags & (kBandZ | kBandX)) {
-                band_stage1<T, N>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX, scratch);
+                if (half)
+                    band_stage1<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
+                                              scratch);
+                else
+                    band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
+                                          scratch);
                 __syncthreads();
             }
-            if (i0 < sh.nz && j0 < sh.nx)
-                tile_cells<T, N>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+            if (i0 < sh.nz && j0 < sh.nx && (!half || c0 < TX / 2))
+                tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             if (ti.flags & kAmax) {
                 const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
                 if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
