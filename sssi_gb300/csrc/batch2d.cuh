@@ -203,14 +203,16 @@ class Batch2d {
     // descriptors are read from device memory, so only these invalidate it)
     struct GraphKey {
         int grid = 0;
+        bool split = false;
         const void *desc = nullptr, *begin = nullptr, *work = nullptr;
         bool operator==(const GraphKey& o) const {
-            return grid == o.grid && desc == o.desc && begin == o.begin && work == o.work;
+            return grid == o.grid && split == o.split && desc == o.desc && begin == o.begin && work == o.work;
         }
     } graph_key_;
     GraphKey current_key() const {
-        return GraphKey{grid_, d_desc_.get(), d_cta_begin_.get(), d_work_.get()};
+        return GraphKey{grid_, split_, d_desc_.get(), d_cta_begin_.get(), d_work_.get()};
     }
+    bool split_ = false;  // the schedule holds half tiles
     DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;  // d_ctr_: graph step base, zero, error flag
     int grid_ = 0, ntiles_ = 0, step_ = 0;
     int ctas_per_sm_ = 1, sms_ = 1;
@@ -218,12 +220,14 @@ class Batch2d {
 };
 
 // Launches one batch step with the programmatic-serialization attribute.
+// split: the work lists hold half tiles.
 template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream);
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, cudaStream_t stream);
 template <typename T, int N>
 int batch2d_occupancy_n();
 template <typename T>
-void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream);
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+                    cudaStream_t stream);
 template <typename T>
 int batch2d_ctas_per_sm(int N);
 

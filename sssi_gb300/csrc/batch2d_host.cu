@@ -352,7 +352,8 @@ void Batch2d<T>::finalize() {
         float total = 0.0f;
         for (const Item& it : items) total += it.cost;
         const int blocks = std::max(1, std::min((int)items.size(), sms_ * ctas_per_sm_));
-        if (total < 2.0f * (float)blocks) {
+        split_ = total < 2.0f * (float)blocks;
+        if (split_) {
             std::vector<Item> split;
             split.reserve(items.size() + items.size() / 4);
             for (const Item& it : items) {
@@ -457,7 +458,7 @@ void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
     BatchConst<T> bc = bc_;
     bc.step_base = base;
     bc.step_offset = offset;
-    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, stream);
+    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, stream);
 }
 
 template <typename T>
@@ -519,16 +520,17 @@ void Batch2d<T>::check_errors() {
 }
 
 template <typename T>
-void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+                    cudaStream_t stream) {
     switch (N) {
-        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, stream); break;
-        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, stream); break;
-        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, stream); break;
-        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, stream); break;
-        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, stream); break;
-        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, stream); break;
-        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, stream); break;
-        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, stream); break;
+        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, stream); break;
+        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, stream); break;
+        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, stream); break;
+        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, stream); break;
+        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, stream); break;
+        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, stream); break;
+        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, stream); break;
+        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, stream); break;
         default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
     }
 }

@@ -583,7 +583,9 @@ struct StageLayout {
 
 constexpr unsigned kWaitLimit = 1u << 24;
 
-template <typename T, int N>
+// kSplit: the work lists may hold half tiles (schedules of small grids); the
+// variant without them keeps the whole-tile path free of their handling.
+template <typename T, int N, bool kSplit>
 __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBlocks)
     batch2d_kernel(const ShotDesc<T>* __restrict__ shots, const __grid_constant__ BatchConst<T> bc) {
     using S = TileShape<T>;
@@ -656,7 +658,7 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 }
             }
             const unsigned top = (unsigned)item.x >> 24;  // static flags | half << 3
-            const unsigned half = (top >> 3) & 3u;         // 0 whole tile, 1 / 2 left / right half
+            const unsigned half = kSplit ? (top >> 3) & 3u : 0u;  // 0 whole tile, 1 / 2 left / right half
             const int z0 = (item.y & 0xffff) * TZ, x0 = ((unsigned)item.y >> 16) * TX + (half == 2u ? TX / 2 : 0);
             info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
@@ -727,20 +729,30 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             unsigned amax_bits = 0u;
             const int i0 = z0 + r0, j0 = x0 + c0;
             T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
-            // a half tile (band tiles of small grids, split so that they do not set the
-            // length of the step) has TX/2 columns: the first half of the threads
-            const bool half = ti.flags & kHalf;
-            if (ti.flags & (kBandZ | kBandX)) {
-                if (half)
-                    band_stage1<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
+            if constexpr (kSplit) {
+                // a half tile (band tiles of small grids, split so that they do not set
+                // the length of the step) has TX/2 columns: the first half of the threads
+                const bool half = ti.flags & kHalf;
+                if (ti.flags & (kBandZ | kBandX)) {
+                    if (half)
+                        band_stage1<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
+                                                  ti.flags & kBandX, scratch);
+                    else
+                        band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
                                               scratch);
-                else
+                    __syncthreads();
+                }
+                if (i0 < sh.nz && j0 < sh.nx && (!half || c0 < TX / 2))
+                    tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+            } else {
+                if (ti.flags & (kBandZ | kBandX)) {
                     band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
                                           scratch);
-                __syncthreads();
+                    __syncthreads();
+                }
+                if (i0 < sh.nz && j0 < sh.nx)
+                    tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             }
-            if (i0 < sh.nz && j0 < sh.nx && (!half || c0 < TX / 2))
-                tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             if (ti.flags & kAmax) {
                 const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
                 if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
@@ -761,13 +773,13 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
 
 }  // namespace batch
 
-template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
+template <typename T, int N, bool kSplit>
+void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
     using G = batch::StageLayout<T, N>;
     static bool configured = false;
     if (!configured) {
-        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)G::kSmem));
+        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem));
         configured = true;
     }
     cudaLaunchConfig_t cfg = {};
@@ -780,19 +792,27 @@ void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int gri
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N>, shots, bc));
+    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit>, shots, bc));
     count_launch();
+}
+
+template <typename T, int N>
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, cudaStream_t stream) {
+    if (split)
+        launch_batch2d_variant<T, N, true>(shots, bc, grid, stream);
+    else
+        launch_batch2d_variant<T, N, false>(shots, bc, grid, stream);
 }
 
 template <typename T, int N>
 int batch2d_occupancy_n() {
     const size_t smem = batch::StageLayout<T, N>::kSmem;
     int n = 0;
-    cudaError_t e =
-        cudaFuncSetAttribute(batch::batch2d_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N>, TileShape<T>::kThreads,
-                                                          smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false>,
+                                                          TileShape<T>::kThreads, smem);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
         n = 1;
@@ -801,7 +821,7 @@ int batch2d_occupancy_n() {
 }
 
 #define SSSI_BATCH2D_INSTANCE(T, N)                                                                           \
-    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, cudaStream_t);      \
+    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, cudaStream_t); \
     template int batch2d_occupancy_n<T, N>();
 
 }  // namespace sssi
