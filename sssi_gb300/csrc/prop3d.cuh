@@ -2,7 +2,8 @@
 // the whole volume, persistent blocks marching along y.
 //
 // Work item: a TZ x TX tile of the (z, x) plane and a chunk of planes along
-// y (chunk length chosen per grid so that the items fill the GPU).  For each output plane the block copies that plane's P tile with its z
+// y (chunks cut per tile by estimated cost, so that the items fill the GPU and
+// tiles next to the damped bands get shorter chunks).  For each output plane the block copies that plane's P tile with its z
 // and x halo, and its P_old and (v dt)^2 tiles, into shared memory (TMA, ring
 // of kStages planes), together with the tile's own cells of P at plane
 // y+2N-1, which enter the y queue; the z and x
@@ -57,9 +58,9 @@ struct Desc3 {
     int64_t ldz;              // Nzp: stride of x
     int64_t ldxy;             // Nzp * Nxp: stride of y
     int nz, nx, ny, nB, nt;
-    int ntz, ntx, nchunk;  // tiles along z and x, chunks along y
-    int ychunk;            // planes per chunk
-    const int* order;      // work items (tile + ntz*ntx*chunk), most expensive first
+    int ntz, ntx;          // tiles along z and x
+    const int2* order[2];  // work items (tile, y0 | y1 << 16: planes y0 .. y1-1), most expensive first, of
+                           // the two candidate schedules (Const3::sched picks one)
     int* next;             // two counters: items taken at steps of parity 0 / 1
     // band coefficients (2D) and memory variables (3D), see the file header
     const T *zb, *zbm1, *xb, *xbm1, *yb, *ybm1;
@@ -80,6 +81,7 @@ struct Const3 {
     T az[16], ax[16];  // composed second-derivative coefficients (z, x)
     T wz[8], wx[8], wy[8];
     int nitems;
+    int sched;             // the schedule in use (Desc3::order)
     const int* step_base;  // the launch computes step *step_base + step_offset
     int step_offset;
     int* err;
@@ -102,22 +104,33 @@ class Prop3d {
     // caller orders this one after it).
     void set_stream(cudaStream_t s) { stream_ = s; }
     void sync_desc();
-    void run(int nsteps);  // whole runs of kGraphSteps go through a CUDA graph
+    // Whole runs of kGraphSteps go through a CUDA graph.  The first steps of a
+    // long run time the two candidate schedules (even chunks along y, or chunks
+    // cut by estimated cost per tile); the faster one is kept.
+    void run(int nsteps);
     void check_errors();
+    int schedule() const { return cc_.sched; }
     const T* current_field() const { return desc_.field[step_ & 1]; }
     int step() const { return step_; }
     static constexpr int kGraphSteps = 16;
 
   private:
     void launch_step(const int* base, int offset, cudaStream_t s);
+    void use_schedule(int c);
     int N_;
     cudaStream_t stream_;
     Desc3<T> desc_{};
     Const3<T> cc_{};
     DeviceBuffer P_[2], vdt2_, zb_, zbm1_, xb_, xbm1_, yb_, ybm1_, zphi_[2], zpsi_, xphi_[2], xpsi_, yphi_[2], ypsi_;
-    DeviceBuffer d_desc_, d_ctr_, d_order_, d_next_;
+    DeviceBuffer d_desc_, d_ctr_, d_order_[2], d_next_;
+    int nitems_[2] = {0, 0}, grid_c_[2] = {1, 1};
     int grid_ = 0, step_ = 0;
     cudaGraphExec_t graph_ = nullptr;
+    // schedule tuning: phase 0 warm-up, 1 / 2 timing schedule 0 / 1, 3 waiting
+    // for the timings, 4 done
+    static constexpr int kTuneSteps = 6, kTuneMinSteps = 48;
+    int tune_ = 0, tune_left_ = 2;
+    cudaEvent_t tev_[4] = {nullptr, nullptr, nullptr, nullptr};  // start and end of the two timed runs
 };
 
 template <typename T, int N>

@@ -221,18 +221,10 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     d.nt = nt;
     d.ntz = (int)((nz + S::TZ - 1) / S::TZ);
     d.ntx = (int)((nx + S::TX - 1) / S::TX);
-    // chunks along y: enough work items for about three per resident block,
-    // each at least 8 planes (a chunk re-reads 4N-2 planes to fill its queues)
     int dev = 0, sms = 1;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
     SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int slots = sms * prop3d_occupancy<T>(N);
-    const int64_t tiles = (int64_t)d.ntz * d.ntx;
-    int64_t yc = std::max<int64_t>(8, (ny * tiles + 3 * slots - 1) / (3 * (int64_t)slots));
-    yc = std::min<int64_t>(yc, 64);
-    const int64_t nch = (ny + yc - 1) / yc;
-    d.ychunk = (int)((ny + nch - 1) / nch);             // even chunks
-    d.nchunk = (int)((ny + d.ychunk - 1) / d.ychunk);  // every chunk starts inside the grid
     d.zb = zb_.template as<T>();
     d.zbm1 = zbm1_.template as<T>();
     d.xb = xb_.template as<T>();
@@ -254,38 +246,85 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     cc_.step_base = d_ctr_.template as<int>() + 1;
     cc_.step_offset = 0;
     cc_.err = d_ctr_.template as<int>() + 2;
-    cc_.nitems = d.ntz * d.ntx * d.nchunk;
-    grid_ = std::max(1, std::min(cc_.nitems, slots));
-    // item order for the dynamic schedule: estimated cost, highest first
-    // (tiles next to a z or x band add a cooperative pass per plane; y band
-    // planes add memory-variable traffic; every chunk fills its queues)
+    // Two candidate schedules of work items, each item a (z, x) tile and a chunk
+    // of planes; the dynamic schedule takes the most expensive first.  Cost
+    // model: a plane costs 1, 1.6 next to a z or x band (cooperative pass per
+    // plane), +0.4 in a y band (memory-variable traffic); every chunk also
+    // fills its queues from 2N-1 planes (0.3 each).
+    //   0: even chunks along y, enough items for about three per resident
+    //      block, 8 to 64 planes;
+    //   1: each tile's planes cut into chunks of about equal estimated cost
+    //      (tiles next to a band get shorter chunks), 4 to 64 planes.
     {
+        SSSI_REQUIRE(ny < 65536, SSSI_ERR_ARG, "ny must be below 65536");
+        const int ntile = d.ntz * d.ntx;
+        auto plane_cost = [&](bool band_zx, int y) {
+            return (band_zx ? 1.6f : 1.0f) + ((nB > 0 && (y < nB || y >= ny - nB)) ? 0.4f : 0.0f);
+        };
+        std::vector<char> bzx(ntile);
+        double total = 0;
+        for (int t = 0; t < ntile; ++t) {
+            const int z0 = (t % d.ntz) * S::TZ, x0 = (t / d.ntz) * S::TX;
+            bzx[t] = nB > 0 && (z0 + S::TZ + N - 1 > nz - nB || x0 - N < nB || x0 + S::TX + N - 2 >= nx - nB);
+            for (int y = 0; y < ny; ++y) total += plane_cost(bzx[t], y);
+        }
+        const float warm = 0.3f * (2 * N - 1);
         struct It {
-            int item;
+            int2 item;
             float cost;
         };
-        std::vector<It> its((size_t)cc_.nitems);
-        for (int it = 0; it < cc_.nitems; ++it) {
-            const int tile = it % (d.ntz * d.ntx), chunk = it / (d.ntz * d.ntx);
-            const int z0 = (tile % d.ntz) * S::TZ, x0 = (tile / d.ntz) * S::TX;
-            const int y0 = chunk * d.ychunk, y1 = (int)std::min<int64_t>(y0 + d.ychunk, ny);
-            const bool band_zx = nB > 0 && (z0 + S::TZ + N - 1 > nz - nB || x0 - N < nB ||
-                                            x0 + S::TX + N - 2 >= nx - nB);
-            int ybands = 0;
-            for (int y = y0; y < y1; ++y) ybands += (nB > 0 && (y < nB || y >= ny - nB)) ? 1 : 0;
-            its[it] = {it, (float)(y1 - y0) * (band_zx ? 1.6f : 1.0f) + 0.4f * ybands + 0.3f * (2 * N - 1)};
+        for (int c = 0; c < 2; ++c) {
+            std::vector<It> its;
+            auto chunk = [&](int t, int y0, int y1) {
+                float cost = warm;
+                for (int y = y0; y < y1; ++y) cost += plane_cost(bzx[t], y);
+                its.push_back({make_int2(t, y0 | (y1 << 16)), cost});
+            };
+            if (c == 0) {
+                int64_t yc = std::max<int64_t>(8, (ny * ntile + 3 * slots - 1) / (3 * (int64_t)slots));
+                yc = std::min<int64_t>(yc, 64);
+                const int64_t nch = (ny + yc - 1) / yc;
+                const int ychunk = (int)((ny + nch - 1) / nch);  // even chunks
+                for (int t = 0; t < ntile; ++t)
+                    for (int y0 = 0; y0 < ny; y0 += ychunk) chunk(t, y0, (int)std::min<int64_t>(y0 + ychunk, ny));
+            } else {
+                const float target = std::max(4.0f, (float)(total / (3.0 * slots)));
+                for (int t = 0; t < ntile; ++t) {
+                    int y0 = 0;
+                    while (y0 < ny) {
+                        float cost = 0;
+                        int y1 = y0;
+                        while (y1 < ny && (y1 - y0 < 4 || (cost < target && y1 - y0 < 64)))
+                            cost += plane_cost(bzx[t], y1++);
+                        if (ny - y1 < 4) y1 = (int)ny;  // no short tail chunk
+                        chunk(t, y0, y1);
+                        y0 = y1;
+                    }
+                }
+            }
+            // most expensive first; among equal costs by first plane, then tile, so that
+            // blocks running at the same time work on nearby planes (L2 reuse of halos)
+            std::sort(its.begin(), its.end(), [](const It& a, const It& b) {
+                if (a.cost != b.cost) return a.cost > b.cost;
+                const int ya = a.item.y & 0xffff, yb = b.item.y & 0xffff;
+                return ya != yb ? ya < yb : a.item.x < b.item.x;
+            });
+            std::vector<int2> order(its.size());
+            for (size_t q = 0; q < its.size(); ++q) order[q] = its[q].item;
+            d_order_[c].allocate(sizeof(int2) * std::max<size_t>(order.size(), 1));
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(d_order_[c].get(), order.data(), sizeof(int2) * order.size(),
+                                            cudaMemcpyHostToDevice, stream_));
+            SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+            d.order[c] = d_order_[c].template as<int2>();
+            nitems_[c] = (int)its.size();
+            grid_c_[c] = std::max(1, std::min(nitems_[c], slots));
         }
-        std::stable_sort(its.begin(), its.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
-        std::vector<int> order(its.size());
-        for (size_t q = 0; q < its.size(); ++q) order[q] = its[q].item;
-        d_order_.allocate(sizeof(int) * std::max<size_t>(order.size(), 1));
-        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_order_.get(), order.data(), sizeof(int) * order.size(),
-                                        cudaMemcpyHostToDevice, stream_));
-        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
-        d.order = d_order_.template as<int>();
         d_next_.allocate(2 * sizeof(int));
         d_next_.zero(stream_);
         d.next = d_next_.template as<int>();
+        use_schedule(0);
+        if (nt < kTuneMinSteps) tune_ = 4;  // short runs keep schedule 0
+        for (auto& e : tev_) SSSI_CHECK_CUDA(cudaEventCreate(&e));
     }
     sync_desc();
 }
@@ -293,6 +332,18 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
 template <typename T>
 Prop3d<T>::~Prop3d() {
     if (graph_) cudaGraphExecDestroy(graph_);
+    for (auto& e : tev_)
+        if (e) cudaEventDestroy(e);
+}
+
+template <typename T>
+void Prop3d<T>::use_schedule(int c) {
+    if (cc_.sched == c && grid_ == grid_c_[c] && cc_.nitems == nitems_[c]) return;
+    cc_.sched = c;
+    cc_.nitems = nitems_[c];
+    grid_ = grid_c_[c];
+    if (graph_) cudaGraphExecDestroy(graph_);  // launch parameters change
+    graph_ = nullptr;
 }
 
 template <typename T>
@@ -330,6 +381,44 @@ void Prop3d<T>::launch_step(const int* base, int offset, cudaStream_t s) {
 template <typename T>
 void Prop3d<T>::run(int nsteps) {
     int q = 0;
+    // schedule tuning (single launches, events around the timed runs)
+    while (q < nsteps && tune_ < 3) {
+        if (tune_left_ == (tune_ == 0 ? 2 : kTuneSteps)) {
+            // a timed run must lie within this call: the caller may queue other
+            // work on the stream between calls
+            if (tune_ > 0 && nsteps - q < kTuneSteps) break;
+            use_schedule(tune_ == 2 ? 1 : 0);
+            if (tune_ > 0) SSSI_CHECK_CUDA(cudaEventRecord(tev_[2 * (tune_ - 1)], stream_));  // start
+        }
+        const int k = std::min(nsteps - q, tune_left_);
+        for (int i = 0; i < k; ++i) launch_step(cc_.step_base, step_ + q + i, stream_);
+        q += k;
+        tune_left_ -= k;
+        if (tune_left_ == 0) {
+            if (tune_ > 0) SSSI_CHECK_CUDA(cudaEventRecord(tev_[2 * (tune_ - 1) + 1], stream_));  // end
+            ++tune_;
+            tune_left_ = kTuneSteps;
+        }
+    }
+    if (tune_ == 3) {
+        // steps left in this call: wait for the timings (once per propagation),
+        // else look without waiting and decide at a later call
+        const cudaError_t e = q < nsteps ? cudaEventSynchronize(tev_[3]) : cudaEventQuery(tev_[3]);
+        if (e == cudaSuccess) {
+            float ms0 = 0, ms1 = 0;
+            SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms0, tev_[0], tev_[1]));
+            SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms1, tev_[2], tev_[3]));
+            use_schedule(ms1 < ms0 ? 1 : 0);
+            tune_ = 4;
+        } else if (e != cudaErrorNotReady) {
+            SSSI_CHECK_CUDA(e);
+        } else {
+            cudaGetLastError();
+        }
+    }
+    nsteps -= q;
+    step_ += q;
+    q = 0;
     if (nsteps >= kGraphSteps) {
         int* base = d_ctr_.template as<int>();
         if (!graph_) {

@@ -432,10 +432,10 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
     if (blockIdx.x == 0 && tid == 0) d.next[(step + 1) & 1] = 0;
     __shared__ int s_item;
     for (int k = blockIdx.x; k < cc.nitems && !failed;) {
-        const int item = d.order[k];
-        const int tile = item % ntile, chunk = item / ntile;
+        const int2 item = d.order[cc.sched][k];
+        const int tile = item.x;
         const int z0 = (tile % d.ntz) * TZ, x0 = (tile / d.ntz) * TX;
-        const int y0 = chunk * d.ychunk, y1 = min(y0 + d.ychunk, ny);
+        const int y0 = item.y & 0xffff, y1 = (unsigned)item.y >> 16;
         const bool bz = nB > 0 && z0 + TZ + N - 1 > nz - nB;
         const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= nx - nB);
         const int i0 = z0 + r0, j = x0 + c0;
