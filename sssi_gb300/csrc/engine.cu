@@ -135,6 +135,11 @@ class Engine final : public EngineBase {
         DeviceBuffer wav, recA, recB, delta, fsnap, amax, inv, Mb, S2, img;
         std::unique_ptr<Prop3d<T>> p3;
         int64_t done3 = 0;
+        cudaStream_t s3 = nullptr;  // 3D: the propagation's own stream (runs beside the 2D batch)
+        ~Run() {
+            p3.reset();
+            if (s3) cudaStreamDestroy(s3);  // released once its work has completed
+        }
     };
 
   public:
@@ -193,7 +198,8 @@ class Engine final : public EngineBase {
             u->recA.allocate(sizeof(T) * std::max<int64_t>(nx * d.ny * nt, 1));
             u->p3->desc().rec = u->recA.template as<T>();
             u->p3->sync_desc();
-            u->p3->set_stream(s_);
+            SSSI_CHECK_CUDA(cudaStreamCreateWithFlags(&u->s3, cudaStreamNonBlocking));
+            u->p3->set_stream(u->s3);
             SSSI_CHECK_CUDA(cudaEventRecord(up_done_, up_));
             r->cells = nz * nx * d.ny * nt;
             runs3_.push_back(std::move(u));
@@ -314,11 +320,14 @@ class Engine final : public EngineBase {
             launches_ += K;
             ran2_ = true;
         }
-        // ---- 3D shots: up to steps_per_round steps each
+        // ---- 3D shots: up to steps_per_round steps each, each on its own stream
+        // (the persistent kernels of the batch and of the 3D shots fill one
+        // another's idle SMs)
         for (auto& up : runs3_) {
             Run& u = *up;
             const int64_t k = std::min<int64_t>(rounds_, u.r->d.nt - u.done3);
             if (k > 0) {
+                SSSI_CHECK_CUDA(cudaStreamWaitEvent(u.s3, up_done_, 0));
                 u.p3->run((int)k);
                 u.done3 += k;
                 cells += (double)u.r->d.nz * u.r->d.nx * u.r->d.ny * k;
@@ -329,6 +338,7 @@ class Engine final : public EngineBase {
 
     void complete(std::vector<Delivery>& out) override {
         wait_stream(s_);
+        for (auto& up : runs3_) wait_stream(up->s3);
         if (ran2_) {
             float ms = 0;
             SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms, ev2_[0], ev2_[1]));
@@ -346,7 +356,8 @@ class Engine final : public EngineBase {
                 const T* rec = u.recA.template as<T>();
                 const size_t n = (size_t)(u.r->d.nx * u.r->d.ny * nt);
                 double* dst = u.r->d.data;
-                hand_over(std::move(runs3_[q]), out, [=](cudaStream_t cs) { deliver<T>(rec, n, dst, cs); });
+                cudaStream_t s3 = u.s3;
+                hand_over(std::move(runs3_[q]), out, [=](cudaStream_t cs) { deliver<T>(rec, n, dst, cs); }, s3);
                 runs3_.erase(runs3_.begin() + q);
                 continue;
             }
@@ -357,6 +368,8 @@ class Engine final : public EngineBase {
     void fail_all(std::vector<ReqPtr>& fin, const std::string& why) override {
         cudaStreamSynchronize(s_);
         cudaStreamSynchronize(up_);
+        for (auto& u : runs3_)
+            if (u->s3) cudaStreamSynchronize(u->s3);
         ran2_ = false;
         for (auto& u : runs2_) {
             u->r->status = SSSI_ERR_INTERNAL;
@@ -386,11 +399,11 @@ class Engine final : public EngineBase {
     // Queues the delivery of a finished run's outputs; the run (and its device
     // buffers) lives until the copies are done.
     template <class F>
-    void hand_over(std::unique_ptr<Run> u, std::vector<Delivery>& out, F&& copy) {
+    void hand_over(std::unique_ptr<Run> u, std::vector<Delivery>& out, F&& copy, cudaStream_t s = nullptr) {
         Delivery dl;
         dl.r = u->r;
         SSSI_CHECK_CUDA(cudaEventCreateWithFlags(&dl.ready, cudaEventDisableTiming));
-        SSSI_CHECK_CUDA(cudaEventRecord(dl.ready, s_));
+        SSSI_CHECK_CUDA(cudaEventRecord(dl.ready, s ? s : s_));
         dl.copy = std::forward<F>(copy);
         dl.keep = std::shared_ptr<Run>(std::move(u));
         out.push_back(std::move(dl));
