@@ -80,6 +80,9 @@ template <typename T>
 struct Const3 {
     T az[16], ax[16];  // composed second-derivative coefficients (z, x)
     T wz[8], wx[8], wy[8];
+    // D- along y over the A_y queue: row u (queue position of the step) holds
+    // the weight of each of the 2N slots, so the slots are read in a fixed order
+    T wyq[16 * 16];
     int nitems;
     int sched;             // the schedule in use (Desc3::order)
     const int* step_base;  // the launch computes step *step_base + step_offset

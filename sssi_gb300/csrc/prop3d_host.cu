@@ -132,6 +132,15 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
         cc_.az[m] = m <= L ? static_cast<T>(az[m]) : T(0);
         cc_.ax[m] = m <= L ? static_cast<T>(ax[m]) : T(0);
     }
+    // at queue position u the slot of A_y(y + k) is (u + N + 1 + k) mod 2N (weight
+    // w_k), the slot of A_y(y - 1 - k) is (u + N - k) mod 2N (weight -w_k)
+    for (int u = 0; u < 16; ++u)
+        for (int q = 0; q < 16; ++q) cc_.wyq[u * 16 + q] = T(0);
+    for (int u = 0; u < 2 * N; ++u)
+        for (int k = 0; k < N; ++k) {
+            cc_.wyq[u * 16 + (u + N + 1 + k) % (2 * N)] = cc_.wy[k];
+            cc_.wyq[u * 16 + (u + N - k) % (2 * N)] = -cc_.wy[k];
+        }
 
     // fields and (v dt)^2 in the padded layout (the padding stays zero)
     for (auto& b : P_) {

@@ -561,24 +561,18 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                 if (act) {
                     T lz[RZ], lx[RZ], ly[RZ];
                     zx_second<T, N>(cc, d, Pb, scratch, bz, bx, i0, j, y, r0, c0, lz, lx);
-                    // D- A_y at plane y from A_y(y-N .. y+N-1), psi_y in the y bands;
-                    // slot of A_y(y + k): (u + N + 1 + k) mod NQ, of A_y(y - 1 - k): (u + N - k) mod NQ
+                    // D- A_y at plane y from A_y(y-N .. y+N-1) (all 2N slots, weights of
+                    // queue position u), psi_y in the y bands
                     {
-                        Col<T> ap[N], am[N];
+                        Col<T> a[NQ];
 #pragma unroll
-                        for (int k = 0; k < N; ++k) {
-                            int sp = u + N + 1 + k, sm = u + N - k;  // < 3 NQ
-                            sp -= sp >= NQ ? NQ : 0;
-                            sp -= sp >= NQ ? NQ : 0;
-                            sm -= sm >= NQ ? NQ : 0;
-                            ap[k] = Aq[sp * NT];
-                            am[k] = Aq[sm * NT];
-                        }
+                        for (int q = 0; q < NQ; ++q) a[q] = Aq[q * NT];
+                        const T* wq = cc.wyq + u * 16;
 #pragma unroll
                         for (int o = 0; o < RZ; ++o) {
-                            T dd = cc.wy[0] * (ap[0].v[o] - am[0].v[o]);
+                            T dd = wq[0] * a[0].v[o];
 #pragma unroll
-                            for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], ap[k].v[o] - am[k].v[o], dd);
+                            for (int q = 1; q < NQ; ++q) dd = fma(wq[q], a[q].v[o], dd);
                             ly[o] = dd;
                         }
                     }
