@@ -77,6 +77,10 @@ struct Layout3 {
     static constexpr unsigned kSmem = kAq + 16u * (2 * N) * Shape3D<T>::kThreads;  // A_y queue: 2N slots per thread
 };
 
+// Band planes: the memory variables of the same cells one plane further on are
+// brought into L1 while this plane is computed (each band plane would
+// otherwise wait for its own round trips to L2).
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 constexpr unsigned kWaitLimit3 = 1u << 24;
 
 // Stage one of a band tile for plane y (every thread of the block): zA rows
@@ -115,6 +119,7 @@ __device__ __noinline__ void band_plane_stage1(const Const3<T>& cc, const Desc3<
                 b[u] = ldg_t(d.zb + q);
                 bm[u] = ldg_t(d.zbm1 + q);
                 m[u] = ldg_t(phi_in + q);
+                if (y + 1 < d.ny) prefetch_l1(phi_in + (int64_t)nB * nx + q);
             }
         }
         T* zA = scratch;
@@ -164,6 +169,7 @@ __device__ __noinline__ void band_plane_stage1(const Const3<T>& cc, const Desc3<
                 b[u] = ldg_t(d.xb + qc[u]);
                 bm[u] = ldg_t(d.xbm1 + qc[u]);
                 m[u] = ldg_t(phi_in + qc[u]);
+                if (y + 1 < d.ny) prefetch_l1(phi_in + (int64_t)nz * 2 * nB + qc[u]);
             }
         }
         T* xA = scratch + G::kXA / sizeof(T);
@@ -221,6 +227,7 @@ __device__ __forceinline__ Col<T> z_band_second(const Const3<T>& cc, const Desc3
             ps[o] = zpsi[q];
         }
     }
+    if (y + 1 < d.ny && in[0] | in[RZ - 1]) prefetch_l1(zpsi + (int64_t)nB * nx + (max(i0, zb0) - zb0) + j * nB);
     const T* za = scratch + c0 * G::ZP + r0;
     T w[RZ * ZW];
 #pragma unroll
@@ -269,6 +276,7 @@ __device__ __forceinline__ Col<T> x_band_second(const Const3<T>& cc, const Desc3
             ps[o] = xpsi[q];
         }
     }
+    if (y + 1 < d.ny && qo >= 0 && i0 < nz) prefetch_l1(xpsi + (int64_t)nz * 2 * nB + qo + i0);
     const T* xa = scratch + G::kXA / sizeof(T) + r0;
     Col<T> a[2 * N];
 #pragma unroll
@@ -304,6 +312,10 @@ __device__ __forceinline__ Col<T> y_band_first(const Desc3<T>& d, int cur, int i
     M m[RZ];
 #pragma unroll
     for (int o = 0; o < RZ; ++o) m[o] = i0 + o < nz ? ldg_t(phi_in + o) : M{};
+    if (pa + 1 < nB || (pa + 1 >= ny - nB && pa + 1 < ny)) {
+        const int cn = pa + 1 < nB ? pa + 1 : nB + pa + 1 - (ny - nB);
+        prefetch_l1(d.yphi[cur] + (int64_t)i0 + (int64_t)j * nz + (int64_t)cn * nz * nx);
+    }
 #pragma unroll
     for (int o = 0; o < RZ; ++o) {
         if (i0 + o < nz) {
@@ -327,6 +339,10 @@ __device__ __forceinline__ Col<T> y_band_second(const Desc3<T>& d, int i0, int j
     M p[RZ];
 #pragma unroll
     for (int o = 0; o < RZ; ++o) p[o] = i0 + o < nz ? psi[o] : M{};
+    if (y + 1 < nB || (y + 1 >= ny - nB && y + 1 < ny)) {
+        const int cn = y + 1 < nB ? y + 1 : nB + y + 1 - (ny - nB);
+        prefetch_l1(d.ypsi + (int64_t)i0 + (int64_t)j * nz + (int64_t)cn * nz * nx);
+    }
 #pragma unroll
     for (int o = 0; o < RZ; ++o) {
         if (i0 + o < nz) {
