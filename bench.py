@@ -91,6 +91,9 @@ def cell_updates(nz, nx, nt):
 # shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
 # python bench.py --case rtm-short`
 FWD_STEP_DRAM_BYTES = 22_955_008
+# the same for one 3D step at 256^3 with 16-cell bands, from `ncu --set full -k
+# regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
+STEP3D_DRAM_BYTES = 389_746_176 + 129_267_456
 
 
 def step_bytes_per_cell(nz, nx, nb):
@@ -368,10 +371,19 @@ def bench_3d(S, args):
     a, b = d32[::2, ::2, :], d64[::2, ::2, :]
     err = float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
     cells = n ** 3 * nt
+    # algorithmic bytes of one step: 16 B per cell, plus per damped cell and axis
+    # the compensated phi (read, write) and psi (read, write), 32 B (the band
+    # coefficients vary in two dimensions only and stay cached)
+    alg3 = 16.0 * n ** 3 + 32.0 * 5 * nb * n ** 2
     return {"metric": "Gcell-updates/s (3D forward shot, 256^3, nt=%d)" % nt,
             "value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_shot": round(ms, 2),
             "us_per_step": round(ms * 1e3 / nt, 2), "dtype": "fp32", "shots": len(times),
-            "achieved_gbs_alg": round(16.0 * n ** 3 / (ms * 1e-3 / nt) / 1e9, 1),
+            "achieved_gbs_alg": round(alg3 / (ms * 1e-3 / nt) / 1e9, 1),
+            "roofline": {"bound": "hbm", "achieved": round(alg3 / (ms * 1e-3 / nt) / 1e9, 1), "peak": peaks()[0],
+                         "unit": "GB/s", "frac": round(alg3 / (ms * 1e-3 / nt) / 1e9 / peaks()[0], 4),
+                         "peak_kind": peaks()[1], "alg_bytes_per_step": int(alg3),
+                         "traffic": STEP3D_DRAM_BYTES if (n, nb) == (256, 16) else None,
+                         "traffic_note": "dram read+write of one step from an ncu capture of the same grid (cold)"},
             "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "ms_per_shot": round(ms64, 1)},
             "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (128 x 128)",
             "config": {"workload": "fwd3d-point-source", "n": n, "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
