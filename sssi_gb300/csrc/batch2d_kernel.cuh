@@ -110,10 +110,10 @@ struct BandScratch {
     static constexpr unsigned kBytes = kX + (sizeof(T) * TZ * CX + 127) / 128 * 128;
 };
 
-// Stage one of a band tile, run by every thread of the block; the caller
-// synchronises the block before the scratch is read.
+// Stage one of a half tile, one cell per item (a half tile has too few
+// four-row units to share them evenly between the threads).
 template <typename T, int N, int TX>
-__device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
+__device__ __noinline__ void band_stage1_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
                                          int x0, bool bz, bool bx, T* scratch) {
     using S = TileShape<T>;
     using B = BandScratch<T, N>;
@@ -223,6 +223,140 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
         for (int u = 0; u < MU; ++u) {
             const int cx = (tid + u * NT) / TZ;
             if (qc[u] >= 0 && cx >= N && cx < N + TX) phi_out[qc[u]] = m[u];
+        }
+    }
+}
+
+// Stage one of a band tile, run by every thread of the block; the caller
+// synchronises the block before the scratch is read.  A thread's unit is four
+// consecutive rows of one scratch column, read from the P box with 16-byte
+// loads; the memory-variable operands of all its units are loaded first, so a
+// tile costs one round trip to L2 per direction.  Per cell the arithmetic is
+// that of the cell-by-cell form: D+ = sum_k w_k (P[+k+1] - P[-k]) in order of
+// k, then phi and A = D+ + phi inside the band.
+template <typename T, int N, int TX>
+__device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
+                                         int x0, bool bz, bool bx, T* scratch) {
+    using S = TileShape<T>;
+    using B = BandScratch<T, N>;
+    using M = typename MemVar<T>::type;
+    constexpr int TZ = S::TZ, NT = S::kThreads;
+    constexpr int CXW = TX + 2 * N - 1;  // xA columns used (pitch TZ)
+    constexpr int L = 2 * N - 1;
+    constexpr int HZ = tile_halo_rows(N);
+    constexpr int SP = TZ + 2 * HZ;
+    const int tid = threadIdx.x;
+    const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
+    if (bz) {
+        // zA row r is global row z0-N+r, box row HZ-N+r; a unit's window is box
+        // rows 4g .. 4g+HZ+3 (within the box for every g)
+        constexpr int G4 = (B::RZ + 3) / 4;
+        constexpr int UNITS = G4 * TX;
+        constexpr int MU = (UNITS + NT - 1) / NT;
+        const int zb0 = nz - nB;
+        // the two phi buffers are distinct: loads of later units may move ahead of
+        // the stores of earlier ones
+        const T* __restrict__ zb = sh.zb;
+        const T* __restrict__ zbm1 = sh.zbm1;
+        const M* __restrict__ phi_in = sh.zphi[ph];
+        M* __restrict__ phi_out = sh.zphi[ph ^ 1];
+        T* zA = scratch;
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int unit = tid + u * NT;
+            if (unit < UNITS) {
+                const int g = unit % G4, c = unit / G4, j = x0 + c;
+                T b[4], bm[4];
+                M m[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    const int p = z0 - N + 4 * g + o;
+                    b[o] = T(0);
+                    bm[o] = T(0);
+                    m[o] = M{};
+                    if (j < nx && p >= zb0 && p < nz) {
+                        const int64_t q = (p - zb0) + (int64_t)j * nB;
+                        b[o] = ldg_t(zb + q);
+                        bm[o] = ldg_t(zbm1 + q);
+                        m[o] = ldg_t(phi_in + q);
+                    }
+                }
+                const T* colp = Pb + (c + L) * SP + 4 * g;
+                T w[HZ + 4];
+#pragma unroll
+                for (int q = 0; q < (HZ + 4) / 4; ++q) {
+                    const V4<T> v = ld4(colp + 4 * q);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) w[4 * q + e] = v.v[e];
+                }
+                T out[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    constexpr int C0 = HZ - N;  // window index of the row's own P
+                    T d = bc.wz[0] * (w[C0 + o + 1] - w[C0 + o]);
+#pragma unroll
+                    for (int n = 1; n < N; ++n) d = fma(bc.wz[n], w[C0 + o + 1 + n] - w[C0 + o - n], d);
+                    const int r = 4 * g + o, p = z0 - N + r;
+                    if (j < nx && p >= zb0 && p < nz) {
+                        m[o] = mem_new(b[o], bm[o], m[o], d);
+                        d = mem_add(d, m[o]);
+                        if (r >= N && r < N + TZ) phi_out[(p - zb0) + (int64_t)j * nB] = m[o];
+                    }
+                    out[o] = d;
+                }
+                st4(zA + c * B::ZP + 4 * g, out);
+            }
+        }
+    }
+    if (bx) {
+        // xA column cx is global column x0-N+cx; its D+ reads box columns cx .. cx+2N-1
+        constexpr int G4 = TZ / 4;
+        constexpr int UNITS = G4 * CXW;
+        constexpr int MU = (UNITS + NT - 1) / NT;
+        const T* __restrict__ xb = sh.xb;
+        const T* __restrict__ xbm1 = sh.xbm1;
+        const M* __restrict__ phi_in = sh.xphi[ph];
+        M* __restrict__ phi_out = sh.xphi[ph ^ 1];
+        T* xA = scratch + B::kX / sizeof(T);
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int unit = tid + u * NT;
+            if (unit < UNITS) {
+                const int g = unit % G4, cx = unit / G4;
+                const int i = z0 + 4 * g, jc = x0 - N + cx;
+                const bool band = jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+                const int64_t qc = band ? i + (int64_t)(jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
+                T b[4], bm[4];
+                M m[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    b[o] = T(0);
+                    bm[o] = T(0);
+                    m[o] = M{};
+                    if (qc >= 0 && i + o < nz) {
+                        b[o] = ldg_t(xb + qc + o);
+                        bm[o] = ldg_t(xbm1 + qc + o);
+                        m[o] = ldg_t(phi_in + qc + o);
+                    }
+                }
+                V4<T> a[2 * N];
+#pragma unroll
+                for (int t = 0; t < 2 * N; ++t) a[t] = ld4(Pb + (cx + t) * SP + HZ + 4 * g);
+                T out[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    T d = bc.wx[0] * (a[N].v[o] - a[N - 1].v[o]);
+#pragma unroll
+                    for (int n = 1; n < N; ++n) d = fma(bc.wx[n], a[N + n].v[o] - a[N - 1 - n].v[o], d);
+                    if (qc >= 0 && i + o < nz) {
+                        m[o] = mem_new(b[o], bm[o], m[o], d);
+                        d = mem_add(d, m[o]);
+                        if (cx >= N && cx < N + TX) phi_out[qc + o] = m[o];
+                    }
+                    out[o] = d;
+                }
+                st4(xA + cx * TZ + 4 * g, out);
+            }
         }
     }
 }
@@ -735,8 +869,8 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 const bool half = ti.flags & kHalf;
                 if (ti.flags & (kBandZ | kBandX)) {
                     if (half)
-                        band_stage1<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
-                                                  ti.flags & kBandX, scratch);
+                        band_stage1_cells<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
+                                                        ti.flags & kBandX, scratch);
                     else
                         band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
                                               scratch);
