@@ -106,9 +106,10 @@ __host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int tz, in
 
 template <typename T>
 struct alignas(128) ShotDesc {
-    CUtensorMap tm_box[2];   // halo box of field k
-    CUtensorMap tm_tile[2];  // tile box of field k
-    CUtensorMap tm_v;        // tile box of (v dt)^2
+    // per tile shape (BatchShape index)
+    CUtensorMap tm_box[2][2];   // halo box of field k
+    CUtensorMap tm_tile[2][2];  // tile box of field k
+    CUtensorMap tm_v[2];        // tile box of (v dt)^2
     ShotTail<T> s;
 };
 
@@ -204,31 +205,47 @@ class Batch2d {
     struct GraphKey {
         int grid = 0;
         bool split = false;
+        int shape = 0;
         const void *desc = nullptr, *begin = nullptr, *work = nullptr;
         bool operator==(const GraphKey& o) const {
-            return grid == o.grid && split == o.split && desc == o.desc && begin == o.begin && work == o.work;
+            return grid == o.grid && split == o.split && shape == o.shape && desc == o.desc && begin == o.begin &&
+                   work == o.work;
         }
     } graph_key_;
     GraphKey current_key() const {
-        return GraphKey{grid_, split_, d_desc_.get(), d_cta_begin_.get(), d_work_.get()};
+        return GraphKey{grid_, split_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(), d_work_[shape_].get()};
     }
+    // tile shape: the schedule in use (BatchShape index) and the tuner (times a
+    // few steps with each shape when a large schedule is built, keeps the faster)
+    int shape_ = 0;
+    bool tune_ = false;
+    int tuned_tiles_ = 0;
+    static constexpr int kTuneSteps = 6, kTuneMinRun = 64;  // steps per shape; shortest run that tunes
+    int tile_z(int shape) const;
+    int tile_x(int shape) const;
+    void schedule(int shape);  // work lists of the enabled shots for a tile shape
+    void use_shape(int shape);
     bool split_ = false;  // the schedule holds half tiles
-    DeviceBuffer d_desc_, d_cta_begin_, d_work_, d_ctr_;  // d_ctr_: graph step base, zero, error flag
+    DeviceBuffer d_desc_, d_ctr_;                // d_ctr_: graph step base, zero, error flag
+    DeviceBuffer d_cta_begin_[2], d_work_[2];    // the schedule of each tile shape
+    int grid_s_[2] = {0, 0}, ntiles_s_[2] = {0, 0};
+    bool split_s_[2] = {false, false};
     int grid_ = 0, ntiles_ = 0, step_ = 0;
-    int ctas_per_sm_ = 1, sms_ = 1;
+    int ctas_per_sm_[2] = {1, 1}, sms_ = 1;
     cudaGraphExec_t graph_ = nullptr;
 };
 
 // Launches one batch step with the programmatic-serialization attribute.
-// split: the work lists hold half tiles.
+// split: the work lists hold half tiles; shape: BatchShape index.
 template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, cudaStream_t stream);
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
+                      cudaStream_t stream);
 template <typename T, int N>
-int batch2d_occupancy_n();
+int batch2d_occupancy_n(int shape);
 template <typename T>
-void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
                     cudaStream_t stream);
 template <typename T>
-int batch2d_ctas_per_sm(int N);
+int batch2d_ctas_per_sm(int N, int shape);
 
 }  // namespace sssi

@@ -80,7 +80,7 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
     int dev = 0;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
     SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
-    ctas_per_sm_ = batch2d_ctas_per_sm<T>(N);
+    for (int v = 0; v < kBatchShapes<T>; ++v) ctas_per_sm_[v] = batch2d_ctas_per_sm<T>(N, v);
 }
 
 template <typename T>
@@ -90,9 +90,9 @@ int Batch2d<T>::add_shot(const double* v, int64_t nz, int64_t nx, int nB, double
     SSSI_REQUIRE(nB >= 0 && nB <= nz && 2 * (int64_t)nB <= nx, SSSI_ERR_ARG,
                  "nBoundary %d does not fit the model (%lld x %lld): need nBoundary <= nz and 2*nBoundary <= nx", nB,
                  (long long)nz, (long long)nx);
-    SSSI_REQUIRE(nz <= 65535LL * TileShape<T>::TZ && nx <= 65535LL * TileShape<T>::TX, SSSI_ERR_ARG,
-                 "model too large (%lld x %lld): at most %lld x %lld", (long long)nz, (long long)nx,
-                 65535LL * TileShape<T>::TZ, 65535LL * TileShape<T>::TX);
+    SSSI_REQUIRE(nz <= 65535LL * 32 && nx <= 65535LL * 32, SSSI_ERR_ARG,
+                 "model too large (%lld x %lld): at most %lld x %lld", (long long)nz, (long long)nx, 65535LL * 32,
+                 65535LL * 32);
     SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
     const int slot = take_slot();
     stale_ = true;
@@ -211,18 +211,21 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
     for (auto* bf : {&S.zphi[0], &S.zphi[1], &S.zpsi}) bf->allocate(zbytes);
     for (auto* bf : {&S.xphi[0], &S.xphi[1], &S.xpsi}) bf->allocate(xbytes);
 
-    const uint32_t box_rows = Sh::TZ + 2 * HZ, box_cols = Sh::TX + 2 * L_;
-    for (int k = 0; k < 2; ++k) {
-        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_box[k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp, cols,
-                                          ldp, box_rows, box_cols),
-                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field halo box");
-        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_tile[k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp, cols,
-                                          ldp, Sh::TZ, Sh::TX),
-                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field tile box");
+    for (int v = 0; v < kBatchShapes<T>; ++v) {  // boxes of every tile shape
+        const uint32_t tz = (uint32_t)tile_z(v), tx = (uint32_t)tile_x(v);
+        const uint32_t box_rows = tz + 2 * HZ, box_cols = tx + 2 * L_;
+        for (int k = 0; k < 2; ++k) {
+            SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_box[v][k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp,
+                                              cols, ldp, box_rows, box_cols),
+                         SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field halo box");
+            SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_tile[v][k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp,
+                                              cols, ldp, tz, tx),
+                         SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field tile box");
+        }
+        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_v[v], S.vdt2.get(), TmaType<T>::kType, sizeof(T), ldp, cols, ldp,
+                                          tz, tx),
+                     SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for (v dt)^2");
     }
-    SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_v, S.vdt2.get(), TmaType<T>::kType, sizeof(T), ldp, cols, ldp,
-                                      Sh::TZ, Sh::TX),
-                 SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for (v dt)^2");
     d.field[0] = S.P[0].template as<T>() + S.origin;
     d.field[1] = S.P[1].template as<T>() + S.origin;
     d.zb = S.zb.template as<T>();
@@ -302,8 +305,55 @@ void Batch2d<T>::drop_graph() {
 }
 
 template <typename T>
+int Batch2d<T>::tile_z(int shape) const {
+    if constexpr (kBatchShapes<T> > 1)
+        if (shape == 1) return BatchShape<T, 1>::TZ;
+    return TileShape<T>::TZ;
+}
+
+template <typename T>
+int Batch2d<T>::tile_x(int shape) const {
+    if constexpr (kBatchShapes<T> > 1)
+        if (shape == 1) return BatchShape<T, 1>::TX;
+    return TileShape<T>::TX;
+}
+
+template <typename T>
 void Batch2d<T>::finalize() {
-    using Sh = TileShape<T>;
+    // the first large schedule (at least four whole tiles' worth per block) is
+    // worth tuning the tile shape for, and one grown eightfold since
+    int64_t tiles = 0;
+    for (const Shot& S : shots_)
+        if (S.enabled)
+            tiles += ((int64_t)(S.desc.s.nz + TileShape<T>::TZ - 1) / TileShape<T>::TZ) *
+                     ((S.desc.s.nx + TileShape<T>::TX - 1) / TileShape<T>::TX);
+    if (kBatchShapes<T> > 1 && tiles >= 4LL * sms_ * ctas_per_sm_[0] && tiles > 8LL * tuned_tiles_) {
+        tune_ = true;
+        tuned_tiles_ = (int)std::min<int64_t>(tiles, 1 << 30);
+    }
+    if (tune_)
+        for (int v = 0; v < kBatchShapes<T>; ++v) schedule(v);  // both, for the tuner
+    else
+        schedule(shape_);
+    use_shape(shape_);
+    stale_ = false;
+}
+
+template <typename T>
+void Batch2d<T>::use_shape(int shape) {
+    shape_ = shape;
+    grid_ = grid_s_[shape];
+    ntiles_ = ntiles_s_[shape];
+    split_ = split_s_[shape];
+    bc_.nshots = (int)shots_.size();
+    bc_.ntiles = ntiles_;
+    bc_.cta_begin = d_cta_begin_[shape].template as<int>();
+    bc_.work = d_work_[shape].template as<int2>();
+}
+
+template <typename T>
+void Batch2d<T>::schedule(int shape) {
+    const int TZs = tile_z(shape), TXs = tile_x(shape);
     // tiles of the enabled shots with an estimated cost: tiles whose stencil
     // reaches a damped band add a cooperative first-derivative pass and the
     // memory-variable traffic
@@ -318,28 +368,29 @@ void Batch2d<T>::finalize() {
     // tiles cost in proportion to their cells
     auto tile_item = [&](int k, int z0, int x0, int width) {
         const ShotTail<T>& d = shots_[k].desc.s;
-        unsigned f = tile_band_flags(N_, Sh::TZ, width, d.nz, d.nx, d.nB, z0, x0);
+        unsigned f = tile_band_flags(N_, TZs, width, d.nz, d.nx, d.nB, z0, x0);
         const bool bz = f & kBandZ, bx = f & kBandX;
         for (int s = 0; s < d.nsrc; ++s)
-            if (d.src_iz[s] >= z0 && d.src_iz[s] < z0 + Sh::TZ && d.src_ix[s] >= x0 && d.src_ix[s] < x0 + width)
+            if (d.src_iz[s] >= z0 && d.src_iz[s] < z0 + TZs && d.src_ix[s] >= x0 && d.src_ix[s] < x0 + width)
                 f |= kSource;
-        const float fill = (float)(std::min(Sh::TZ, d.nz - z0) * std::max(0, std::min(width, d.nx - x0))) /
-                           (float)(Sh::TZ * Sh::TX);
+        const float fill = (float)(std::min(TZs, d.nz - z0) * std::max(0, std::min(width, d.nx - x0))) /
+                           (float)(TZs * TXs);
         return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))};
     };
     std::vector<Item> items;
     {
         size_t n = 0;
         for (const Shot& S : shots_)
-            if (S.enabled) n += (size_t)S.desc.s.ntz * S.desc.s.ntx;
+            if (S.enabled) n += (size_t)((S.desc.s.nz + TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
         items.reserve(n);
     }
     for (int k = 0; k < (int)shots_.size(); ++k) {
         if (!shots_[k].enabled) continue;
         const ShotTail<T>& d = shots_[k].desc.s;
-        for (int q = 0; q < d.ntz * d.ntx; ++q) {
-            const int z0 = (q % d.ntz) * Sh::TZ, x0 = (q / d.ntz) * Sh::TX;
-            items.push_back(tile_item(k, z0, x0, Sh::TX));
+        const int ntz = (d.nz + TZs - 1) / TZs, ntx = (d.nx + TXs - 1) / TXs;
+        for (int q = 0; q < ntz * ntx; ++q) {
+            const int z0 = (q % ntz) * TZs, x0 = (q / ntz) * TXs;
+            items.push_back(tile_item(k, z0, x0, TXs));
         }
     }
     // A band tile takes several times as long as an interior one.  When a block
@@ -351,14 +402,14 @@ void Batch2d<T>::finalize() {
     {
         float total = 0.0f;
         for (const Item& it : items) total += it.cost;
-        const int blocks = std::max(1, std::min((int)items.size(), sms_ * ctas_per_sm_));
-        split_ = total < 2.0f * (float)blocks;
-        if (split_) {
+        const int blocks = std::max(1, std::min((int)items.size(), sms_ * ctas_per_sm_[shape_]));
+        split_s_[shape] = total < 2.0f * (float)blocks;
+        if (split_s_[shape]) {
             std::vector<Item> split;
             split.reserve(items.size() + items.size() / 4);
             for (const Item& it : items) {
                 const ShotTail<T>& d = shots_[it.shot].desc.s;
-                if (!(it.flags & (kBandZ | kBandX)) || d.nx - it.x0 <= Sh::TX / 2) {
+                if (!(it.flags & (kBandZ | kBandX)) || d.nx - it.x0 <= TXs / 2) {
                     split.push_back(it);
                     continue;
                 }
@@ -366,7 +417,7 @@ void Batch2d<T>::finalize() {
                     // the half keeps the whole tile's band flags, so that every cell is
                     // computed by the same formula as in the unsplit tile (results do
                     // not depend on which shots share the batch)
-                    Item hi = tile_item(it.shot, it.z0, it.x0 + h * (Sh::TX / 2), Sh::TX / 2);
+                    Item hi = tile_item(it.shot, it.z0, it.x0 + h * (TXs / 2), TXs / 2);
                     const float band = (it.flags & kBandZ ? 1.2f : 0.0f) + (it.flags & kBandX ? 1.2f : 0.0f);
                     const float own = (hi.flags & kBandZ ? 1.2f : 0.0f) + (hi.flags & kBandX ? 1.2f : 0.0f);
                     hi.cost *= (1.0f + band) / (1.0f + own);
@@ -379,34 +430,100 @@ void Batch2d<T>::finalize() {
             items.swap(split);
         }
     }
-    ntiles_ = (int)items.size();
-    grid_ = std::max(1, std::min(ntiles_, sms_ * ctas_per_sm_));
+    const int ntiles = (int)items.size();
+    const int grid = std::max(1, std::min(ntiles, sms_ * ctas_per_sm_[shape]));
+    ntiles_s_[shape] = ntiles;
+    grid_s_[shape] = grid;
     // longest processing time first onto the least loaded CTA
     std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
     std::vector<int> owner(items.size());
-    std::vector<int> begin(grid_ + 1, 0);
+    std::vector<int> begin(grid + 1, 0);
     {
+        // Longest processing time first onto the least loaded block (a heap), except
+        // for the longest run of equal costs (the whole interior tiles), which is
+        // spread to level the loads directly: the same assignment up to ties, in
+        // time linear in the tiles, so large batches reschedule quickly.
         using P = std::pair<float, int>;
         std::vector<P> heap;  // min-heap on load
-        heap.reserve(grid_);
-        for (int c = 0; c < grid_; ++c) heap.push_back({0.0f, c});
+        heap.reserve(grid);
+        for (int c = 0; c < grid; ++c) heap.push_back({0.0f, c});
         const auto cmp = std::greater<P>();
-        for (size_t q = 0; q < items.size(); ++q) {
-            std::pop_heap(heap.begin(), heap.end(), cmp);
-            P& top = heap.back();
-            owner[q] = top.second;
-            ++begin[top.second + 1];
-            top.first += items[q].cost;
-            std::push_heap(heap.begin(), heap.end(), cmp);
+        auto lpt = [&](size_t a, size_t b) {
+            for (size_t q = a; q < b; ++q) {
+                std::pop_heap(heap.begin(), heap.end(), cmp);
+                P& top = heap.back();
+                owner[q] = top.second;
+                top.first += items[q].cost;
+                std::push_heap(heap.begin(), heap.end(), cmp);
+            }
+        };
+        size_t ra = 0, rb = 0;  // the longest run of equal costs
+        for (size_t q = 0; q < items.size();) {
+            size_t e = q;
+            while (e < items.size() && items[e].cost == items[q].cost) ++e;
+            if (e - q > rb - ra) {
+                ra = q;
+                rb = e;
+            }
+            q = e;
         }
+        lpt(0, ra);
+        if (rb > ra) {
+            const float c = items[ra].cost;
+            const int64_t m = (int64_t)(rb - ra);
+            std::vector<double> load(grid);
+            double sum = 0;
+            for (const P& h : heap) {
+                load[h.second] = h.first;
+                sum += h.first;
+            }
+            const double level = (sum + (double)m * c) / grid;
+            std::vector<int64_t> cnt(grid);
+            int64_t given = 0;
+            for (int b = 0; b < grid; ++b) {
+                cnt[b] = std::max<int64_t>(0, (int64_t)std::floor((level - load[b]) / c));
+                given += cnt[b];
+            }
+            if (given > m) {  // rounding: take back from the most loaded
+                std::vector<int> order(grid);
+                for (int b = 0; b < grid; ++b) order[b] = b;
+                std::sort(order.begin(), order.end(),
+                          [&](int x, int y) { return load[x] + cnt[x] * c > load[y] + cnt[y] * c; });
+                for (int k = 0; given > m; k = (k + 1) % grid)
+                    if (cnt[order[k]] > 0) {
+                        --cnt[order[k]];
+                        --given;
+                    }
+            }
+            if (given < m) {  // the rest one each to the least loaded
+                std::vector<int> order(grid);
+                for (int b = 0; b < grid; ++b) order[b] = b;
+                std::sort(order.begin(), order.end(),
+                          [&](int x, int y) { return load[x] + cnt[x] * c < load[y] + cnt[y] * c; });
+                for (int k = 0; given < m; k = (k + 1) % grid) {
+                    ++cnt[order[k]];
+                    ++given;
+                }
+            }
+            // deal the run out block by block in turn, so that neighbouring tiles
+            // go to different blocks
+            size_t q = ra;
+            for (int64_t round = 0; q < rb; ++round)
+                for (int b = 0; b < grid && q < rb; ++b)
+                    if (cnt[b] > round) owner[q++] = b;
+            for (P& h : heap) h.first = (float)(load[h.second] + cnt[h.second] * c);
+            std::make_heap(heap.begin(), heap.end(), cmp);
+        }
+        lpt(rb, items.size());
+        for (size_t q = 0; q < items.size(); ++q) ++begin[owner[q] + 1];
     }
-    for (int c = 0; c < grid_; ++c) begin[c + 1] += begin[c];
+    for (int c = 0; c < grid; ++c) begin[c + 1] += begin[c];
     std::vector<int2> work(items.size());
     {
         std::vector<int> fill(begin.begin(), begin.end() - 1);
         for (size_t q = 0; q < items.size(); ++q) {
             const Item& it = items[q];
-            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0 / Sh::TZ, it.x0 / Sh::TX);
+            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0 / TZs, it.x0 / TXs);
         }
     }
 
@@ -423,20 +540,17 @@ void Batch2d<T>::finalize() {
     if (!hdesc.empty())
         SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.get(), hdesc.data(), sizeof(ShotDesc<T>) * hdesc.size(),
                                         cudaMemcpyHostToDevice, stream_));
-    if (d_cta_begin_.bytes() < sizeof(int) * begin.size()) d_cta_begin_.allocate(sizeof(int) * begin.size());
-    if (d_work_.bytes() < sizeof(int2) * std::max<size_t>(work.size(), 1))
-        d_work_.allocate(sizeof(int2) * std::max<size_t>(work.size(), 1));
-    SSSI_CHECK_CUDA(cudaMemcpyAsync(d_cta_begin_.get(), begin.data(), sizeof(int) * begin.size(),
+    DeviceBuffer& d_begin = d_cta_begin_[shape];
+    DeviceBuffer& d_work = d_work_[shape];
+    if (d_begin.bytes() < sizeof(int) * begin.size()) d_begin.allocate(sizeof(int) * begin.size());
+    if (d_work.bytes() < sizeof(int2) * std::max<size_t>(work.size(), 1))
+        d_work.allocate(sizeof(int2) * std::max<size_t>(work.size(), 1));
+    SSSI_CHECK_CUDA(cudaMemcpyAsync(d_begin.get(), begin.data(), sizeof(int) * begin.size(),
                                     cudaMemcpyHostToDevice, stream_));
     if (!work.empty())
-        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_work_.get(), work.data(), sizeof(int2) * work.size(),
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(d_work.get(), work.data(), sizeof(int2) * work.size(),
                                         cudaMemcpyHostToDevice, stream_));
     SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
-    bc_.nshots = (int)shots_.size();
-    bc_.ntiles = ntiles_;
-    bc_.cta_begin = d_cta_begin_.template as<int>();
-    bc_.work = d_work_.template as<int2>();
-    stale_ = false;
 }
 
 template <typename T>
@@ -458,14 +572,38 @@ void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
     BatchConst<T> bc = bc_;
     bc.step_base = base;
     bc.step_offset = offset;
-    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, stream);
+    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, shape_, stream);
 }
 
 template <typename T>
 void Batch2d<T>::run(int nsteps) {
     SSSI_REQUIRE(grid_ > 0 && !stale_, SSSI_ERR_INTERNAL, "Batch2d::run: the schedule is out of date (finalize)");
     int q = 0;
-    if (nsteps >= kGraphSteps) {
+    if (tune_ && nsteps >= kTuneMinRun) {
+        // tile-shape tuning: kTuneSteps steps with each shape, timed with events,
+        // then the faster shape's schedule for the rest (the per-cell arithmetic
+        // does not depend on the tiling, so the results do not either)
+        tune_ = false;
+        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+        float ms[2] = {0.0f, 0.0f};
+        cudaError_t e = cudaSuccess;
+        for (auto& x : ev)
+            if (e == cudaSuccess) e = cudaEventCreate(&x);
+        for (int v = 0; v < kBatchShapes<T> && e == cudaSuccess; ++v) {
+            use_shape(v);
+            e = cudaEventRecord(ev[2 * v], stream_);
+            for (int i = 0; i < kTuneSteps && e == cudaSuccess; ++i) launch_step(bc_.step_base, step_ + q + i, stream_);
+            q += kTuneSteps;
+            if (e == cudaSuccess) e = cudaEventRecord(ev[2 * v + 1], stream_);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[2 * kBatchShapes<T> - 1]);
+        for (int v = 0; v < kBatchShapes<T> && e == cudaSuccess; ++v) e = cudaEventElapsedTime(&ms[v], ev[2 * v], ev[2 * v + 1]);
+        for (auto& x : ev)
+            if (x) cudaEventDestroy(x);
+        SSSI_CHECK_CUDA(e);
+        use_shape((kBatchShapes<T> > 1 && ms[1] < ms[0]) ? 1 : 0);
+    }
+    if (nsteps - q >= kGraphSteps) {
         int* base = d_ctr_.template as<int>();
         if (graph_ && !(graph_key_ == current_key())) drop_graph();
         if (!graph_) {
@@ -492,7 +630,7 @@ void Batch2d<T>::run(int nsteps) {
             if (e != cudaSuccess) graph_ = nullptr;
             SSSI_CHECK_CUDA(e);
         }
-        launch_store_int(base, step_, stream_);
+        launch_store_int(base, step_ + q, stream_);
         count_launch();
         for (; q + kGraphSteps <= nsteps; q += kGraphSteps) {
             SSSI_CHECK_CUDA(cudaGraphLaunch(graph_, stream_));
@@ -520,32 +658,32 @@ void Batch2d<T>::check_errors() {
 }
 
 template <typename T>
-void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
                     cudaStream_t stream) {
     switch (N) {
-        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, stream); break;
-        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, stream); break;
-        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, stream); break;
-        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, stream); break;
-        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, stream); break;
-        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, stream); break;
-        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, stream); break;
-        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, stream); break;
+        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, shape, stream); break;
+        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, shape, stream); break;
+        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, shape, stream); break;
+        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, shape, stream); break;
+        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, shape, stream); break;
+        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, shape, stream); break;
+        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, shape, stream); break;
+        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, shape, stream); break;
         default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
     }
 }
 
 template <typename T>
-int batch2d_ctas_per_sm(int N) {
+int batch2d_ctas_per_sm(int N, int shape) {
     switch (N) {
-        case 1: return batch2d_occupancy_n<T, 1>();
-        case 2: return batch2d_occupancy_n<T, 2>();
-        case 3: return batch2d_occupancy_n<T, 3>();
-        case 4: return batch2d_occupancy_n<T, 4>();
-        case 5: return batch2d_occupancy_n<T, 5>();
-        case 6: return batch2d_occupancy_n<T, 6>();
-        case 7: return batch2d_occupancy_n<T, 7>();
-        default: return batch2d_occupancy_n<T, 8>();
+        case 1: return batch2d_occupancy_n<T, 1>(shape);
+        case 2: return batch2d_occupancy_n<T, 2>(shape);
+        case 3: return batch2d_occupancy_n<T, 3>(shape);
+        case 4: return batch2d_occupancy_n<T, 4>(shape);
+        case 5: return batch2d_occupancy_n<T, 5>(shape);
+        case 6: return batch2d_occupancy_n<T, 6>(shape);
+        case 7: return batch2d_occupancy_n<T, 7>(shape);
+        default: return batch2d_occupancy_n<T, 8>(shape);
     }
 }
 

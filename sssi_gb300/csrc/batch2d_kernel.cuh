@@ -100,9 +100,9 @@ __device__ __forceinline__ float2 ldg_t(const float2* p) { return __ldg(p); }
 // rows.  The second derivative D- A (+ psi) then reads them back.  All global
 // operands of a batch are loaded before any memory variable is stored, so a
 // batch costs one round trip to L2.
-template <typename T, int N>
+template <typename T, int N, class Sh>
 struct BandScratch {
-    static constexpr int TZ = TileShape<T>::TZ, TX = TileShape<T>::TX;
+    static constexpr int TZ = Sh::TZ, TX = Sh::TX;
     static constexpr int RZ = TZ + 2 * N - 1;    // zA rows
     static constexpr int ZP = (RZ + 3) / 4 * 4;  // pitch of a zA column
     static constexpr int CX = TX + 2 * N - 1;    // xA columns (pitch TZ)
@@ -112,11 +112,11 @@ struct BandScratch {
 
 // Stage one of a half tile, one cell per item (a half tile has too few
 // four-row units to share them evenly between the threads).
-template <typename T, int N, int TX>
+template <typename T, int N, class Sh, int TX>
 __device__ __noinline__ void band_stage1_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
                                          int x0, bool bz, bool bx, T* scratch) {
-    using S = TileShape<T>;
-    using B = BandScratch<T, N>;
+    using S = Sh;
+    using B = BandScratch<T, N, Sh>;
     using M = typename MemVar<T>::type;
     constexpr int TZ = S::TZ, NT = S::kThreads;
     constexpr int CXW = TX + 2 * N - 1;  // xA columns used (pitch TZ)
@@ -234,11 +234,11 @@ __device__ __noinline__ void band_stage1_cells(const BatchConst<T>& bc, const Sh
 // tile costs one round trip to L2 per direction.  Per cell the arithmetic is
 // that of the cell-by-cell form: D+ = sum_k w_k (P[+k+1] - P[-k]) in order of
 // k, then phi and A = D+ + phi inside the band.
-template <typename T, int N, int TX>
+template <typename T, int N, class Sh, int TX>
 __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb, int z0,
                                          int x0, bool bz, bool bx, T* scratch) {
-    using S = TileShape<T>;
-    using B = BandScratch<T, N>;
+    using S = Sh;
+    using B = BandScratch<T, N, Sh>;
     using M = typename MemVar<T>::type;
     constexpr int TZ = S::TZ, NT = S::kThreads;
     constexpr int CXW = TX + 2 * N - 1;  // xA columns used (pitch TZ)
@@ -472,12 +472,12 @@ __device__ __forceinline__ void add_sources(const ShotTail<T>& sh, int tau, int 
 // All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  kBandZ / kBandX:
 // the tile is a band tile in z / x, its first derivatives are in `scratch`;
 // otherwise the composed stencil is used in that direction.
-template <typename T, int N, int RX>
+template <typename T, int N, class Sh, int RX>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
                                            unsigned flags, const T* scratch, unsigned& amax_bits) {
-    using S = TileShape<T>;
-    using B = BandScratch<T, N>;
+    using S = Sh;
+    using B = BandScratch<T, N, Sh>;
     using M = typename MemVar<T>::type;
     constexpr int TZ = S::TZ;
     constexpr int L = 2 * N - 1;
@@ -694,9 +694,9 @@ __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned 
 }
 
 // Shared-memory layout of one pipeline stage (byte offsets, 128-aligned).
-template <typename T, int N>
+template <typename T, int N, class Sh>
 struct StageLayout {
-    using S = TileShape<T>;
+    using S = Sh;
     static constexpr int L = 2 * N - 1;
     static constexpr int HZ = tile_halo_rows(N);
     static constexpr int SP = S::TZ + 2 * HZ;
@@ -712,18 +712,19 @@ struct StageLayout {
     static constexpr int kStages = 2;                             // tiles in the copy pipeline
     static constexpr unsigned kBar = kStages * kStage;            // one mbarrier per stage
     static constexpr unsigned kScratch = kBar + 128;              // band scratch
-    static constexpr unsigned kSmem = kScratch + BandScratch<T, N>::kBytes;
+    static constexpr unsigned kSmem = kScratch + BandScratch<T, N, Sh>::kBytes;
 };
 
 constexpr unsigned kWaitLimit = 1u << 24;
 
 // kSplit: the work lists may hold half tiles (schedules of small grids); the
 // variant without them keeps the whole-tile path free of their handling.
-template <typename T, int N, bool kSplit>
-__global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBlocks)
+template <typename T, int N, bool kSplit, class Sh>
+__global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
     batch2d_kernel(const ShotDesc<T>* __restrict__ shots, const __grid_constant__ BatchConst<T> bc) {
-    using S = TileShape<T>;
-    using G = StageLayout<T, N>;
+    using S = Sh;
+    using G = StageLayout<T, N, Sh>;
+    constexpr int V = Sh::kIndex;  // tensor maps of this shape
     constexpr int TZ = S::TZ, TX = S::TX, RX = S::RX;
     constexpr int HZ = G::HZ, L = G::L;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -767,9 +768,9 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
             inflight |= 1u << s;
             fence_proxy_async_shared();
             mbar_arrive_expect_tx(&bar[s], G::kTx);
-            tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], g.oz + z0 - HZ, x0);
-            tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], g.oz + z0, x0 + L);
-            tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], g.oz + z0, x0 + L);
+            tma_load_2d(st + G::kP, &shots[k].tm_box[V][cur], &bar[s], g.oz + z0 - HZ, x0);
+            tma_load_2d(st + G::kO, &shots[k].tm_tile[V][cur ^ 1], &bar[s], g.oz + z0, x0 + L);
+            tma_load_2d(st + G::kV, &shots[k].tm_v[V], &bar[s], g.oz + z0, x0 + L);
         }
     };
     // warp 0: put the prefetched item into stage s (tile = its position in the
@@ -806,9 +807,9 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 inflight |= 1u << s;
                 fence_proxy_async_shared();
                 mbar_arrive_expect_tx(&bar[s], G::kTx);
-                tma_load_2d(st + G::kP, &shots[k].tm_box[cur], &bar[s], oz + z0 - HZ, x0);
-                tma_load_2d(st + G::kO, &shots[k].tm_tile[cur ^ 1], &bar[s], oz + z0, x0 + L);
-                tma_load_2d(st + G::kV, &shots[k].tm_v, &bar[s], oz + z0, x0 + L);
+                tma_load_2d(st + G::kP, &shots[k].tm_box[V][cur], &bar[s], oz + z0 - HZ, x0);
+                tma_load_2d(st + G::kO, &shots[k].tm_tile[V][cur ^ 1], &bar[s], oz + z0, x0 + L);
+                tma_load_2d(st + G::kV, &shots[k].tm_v[V], &bar[s], oz + z0, x0 + L);
             }
         }
         __syncwarp();
@@ -869,23 +870,23 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
                 const bool half = ti.flags & kHalf;
                 if (ti.flags & (kBandZ | kBandX)) {
                     if (half)
-                        band_stage1_cells<T, N, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
+                        band_stage1_cells<T, N, Sh, TX / 2>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
                                                         ti.flags & kBandX, scratch);
                     else
-                        band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
+                        band_stage1<T, N, Sh, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
                                               scratch);
                     __syncthreads();
                 }
                 if (i0 < sh.nz && j0 < sh.nx && (!half || c0 < TX / 2))
-                    tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+                    tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             } else {
                 if (ti.flags & (kBandZ | kBandX)) {
-                    band_stage1<T, N, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
+                    band_stage1<T, N, Sh, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
                                           scratch);
                     __syncthreads();
                 }
                 if (i0 < sh.nz && j0 < sh.nx)
-                    tile_cells<T, N, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+                    tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             }
             if (ti.flags & kAmax) {
                 const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
@@ -907,18 +908,18 @@ __global__ void __launch_bounds__(TileShape<T>::kThreads, TileShape<T>::kMinBloc
 
 }  // namespace batch
 
-template <typename T, int N, bool kSplit>
+template <typename T, int N, bool kSplit, class Sh>
 void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
-    using G = batch::StageLayout<T, N>;
+    using G = batch::StageLayout<T, N, Sh>;
     static bool configured = false;
     if (!configured) {
-        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit>,
+        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit, Sh>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem));
         configured = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(TileShape<T>::kThreads);
+    cfg.blockDim = dim3(Sh::kThreads);
     cfg.dynamicSmemBytes = G::kSmem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
@@ -926,27 +927,41 @@ void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, i
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit>, shots, bc));
+    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit, Sh>, shots, bc));
     count_launch();
 }
 
-template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, cudaStream_t stream) {
+template <typename T, int N, class Sh>
+void launch_batch2d_shape(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+                          cudaStream_t stream) {
     if (split)
-        launch_batch2d_variant<T, N, true>(shots, bc, grid, stream);
+        launch_batch2d_variant<T, N, true, Sh>(shots, bc, grid, stream);
     else
-        launch_batch2d_variant<T, N, false>(shots, bc, grid, stream);
+        launch_batch2d_variant<T, N, false, Sh>(shots, bc, grid, stream);
 }
 
 template <typename T, int N>
-int batch2d_occupancy_n() {
-    const size_t smem = batch::StageLayout<T, N>::kSmem;
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
+                      cudaStream_t stream) {
+    if constexpr (kBatchShapes<T> > 1) {
+        if (shape == 1) {
+            launch_batch2d_shape<T, N, BatchShape<T, 1>>(shots, bc, grid, split, stream);
+            return;
+        }
+    }
+    SSSI_REQUIRE(shape == 0, SSSI_ERR_INTERNAL, "tile shape %d not built for this type", shape);
+    launch_batch2d_shape<T, N, BatchShape<T, 0>>(shots, bc, grid, split, stream);
+}
+
+template <typename T, int N, class Sh>
+int batch2d_occupancy_shape() {
+    const size_t smem = batch::StageLayout<T, N, Sh>::kSmem;
     int n = 0;
-    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false>,
+    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false, Sh>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false>,
-                                                          TileShape<T>::kThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false, Sh>, Sh::kThreads,
+                                                          smem);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
         n = 1;
@@ -954,8 +969,16 @@ int batch2d_occupancy_n() {
     return n;
 }
 
-#define SSSI_BATCH2D_INSTANCE(T, N)                                                                           \
-    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, cudaStream_t); \
-    template int batch2d_occupancy_n<T, N>();
+template <typename T, int N>
+int batch2d_occupancy_n(int shape) {
+    if constexpr (kBatchShapes<T> > 1) {
+        if (shape == 1) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>>();
+    }
+    return batch2d_occupancy_shape<T, N, BatchShape<T, 0>>();
+}
+
+#define SSSI_BATCH2D_INSTANCE(T, N)                                                                                \
+    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, int, cudaStream_t); \
+    template int batch2d_occupancy_n<T, N>(int);
 
 }  // namespace sssi

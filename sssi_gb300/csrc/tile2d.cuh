@@ -22,6 +22,8 @@
 #pragma once
 
 #include "cpml2d.cuh"
+#include <type_traits>
+
 #include "tma.cuh"
 
 namespace sssi {
@@ -40,6 +42,24 @@ struct TileShape<double> {
     static constexpr int TZ = 32, TX = 32, RX = 2;
     static constexpr int kThreads = (TZ / 4) * (TX / RX), kMinBlocks = 2;
 };
+
+// Tile shapes of the batched step: shape 0 is TileShape<T>; FP32 also has
+// shape 1, 32 x 32 tiles with four blocks per SM, which the batch's tuner
+// picks when it steps faster (large single grids).
+template <typename T, int V>
+struct BatchShape;
+template <typename T>
+struct BatchShape<T, 0> : TileShape<T> {
+    static constexpr int kIndex = 0;
+};
+template <>
+struct BatchShape<float, 1> {
+    static constexpr int TZ = 32, TX = 32, RX = 2;
+    static constexpr int kThreads = (TZ / 4) * (TX / RX), kMinBlocks = 4;
+    static constexpr int kIndex = 1;
+};
+template <typename T>
+constexpr int kBatchShapes = std::is_same<T, float>::value ? 2 : 1;
 
 template <typename T>
 struct MemVar;

@@ -79,6 +79,21 @@ def test_fwd_fast_fp64_and_fp32(gpu, co, oracle_mod):
     assert np.array_equal(dd, d_ref)
 
 
+def test_large_grid_tile_shapes(gpu, co, oracle_mod):
+    """A grid large enough for the batch's tile-shape tuner (it times both tile
+    shapes on the first steps and keeps the faster): FP32 against the FP64
+    oracle, reverse propagation of random surface traces (the final field
+    covers the top rows and both side bands)."""
+    S = gpu
+    rng = np.random.default_rng(21)
+    nz, nx, nt, N, nB = 1536, 1664, 120, 4, 20
+    v = rng.uniform(1500, 4000, (nz, nx))
+    data = np.asfortranarray(rng.standard_normal((nx, nt)))
+    m_ref, _ = co.rvs2d(v, data, N, nB, 10.0, 10.0, 8e-4, want_snapshot=False)
+    m32, _ = S.rvsTimeCpmlFor2dAw(v, data, N, nB, 10.0, 10.0, 8e-4, mode="fp32", want_snapshot=False)
+    assert oracle_mod.rel_l2(m32, m_ref) <= TOL_FP32
+
+
 def test_device_pointers(gpu, co):
     """Inputs/outputs already in HBM (torch tensors, column-major)."""
     import torch
