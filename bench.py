@@ -441,11 +441,18 @@ def bench_batch(S, args):
     with S.Plan(N_ORDER, DZ, DX, mode="fp32") as plan:
         V, nt, iz, ix = shots[0]
         plan.wait(plan.submit_fwd2d(V, 200, [iz], [ix], waves[0][:, :200], NB, dt))  # warm-up
-        t0 = time.perf_counter()
-        tickets = [plan.submit_fwd2d(V, nt, [iz], [ix], w, NB, dt) for (V, nt, iz, ix), w in zip(shots, waves)]
-        outs = [plan.wait(t)["data"] for t in tickets]
-        el = time.perf_counter() - t0
-        st = plan.stats()
+        # the batch twice: the first pass fills the device-memory pool (a serving
+        # plan runs warm); the second is the measurement
+        walls = []
+        for rep in range(2):
+            st0 = plan.stats()
+            t0 = time.perf_counter()
+            tickets = [plan.submit_fwd2d(V, nt, [iz], [ix], w, NB, dt) for (V, nt, iz, ix), w in zip(shots, waves)]
+            outs = [plan.wait(t)["data"] for t in tickets]
+            walls.append(time.perf_counter() - t0)
+            st1 = plan.stats()
+        el = walls[-1]
+        st = {k: (st1[k] - st0[k]) if isinstance(st1[k], float) or k == "batch_steps" else st1[k] for k in st1}
     # the same kind of shots one call at a time
     sample = list(range(0, 64, 8))
     t0 = time.perf_counter()
@@ -473,7 +480,8 @@ def bench_batch(S, args):
                            "bytes_per_cell": round(alg_bytes / cells, 2)},
               "timing": "CUDA events around each round of batched steps inside the plan (whole batch, all rounds)"}
     return {"metric": "Gcell-updates/s (64-shot batched forward modelling, 800x2400 model)",
-            "value": round(value, 2), "unit": UNIT, "wall_s": round(el, 3), "shots_per_s": round(64 / el, 2),
+            "value": round(value, 2), "unit": UNIT, "wall_s": round(el, 3), "first_pass_wall_s": round(walls[0], 3),
+            "shots_per_s": round(64 / el, 2),
             "cell_updates": cells, "dtype": "fp32", "batch_steps": int(st["batch_steps"]),
             "plan_host_s": {k: round(st[k], 3) for k in ("admit_s", "round_s", "gpu_wait_s", "deliver_s")},
             "step_kernel": kernel,
