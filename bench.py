@@ -52,6 +52,18 @@ def ext_boundary(V, nB):
     return np.concatenate([W, np.repeat(W[-1:, :], nB, 0)], axis=0)
 
 
+def ext_boundary_3d(V, nB):
+    """The 3D padding: edge values replicated nB times on both x sides, both y
+    sides and below (no layer on top)."""
+    return np.asfortranarray(np.pad(V, ((0, nB), (nB, nB), (nB, nB)), mode="edge"))
+
+
+def model_3d_c4(nb=16):
+    """The 3D workload's model: the seeded dipping-layer model on a 256^3
+    physical grid, padded with the damping bands to 272 x 288 x 288."""
+    return ext_boundary_3d(dipping_model_3d(256), nb)
+
+
 def ricker(f, n, dt):
     t = np.arange(n) * dt
     tau = t - 1.0 / f
@@ -91,9 +103,9 @@ def cell_updates(nz, nx, nt):
 # shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
 # python bench.py --case rtm-short`
 FWD_STEP_DRAM_BYTES = 22_955_008
-# the same for one 3D step at 256^3 with 16-cell bands, from `ncu --set full -k
-# regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
-STEP3D_DRAM_BYTES = 389_746_176 + 129_267_456
+# the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
+# `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
+STEP3D_DRAM_BYTES = 488_232_960 + 172_346_880
 
 
 def step_bytes_per_cell(nz, nx, nb):
@@ -333,25 +345,26 @@ def dipping_model_3d(n, seed=20240617):
 
 
 def bench_3d(S, args):
-    """3D forward modelling, 256^3, nt = 2000, N = 4, 16-cell CPML, point source
-    at the surface centre; FP32 timed, receivers (every 2 cells) compared with
-    the FP64 path."""
+    """3D forward modelling: a 256^3 physical grid padded with 16-cell CPML
+    bands to 272 x 288 x 288, nt = 2000, N = 4, point source at the surface
+    centre; FP32 timed, receivers (every 2 cells) compared with the FP64 path."""
     import torch
 
-    n, nt, nb, dt3 = 256, args.nt3d, 16, 8e-4
-    v = dipping_model_3d(n)
+    nt, nb, dt3 = args.nt3d, 16, 8e-4
+    v = model_3d_c4(nb)
+    nz, nx, ny = v.shape
     dv = torch.from_numpy(np.ascontiguousarray(v.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
     w = np.ascontiguousarray(ricker(20.0, nt, dt3)[None, :])
     iz = np.array([0], dtype=np.int64)
-    ix = np.array([n // 2], dtype=np.int64)
-    iy = np.array([n // 2], dtype=np.int64)
+    ix = np.array([nx // 2], dtype=np.int64)
+    iy = np.array([ny // 2], dtype=np.int64)
 
     def run(mode, data):
         S.api.check(S.api.lib().sssi_fwdTimeCpmlFor3dAwPoint(
-            S.api._addr(dv), n, n, n, nt, N_ORDER, nb, 10.0, 10.0, 10.0, dt3, 1, iz.ctypes.data, ix.ctypes.data,
+            S.api._addr(dv), nz, nx, ny, nt, N_ORDER, nb, 10.0, 10.0, 10.0, dt3, 1, iz.ctypes.data, ix.ctypes.data,
             iy.ctypes.data, w.ctypes.data, S.api._addr(data), None, S.api._mode(mode)))
 
-    d32 = torch.zeros((nt, n, n), dtype=torch.float64, device="cuda").permute(2, 1, 0)
+    d32 = torch.zeros((nt, ny, nx), dtype=torch.float64, device="cuda").permute(2, 1, 0)
     run("fp32", d32)  # warm-up
     times = []
     for _ in range(max(1, args.steps3d)):
@@ -363,30 +376,31 @@ def bench_3d(S, args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     ms = float(np.mean(times))
-    d64 = torch.zeros((nt, n, n), dtype=torch.float64, device="cuda").permute(2, 1, 0)
+    d64 = torch.zeros((nt, ny, nx), dtype=torch.float64, device="cuda").permute(2, 1, 0)
     t0 = time.perf_counter()
     run("fp64", d64)
     torch.cuda.synchronize()
     ms64 = (time.perf_counter() - t0) * 1e3
     a, b = d32[::2, ::2, :], d64[::2, ::2, :]
     err = float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
-    cells = n ** 3 * nt
+    cells = nz * nx * ny * nt
     # algorithmic bytes of one step: 16 B per cell, plus per damped cell and axis
     # the compensated phi (read, write) and psi (read, write), 32 B (the band
     # coefficients vary in two dimensions only and stay cached)
-    alg3 = 16.0 * n ** 3 + 32.0 * 5 * nb * n ** 2
-    return {"metric": "Gcell-updates/s (3D forward shot, 256^3, nt=%d)" % nt,
+    alg3 = 16.0 * nz * nx * ny + 32.0 * nb * (nx * ny + 2 * nz * ny + 2 * nz * nx)
+    return {"metric": "Gcell-updates/s (3D forward shot, 256^3 + 16-cell bands = 272x288x288, nt=%d)" % nt,
             "value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_shot": round(ms, 2),
             "us_per_step": round(ms * 1e3 / nt, 2), "dtype": "fp32", "shots": len(times),
             "achieved_gbs_alg": round(alg3 / (ms * 1e-3 / nt) / 1e9, 1),
             "roofline": {"bound": "hbm", "achieved": round(alg3 / (ms * 1e-3 / nt) / 1e9, 1), "peak": peaks()[0],
                          "unit": "GB/s", "frac": round(alg3 / (ms * 1e-3 / nt) / 1e9 / peaks()[0], 4),
                          "peak_kind": peaks()[1], "alg_bytes_per_step": int(alg3),
-                         "traffic": STEP3D_DRAM_BYTES if (n, nb) == (256, 16) else None,
+                         "traffic": STEP3D_DRAM_BYTES,
                          "traffic_note": "dram read+write of one step from an ncu capture of the same grid (cold)"},
             "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "ms_per_shot": round(ms64, 1)},
-            "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (128 x 128)",
-            "config": {"workload": "fwd3d-point-source", "n": n, "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
+            "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (144 x 144)",
+            "config": {"workload": "fwd3d-point-source", "grid": [nz, nx, ny], "physical": [256, 256, 256],
+                       "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
                        "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",
                        "source": "20 Hz Ricker at the surface centre"}}
 
@@ -658,8 +672,8 @@ CASES = {
     "step2d-fp32-large": (4096, 4096, 6, "fp32"),
     "step2d-fp64-large": (4096, 4096, 4, "fp64"),
     "step2d-strict-large": (4096, 4096, 3, "fp64-strict"),
-    "step3d-fp32": (256, 256, 6, "fp32"),  # n^3 grid, 16-cell CPML
-    "step3d-fp32-nb0": (256, 256, 6, "fp32"),  # n^3 grid without damped bands
+    "step3d-fp32": (272, 288, 6, "fp32"),  # the 3D workload's grid (256^3 + 16-cell CPML)
+    "step3d-fp32-nb0": (272, 288, 6, "fp32"),  # the same grid without damped bands
 }
 
 
@@ -678,12 +692,13 @@ def run_case(name):
         return
     nz, nx, nt, mode = CASES[name]
     if name.startswith("step3d"):
-        v = dipping_model_3d(nz)
         nb = 0 if name.endswith("nb0") else 16
-        d, _ = S.fwdTimeCpmlFor3dAwPoint(v, nt, [0], [nz // 2], [nz // 2], ricker(20.0, nt, 8e-4)[None, :],
+        v = model_3d_c4(16)  # the 3D workload's 272 x 288 x 288 grid
+        n3 = v.shape
+        d, _ = S.fwdTimeCpmlFor3dAwPoint(v, nt, [0], [n3[1] // 2], [n3[2] // 2], ricker(20.0, nt, 8e-4)[None, :],
                                          N_ORDER, nb, 10.0, 10.0, 10.0, 8e-4, mode=mode)
         torch.cuda.synchronize()
-        print(f"case {name}: {nz}^3 nt={nt} {mode} ok, data max {np.abs(d).max():.3e}")
+        print(f"case {name}: {n3} nt={nt} {mode} ok, data max {np.abs(d).max():.3e}")
         return
     rng = np.random.default_rng(1)
     v = rng.uniform(1500.0, 4000.0, (nz, nx))
