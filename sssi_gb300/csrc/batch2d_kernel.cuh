@@ -381,9 +381,21 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
         const int k = (tau - 1) / stride;
         const float scale = fp16_scale_from_amax(sh.amax[k]);
         __half* pack = sh.pack + (int64_t)k * ncell;
-        for (int c = 0; c < ncol; ++c)
-            for (int o = 0; o < nrow; ++o)
-                pack[(i0 + o) + (int64_t)(j0 + c) * nz] = __float2half_rn(f32(pc.v[c][o]) * scale);
+        for (int c = 0; c < ncol; ++c) {
+            const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
+            if (nrow == 4 && (q0 & 3) == 0 && (ncell & 3) == 0) {  // four halves in one 8-byte store
+                const __half2 lo = __halves2half2(__float2half_rn(f32(pc.v[c][0]) * scale),
+                                                  __float2half_rn(f32(pc.v[c][1]) * scale));
+                const __half2 hi = __halves2half2(__float2half_rn(f32(pc.v[c][2]) * scale),
+                                                  __float2half_rn(f32(pc.v[c][3]) * scale));
+                uint2 w;
+                w.x = *reinterpret_cast<const unsigned*>(&lo);
+                w.y = *reinterpret_cast<const unsigned*>(&hi);
+                *reinterpret_cast<uint2*>(pack + q0) = w;
+            } else {
+                for (int o = 0; o < nrow; ++o) pack[q0 + o] = __float2half_rn(f32(pc.v[c][o]) * scale);
+            }
+        }
         if (i0 == 0 && j0 == 0) sh.inv_scale[k] = 1.0f / scale;
     }
     if (sh.amax && tau % stride == 0) {
@@ -430,6 +442,41 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
             const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
             __half h[4];
             float2 m[4], s2[4];
+            if (nrow == 4 && (q0 & 3) == 0 && (ncell & 3) == 0) {
+                // a whole aligned column of four cells: 8- and 16-byte accesses
+                const uint2 hv = *reinterpret_cast<const uint2*>(f16 + q0);
+                const __half2 h01 = *reinterpret_cast<const __half2*>(&hv.x);
+                const __half2 h23 = *reinterpret_cast<const __half2*>(&hv.y);
+                h[0] = __low2half(h01);
+                h[1] = __high2half(h01);
+                h[2] = __low2half(h23);
+                h[3] = __high2half(h23);
+                const float4 ma = *reinterpret_cast<const float4*>(im + q0);
+                const float4 mb = *reinterpret_cast<const float4*>(im + q0 + 2);
+                const float4 sa = *reinterpret_cast<const float4*>(is2 + q0);
+                const float4 sb = *reinterpret_cast<const float4*>(is2 + q0 + 2);
+                m[0] = make_float2(ma.x, ma.y);
+                m[1] = make_float2(ma.z, ma.w);
+                m[2] = make_float2(mb.x, mb.y);
+                m[3] = make_float2(mb.z, mb.w);
+                s2[0] = make_float2(sa.x, sa.y);
+                s2[1] = make_float2(sa.z, sa.w);
+                s2[2] = make_float2(sb.x, sb.y);
+                s2[3] = make_float2(sb.z, sb.w);
+                float2 mn[4], sn[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    const float f = __half2float(h[o]) * inv;
+                    const float r = f32(pn.v[c][o]);
+                    mn[o] = comp_add(m[o], __fmul_rn(f, r));
+                    sn[o] = comp_add(s2[o], __fmul_rn(f, f));
+                }
+                *reinterpret_cast<float4*>(im + q0) = make_float4(mn[0].x, mn[0].y, mn[1].x, mn[1].y);
+                *reinterpret_cast<float4*>(im + q0 + 2) = make_float4(mn[2].x, mn[2].y, mn[3].x, mn[3].y);
+                *reinterpret_cast<float4*>(is2 + q0) = make_float4(sn[0].x, sn[0].y, sn[1].x, sn[1].y);
+                *reinterpret_cast<float4*>(is2 + q0 + 2) = make_float4(sn[2].x, sn[2].y, sn[3].x, sn[3].y);
+                continue;
+            }
 #pragma unroll
             for (int o = 0; o < 4; ++o)
                 if (o < nrow) {
