@@ -102,7 +102,7 @@ def cell_updates(nz, nx, nt):
 # dram__bytes_read.sum + dram__bytes_write.sum of one forward step of the RTM
 # shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
 # python bench.py --case rtm-short`
-FWD_STEP_DRAM_BYTES = 22_955_008
+FWD_STEP_DRAM_BYTES = 22_948_352
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
 STEP3D_DRAM_BYTES = 488_232_960 + 172_346_880
