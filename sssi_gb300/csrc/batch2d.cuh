@@ -117,6 +117,7 @@ template <typename T>
 struct BatchConst {
     T az[16], ax[16];  // composed second-derivative coefficients a_0 .. a_l
     T wz[8], wx[8];    // first-derivative weights c_k / d
+    float2 az2[16], ax2[16];  // FP32: {a_m, a_m}, operands of the two-cell (packed) instructions
     int nshots;
     int ntiles;  // host bookkeeping only: the kernel ends at the end of its work list
     const int* cta_begin;  // gridDim.x + 1: each CTA's range in `work`

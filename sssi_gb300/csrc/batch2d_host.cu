@@ -71,6 +71,9 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
     for (int m = 0; m < 16; ++m) {
         bc_.az[m] = m <= L_ ? static_cast<T>(az[m]) : T(0);
         bc_.ax[m] = m <= L_ ? static_cast<T>(ax[m]) : T(0);
+        const float fz = static_cast<float>(bc_.az[m]), fx = static_cast<float>(bc_.ax[m]);
+        bc_.az2[m] = make_float2(fz, fz);
+        bc_.ax2[m] = make_float2(fx, fx);
     }
     d_ctr_.allocate(4 * sizeof(int));  // graph step base, zero, error flag, spare
     d_ctr_.zero(stream);

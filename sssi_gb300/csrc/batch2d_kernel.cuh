@@ -83,6 +83,13 @@ struct TileInfo {
     unsigned flags;  // kBandZ | kBandX | kSource | kRare | kAmax
 };
 
+// FP32 cells go through the packed two-lane instructions (fma.rn.f32x2 and
+// friends) where both operands sit in aligned register pairs: each lane rounds
+// exactly as the scalar instruction does, so results are unchanged and the
+// instruction count of the stencil sums is about halved.
+template <typename T>
+constexpr bool kPacked = std::is_same<T, float>::value;
+
 template <typename T, int RX>
 struct Blk {
     T v[RX][4];
@@ -552,13 +559,40 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 w[4 * q + 2] = v.v[2];
                 w[4 * q + 3] = v.v[3];
             }
+            if constexpr (kPacked<T>) {
+                // rows 2h, 2h+1 as one pair: offsets m of even parity keep both operands
+                // in aligned register pairs (packed instructions); odd offsets stay scalar.
+                // Per row the operations and their order are those of the scalar form.
 #pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                pc.v[c][o] = w[HZ + o];
-                T acc = bc.az[0] * w[HZ + o];
+                for (int h = 0; h < 2; ++h) {
+                    constexpr int b0 = HZ;
+                    const int o = 2 * h;
+                    pc.v[c][o] = w[b0 + o];
+                    pc.v[c][o + 1] = w[b0 + o + 1];
+                    float2 acc = __fmul2_rn(bc.az2[0], make_float2(w[b0 + o], w[b0 + o + 1]));
 #pragma unroll
-                for (int m = 1; m <= L; ++m) acc = fma(bc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
-                lz.v[c][o] = acc;
+                    for (int m = 1; m <= L; ++m) {
+                        if (m % 2 == 0) {
+                            const float2 sum = __fadd2_rn(make_float2(w[b0 + o + m], w[b0 + o + 1 + m]),
+                                                          make_float2(w[b0 + o - m], w[b0 + o + 1 - m]));
+                            acc = __ffma2_rn(bc.az2[m], sum, acc);
+                        } else {
+                            acc.x = fmaf(bc.az[m], w[b0 + o + m] + w[b0 + o - m], acc.x);
+                            acc.y = fmaf(bc.az[m], w[b0 + o + 1 + m] + w[b0 + o + 1 - m], acc.y);
+                        }
+                    }
+                    lz.v[c][o] = acc.x;
+                    lz.v[c][o + 1] = acc.y;
+                }
+            } else {
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    pc.v[c][o] = w[HZ + o];
+                    T acc = bc.az[0] * w[HZ + o];
+#pragma unroll
+                    for (int m = 1; m <= L; ++m) acc = fma(bc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
+                    lz.v[c][o] = acc;
+                }
             }
         }
     } else {
@@ -623,20 +657,46 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
     // ---------------- x ----------------
     if (!bx) {
         const T* rowp = Pb + r0 + HZ;  // the thread's 4 rows; column offset added below
+        if constexpr (kPacked<T>) {
+            float2 acc[RX][2];
 #pragma unroll
-        for (int c = 0; c < RX; ++c)
+            for (int c = 0; c < RX; ++c) acc[c][0] = acc[c][1] = make_float2(0.0f, 0.0f);
 #pragma unroll
-            for (int o = 0; o < 4; ++o) lx.v[c][o] = T(0);
+            for (int q = 0; q < RX + 2 * L; ++q) {
+                const V4<T> v = ld4(rowp + (c0 + q) * SP);
 #pragma unroll
-        for (int q = 0; q < RX + 2 * L; ++q) {
-            const V4<T> v = ld4(rowp + (c0 + q) * SP);
+                for (int c = 0; c < RX; ++c) {
+                    const int m = q - L - c;
+                    if (m >= -L && m <= L) {
+                        const float2 a = bc.ax2[m < 0 ? -m : m];
+                        acc[c][0] = __ffma2_rn(a, make_float2(v.v[0], v.v[1]), acc[c][0]);
+                        acc[c][1] = __ffma2_rn(a, make_float2(v.v[2], v.v[3]), acc[c][1]);
+                    }
+                }
+            }
 #pragma unroll
             for (int c = 0; c < RX; ++c) {
-                const int m = q - L - c;  // offset of column q from output column c
-                if (m >= -L && m <= L) {
-                    const T a = bc.ax[m < 0 ? -m : m];
+                lx.v[c][0] = acc[c][0].x;
+                lx.v[c][1] = acc[c][0].y;
+                lx.v[c][2] = acc[c][1].x;
+                lx.v[c][3] = acc[c][1].y;
+            }
+        } else {
 #pragma unroll
-                    for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(a, v.v[o], lx.v[c][o]);
+            for (int c = 0; c < RX; ++c)
+#pragma unroll
+                for (int o = 0; o < 4; ++o) lx.v[c][o] = T(0);
+#pragma unroll
+            for (int q = 0; q < RX + 2 * L; ++q) {
+                const V4<T> v = ld4(rowp + (c0 + q) * SP);
+#pragma unroll
+                for (int c = 0; c < RX; ++c) {
+                    const int m = q - L - c;  // offset of column q from output column c
+                    if (m >= -L && m <= L) {
+                        const T a = bc.ax[m < 0 ? -m : m];
+#pragma unroll
+                        for (int o = 0; o < 4; ++o) lx.v[c][o] = fma(a, v.v[o], lx.v[c][o]);
+                    }
                 }
             }
         }
@@ -701,11 +761,33 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         const V4<T> po = ld4(Ob + (c0 + c) * TZ + r0);
         const V4<T> vv = ld4(Vb + (c0 + c) * TZ + r0);
         T lap[4];
+        if constexpr (kPacked<T>) {
 #pragma unroll
-        for (int o = 0; o < 4; ++o) lap[o] = lz.v[c][o] + lx.v[c][o];
+            for (int h = 0; h < 2; ++h) {
+                const float2 l2 = __fadd2_rn(make_float2(lz.v[c][2 * h], lz.v[c][2 * h + 1]),
+                                             make_float2(lx.v[c][2 * h], lx.v[c][2 * h + 1]));
+                lap[2 * h] = l2.x;
+                lap[2 * h + 1] = l2.y;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < 4; ++o) lap[o] = lz.v[c][o] + lx.v[c][o];
+        }
         if (flags & kSource) add_sources<T>(sh, tau, i0, j, lap);
+        if constexpr (kPacked<T>) {
 #pragma unroll
-        for (int o = 0; o < 4; ++o) pn.v[c][o] = fma(vv.v[o], lap[o], fma(T(2), pc.v[c][o], -po.v[o]));
+            for (int h = 0; h < 2; ++h) {
+                const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc.v[c][2 * h], pc.v[c][2 * h + 1]),
+                                            make_float2(-po.v[2 * h], -po.v[2 * h + 1]));
+                const float2 u = __ffma2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]),
+                                            make_float2(lap[2 * h], lap[2 * h + 1]), t);
+                pn.v[c][2 * h] = u.x;
+                pn.v[c][2 * h + 1] = u.y;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < 4; ++o) pn.v[c][o] = fma(vv.v[o], lap[o], fma(T(2), pc.v[c][o], -po.v[o]));
+        }
         T* dst = Pnew + i0 + (int64_t)j * sh.ldp;
         if (full_rows) {
             st4(dst, pn.v[c]);
@@ -805,7 +887,9 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
         if (item.x >= 0 && lane < kTailVec)
             tail_reg = reinterpret_cast<const uint4*>(&shots[item.x & 0xffffff].s)[lane];
     };
-    // lane 0 of warp 0: the three copies of a stage prepared earlier (first stages)
+    // lane 0 of warp 0: the three copies of a stage prepared earlier (first
+    // stages).  Every stage's barrier completes one phase per use: a stage with
+    // nothing to copy (no tile, or an inactive shot) gets a plain arrival.
     auto issue = [&](int s) {
         unsigned char* st = smem + s * G::kStage;
         const TileInfo* info = reinterpret_cast<const TileInfo*>(st + G::kInfo);
@@ -821,8 +905,9 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
         }
     };
     // warp 0: put the prefetched item into stage s (tile = its position in the
-    // list); with `copy`, lane 0 also issues the stage's three copies.  Lane 0
-    // works from registers: the item and the head of the shot's tail.
+    // list); with `copy`, lane 0 also issues the stage's three copies (or the
+    // plain arrival).  Lane 0 works from registers: the item and the head of the
+    // shot's tail.
     auto prepare = [&](int w, int s, bool copy) {
         unsigned char* st = smem + s * G::kStage;
         TileInfo* info = reinterpret_cast<TileInfo*>(st + G::kInfo);
@@ -888,10 +973,12 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
     for (int k = 0;; ++k) {
         const int s = k % NS;
         const unsigned char* st = smem + s * G::kStage;
+        // One block barrier per tile: past it every thread has finished tile k-1
+        // (its stage and the band scratch are free to reuse) and sees the
+        // TileInfo of tile k, which warp 0 wrote before that barrier.
         const TileInfo ti = *reinterpret_cast<const TileInfo*>(st + G::kInfo);
         if (ti.tile == kNoTile) break;
         if (tid < 32) {
-            // stage (k-1) % NS was released by the barrier that ended iteration k-1
             prepare(wbeg + k + NS - 1, (k + NS - 1) % NS, true);
             fetch(wbeg + k + NS);
         }
@@ -940,7 +1027,7 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
                 if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
             }
         }
-        __syncthreads();  // stage s is refilled by the next iteration's prepare
+        __syncthreads();
     }
     if (failed) {
         if (tid == 0) {
