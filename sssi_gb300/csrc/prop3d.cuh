@@ -83,6 +83,9 @@ struct Const3 {
     // D- along y over the A_y queue: row u (queue position of the step) holds
     // the weight of each of the 2N slots, so the slots are read in a fixed order
     T wyq[16 * 16];
+    // FP32: the same coefficients as pairs {c, c}, operands of the two-cell
+    // (packed) instructions
+    float2 az2[16], ax2[16], wy2[8], wyq2[16 * 16];
     int nitems;
     int sched;             // the schedule in use (Desc3::order)
     const int* step_base;  // the launch computes step *step_base + step_offset

@@ -141,6 +141,13 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
             cc_.wyq[u * 16 + (u + N + 1 + k) % (2 * N)] = cc_.wy[k];
             cc_.wyq[u * 16 + (u + N - k) % (2 * N)] = -cc_.wy[k];
         }
+    auto pair = [](T c) { return make_float2(static_cast<float>(c), static_cast<float>(c)); };
+    for (int m = 0; m < 16; ++m) {
+        cc_.az2[m] = pair(cc_.az[m]);
+        cc_.ax2[m] = pair(cc_.ax[m]);
+    }
+    for (int k = 0; k < 8; ++k) cc_.wy2[k] = pair(cc_.wy[k]);
+    for (int q = 0; q < 16 * 16; ++q) cc_.wyq2[q] = pair(cc_.wyq[q]);
 
     // fields and (v dt)^2 in the padded layout (the padding stays zero)
     for (auto& b : P_) {

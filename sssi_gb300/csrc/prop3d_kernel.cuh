@@ -371,12 +371,34 @@ __device__ __forceinline__ void zx_second(const Const3<T>& cc, const Desc3<T>& d
 #pragma unroll
             for (int e = 0; e < RZ; ++e) w[RZ * q + e] = v.v[e];
         }
+        if constexpr (batch::kPacked<T>) {
+            // rows o, o+1 as one pair; offsets of even parity keep both operands in
+            // aligned register pairs, odd ones stay scalar (same operations per row)
 #pragma unroll
-        for (int o = 0; o < RZ; ++o) {
-            T acc = cc.az[0] * w[HZ + o];
+            for (int o = 0; o < RZ; o += 2) {
+                float2 acc = __fmul2_rn(cc.az2[0], make_float2(w[HZ + o], w[HZ + o + 1]));
 #pragma unroll
-            for (int m = 1; m <= L; ++m) acc = fma(cc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
-            lz[o] = acc;
+                for (int m = 1; m <= L; ++m) {
+                    if (m % 2 == 0) {
+                        const float2 sum = __fadd2_rn(make_float2(w[HZ + o + m], w[HZ + o + 1 + m]),
+                                                      make_float2(w[HZ + o - m], w[HZ + o + 1 - m]));
+                        acc = __ffma2_rn(cc.az2[m], sum, acc);
+                    } else {
+                        acc.x = fmaf(cc.az[m], w[HZ + o + m] + w[HZ + o - m], acc.x);
+                        acc.y = fmaf(cc.az[m], w[HZ + o + 1 + m] + w[HZ + o + 1 - m], acc.y);
+                    }
+                }
+                lz[o] = acc.x;
+                lz[o + 1] = acc.y;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < RZ; ++o) {
+                T acc = cc.az[0] * w[HZ + o];
+#pragma unroll
+                for (int m = 1; m <= L; ++m) acc = fma(cc.az[m], w[HZ + o + m] + w[HZ + o - m], acc);
+                lz[o] = acc;
+            }
         }
     } else {
         const Col<T> z = z_band_second<T, N>(cc, d, scratch, i0, j, y, r0, c0);
@@ -385,14 +407,32 @@ __device__ __forceinline__ void zx_second(const Const3<T>& cc, const Desc3<T>& d
     }
     if (!bx) {
         const T* rowp = Pb + r0 + HZ + c0 * SP;
+        if constexpr (batch::kPacked<T>) {
+            float2 acc[RZ / 2];
 #pragma unroll
-        for (int o = 0; o < RZ; ++o) lx[o] = T(0);
+            for (int h = 0; h < RZ / 2; ++h) acc[h] = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int q = 0; q <= 2 * L; ++q) {
-            const Col<T> v = ldc(rowp + q * SP);
-            const T a = cc.ax[q < L ? L - q : q - L];
+            for (int q = 0; q <= 2 * L; ++q) {
+                const Col<T> v = ldc(rowp + q * SP);
+                const float2 a = cc.ax2[q < L ? L - q : q - L];
 #pragma unroll
-            for (int o = 0; o < RZ; ++o) lx[o] = fma(a, v.v[o], lx[o]);
+                for (int h = 0; h < RZ / 2; ++h) acc[h] = __ffma2_rn(a, make_float2(v.v[2 * h], v.v[2 * h + 1]), acc[h]);
+            }
+#pragma unroll
+            for (int h = 0; h < RZ / 2; ++h) {
+                lx[2 * h] = acc[h].x;
+                lx[2 * h + 1] = acc[h].y;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < RZ; ++o) lx[o] = T(0);
+#pragma unroll
+            for (int q = 0; q <= 2 * L; ++q) {
+                const Col<T> v = ldc(rowp + q * SP);
+                const T a = cc.ax[q < L ? L - q : q - L];
+#pragma unroll
+                for (int o = 0; o < RZ; ++o) lx[o] = fma(a, v.v[o], lx[o]);
+            }
         }
     } else {
         const Col<T> x = x_band_second<T, N>(cc, d, scratch, i0, j, y, r0, c0);
@@ -545,12 +585,27 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                 {
                     const int pa = s + N - 1;
                     T a[RZ];
+                    if constexpr (batch::kPacked<T>) {
+                        // x - y as fma(-1, y, x): the same rounding as the subtraction
+                        const float2 m1 = make_float2(-1.0f, -1.0f);
 #pragma unroll
-                    for (int o = 0; o < RZ; ++o) {
-                        T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
+                        for (int o = 0; o < RZ; o += 2) {
+                            auto pr = [&](int k) { return make_float2(Pq[k][o], Pq[k][o + 1]); };
+                            float2 dd = __fmul2_rn(cc.wy2[0], __ffma2_rn(m1, pr(N - 1), pr(N)));
 #pragma unroll
-                        for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
-                        a[o] = dd;
+                            for (int k = 1; k < N; ++k)
+                                dd = __ffma2_rn(cc.wy2[k], __ffma2_rn(m1, pr(N - 1 - k), pr(N + k)), dd);
+                            a[o] = dd.x;
+                            a[o + 1] = dd.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) {
+                            T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
+#pragma unroll
+                            for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
+                            a[o] = dd;
+                        }
                     }
                     if (item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
                         Col<T> av;
@@ -583,13 +638,26 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                         Col<T> a[NQ];
 #pragma unroll
                         for (int q = 0; q < NQ; ++q) a[q] = Aq[q * NT];
-                        const T* wq = cc.wyq + u * 16;
+                        if constexpr (batch::kPacked<T>) {
+                            const float2* wq = cc.wyq2 + u * 16;
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) {
-                            T dd = wq[0] * a[0].v[o];
+                            for (int o = 0; o < RZ; o += 2) {
+                                float2 dd = __fmul2_rn(wq[0], make_float2(a[0].v[o], a[0].v[o + 1]));
 #pragma unroll
-                            for (int q = 1; q < NQ; ++q) dd = fma(wq[q], a[q].v[o], dd);
-                            ly[o] = dd;
+                                for (int q = 1; q < NQ; ++q)
+                                    dd = __ffma2_rn(wq[q], make_float2(a[q].v[o], a[q].v[o + 1]), dd);
+                                ly[o] = dd.x;
+                                ly[o + 1] = dd.y;
+                            }
+                        } else {
+                            const T* wq = cc.wyq + u * 16;
+#pragma unroll
+                            for (int o = 0; o < RZ; ++o) {
+                                T dd = wq[0] * a[0].v[o];
+#pragma unroll
+                                for (int q = 1; q < NQ; ++q) dd = fma(wq[q], a[q].v[o], dd);
+                                ly[o] = dd;
+                            }
                         }
                     }
                     if (item_yband && (y < nB || y >= ny - nB)) {
@@ -603,8 +671,18 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                     // update
                     const int64_t qi = (int64_t)i0 + (int64_t)j * nz + (int64_t)y * nz * nx;  // interior index
                     T lap[RZ], pn[RZ];
+                    if constexpr (batch::kPacked<T>) {
 #pragma unroll
-                    for (int o = 0; o < RZ; ++o) lap[o] = (lz[o] + lx[o]) + ly[o];
+                        for (int o = 0; o < RZ; o += 2) {
+                            const float2 l = __fadd2_rn(__fadd2_rn(make_float2(lz[o], lz[o + 1]), make_float2(lx[o], lx[o + 1])),
+                                                        make_float2(ly[o], ly[o + 1]));
+                            lap[o] = l.x;
+                            lap[o + 1] = l.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) lap[o] = (lz[o] + lx[o]) + ly[o];
+                    }
                     if (item_src) {
                         if (d.src_dense) {
                             const T* sd = d.src_dense + (int64_t)(tau - d.dense_t0) * ((int64_t)nz * nx * ny) + qi;
@@ -622,8 +700,19 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                     const T* pc = Pq[0];
                     const Col<T> po = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kO) + c0 * TZ + r0);
                     const Col<T> vv = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kV) + c0 * TZ + r0);
+                    if constexpr (batch::kPacked<T>) {
 #pragma unroll
-                    for (int o = 0; o < RZ; ++o) pn[o] = fma(vv.v[o], lap[o], fma(T(2), pc[o], -po.v[o]));
+                        for (int o = 0; o < RZ; o += 2) {
+                            const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc[o], pc[o + 1]),
+                                                        make_float2(-po.v[o], -po.v[o + 1]));
+                            const float2 r = __ffma2_rn(make_float2(vv.v[o], vv.v[o + 1]), make_float2(lap[o], lap[o + 1]), t);
+                            pn[o] = r.x;
+                            pn[o + 1] = r.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) pn[o] = fma(vv.v[o], lap[o], fma(T(2), pc[o], -po.v[o]));
+                    }
                     T* dst = Pnew + own + (int64_t)y * ldxy;
                     if (i0 + RZ <= nz) {
                         stc(dst, pn);
