@@ -99,10 +99,15 @@ inline unsigned sched_word(const ShotTail<T>& d) {
 }
 
 // A work item: shot k (< 2^24) with the tile's step-independent flags in the
-// top byte, and the tile's position (tz, tx) in tiles (each < 2^16).
-__host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int tz, int tx) {
-    return make_int2((int)((unsigned)k | (flags << 24)), (int)((unsigned)tz | ((unsigned)tx << 16)));
+// top byte; the tile's first row z0 (a multiple of 4, at least -kZBias: a
+// shot's tile rows may start above row 0, see Batch2d::schedule) as
+// (z0 + kZBias) / 4, and its column tx in tiles (each < 2^16).
+constexpr int kZBias = 64;
+constexpr int kMaxTileRow = 4 * 0xffff - kZBias;  // largest z0
+__host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int z0, int tx) {
+    return make_int2((int)((unsigned)k | (flags << 24)), (int)((unsigned)((z0 + kZBias) >> 2) | ((unsigned)tx << 16)));
 }
+__host__ __device__ inline int work_item_z0(int2 item) { return (int)(item.y & 0xffff) * 4 - kZBias; }
 
 template <typename T>
 struct alignas(128) ShotDesc {

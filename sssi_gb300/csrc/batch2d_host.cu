@@ -376,23 +376,48 @@ void Batch2d<T>::schedule(int shape) {
         for (int s = 0; s < d.nsrc; ++s)
             if (d.src_iz[s] >= z0 && d.src_iz[s] < z0 + TZs && d.src_ix[s] >= x0 && d.src_ix[s] < x0 + width)
                 f |= kSource;
-        const float fill = (float)(std::min(TZs, d.nz - z0) * std::max(0, std::min(width, d.nx - x0))) /
-                           (float)(TZs * TXs);
+        const int rows = std::min(z0 + TZs, d.nz) - std::max(z0, 0);
+        const float fill = (float)(rows * std::max(0, std::min(width, d.nx - x0))) / (float)(TZs * TXs);
         return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))};
+    };
+    // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of 4; the
+    // rows above the grid are not computed).  The lowest rows whose second z
+    // derivative reaches the damped band (zb0 - N + 1 on, zb0 = nz - nB) take
+    // the two-stage form; a shift that puts them into one tile row instead of
+    // two, with no more tile rows in all, saves a row of band tiles.  zs is a
+    // function of the shot's grid and the tile shape only, so every cell of a
+    // shot uses the same formula whichever shots share the batch.
+    auto row_shift = [&](const ShotTail<T>& d) {
+        const int cut = d.nz - d.nB - N_ + 1;
+        if (d.nB <= 0 || cut < 0) return 0;
+        auto cost = [&](int zs) {
+            float c = 0.0f;
+            for (int z0 = -zs; z0 < d.nz; z0 += TZs) {
+                const int rows = std::min(z0 + TZs, d.nz) - std::max(z0, 0);
+                const bool bz = tile_band_flags(N_, TZs, TXs, d.nz, d.nx, d.nB, z0, TXs) & kBandZ;
+                c += (0.3f + 0.7f * (float)rows / (float)TZs) * (bz ? 2.2f : 1.0f);
+            }
+            return c;
+        };
+        const int zs = (TZs - (cut / 4 * 4) % TZs) % TZs;
+        return (zs > 0 && cost(zs) < cost(0) - 1e-3f) ? zs : 0;
     };
     std::vector<Item> items;
     {
         size_t n = 0;
         for (const Shot& S : shots_)
-            if (S.enabled) n += (size_t)((S.desc.s.nz + TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
+            if (S.enabled) n += (size_t)((S.desc.s.nz + 2 * TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
         items.reserve(n);
     }
     for (int k = 0; k < (int)shots_.size(); ++k) {
         if (!shots_[k].enabled) continue;
         const ShotTail<T>& d = shots_[k].desc.s;
-        const int ntz = (d.nz + TZs - 1) / TZs, ntx = (d.nx + TXs - 1) / TXs;
+        const int zs = row_shift(d);
+        const int ntz = (d.nz + zs + TZs - 1) / TZs, ntx = (d.nx + TXs - 1) / TXs;
+        SSSI_REQUIRE((ntz - 1) * TZs - zs <= kMaxTileRow && ntx <= 0xffff, SSSI_ERR_ARG,
+                     "grid of %d x %d cells too large for the batched step", d.nz, d.nx);
         for (int q = 0; q < ntz * ntx; ++q) {
-            const int z0 = (q % ntz) * TZs, x0 = (q / ntz) * TXs;
+            const int z0 = (q % ntz) * TZs - zs, x0 = (q / ntz) * TXs;
             items.push_back(tile_item(k, z0, x0, TXs));
         }
     }
@@ -526,7 +551,7 @@ void Batch2d<T>::schedule(int shape) {
         std::vector<int> fill(begin.begin(), begin.end() - 1);
         for (size_t q = 0; q < items.size(); ++q) {
             const Item& it = items[q];
-            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0 / TZs, it.x0 / TXs);
+            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0, it.x0 / TXs);
         }
     }
 

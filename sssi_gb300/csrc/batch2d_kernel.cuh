@@ -198,7 +198,7 @@ __device__ __noinline__ void band_stage1_cells(const BatchConst<T>& bc, const Sh
             const int idx = tid + u * NT;
             const int r = idx % TZ, cx = idx / TZ;
             const int i = z0 + r, jc = x0 - N + cx;
-            const bool band = jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+            const bool band = i >= 0 && jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
             qc[u] = (idx < CELLS && i < nz && band) ? i + (int64_t)(jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
             b[u] = T(0);
             bm[u] = T(0);
@@ -331,7 +331,7 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
             if (unit < UNITS) {
                 const int g = unit % G4, cx = unit / G4;
                 const int i = z0 + 4 * g, jc = x0 - N + cx;
-                const bool band = jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+                const bool band = i >= 0 && jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
                 const int64_t qc = band ? i + (int64_t)(jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
                 T b[4], bm[4];
                 M m[4];
@@ -809,7 +809,7 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 // the work item's step-independent flags (bands, point sources) and the
 // shot's sched word.
 __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned f, int tau) {
-    if ((sched & kSchedDense) || ((sched & kSchedRow) && z0 == 0)) f |= kSource;
+    if ((sched & kSchedDense) || ((sched & kSchedRow) && z0 <= 0)) f |= kSource;  // z0 <= 0: the tile holds row 0
     bool rare = (sched & (kSchedSnap | kSchedImg64)) != 0u;
     if (sched & (kSchedAmax | kSchedPack | kSchedImg16)) {  // outputs every stride steps
         const int stride = (int)(sched >> 8);
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
             }
             const unsigned top = (unsigned)item.x >> 24;  // static flags | half << 3
             const unsigned half = kSplit ? (top >> 3) & 3u : 0u;  // 0 whole tile, 1 / 2 left / right half
-            const int z0 = (item.y & 0xffff) * TZ, x0 = ((unsigned)item.y >> 16) * TX + (half == 2u ? TX / 2 : 0);
+            const int z0 = work_item_z0(item), x0 = ((unsigned)item.y >> 16) * TX + (half == 2u ? TX / 2 : 0);
             info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
             info->tloc = tloc;
@@ -996,6 +996,8 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
             const T* Vb = reinterpret_cast<const T*>(st + G::kV);
             const int z0 = ti.z0, x0 = ti.x0;
             unsigned amax_bits = 0u;
+            // rows above the grid (the first tile row of a shifted shot) are skipped:
+            // j0 >= 0, so (j0 | i0) >= 0 tests i0 >= 0
             const int i0 = z0 + r0, j0 = x0 + c0;
             T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
             if constexpr (kSplit) {
@@ -1011,7 +1013,7 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
                                               scratch);
                     __syncthreads();
                 }
-                if (i0 < sh.nz && j0 < sh.nx && (!half || c0 < TX / 2))
+                if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx && (!half || c0 < TX / 2))
                     tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             } else {
                 if (ti.flags & (kBandZ | kBandX)) {
@@ -1019,7 +1021,7 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
                                           scratch);
                     __syncthreads();
                 }
-                if (i0 < sh.nz && j0 < sh.nx)
+                if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx)
                     tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             }
             if (ti.flags & kAmax) {
