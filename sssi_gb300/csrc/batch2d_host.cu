@@ -380,7 +380,8 @@ void Batch2d<T>::schedule(int shape) {
         const float fill = (float)(rows * std::max(0, std::min(width, d.nx - x0))) / (float)(TZs * TXs);
         return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))};
     };
-    // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of 4; the
+    // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of one
+    // 32-byte sector of rows, so that the tiles' copies stay sector-aligned; the
     // rows above the grid are not computed).  The lowest rows whose second z
     // derivative reaches the damped band (zb0 - N + 1 on, zb0 = nz - nB) take
     // the two-stage form; a shift that puts them into one tile row instead of
@@ -399,7 +400,8 @@ void Batch2d<T>::schedule(int shape) {
             }
             return c;
         };
-        const int zs = (TZs - (cut / 4 * 4) % TZs) % TZs;
+        constexpr int kSector = 32 / (int)sizeof(T);  // rows per 32-byte sector
+        const int zs = (TZs - (cut / kSector * kSector) % TZs) % TZs;
         return (zs > 0 && cost(zs) < cost(0) - 1e-3f) ? zs : 0;
     };
     std::vector<Item> items;
