@@ -99,15 +99,18 @@ inline unsigned sched_word(const ShotTail<T>& d) {
 }
 
 // A work item: shot k (< 2^24) with the tile's step-independent flags in the
-// top byte; the tile's first row z0 (a multiple of 4, at least -kZBias: a
-// shot's tile rows may start above row 0, see Batch2d::schedule) as
-// (z0 + kZBias) / 4, and its column tx in tiles (each < 2^16).
-constexpr int kZBias = 64;
+// top byte; the tile's first row z0 and first column x0 (a shot's tiles may
+// start above row 0 and left of column 0, see Batch2d::schedule) as
+// (z0 + kZBias) / 4 and (x0 + kXBias) / 2, 16 bits each.
+constexpr int kZBias = 64, kXBias = 64;
 constexpr int kMaxTileRow = 4 * 0xffff - kZBias;  // largest z0
-__host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int z0, int tx) {
-    return make_int2((int)((unsigned)k | (flags << 24)), (int)((unsigned)((z0 + kZBias) >> 2) | ((unsigned)tx << 16)));
+constexpr int kMaxTileCol = 2 * 0xffff - kXBias;  // largest x0
+__host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int z0, int x0) {
+    return make_int2((int)((unsigned)k | (flags << 24)),
+                     (int)((unsigned)((z0 + kZBias) >> 2) | ((unsigned)((x0 + kXBias) >> 1) << 16)));
 }
 __host__ __device__ inline int work_item_z0(int2 item) { return (int)(item.y & 0xffff) * 4 - kZBias; }
+__host__ __device__ inline int work_item_x0(int2 item) { return (int)((unsigned)item.y >> 16) * 2 - kXBias; }
 
 template <typename T>
 struct alignas(128) ShotDesc {

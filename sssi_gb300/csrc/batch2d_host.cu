@@ -377,7 +377,8 @@ void Batch2d<T>::schedule(int shape) {
             if (d.src_iz[s] >= z0 && d.src_iz[s] < z0 + TZs && d.src_ix[s] >= x0 && d.src_ix[s] < x0 + width)
                 f |= kSource;
         const int rows = std::min(z0 + TZs, d.nz) - std::max(z0, 0);
-        const float fill = (float)(rows * std::max(0, std::min(width, d.nx - x0))) / (float)(TZs * TXs);
+        const int cols = std::max(0, std::min(x0 + width, d.nx) - std::max(x0, 0));
+        const float fill = (float)(rows * cols) / (float)(TZs * TXs);
         return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))};
     };
     // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of one
@@ -404,22 +405,48 @@ void Batch2d<T>::schedule(int shape) {
         const int zs = (TZs - (cut / kSector * kSector) % TZs) % TZs;
         return (zs > 0 && cost(zs) < cost(0) - 1e-3f) ? zs : 0;
     };
+    // Likewise tile columns start at column -xs (0 <= xs <= 8, even): the shift
+    // with the least estimated cost, which mostly means the columns reaching
+    // the right band in one tile column instead of two (the left band needs
+    // xs <= 8 to stay in one).
+    auto col_shift = [&](const ShotTail<T>& d) {
+        if (d.nB <= 0) return 0;
+        auto cost = [&](int xs) {
+            float c = 0.0f;
+            for (int x0 = -xs; x0 < d.nx; x0 += TXs) {
+                const int cols = std::min(x0 + TXs, d.nx) - std::max(x0, 0);
+                const bool bx = tile_band_flags(N_, TZs, TXs, d.nz, d.nx, d.nB, 0, x0) & kBandX;
+                c += (0.3f + 0.7f * (float)cols / (float)TXs) * (bx ? 2.2f : 1.0f);
+            }
+            return c;
+        };
+        int best = 0;
+        float cbest = cost(0);
+        for (int xs = 2; xs <= 8; xs += 2) {
+            const float c = cost(xs);
+            if (c < cbest - 1e-3f) {
+                best = xs;
+                cbest = c;
+            }
+        }
+        return best;
+    };
     std::vector<Item> items;
     {
         size_t n = 0;
         for (const Shot& S : shots_)
-            if (S.enabled) n += (size_t)((S.desc.s.nz + 2 * TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
+            if (S.enabled) n += (size_t)((S.desc.s.nz + 2 * TZs - 1) / TZs) * ((S.desc.s.nx + 2 * TXs - 1) / TXs);
         items.reserve(n);
     }
     for (int k = 0; k < (int)shots_.size(); ++k) {
         if (!shots_[k].enabled) continue;
         const ShotTail<T>& d = shots_[k].desc.s;
-        const int zs = row_shift(d);
-        const int ntz = (d.nz + zs + TZs - 1) / TZs, ntx = (d.nx + TXs - 1) / TXs;
-        SSSI_REQUIRE((ntz - 1) * TZs - zs <= kMaxTileRow && ntx <= 0xffff, SSSI_ERR_ARG,
+        const int zs = row_shift(d), xs = col_shift(d);
+        const int ntz = (d.nz + zs + TZs - 1) / TZs, ntx = (d.nx + xs + TXs - 1) / TXs;
+        SSSI_REQUIRE((ntz - 1) * TZs - zs <= kMaxTileRow && (ntx - 1) * TXs - xs <= kMaxTileCol, SSSI_ERR_ARG,
                      "grid of %d x %d cells too large for the batched step", d.nz, d.nx);
         for (int q = 0; q < ntz * ntx; ++q) {
-            const int z0 = (q % ntz) * TZs - zs, x0 = (q / ntz) * TXs;
+            const int z0 = (q % ntz) * TZs - zs, x0 = (q / ntz) * TXs - xs;
             items.push_back(tile_item(k, z0, x0, TXs));
         }
     }
@@ -553,7 +580,7 @@ void Batch2d<T>::schedule(int shape) {
         std::vector<int> fill(begin.begin(), begin.end() - 1);
         for (size_t q = 0; q < items.size(); ++q) {
             const Item& it = items[q];
-            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0, it.x0 / TXs);
+            work[fill[owner[q]]++] = pack_work_item(it.shot, it.flags, it.z0, it.x0);
         }
     }
 

@@ -148,7 +148,7 @@ __device__ __noinline__ void band_stage1_cells(const BatchConst<T>& bc, const Sh
             const int idx = tid + u * NT;
             const int r = idx % B::RZ, c = idx / B::RZ;
             const int ip = z0 - N + r, j = x0 + c;
-            in[u] = idx < CELLS && j < nx && ip >= zb0 && ip < nz;
+            in[u] = idx < CELLS && (unsigned)j < (unsigned)nx && ip >= zb0 && ip < nz;
             b[u] = T(0);
             bm[u] = T(0);
             m[u] = M{};
@@ -281,7 +281,7 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
                     b[o] = T(0);
                     bm[o] = T(0);
                     m[o] = M{};
-                    if (j < nx && p >= zb0 && p < nz) {
+                    if ((unsigned)j < (unsigned)nx && p >= zb0 && p < nz) {
                         const int64_t q = (p - zb0) + (int64_t)j * nB;
                         b[o] = ldg_t(zb + q);
                         bm[o] = ldg_t(zbm1 + q);
@@ -304,7 +304,7 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
 #pragma unroll
                     for (int n = 1; n < N; ++n) d = fma(bc.wz[n], w[C0 + o + 1 + n] - w[C0 + o - n], d);
                     const int r = 4 * g + o, p = z0 - N + r;
-                    if (j < nx && p >= zb0 && p < nz) {
+                    if ((unsigned)j < (unsigned)nx && p >= zb0 && p < nz) {
                         m[o] = mem_new(b[o], bm[o], m[o], d);
                         d = mem_add(d, m[o]);
                         if (r >= N && r < N + TZ) phi_out[(p - zb0) + (int64_t)j * nB] = m[o];
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
             }
             const unsigned top = (unsigned)item.x >> 24;  // static flags | half << 3
             const unsigned half = kSplit ? (top >> 3) & 3u : 0u;  // 0 whole tile, 1 / 2 left / right half
-            const int z0 = work_item_z0(item), x0 = ((unsigned)item.y >> 16) * TX + (half == 2u ? TX / 2 : 0);
+            const int z0 = work_item_z0(item), x0 = work_item_x0(item) + (half == 2u ? TX / 2 : 0);
             info->tile = w < wend ? w : kNoTile;
             info->shot = shot;
             info->tloc = tloc;
@@ -996,8 +996,9 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
             const T* Vb = reinterpret_cast<const T*>(st + G::kV);
             const int z0 = ti.z0, x0 = ti.x0;
             unsigned amax_bits = 0u;
-            // rows above the grid (the first tile row of a shifted shot) are skipped:
-            // j0 >= 0, so (j0 | i0) >= 0 tests i0 >= 0
+            // rows above and columns left of the grid (first tiles of a shifted
+            // shot) are skipped; x0 and c0 are even, so a thread's columns are
+            // all on one side of column 0
             const int i0 = z0 + r0, j0 = x0 + c0;
             T* scratch = reinterpret_cast<T*>(smem + G::kScratch);
             if constexpr (kSplit) {
