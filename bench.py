@@ -102,10 +102,15 @@ def cell_updates(nz, nx, nt):
 # dram__bytes_read.sum + dram__bytes_write.sum of one forward step of the RTM
 # shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
 # python bench.py --case rtm-short`
-FWD_STEP_DRAM_BYTES = 22_948_352
+FWD_STEP_DRAM_BYTES = 22_306_816
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
-STEP3D_DRAM_BYTES = 488_232_960 + 172_346_880
+STEP3D_DRAM_BYTES = 460_690_688 + 170_586_880
+# the same for one batched step of the 64-shot workload while all 64 shots are
+# active (the 301st launch), from `ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum,gpu__time_duration.sum -k regex:batch2d -s 300 -c 2
+# python bench.py --case batch64`
+BATCH_STEP_DRAM_BYTES = 1_209_735_680 + 374_187_264
 
 
 def step_bytes_per_cell(nz, nx, nb):
@@ -491,7 +496,12 @@ def bench_batch(S, args):
               "device_s": round(kern_s, 4),
               "roofline": {"bound": "hbm", "achieved": round(alg_bytes / kern_s / 1e9, 1), "peak": peak,
                            "unit": "GB/s", "frac": round(alg_bytes / kern_s / 1e9 / peak, 4), "peak_kind": peak_kind,
-                           "bytes_per_cell": round(alg_bytes / cells, 2)},
+                           "bytes_per_cell": round(alg_bytes / cells, 2),
+                           "traffic": BATCH_STEP_DRAM_BYTES,
+                           "traffic_note": "dram read+write of one step with all 64 shots active (ncu, cold); "
+                                           "its algorithmic bytes are " + str(int(sum(
+                                               V.shape[0] * V.shape[1] * step_bytes_per_cell(V.shape[0], V.shape[1], NB)
+                                               for (V, _, _, _) in shots)))},
               "timing": "CUDA events around each round of batched steps inside the plan (whole batch, all rounds)"}
     return {"metric": "Gcell-updates/s (64-shot batched forward modelling, 800x2400 model)",
             "value": round(value, 2), "unit": UNIT, "wall_s": round(el, 3), "first_pass_wall_s": round(walls[0], 3),
@@ -684,6 +694,17 @@ def run_case(name):
     import sssi_gb300 as S
 
     torch.cuda.set_device(0)
+    if name == "batch64":
+        # the 64-shot batch submitted once to an FP32 plan (launch 301 is a step
+        # with all 64 shots active)
+        dt = 8e-4
+        shots = batch_shots()
+        with S.Plan(N_ORDER, DZ, DX, mode="fp32") as plan:
+            tickets = [plan.submit_fwd2d(V, nt, [iz], [ix], ricker(20.0, nt, dt)[None, :], NB, dt)
+                       for (V, nt, iz, ix) in shots]
+            outs = [plan.wait(t)["data"] for t in tickets]
+        print(f"case {name}: 64 shots ok, data max {max(float(np.abs(o).max()) for o in outs):.3e}")
+        return
     if name == "rtm-short":
         V, VS, w, siz, six, nz, nx = workload()
         img = S.rtmTimeCpmlFor2dAw(V, VS, w[:64], siz, six, N_ORDER, NB, DZ, DX, DT, epsilon=EPS, mode="fp32",
@@ -710,7 +731,7 @@ def run_case(name):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short"],
+    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short", "batch64"],
                     help="run one small fixed workload for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
