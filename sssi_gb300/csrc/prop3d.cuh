@@ -59,6 +59,7 @@ struct Desc3 {
     int64_t ldxy;             // Nzp * Nxp: stride of y
     int nz, nx, ny, nB, nt;
     int ntz, ntx;          // tiles along z and x
+    int zs;                // tile rows start at row -zs (Prop3d: the bottom band's rows in one tile row)
     const int2* order[2];  // work items (tile, y0 | y1 << 16: planes y0 .. y1-1), most expensive first, of
                            // the two candidate schedules (Const3::sched picks one)
     int* next;             // two counters: items taken at steps of parity 0 / 1

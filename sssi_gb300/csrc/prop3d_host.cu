@@ -235,7 +235,26 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     d.ny = (int)ny;
     d.nB = nB;
     d.nt = nt;
-    d.ntz = (int)((nz + S::TZ - 1) / S::TZ);
+    // Tile rows start at row -zs (whole 32-byte sectors of rows): the rows whose z
+    // second derivative reaches the bottom band (nz - nB - N + 1 on) then fall in
+    // one tile row instead of two, when that does not add a tile row.  Rows above
+    // the grid are not computed.
+    d.zs = 0;
+    {
+        const int64_t cut = nz - nB - N + 1;
+        if (nB > 0 && cut >= 0) {
+            constexpr int kSector = 32 / (int)sizeof(T);
+            const int zs = (int)((S::TZ - (cut / kSector * kSector) % S::TZ) % S::TZ);
+            auto band_rows = [&](int s0) {
+                int n = 0;
+                for (int64_t z0 = -s0; z0 < nz; z0 += S::TZ) n += z0 + S::TZ + N - 1 > nz - nB;
+                return n;
+            };
+            if (zs > 0 && (nz + zs + S::TZ - 1) / S::TZ == (nz + S::TZ - 1) / S::TZ && band_rows(zs) < band_rows(0))
+                d.zs = zs;
+        }
+    }
+    d.ntz = (int)((nz + d.zs + S::TZ - 1) / S::TZ);
     d.ntx = (int)((nx + S::TX - 1) / S::TX);
     int dev = 0, sms = 1;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
@@ -280,7 +299,7 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
         std::vector<char> bzx(ntile);
         double total = 0;
         for (int t = 0; t < ntile; ++t) {
-            const int z0 = (t % d.ntz) * S::TZ, x0 = (t / d.ntz) * S::TX;
+            const int z0 = (t % d.ntz) * S::TZ - d.zs, x0 = (t / d.ntz) * S::TX;
             bzx[t] = nB > 0 && (z0 + S::TZ + N - 1 > nz - nB || x0 - N < nB || x0 + S::TX + N - 2 >= nx - nB);
             for (int y = 0; y < ny; ++y) total += plane_cost(bzx[t], y);
         }

@@ -160,7 +160,7 @@ __device__ __noinline__ void band_plane_stage1(const Const3<T>& cc, const Desc3<
             const int idx = tid + u * NT;
             const int r = idx % TZ, cx = idx / TZ;
             const int i = z0 + r, jc = x0 - N + cx;
-            const bool band = jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+            const bool band = i >= 0 && jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
             qc[u] = (idx < CELLS && i < nz && band) ? i + (jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
             b[u] = T(0);
             bm[u] = T(0);
@@ -490,12 +490,12 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
     for (int k = blockIdx.x; k < cc.nitems && !failed;) {
         const int2 item = d.order[cc.sched][k];
         const int tile = item.x;
-        const int z0 = (tile % d.ntz) * TZ, x0 = (tile / d.ntz) * TX;
+        const int z0 = (tile % d.ntz) * TZ - d.zs, x0 = (tile / d.ntz) * TX;
         const int y0 = item.y & 0xffff, y1 = (unsigned)item.y >> 16;
         const bool bz = nB > 0 && z0 + TZ + N - 1 > nz - nB;
         const bool bx = nB > 0 && (x0 - N < nB || x0 + TX + N - 2 >= nx - nB);
         const int i0 = z0 + r0, j = x0 + c0;
-        const bool act = i0 < nz && j < nx;
+        const bool act = i0 < nz && (j | i0) >= 0 && j < nx;  // j >= 0: tests i0 >= 0 (rows above the grid)
         // per-item facts (uniform over the block): what the planes of this item
         // need beyond the stencil
         bool item_src = d.src_dense != nullptr;
