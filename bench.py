@@ -105,12 +105,12 @@ def cell_updates(nz, nx, nt):
 FWD_STEP_DRAM_BYTES = 22_306_816
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
-STEP3D_DRAM_BYTES = 460_690_688 + 170_586_880
+STEP3D_DRAM_BYTES = 454_952_448 + 170_105_600
 # the same for one batched step of the 64-shot workload while all 64 shots are
 # active (the 301st launch), from `ncu --metrics dram__bytes_read.sum,
 # dram__bytes_write.sum,gpu__time_duration.sum -k regex:batch2d -s 300 -c 2
 # python bench.py --case batch64`
-BATCH_STEP_DRAM_BYTES = 1_209_735_680 + 374_187_264
+BATCH_STEP_DRAM_BYTES = 1_209_339_392 + 373_152_000
 
 
 def step_bytes_per_cell(nz, nx, nb):

@@ -366,9 +366,20 @@ void Batch2d<T>::schedule(int shape) {
         float cost;
     };
     // a tile (or a half of width TX/2 at x0) with its step-independent flags and cost:
-    // measured, a tile next to a band costs about 1.2 interior tiles more per banded
-    // direction (the cooperative pass and the memory-variable round trips); partial
-    // tiles cost in proportion to their cells
+    // a tile next to a band costs more per banded direction (the cooperative pass and
+    // the memory variables), partial tiles cost in proportion to their cells.  The
+    // extra cost, measured: 1.2 interior tiles when the batch is small (its fields
+    // stay in L2), 2.0 when it streams from HBM (at least 8 tiles per block), where
+    // the memory variables' own bytes weigh more (the 64-shot batch and 4096^2
+    // single grids step 0.7-0.8 % faster with 2.0; a two-shot 620 x 1240 forward
+    // phase 4 % slower).
+    float band_w = 1.2f;
+    {
+        int64_t n = 0;
+        for (const Shot& S : shots_)
+            if (S.enabled) n += (int64_t)((S.desc.s.nz + TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
+        if (n >= 8LL * sms_ * ctas_per_sm_[shape]) band_w = 2.0f;
+    }
     auto tile_item = [&](int k, int z0, int x0, int width) {
         const ShotTail<T>& d = shots_[k].desc.s;
         unsigned f = tile_band_flags(N_, TZs, width, d.nz, d.nx, d.nB, z0, x0);
@@ -379,7 +390,7 @@ void Batch2d<T>::schedule(int shape) {
         const int rows = std::min(z0 + TZs, d.nz) - std::max(z0, 0);
         const int cols = std::max(0, std::min(x0 + width, d.nx) - std::max(x0, 0));
         const float fill = (float)(rows * cols) / (float)(TZs * TXs);
-        return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? 1.2f : 0.0f) + (bx ? 1.2f : 0.0f))};
+        return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? band_w : 0.0f) + (bx ? band_w : 0.0f))};
     };
     // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of one
     // 32-byte sector of rows, so that the tiles' copies stay sector-aligned; the
@@ -475,8 +486,8 @@ void Batch2d<T>::schedule(int shape) {
                     // computed by the same formula as in the unsplit tile (results do
                     // not depend on which shots share the batch)
                     Item hi = tile_item(it.shot, it.z0, it.x0 + h * (TXs / 2), TXs / 2);
-                    const float band = (it.flags & kBandZ ? 1.2f : 0.0f) + (it.flags & kBandX ? 1.2f : 0.0f);
-                    const float own = (hi.flags & kBandZ ? 1.2f : 0.0f) + (hi.flags & kBandX ? 1.2f : 0.0f);
+                    const float band = (it.flags & kBandZ ? band_w : 0.0f) + (it.flags & kBandX ? band_w : 0.0f);
+                    const float own = (hi.flags & kBandZ ? band_w : 0.0f) + (hi.flags & kBandX ? band_w : 0.0f);
                     hi.cost *= (1.0f + band) / (1.0f + own);
                     hi.flags = (hi.flags & ~(kBandZ | kBandX)) | (it.flags & (kBandZ | kBandX));
                     hi.x0 = it.x0;  // the work item keeps the tile position; the half selects the columns
