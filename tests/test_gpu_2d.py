@@ -94,6 +94,33 @@ def test_large_grid_tile_shapes(gpu, co, oracle_mod):
     assert oracle_mod.rel_l2(m32, m_ref) <= TOL_FP32
 
 
+def test_shifted_tile_grid(gpu, co, oracle_mod):
+    """A 68 x 80 grid with 20-cell bands: the rows and columns whose second
+    derivatives reach the bottom and right bands fit one tile row / column
+    only when the tile grid starts above and left of the grid, so the batched
+    step shifts it (FP64 and FP32 tile shapes alike).  Sources in the top-left
+    and top-right corners and next to the bottom band; every cell of every
+    step is checked against the oracle, forward and reverse."""
+    S = gpu
+    nz, nx, nt, N, nB = 68, 80, 160, 4, 20
+    rng = np.random.default_rng(68)
+    v = rng.uniform(1500, 4000, (nz, nx))
+    trace = oracle_mod.ricker(25.0, nt, 1e-3)
+    src = np.zeros((nz, nx, nt), order="F")
+    src[0, 1, :] = trace
+    src[3, 77, :] = 0.5 * trace
+    src[60, 40, :] = -0.7 * trace
+    d_ref, s_ref = co.fwd2d(v, src, N, nB, 10.0, 10.0, 1e-3)
+    m_ref, r_ref = co.rvs2d(v, d_ref, N, nB, 10.0, 10.0, 1e-3)
+    for mode, tol in (("fp64", TOL_FP64), ("fp32", TOL_FP32)):
+        d, s = S.fwdTimeCpmlFor2dAw(v, src, N, nB, 10.0, 10.0, 1e-3, mode=mode)
+        assert oracle_mod.rel_l2(d, d_ref) <= tol
+        assert oracle_mod.rel_l2(s, s_ref) <= tol
+        m, r = S.rvsTimeCpmlFor2dAw(v, d_ref, N, nB, 10.0, 10.0, 1e-3, mode=mode)
+        assert oracle_mod.rel_l2(m, m_ref) <= tol
+        assert oracle_mod.rel_l2(r, r_ref) <= tol
+
+
 def test_device_pointers(gpu, co):
     """Inputs/outputs already in HBM (torch tensors, column-major)."""
     import torch
