@@ -416,10 +416,11 @@ void Batch2d<T>::schedule(int shape) {
         const int zs = (TZs - (cut / kSector * kSector) % TZs) % TZs;
         return (zs > 0 && cost(zs) < cost(0) - 1e-3f) ? zs : 0;
     };
-    // Likewise tile columns start at column -xs (0 <= xs <= 8, even): the shift
-    // with the least estimated cost, which mostly means the columns reaching
-    // the right band in one tile column instead of two (the left band needs
-    // xs <= 8 to stay in one).
+    // Likewise tile columns start at column -xs (0 <= xs <= 8, even, so that a
+    // thread's two columns are on one side of column 0): the shift with the
+    // least estimated cost, which mostly means the columns reaching the right
+    // band in one tile column instead of two (larger shifts would push the left
+    // band's columns into a second tile column for the usual band widths).
     auto col_shift = [&](const ShotTail<T>& d) {
         if (d.nB <= 0) return 0;
         auto cost = [&](int xs) {
