@@ -11,12 +11,20 @@ model.  One shot = forward modelling in both models + reverse propagation of
 dataTrue - dataSmooth + zero-lag imaging: 3 * 620 * 1240 * 4000 = 9.23e9
 cell-updates.
 
-Headline arm (default): FP32 wavefield, compensated/FP64 CPML memory, FP16
-forward snapshots with one power-of-two scale each, stored and imaged every
-4th step, FP64 image sums.  The FP64 drop-in (fused FP64) is measured beside
-it.  ``value`` times the shot with every input already in HBM; ``e2e`` calls
-the same C ABI with host buffers (models and wavelet copied in, image copied
-out inside the timed region).
+Headline arm (default): the FP64 drop-in (fused FP64, within 1e-12 relative
+L2 of the reference C), the same arithmetic width as the reference's CPU
+code.  ``value`` times the shot with every input already in HBM; ``e2e``
+calls the same C ABI entry point (sssi_rtmTimeCpmlFor2dAw) with host buffers
+(models and wavelet copied in, image copied out inside the timed region).
+The FP64 stencil is bound by the FP64 pipe on GB300, so its roofline is FP64
+operations per second against the FP64 FMA rate measured in the same run.
+
+Beside it, in the same JSON line: ``fp32`` (the precision form: FP32
+wavefield, compensated FP32 memory variables and imaging sums, FP16 forward
+snapshots every 4th step; with its HBM roofline and its error against
+FP64), ``c1`` (plain 2D forward modelling of 220 x 340 x 2000 through the
+MEX-shaped dense API with host buffers), ``fwd3d``, ``batch2d`` and
+``serve``.
 
 ``--impl reference`` times the CPU implementation of the same shot (the C
 restatement of the reference's algorithm, OpenMP over every host core) on a
@@ -103,6 +111,10 @@ def cell_updates(nz, nx, nt):
 # shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
 # python bench.py --case rtm-short`
 FWD_STEP_DRAM_BYTES = 22_306_816
+# the same for one FP64 forward step of the RTM shot (fused FP64), from
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:batch2d -s 40 -c 1
+# python bench.py --case rtm-short-fp64`; None until captured
+FWD64_STEP_DRAM_BYTES = None
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
 STEP3D_DRAM_BYTES = 454_952_448 + 170_105_600
@@ -111,6 +123,20 @@ STEP3D_DRAM_BYTES = 454_952_448 + 170_105_600
 # dram__bytes_write.sum,gpu__time_duration.sum -k regex:batch2d -s 300 -c 2
 # python bench.py --case batch64`
 BATCH_STEP_DRAM_BYTES = 1_209_339_392 + 373_152_000
+
+
+# FP64 instructions per cell of one step in the composed-stencil form of the
+# fused FP64 kernel: z sum 1 mul + 7 (add + fma), x sum 15 fma, update
+# lz + lx, 2P - Pold, (v dt)^2 * lap + ... (3): the least any cell needs
+# (cells next to a damped band take the two-stage form and more).
+FP64_OPS_PER_CELL = 33
+
+
+def step_bytes_per_cell_fp64(nz, nx, nb):
+    """Algorithmic HBM bytes of one FP64 step per cell: 32 B for P(t), P(t-1),
+    (v dt)^2 read and P(t+1) written, plus 48 B per damped cell and axis
+    (phi and psi read and written, b and b-1 read)."""
+    return 32 + 48 * (nb / nz + 2 * nb / nx)
 
 
 def step_bytes_per_cell(nz, nx, nb):
@@ -241,58 +267,97 @@ def run_gpu(args):
         return ms, phases, launches // max(steps, 1)
 
     S.enable_timing(True)
+    # headline: the FP64 drop-in, timed with the clocks sampled
     clocks = ClockSampler()
     clocks.start()
-    ms32, ph32, launches32 = timed_shots("fp32", STRIDE, args.steps, args.warmup)
+    ms64, ph64, launches64 = timed_shots("fp64", 1, args.steps, args.warmup)
     clk = clocks.stop()
-    ms32_e2e, _, _ = timed_shots("fp32", STRIDE, max(1, args.steps // 2), 1, host=True)
-    fp64_steps = max(1, min(args.steps, args.fp64_steps))
-    ms64, ph64, _ = timed_shots("fp64", 1, fp64_steps, 1)
+    ms64_e2e, _, _ = timed_shots("fp64", 1, max(2, args.steps // 2), 1, host=True)
+    # the precision form beside it
+    ms32, ph32, launches32 = timed_shots("fp32", STRIDE, args.steps, args.warmup)
+    ms32_e2e, _, _ = timed_shots("fp32", STRIDE, max(2, args.steps // 2), 1, host=True)
+    fma_rate = S.measure_fp64_rate()
 
     accuracy = rtm_accuracy(S, dV, dVS, dw, siz, six, nz, nx) if (rank == 0 and not args.no_accuracy) else None
 
     cells = cell_updates(nz, nx, NT)
-    value = world * cells / (ms32 * 1e-3) / 1e9
-    e2e = world * cells / (ms32_e2e * 1e-3) / 1e9
+    value = world * cells / (ms64 * 1e-3) / 1e9
+    e2e = world * cells / (ms64_e2e * 1e-3) / 1e9
+    value32 = world * cells / (ms32 * 1e-3) / 1e9
+    e2e32 = world * cells / (ms32_e2e * 1e-3) / 1e9
+    h2d = int(2 * nz * nx * 8 + NT * 8)
+    d2h = int(nz * nx * 8)
+    peak, peak_kind = peaks()
 
-    # roofline of the dominant kernel: the fused step, timed over the forward phase
+    # roofline of the dominant kernel, the fused FP64 step, timed over the
+    # forward phase (CUDA events on the launching stream): one forward step
+    # advances the shots in v and in vs and stores the vs field (FP64 snapshot)
+    fwd64_ms = float(np.mean([p[0][0] for p in ph64]))
+    step64_ms = fwd64_ms / NT
+    ops64 = 2 * nz * nx * FP64_OPS_PER_CELL
+    achieved64 = ops64 / (step64_ms * 1e-3) / 1e9
+    bytes64 = nz * nx * (2 * step_bytes_per_cell_fp64(nz, nx, NB) + 8)
+    hbm64 = bytes64 / (step64_ms * 1e-3) / 1e9
+
+    # the same for the FP32 step (HBM-bound)
     fwd_ms = float(np.mean([p[0][0] for p in ph32]))
-    fwd_launch = ph32[0][0][1]
-    per_launch_ms = fwd_ms / fwd_launch
+    per_launch_ms = fwd_ms / NT
     bytes_cell = step_bytes_per_cell(nz, nx, NB)
     # a forward launch advances the shots in v and in vs, and packs the vs field
     # to FP16 every STRIDE steps
     alg_bytes = nz * nx * (2 * bytes_cell + 2.0 / STRIDE)
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
-    peak, peak_kind = peaks()
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms32, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded layered model, Ricker source)",
+        "warmup": args.warmup, "ms_per_step": round(ms64, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded layered model, Ricker source)",
         "config": {"workload": "rtm2d-single-shot", "nz": nz, "nx": nx, "nt": NT, "nDiffOrder": N_ORDER,
-                   "nBoundary": NB, "dt": DT, "dx": DX, "snapshot": f"fp16 every {STRIDE} steps",
-                   "cell_updates_per_step": cells, "l2": "flushed (512 MB write) before every timed step",
+                   "nBoundary": NB, "dt": DT, "dx": DX, "arithmetic": "fused FP64 (<= 1e-12 of the reference)",
+                   "snapshot": "fp64 every step", "cell_updates_per_step": cells,
+                   "l2": "flushed (512 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single-gpu"},
-        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(2 * nz * nx * 8 + NT * 8),
-                "d2h_bytes_per_step": int(nz * nx * 8), "ms_per_step": round(ms32_e2e, 3),
-                "api": "sssi_rtmTimeCpmlFor2dAw (host buffers)"},
-        "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms64, 3),
-                 "mode": "fp64 (fused multiply-add)", "steps": fp64_steps},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": FWD_STEP_DRAM_BYTES,
-                     "traffic_note": "dram read+write of one forward step from an ncu capture of the same grid "
-                                     "(caches flushed per pass); the timed steps run from L2",
-                     "alg_bytes_per_launch": int(alg_bytes), "peak_kind": peak_kind,
-                     "kernel": "cpml2d step (fp32, forward phase)", "bytes_per_cell": round(bytes_cell, 2),
-                     "launch_ms": round(per_launch_ms, 5)},
-        "gpu_launches": int(launches32),
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(ms64_e2e, 3), "api": "sssi_rtmTimeCpmlFor2dAw (host buffers)"},
+        "roofline": {"bound": "fp64", "achieved": round(achieved64, 1), "peak": round(fma_rate / 1e9, 1),
+                     "unit": "Gop/s", "frac": round(achieved64 * 1e9 / fma_rate, 4), "traffic": FWD64_STEP_DRAM_BYTES,
+                     "traffic_note": "dram read+write of one FP64 forward step from an ncu capture of the same grid "
+                                     "(caches flushed per pass); its algorithmic bytes are " + str(int(bytes64)),
+                     "peak_kind": "measured in this run: FP64 fused multiply-adds per second "
+                                  "(sssi_measure_fp64_rate, 8 independent chains per thread)",
+                     "ops_per_cell": FP64_OPS_PER_CELL, "alg_ops_per_launch": int(ops64),
+                     "kernel": "batch2d step (fused fp64, forward phase)", "launch_ms": round(step64_ms, 5),
+                     "tflops": round(achieved64 * 1e9 * (57.0 / 33.0) / 1e12, 3),
+                     "hbm": {"achieved": round(hbm64, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(hbm64 / peak, 4), "peak_kind": peak_kind,
+                             "bytes_per_cell": round(step_bytes_per_cell_fp64(nz, nx, NB), 2)}},
+        "gpu_launches": int(launches64),
         "clocks": clk,
-        "phases_ms": {"forward": round(fwd_ms, 2), "reverse+imaging": round(float(np.mean([p[1][0] for p in ph32])), 2),
-                      "finish": round(float(np.mean([p[2][0] for p in ph32])), 3)},
+        "phases_ms": {"forward": round(fwd64_ms, 2),
+                      "reverse+imaging": round(float(np.mean([p[1][0] for p in ph64])), 2),
+                      "finish": round(float(np.mean([p[2][0] for p in ph64])), 3)},
+        "fp32": {"value": round(value32, 3), "unit": UNIT, "ms_per_step": round(ms32, 3), "dtype": "fp32",
+                 "form": f"FP32 wavefield, compensated FP32 memory variables and imaging sums, FP16 forward "
+                         f"snapshots every {STRIDE} steps",
+                 "speedup_vs_fp64": round(value32 / value, 2), "gpu_launches": int(launches32),
+                 "e2e": {"value": round(e2e32, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h, "ms_per_step": round(ms32_e2e, 3),
+                         "api": "sssi_rtmTimeCpmlFor2dAw (host buffers)"},
+                 "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                              "frac": round(achieved / peak, 4), "traffic": FWD_STEP_DRAM_BYTES,
+                              "traffic_note": "dram read+write of one forward step from an ncu capture of the same "
+                                              "grid (caches flushed per pass); the timed steps run from L2",
+                              "alg_bytes_per_launch": int(alg_bytes), "peak_kind": peak_kind,
+                              "kernel": "batch2d step (fp32, forward phase)", "bytes_per_cell": round(bytes_cell, 2),
+                              "launch_ms": round(per_launch_ms, 5)},
+                 "phases_ms": {"forward": round(fwd_ms, 2),
+                               "reverse+imaging": round(float(np.mean([p[1][0] for p in ph32])), 2),
+                               "finish": round(float(np.mean([p[2][0] for p in ph32])), 3)}},
     }
     if accuracy is not None:
-        line["accuracy"] = accuracy
+        line["fp32"]["accuracy"] = accuracy
+    if rank == 0 and not args.no_c1:
+        line["c1"] = bench_c1(S, args)
     if rank == 0 and not args.no_3d:
         line["fwd3d"] = bench_3d(S, args)
     if rank == 0 and not args.no_batch:
@@ -305,6 +370,84 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def c1_model(seed=20240515):
+    """The plain forward-modelling workload: a seeded 4-layer model on a 200 x
+    300 physical grid (flat interfaces at sorted random depths, velocities
+    sorted uniform in [1500, 4000] m/s), padded by extBoundary with 20 cells
+    to 220 x 340."""
+    rng = np.random.default_rng(seed)
+    nz0, nx0 = 200, 300
+    depths = np.sort(rng.choice(np.arange(20, nz0 - 10), 3, replace=False))
+    vel = np.sort(rng.uniform(1500.0, 4000.0, 4))
+    v = np.empty((nz0, nx0))
+    edges = [0, *depths, nz0]
+    for k in range(4):
+        v[edges[k]:edges[k + 1], :] = vel[k]
+    return np.asfortranarray(ext_boundary(v, 20))
+
+
+def bench_c1(S, args):
+    """Plain 2D forward modelling as the MATLAB application calls the MEX
+    (mainWaveTimeCpmlFor2dAw.m:131): 220 x 340 padded model, nt = 2000, dt =
+    1 ms, N = 4, nB = 20, dense nz x nx x nt source holding a 20 Hz Ricker at
+    physical (2, 150), data and the full snapshot returned.  Timed through
+    sssi_fwdTimeCpmlFor2dAw with pinned host buffers (1.2 GB of source in, 1.2
+    GB of snapshot out per call, inside the timed region) and with device
+    buffers; fused FP64 (the default of the MEX gateways) and strict FP64."""
+    import torch
+
+    v = c1_model()
+    nz, nx = v.shape
+    nt, dt = 2000, 1e-3
+    w = ricker(20.0, nt, dt)
+    src_h = torch.zeros((nt, nx, nz), dtype=torch.float64).pin_memory()
+    src_h[:, 170, 2] = torch.from_numpy(w)
+    src_h = src_h.permute(2, 1, 0)
+    snap_h = torch.empty((nt, nx, nz), dtype=torch.float64).pin_memory().permute(2, 1, 0)
+    data_h = torch.empty((nt, nx), dtype=torch.float64).pin_memory().T
+    v_h = torch.from_numpy(np.ascontiguousarray(v.T)).pin_memory().T
+    src_d, snap_d = src_h.cuda(), torch.empty_like(src_h, device="cuda")
+    data_d, v_d = torch.empty_like(data_h, device="cuda"), v_h.cuda()
+
+    def call(mode, vv, src, data, snap):
+        S.api.check(S.api.lib().sssi_fwdTimeCpmlFor2dAw(
+            S.api._addr(vv), S.api._addr(src), nz, nx, nt, N_ORDER, 20, 10.0, 10.0, dt, S.api._addr(data),
+            S.api._addr(snap), S.api._mode(mode)))
+
+    def timed(mode, host, reps):
+        ops = (v_h, src_h, data_h, snap_h) if host else (v_d, src_d, data_d, snap_d)
+        call(mode, *ops)
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call(mode, *ops)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts)), S.last_timing()
+
+    cells = nz * nx * nt
+    out = {"metric": "Gcell-updates/s (2D forward modelling 220x340, nt=2000, dense source and snapshot)",
+           "unit": UNIT, "cell_updates": cells, "dtype": "f64",
+           "h2d_bytes_per_call": int(8 * (nz * nx + nz * nx * nt)), "d2h_bytes_per_call": int(8 * (nx * nt + nz * nx * nt)),
+           "config": {"workload": "fwd2d-dense-c1", "grid": [nz, nx], "nt": nt, "dt": dt, "nDiffOrder": N_ORDER,
+                      "nBoundary": 20, "model": "seeded 4-layer model, 1500-4000 m/s",
+                      "source": "20 Hz Ricker at physical (2, 150), dense nz x nx x nt"}}
+    data = {}
+    for mode in ("fp64", "fp64-strict"):
+        ms_h, ph_h = timed(mode, True, 3)
+        ms_d, ph_d = timed(mode, False, 3)
+        data[mode] = data_d.clone()
+        out[mode] = {"e2e": round(cells / (ms_h * 1e-3) / 1e9, 3), "ms_e2e": round(ms_h, 2),
+                     "value": round(cells / (ms_d * 1e-3) / 1e9, 3), "ms_device": round(ms_d, 2),
+                     "propagation_ms_host_call": round(ph_h[0][0], 2) if ph_h else None}
+    a, b = data["fp64"], data["fp64-strict"]
+    out["fp64_vs_strict_data_rel_l2"] = float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
+    return out
 
 
 def rtm_accuracy(S, dV, dVS, dw, siz, six, nz, nx):
@@ -705,10 +848,11 @@ def run_case(name):
             outs = [plan.wait(t)["data"] for t in tickets]
         print(f"case {name}: 64 shots ok, data max {max(float(np.abs(o).max()) for o in outs):.3e}")
         return
-    if name == "rtm-short":
+    if name in ("rtm-short", "rtm-short-fp64"):
         V, VS, w, siz, six, nz, nx = workload()
-        img = S.rtmTimeCpmlFor2dAw(V, VS, w[:64], siz, six, N_ORDER, NB, DZ, DX, DT, epsilon=EPS, mode="fp32",
-                                   snap_stride=STRIDE)
+        fp64 = name.endswith("fp64")
+        img = S.rtmTimeCpmlFor2dAw(V, VS, w[:64], siz, six, N_ORDER, NB, DZ, DX, DT, epsilon=EPS,
+                                   mode="fp64" if fp64 else "fp32", snap_stride=1 if fp64 else STRIDE)
         print(f"case {name}: image max {np.abs(img).max():.3e}")
         return
     nz, nx, nt, mode = CASES[name]
@@ -731,17 +875,17 @@ def run_case(name):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short", "batch64"],
+    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short", "rtm-short-fp64", "batch64"],
                     help="run one small fixed workload for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-nt", type=int, default=200, help="time steps of the bounded CPU sample")
-    ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the fp32-vs-fp64 error report")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D forward-modelling line")
+    ap.add_argument("--no-c1", action="store_true", help="skip the plain forward-modelling (dense API) line")
     ap.add_argument("--nt3d", type=int, default=2000)
     ap.add_argument("--steps3d", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-shot batched line")

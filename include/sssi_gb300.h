@@ -72,6 +72,11 @@ int sssi_set_stream(void *stream);
 int sssi_enable_timing(int on);
 int sssi_last_timing(double *phase_ms, int64_t *phase_launches, int max_phases, int *n_phases);
 
+/* No counterpart in the reference: a measurement helper.  FP64 fused
+ * multiply-adds per second this GPU sustains (eight independent chains per
+ * thread, every SM busy); the FP64 stencil kernels are bound by this rate. */
+int sssi_measure_fp64_rate(double *fma_per_s);
+
 /* ---- host-side building blocks ---- */
 
 /* Staggered-grid first-derivative coefficients of half-order `order`
@@ -254,18 +259,27 @@ int sssi_plan_stats_get(sssi_plan *plan, sssi_plan_stats *stats);
  * cudaFree, or a host program that forbids heap use after start-up.
  *
  * Same inputs, outputs and results as sssi_fwdTimeCpmlFor2dAw in the FP64
- * modes, but every pointer must be device memory owned by the caller, and all
- * working state lives in one array of SSSI_NOALLOC_SCRATCH_BYTES compiled
- * into the library, which every GPU that uses this function keeps until the
- * process exits.  The function calls no allocating routine.  Grids whose
- * state does not fit (beyond about 620 x 1240 at nDiffOrder 4) are refused
- * with SSSI_ERR_ARG and a message giving the size needed.
+ * modes (bit-identical in SSSI_MODE_FP64_STRICT), but every pointer must be
+ * device memory owned by the caller, and all working state lives in one array
+ * of SSSI_NOALLOC_SCRATCH_BYTES compiled into the library.  The function calls
+ * no allocating routine.  nz and nx must be below 2^30 and nt below 2^31;
+ * grids whose state does not fit the array (beyond about 620 x 1240 at
+ * nDiffOrder 4) are refused with SSSI_ERR_ARG and a message giving the size
+ * needed.
+ *
+ * The array is reserved on a GPU when the library's module is first loaded
+ * there, which with CUDA's lazy module loading is the first call of this
+ * function on that GPU, and is then held until the process exits: a caller
+ * that gives all free GPU memory to its own pool should make one call (nt = 0
+ * is enough) before doing so.  The device address of the array is looked up
+ * on every call for the calling thread's current device.
  *
  * All calls share that one array: calls whose work overlaps on the GPU (from
- * two threads or two streams) corrupt each other and must be serialised by
- * the caller.  Each call clears the state that has to start at zero.  The
- * first call on each device looks up the array's device address with that
- * device current; make that first call before any stream capture begins. */
+ * two streams) corrupt each other and must be serialised by the caller; calls
+ * from several host threads are serialised inside the function.  Each call
+ * clears the state that has to start at zero.  The call blocks until its
+ * work is done, so it must not be made while a stream of the calling thread
+ * is being captured into a CUDA graph. */
 int sssi_fwdTimeCpmlFor2dAwNoAlloc(const double *v, const double *source, int64_t nz, int64_t nx, int64_t nt,
                                    int nDiffOrder, int nBoundary, double dz, double dx, double dt, double *data,
                                    double *snapshot, int mode);

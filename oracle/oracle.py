@@ -39,7 +39,11 @@ import numpy as np
 ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
-REFERENCE_SRC = Path(os.environ.get("SSSI_REFERENCE_SRC", "/root/reference/src/fd_cmex"))
+# The reference's src/fd_cmex directory, where its tree exists (the environment
+# variable SSSI_REFERENCE_SRC); without it the reference gateways are not built
+# and the tests that need them skip.
+_REF_ENV = os.environ.get("SSSI_REFERENCE_SRC", "")
+REFERENCE_SRC = Path(_REF_ENV) if _REF_ENV else None
 
 _i64 = ctypes.c_int64
 # glibc's log/exp, as the C gateways use (numpy's vectorised loops may round differently)
@@ -53,8 +57,10 @@ def build(reference: bool | None = None) -> None:
     reference tree is present, or when ``reference`` is True)."""
     subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "all"], check=True)
     if reference is None:
-        reference = (REFERENCE_SRC / "fwdTimeCpmlFor2dAw_mex.c").exists()
+        reference = REFERENCE_SRC is not None and (REFERENCE_SRC / "fwdTimeCpmlFor2dAw_mex.c").exists()
     if reference:
+        if REFERENCE_SRC is None:
+            raise RuntimeError("set SSSI_REFERENCE_SRC to the reference's src/fd_cmex directory")
         subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF_SRC={REFERENCE_SRC}"], check=True)
 
 

@@ -17,6 +17,7 @@ from .api import (  # noqa: F401
     fwdTimeCpmlFor3dAw,
     fwdTimeCpmlFor3dAwPoint,
     launch_count,
+    measure_fp64_rate,
     release_cache,
     rtmTimeCpmlFor2dAw,
     rvsTimeCpmlFor2dAw,

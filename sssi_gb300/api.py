@@ -9,9 +9,11 @@ numpy arrays (host) or CUDA torch tensors (device; they must be Fortran
 ordered, i.e. ``t.T.contiguous().T`` / created via ``permute``); outputs come
 back as the same kind.
 
-``mode`` selects the arithmetic (``"fp64-strict"``: the reference's rounding
-sequence, bit-identical to the reference C; ``"fp64"``: folded coefficients
-and fused multiply-adds; ``"fp32"``: FP32 wavefield with FP64 CPML memory).
+``mode`` selects the arithmetic (``"fp64"``, the default as in the MEX
+gateways: folded coefficients and fused multiply-adds, within 1e-12 relative
+L2 of the reference; ``"fp64-strict"``: the reference's rounding sequence,
+bit-identical to the reference C; ``"fp32"``: FP32 wavefield with
+compensated FP32 CPML memory variables).
 """
 from __future__ import annotations
 
@@ -93,7 +95,7 @@ def dampPml(u, v, L: float) -> np.ndarray:
     return d
 
 
-def fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64-strict", want_snapshot=True):
+def fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
     """[data, snapshot] = fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt)."""
     pv, kv, vshape = _in(v, "v")
     ps, ks, sshape = _in(source, "source")
@@ -111,7 +113,7 @@ def fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp
 
 
 def fwdTimeCpmlFor2dAwPoint(v, nt, src_iz, src_ix, wavelets, nDiffOrder, nBoundary, dz, dx, dt, *,
-                            mode="fp64-strict", want_snapshot=False):
+                            mode="fp64", want_snapshot=False):
     """Forward modelling with point sources: source s at interior (src_iz[s], src_ix[s])
     with amplitude wavelets[s, t].  Returns (data, snapshot or None)."""
     pv, kv, vshape = _in(v, "v")
@@ -129,7 +131,7 @@ def fwdTimeCpmlFor2dAwPoint(v, nt, src_iz, src_ix, wavelets, nDiffOrder, nBounda
     return data, snap
 
 
-def rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64-strict", want_snapshot=True):
+def rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
     """[model, snapshot] = rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt)."""
     pv, kv, vshape = _in(v, "v")
     pd, kd, dshape = _in(data, "data")
@@ -147,7 +149,7 @@ def rvsTimeCpmlFor2dAw(v, data, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64
     return model, snap
 
 
-def fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt, *, mode="fp64-strict",
+def fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt, *, mode="fp64",
                        want_snapshot=True):
     """[data, snapshot] = fwdTimeCpmlFor3dAw(v, source, nDiffOrder, nBoundary, dz, dx, dy, dt)."""
     pv, kv, vshape = _in(v, "v")
@@ -189,7 +191,7 @@ def fwdTimeCpmlFor3dAwPoint(v, nt, src_iz, src_ix, src_iy, wavelets, nDiffOrder,
 
 
 def rtmTimeCpmlFor2dAw(v, vs, wavelet, src_iz, src_ix, nDiffOrder, nBoundary, dz, dx, dt, *, epsilon=1e-3,
-                       mode="fp64-strict", snap_stride=4, want_data=False):
+                       mode="fp64", snap_stride=4, want_data=False):
     """One RTM shot: image = M./s2 of mainRtmTimeCpmlFor2dAw.m:268-275,315 for a
     point source at interior (src_iz, src_ix).  Returns image, or (image,
     dataTrue, dataSmooth) with ``want_data``."""
@@ -229,6 +231,13 @@ def last_timing():
     n = ctypes.c_int(0)
     check(lib().sssi_last_timing(ms.ctypes.data, nl.ctypes.data, 16, ctypes.addressof(n)))
     return [(float(ms[k]), int(nl[k])) for k in range(min(n.value, 16))]
+
+
+def measure_fp64_rate() -> float:
+    """FP64 fused multiply-adds per second of the current GPU (measurement helper)."""
+    r = ctypes.c_double(0.0)
+    check(lib().sssi_measure_fp64_rate(ctypes.addressof(r)))
+    return r.value
 
 
 def release_cache() -> None:

@@ -30,16 +30,6 @@ void pick_launch(int64_t nz, int64_t nx, int& bz, int& w) {
     }
 }
 
-// SSSI_ENGINE=xmarch routes the fused FP64 mode to the row-marching kernel
-// (the one strict FP64 always uses) instead of the tiled kernel.
-bool xmarch_engine() {
-    static const bool x = [] {
-        const char* e = std::getenv("SSSI_ENGINE");
-        return e && std::strcmp(e, "xmarch") == 0;
-    }();
-    return x;
-}
-
 void check_common(int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx, double dt, int mode) {
     SSSI_REQUIRE(nz > 0 && nx > 0 && nt >= 0, SSSI_ERR_ARG, "bad sizes nz=%lld nx=%lld nt=%lld", (long long)nz,
                  (long long)nx, (long long)nt);
@@ -549,7 +539,7 @@ extern "C" int sssi_fwdTimeCpmlFor2dAw(const double* v, const double* source, in
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
+        if (mode == SSSI_MODE_FP64_STRICT)
             fwd2d_dense<Cpml2d<double, double>>(v, source, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, data,
                                                 snapshot, mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
@@ -571,7 +561,7 @@ extern "C" int sssi_fwdTimeCpmlFor2dAwPoint(const double* v, int64_t nz, int64_t
         SSSI_REQUIRE(nsrc >= 0 && nsrc <= kMaxPointSources, SSSI_ERR_ARG, "nsrc must be in 0..%d", kMaxPointSources);
         SSSI_REQUIRE(nsrc == 0 || (src_iz && src_ix && wavelets), SSSI_ERR_ARG, "point-source arrays are NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
+        if (mode == SSSI_MODE_FP64_STRICT)
             fwd2d_point<Cpml2d<double, double>>(v, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, nsrc, src_iz, src_ix,
                                                 wavelets, data, snapshot, mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
@@ -590,7 +580,7 @@ extern "C" int sssi_rvsTimeCpmlFor2dAw(const double* v, const double* data, int6
         check_common(nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, mode);
         SSSI_REQUIRE(v != nullptr, SSSI_ERR_ARG, "v is NULL");
         ensure_device();
-        if (mode == SSSI_MODE_FP64_STRICT || xmarch_engine())
+        if (mode == SSSI_MODE_FP64_STRICT)
             rvs2d_dense<Cpml2d<double, double>>(v, data, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, model, snapshot,
                                                 mode == SSSI_MODE_FP64_STRICT);
         else if (mode == SSSI_MODE_FP32)
@@ -615,7 +605,7 @@ extern "C" int sssi_rtmTimeCpmlFor2dAw(const double* v, const double* vs, int64_
         if (mode == SSSI_MODE_FP32)
             brtm2d<float>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon,
                           snap_stride, image, data_true, data_smooth);
-        else if (mode == SSSI_MODE_FP64 && !xmarch_engine())
+        else if (mode == SSSI_MODE_FP64)
             brtm2d<double>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon, 1,
                            image, data_true, data_smooth);
         else

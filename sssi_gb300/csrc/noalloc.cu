@@ -12,19 +12,33 @@
 // routine, allocates no host heap memory and throws no C++ exception.
 //
 // Costs and rules of the fixed array:
-//   - every GPU that loads this part of the library holds kScratchBytes of
-//     device memory until the process exits;
+//   - the array is reserved on a GPU when this part of the library is first
+//     loaded there, which with CUDA's default lazy module loading is the
+//     first call of this function on that GPU; from then on the GPU holds
+//     kScratchBytes of device memory until the process exits.  A caller that
+//     hands all free GPU memory to its own pool should make one call first
+//     (a zero-step call, nt = 0, is enough);
 //   - every call uses the same array, so calls whose work overlaps on the GPU
 //     (two host threads, or two streams) race and corrupt each other; callers
-//     must serialise them;
+//     must serialise them (host threads are serialised inside the call, the
+//     GPU work of calls on different streams is not);
 //   - the array keeps the previous call's contents; each call clears the parts
 //     that must start at zero (both wavefields and the CPML memory variables)
 //     and overwrites the rest;
-//   - the device address of the array is looked up once per device, on the
-//     first call made with that device current (cudaGetSymbolAddress); make
-//     that first call before any stream capture begins.
+//   - the device address of the array is looked up on every call, with the
+//     calling thread's current device (cudaGetSymbolAddress), so it stays right
+//     after a device reset;
+//   - the call blocks until its work is done (it synchronises its stream), so
+//     it must not be called while any stream of the calling thread is being
+//     captured into a CUDA graph.
+//
+// The band damping factors are computed on the host with the same formula and
+// the same libm exp as the allocating entry points, through one fixed host
+// staging array, so the strict FP64 mode is bit-identical to them.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 
@@ -35,14 +49,19 @@ namespace sssi {
 namespace {
 
 constexpr size_t kScratchBytes = size_t(SSSI_NOALLOC_SCRATCH_BYTES);
-constexpr int kMaxDevices = 64;
 
 // The working state of the entry point.  Host code must not use this name as
 // an address: it looks the device address up with cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
+// Host staging for the band damping factors: the band strip of v comes down,
+// is turned into b = exp(-d dt) (then b - 1) in place, and goes up again.  The
+// layout check bounds every band array to a fifth of the device array.
+constexpr size_t kStageDoubles = kScratchBytes / 5 / sizeof(double);
+static double g_noalloc_stage[kStageDoubles];
+
+// Held for a whole call: the staging array and the device array are shared.
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {};
 
 int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -54,20 +73,12 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
+// Device address of g_noalloc_scratch on the current device.
 cudaError_t scratch_address(unsigned char** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+    *out = static_cast<unsigned char*>(p);
     return cudaSuccess;
 }
 
@@ -170,47 +181,56 @@ Layout plan(int64_t nz, int64_t nx, int L, int nB, int bz) {
     return g;
 }
 
-// (v dt)^2 and the damping factors of the three CPML bands, computed on the
-// device from the caller's velocity (C-gateway formulas, fwd...mex.c:100-145).
-__global__ void noalloc_setup_kernel(const double* v, int nz, int nx, int nB, double dz, double dx, double dt,
-                                     double logR, double* vdt2, double* zb, double* zbm1, double* xb, double* xbm1) {
-    const int64_t n = (int64_t)nz * nx;
-    const int64_t nzb = (int64_t)nB * nx;
-    const int64_t nxb = (int64_t)nz * 2 * nB;
+// (v dt)^2 on the device from the caller's velocity, rounded as the
+// allocating entry points round it: (v*dt) * (v*dt).
+__global__ void noalloc_vdt2_kernel(const double* v, int64_t n, double dt, double* vdt2) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n + nzb + nxb; q += stride) {
-        if (q < n) {
-            const double vdt = v[q] * dt;
-            vdt2[q] = vdt * vdt;
-        } else if (q < n + nzb) {
-            const int64_t k = q - n;
-            const int r = (int)(k % nB);
-            const int64_t j = k / nB;
-            const double L = nB * dz, u = (r + 1) * dz;
-            const double d0 = -(3.0 * v[(nz - nB + r) + j * nz]) / (2 * L) * logR;
-            const double d = d0 * (u / L) * (u / L);
-            const double e = exp(-d * dt);
-            zb[k] = e;
-            zbm1[k] = e - 1;
-        } else {
-            const int64_t k = q - n - nzb;
-            const int64_t i = k % nz;
-            const int c = (int)(k / nz);
-            const int64_t j = c < nB ? c : nx - nB + (c - nB);
-            const double L = nB * dx, u = c < nB ? (nB - c) * dx : (c - nB + 1) * dx;
-            const double d0 = -(3.0 * v[i + j * nz]) / (2 * L) * logR;
-            const double d = d0 * (u / L) * (u / L);
-            const double e = exp(-d * dt);
-            xb[k] = e;
-            xbm1[k] = e - 1;
-        }
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
+        const double vdt = __dmul_rn(v[q], dt);
+        vdt2[q] = __dmul_rn(vdt, vdt);
     }
+}
+
+// Damping factors of one band, C-gateway formulas (fwdTimeCpmlFor2dAw_mex.c:100-145)
+// through damp_c_order and the host's exp, exactly as damping_bands_2d_strips
+// computes them: the band strip of v (rows x cols, pitch ld doubles, at vsrc)
+// comes down into the staging array, b = exp(-d dt) goes up to b_out, then
+// b - 1 to bm1_out.  u_of(r, c) is the distance into the band, L its width.
+template <class U>
+cudaError_t band_factors(const double* vsrc, int64_t ld, int64_t rows, int64_t cols, U u_of, double L, double dt,
+                         double* b_out, double* bm1_out, cudaStream_t s) {
+    const int64_t n = rows * cols;
+    if (n == 0) return cudaSuccess;
+    if ((size_t)n > kStageDoubles) return cudaErrorInvalidValue;
+    double* h = g_noalloc_stage;
+    cudaError_t e = cudaMemcpy2DAsync(h, sizeof(double) * rows, vsrc, sizeof(double) * ld, sizeof(double) * rows,
+                                      cols, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    for (int64_t c = 0; c < cols; ++c)
+        for (int64_t r = 0; r < rows; ++r) {
+            const double d = damp_c_order(u_of(r, c), h[r + c * rows], L);
+            h[r + c * rows] = std::exp(-d * dt);
+        }
+    e = cudaMemcpyAsync(b_out, h, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    for (int64_t q = 0; q < n; ++q) h[q] = h[q] - 1;
+    e = cudaMemcpyAsync(bm1_out, h, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
 }
 
 int run(const double* v, const double* source, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
         double dx, double dt, double* data, double* snapshot, int mode) {
     if (!(nz > 0 && nx > 0 && nt >= 0)) return fail(SSSI_ERR_ARG, "bad sizes nz=%lld nx=%lld nt=%lld", (long long)nz,
                                                      (long long)nx, (long long)nt);
+    // bounds before any size arithmetic: the layout sums and the per-step
+    // offsets t * nz * nx must not wrap
+    if (nz >= (int64_t(1) << 30) || nx >= (int64_t(1) << 30) || nt >= (int64_t(1) << 31) ||
+        nz * nx > INT64_MAX / std::max<int64_t>(nt, 1))
+        return fail(SSSI_ERR_ARG, "sizes out of range: nz=%lld nx=%lld nt=%lld (nz, nx < 2^30, nt < 2^31)",
+                    (long long)nz, (long long)nx, (long long)nt);
     if (N < 1 || N > kMaxOrder) return fail(SSSI_ERR_ARG, "nDiffOrder must be in 1..%d (got %d)", kMaxOrder, N);
     if (nB < 0 || nB > nz || 2 * (int64_t)nB > nx)
         return fail(SSSI_ERR_ARG, "nBoundary %d does not fit the model (%lld x %lld)", nB, (long long)nz,
@@ -238,6 +258,7 @@ int run(const double* v, const double* source, int64_t nz, int64_t nx, int64_t n
                     "entry point has a fixed %zu bytes (use sssi_fwdTimeCpmlFor2dAw for larger grids)",
                     (long long)nz, (long long)nx, N, g.total, kScratchBytes);
 
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
     unsigned char* base = nullptr;
     cudaError_t e = scratch_address(&base);
     if (e != cudaSuccess) return fail(SSSI_ERR_CUDA, "cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
@@ -252,11 +273,22 @@ int run(const double* v, const double* source, int64_t nz, int64_t nx, int64_t n
         if (e != cudaSuccess) return fail(SSSI_ERR_CUDA, "cudaMemsetAsync failed: %s", cudaGetErrorString(e));
     }
     auto at = [&](size_t off) { return reinterpret_cast<double*>(base + off); };
-    noalloc_setup_kernel<<<152 * 4, 256, 0, s>>>(v, (int)nz, (int)nx, nB, dz, dx, dt, std::log(1e-6), at(g.vdt2),
-                                                  at(g.zb), at(g.zbm1), at(g.xb), at(g.xbm1));
+    noalloc_vdt2_kernel<<<152 * 4, 256, 0, s>>>(v, nz * nx, dt, at(g.vdt2));
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(SSSI_ERR_CUDA, "set-up kernel launch failed: %s", cudaGetErrorString(e));
+    // bottom band: rows nz-nB .. nz-1, u = (r+1) dz; side bands: columns 0 .. nB-1
+    // (u = (nB-c) dx) and nx-nB .. nx-1 (u = (c+1) dx), each nz rows
+    const double Lz = nB * dz, Lx = nB * dx;
+    e = band_factors(v + (nz - nB), nz, nB, nx, [&](int64_t r, int64_t) { return (r + 1) * dz; }, Lz, dt,
+                     at(g.zb), at(g.zbm1), s);
+    if (e == cudaSuccess)
+        e = band_factors(v, nz, nz, nB, [&](int64_t, int64_t c) { return (nB - c) * dx; }, Lx, dt, at(g.xb),
+                         at(g.xbm1), s);
+    if (e == cudaSuccess)
+        e = band_factors(v + (nx - nB) * nz, nz, nz, nB, [&](int64_t, int64_t c) { return (c + 1) * dx; }, Lx, dt,
+                         at(g.xb) + nz * nB, at(g.xbm1) + nz * nB, s);
+    if (e != cudaSuccess) return fail(SSSI_ERR_CUDA, "damping set-up failed: %s", cudaGetErrorString(e));
 
     double c[kMaxOrder];
     coefficients_on_stack(N, c);

@@ -19,9 +19,9 @@
 
 static int sssi_mex_mode(void) {
     const char *m = getenv("SSSI_MEX_MODE");
-    if (m && !strcmp(m, "fp64")) return SSSI_MODE_FP64;
+    if (m && !strcmp(m, "strict")) return SSSI_MODE_FP64_STRICT;
     if (m && !strcmp(m, "fp32")) return SSSI_MODE_FP32;
-    return SSSI_MODE_FP64_STRICT;
+    return SSSI_MODE_FP64;
 }
 
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {

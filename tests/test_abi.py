@@ -123,3 +123,13 @@ def test_mex_gateway_3d_error_message():
     gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeCpmlFor3dAw_mex.so")
     with pytest.raises(O.MexError, match="All 8 input arguments shall be provided!"):
         O.shim_call(gw, 2, np.ones((3, 3, 3)), np.zeros((3, 3, 3, 2)), 2, 1, 10.0, 10.0, 10.0)
+
+
+def test_no_alloc_rejects_sizes_out_of_range(lib):
+    """The no-allocation entry point bounds nz, nx and nt before any size
+    arithmetic (a huge nx must not wrap into a small layout), without a GPU."""
+    big = (1 << 61) + 1000
+    for nz, nx, nt in ((40, big, 3), (big, 40, 3), (40, 40, 1 << 40), (1 << 29, 1 << 29, 1 << 20)):
+        rc = lib.sssi_fwdTimeCpmlFor2dAwNoAlloc(None, None, nz, nx, nt, 4, 5, 10.0, 10.0, 1e-3, None, None, 1)
+        assert rc == 1, (nz, nx, nt)
+        assert b"out of range" in lib.sssi_last_error()

@@ -175,3 +175,81 @@ def test_errors_on_gpu(gpu):
         S.fwdTimeCpmlFor2dAw(v, np.zeros((20, 30, 4)), 4, 16, 10.0, 10.0, 1e-3)
     with pytest.raises(ValueError):
         S.fwdTimeCpmlFor2dAw(v, np.zeros((21, 30, 4)), 4, 3, 10.0, 10.0, 1e-3)
+
+
+def _gateway(oracle_mod, name):
+    import subprocess
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    subprocess.run(["make", "-s", "-C", str(root / "oracle"), "mexgw"], check=True)
+    return oracle_mod.load_shim_library(root / "oracle" / "_build" / f"mexgw_{name}.so")
+
+
+@pytest.mark.parametrize("k", [0, 4, 9, 14])
+def test_mex_gateways_2d_golden(gpu, golden, oracle_mod, monkeypatch, k):
+    """The 2D MEX gateways (built on the test shim) driven with data, as MATLAB
+    calls them: [data, snapshot] = fwdTimeCpmlFor2dAw_mex(v, source, N, nB, dz, dx, dt)
+    and [model, snapshot] = rvsTimeCpmlFor2dAw_mex(v, data, N, nB, dz, dx, dt).
+    Default mode (fused FP64) within 1e-12 of the reference's golden outputs;
+    SSSI_MEX_MODE=strict bit-identical to them."""
+    fwd = _gateway(oracle_mod, "fwdTimeCpmlFor2dAw_mex")
+    rvs = _gateway(oracle_mod, "rvsTimeCpmlFor2dAw_mex")
+    g = golden("fwd2d_rvs2d.npz")
+    nz, nx, nt, N, nB, v, src = _case(g, k)
+    L = 2 * N - 1
+    for mode in (None, "strict"):
+        if mode:
+            monkeypatch.setenv("SSSI_MEX_MODE", mode)
+        else:
+            monkeypatch.delenv("SSSI_MEX_MODE", raising=False)
+        data, snap = oracle_mod.shim_call(fwd, 2, v, src, N, nB, 10.0, 10.0, 1e-3)
+        assert data.shape == (nx, nt) and snap.shape == (nz, nx, nt)
+        model, rsnap = oracle_mod.shim_call(rvs, 2, v, g[f"c{k}_data"], N, nB, 10.0, 10.0, 1e-3)
+        assert model.shape == (nz + 2 * L, nx + 2 * L) and rsnap.shape == (nz, nx, nt)
+        pairs = [(data, g[f"c{k}_data"]), (snap[:, :, nt // 2], g[f"c{k}_snap_mid"]),
+                 (snap[:, :, -1], g[f"c{k}_snap_last"]), (model, g[f"c{k}_model"]),
+                 (rsnap[:, :, 0], g[f"c{k}_rsnap_first"]), (rsnap[:, :, nt // 2], g[f"c{k}_rsnap_mid"])]
+        for got, ref in pairs:
+            if mode == "strict":
+                assert np.array_equal(got, ref)
+            else:
+                assert oracle_mod.rel_l2(got, ref) <= TOL_FP64
+
+
+def test_mex_gateway_fp32_mode(gpu, golden, oracle_mod, monkeypatch):
+    """SSSI_MEX_MODE=fp32: the same gateway call in the FP32 form, within 1e-4."""
+    fwd = _gateway(oracle_mod, "fwdTimeCpmlFor2dAw_mex")
+    g = golden("fwd2d_rvs2d.npz")
+    nz, nx, nt, N, nB, v, src = _case(g, 3)
+    monkeypatch.setenv("SSSI_MEX_MODE", "fp32")
+    data, _ = oracle_mod.shim_call(fwd, 1, v, src, N, nB, 10.0, 10.0, 1e-3)
+    assert oracle_mod.rel_l2(data, g["c3_data"]) <= TOL_FP32
+
+
+@pytest.mark.slow
+def test_c1_full_size(gpu, co):
+    """The plain forward-modelling workload at its full size (220 x 340 padded,
+    nt = 2000, dt = 1 ms, N = 4, nB = 20, dense source with a 20 Hz Ricker at
+    physical (2, 150)): strict FP64 bit-identical to the oracle on the data and
+    on every snapshot, fused FP64 within 1e-12."""
+    from bench import c1_model, ricker
+
+    S = gpu
+    v = c1_model()
+    nz, nx = v.shape
+    nt, dt = 2000, 1e-3
+    src = np.zeros((nz, nx, nt), order="F")
+    src[2, 170, :] = ricker(20.0, nt, dt)
+    d_ref, s_ref = co.fwd2d(v, src, 4, 20, 10.0, 10.0, dt)
+    d, s = S.fwdTimeCpmlFor2dAw(v, src, 4, 20, 10.0, 10.0, dt, mode="fp64-strict")
+    assert np.array_equal(d, d_ref)
+    assert np.array_equal(s, s_ref)
+    del s
+    d64, s64 = S.fwdTimeCpmlFor2dAw(v, src, 4, 20, 10.0, 10.0, dt, mode="fp64")
+    assert oracle_rel(d64, d_ref) <= TOL_FP64
+    assert oracle_rel(s64, s_ref) <= TOL_FP64
+
+
+def oracle_rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))

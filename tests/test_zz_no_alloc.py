@@ -4,8 +4,10 @@ whose GPU memory belongs to its own pool, a loop that cannot afford the
 synchronisation of cudaMalloc/cudaFree).  It keeps its working state in a
 fixed array inside the library; these tests check, through the C ABI, that two
 calls in a row give the same result as the allocating entry point
-sssi_fwdTimeCpmlFor2dAw, and that grids too large for the array and host
-pointers are refused.  The file name makes pytest collect it last."""
+sssi_fwdTimeCpmlFor2dAw (bit for bit in the strict FP64 mode, which also
+reproduces the golden vectors of the reference C), and that grids too large
+for the array and host pointers are refused.  The file name makes pytest
+collect it last."""
 import ctypes
 
 import numpy as np
@@ -62,9 +64,35 @@ def test_no_alloc_matches_allocating_entry_point(gpu, mode, shape):
                                               mode)
         assert rc == 0, L.sssi_last_error()
         torch.cuda.synchronize()
+        if mode == 0:  # strict FP64: the same bits as the allocating entry point
+            assert torch.equal(d, d_ref) and torch.equal(s, s_ref), call
         assert _rel(d, d_ref) <= TOL_FP64, call
         assert _rel(s, s_ref) <= TOL_FP64, call
         assert float(d.abs().max()) > 0
+
+
+@pytest.mark.parametrize("k", [0, 7, 14])
+def test_no_alloc_strict_reproduces_golden(gpu, golden, k):
+    """Strict FP64 through the fixed array reproduces the reference C's outputs."""
+    import torch
+
+    from sssi_gb300._native import lib
+    from tests.golden.make_golden import dense_source
+
+    L = lib()
+    g = golden("fwd2d_rvs2d.npz")
+    nz, nx, nt, N, nB = (int(x) for x in g[f"c{k}_params"])
+    v = _dev(g[f"c{k}_v"])
+    src = _dev(dense_source(nz, nx, nt, g[f"c{k}_trace"], g[f"c{k}_imp"], g[f"c{k}_amp"]))
+    for call in range(2):
+        d, s = _zeros((nx, nt)), _zeros((nz, nx, nt))
+        rc = L.sssi_fwdTimeCpmlFor2dAwNoAlloc(v.data_ptr(), src.data_ptr(), nz, nx, nt, N, nB, 10.0, 10.0, 1e-3,
+                                              d.data_ptr(), s.data_ptr(), 0)
+        assert rc == 0, L.sssi_last_error()
+        torch.cuda.synchronize()
+        assert np.array_equal(d.cpu().numpy(), g[f"c{k}_data"]), call
+        assert np.array_equal(s[:, :, nt // 2].cpu().numpy(), g[f"c{k}_snap_mid"]), call
+        assert np.array_equal(s[:, :, -1].cpu().numpy(), g[f"c{k}_snap_last"]), call
 
 
 def test_no_alloc_refuses_oversize_grid(gpu):
