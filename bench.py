@@ -112,9 +112,10 @@ def cell_updates(nz, nx, nt):
 # python bench.py --case rtm-short`
 FWD_STEP_DRAM_BYTES = 22_306_816
 # the same for one FP64 forward step of the RTM shot (fused FP64), from
-# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:batch2d -s 40 -c 1
-# python bench.py --case rtm-short-fp64`; None until captured
-FWD64_STEP_DRAM_BYTES = None
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+# --clock-control none -k regex:batch2d -s 40 -c 2 python bench.py --case rtm-short-fp64`
+# (42,652,672 B read, 10,240 B written: the step's writes stay in L2)
+FWD64_STEP_DRAM_BYTES = 42_662_912
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
 STEP3D_DRAM_BYTES = 454_952_448 + 170_105_600

@@ -187,134 +187,79 @@ void rvs2d_dense(const double* v, const double* data, int64_t nz, int64_t nx, in
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
-// ---------------------------------------------------------------- RTM shot
-template <class Prop>
-void rtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx,
-           double dt, const double* wavelet, int64_t src_iz, int64_t src_ix, double eps, int mode, int stride,
-           double* image, double* data_true, double* data_smooth) {
-    using T = typename Prop::value_type;
+// ---------------------------------------------------------------- RTM shot, strict FP64
+// The reference's operation order throughout: the row-marching kernel for the
+// three propagations, every reverse snapshot kept, and the imaging sums taken
+// in ascending time (mainRtmTimeCpmlFor2dAw.m:268-275), so the image is
+// bit-identical to the reference's.
+void rtm2d_strict(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz,
+                  double dx, double dt, const double* wavelet, int64_t src_iz, int64_t src_ix, double eps,
+                  double* image, double* data_true, double* data_smooth) {
+    using Prop = Cpml2d<double, double>;
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    const bool strict = mode == SSSI_MODE_FP64_STRICT;
-    const bool f16 = mode == SSSI_MODE_FP32;
-    if (!f16) stride = 1;
-    SSSI_REQUIRE(stride >= 1, SSSI_ERR_ARG, "snap_stride must be >= 1");
-    constexpr bool kDouble = std::is_same<T, double>::value;
-    SSSI_REQUIRE(f16 || kDouble, SSSI_ERR_INTERNAL, "FP64 RTM needs an FP64 propagator");
     std::vector<double> vh = host_copy(v, (size_t)n, s);
     std::vector<double> vsh = host_copy(vs, (size_t)n, s);
-    Prop A(vh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
-    Prop B(vsh.data(), nz, nx, N, nB, dz, dx, dt, strict, s);
+    Prop A(vh.data(), nz, nx, N, nB, dz, dx, dt, true, s);
+    Prop B(vsh.data(), nz, nx, N, nB, dz, dx, dt, true, s);
     int bz, w;
     pick_launch(nz, nx, bz, w);
     A.set_launch(bz, w);
     B.set_launch(bz, w);
-    Staged<T> wav(wavelet, (size_t)nt, true, s);
+    Staged<double> wav(wavelet, (size_t)nt, true, s);
     A.set_point_sources(1, &src_iz, &src_ix, wav.ptr, (int)nt);
     B.set_point_sources(1, &src_iz, &src_ix, wav.ptr, (int)nt);
     const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
-    Staged<T> dtrue(data_true, ndata, false, s), dsmooth(data_smooth, ndata, false, s);
+    Staged<double> dtrue(data_true, ndata, false, s), dsmooth(data_smooth, ndata, false, s);
     DeviceBuffer dtrue_own, dsmooth_own, delta;
-    T* d_true = dtrue.ptr;
-    T* d_smooth = dsmooth.ptr;
+    double* d_true = dtrue.ptr;
+    double* d_smooth = dsmooth.ptr;
     if (!d_true) {
-        dtrue_own.allocate(sizeof(T) * ndata);
-        d_true = dtrue_own.as<T>();
+        dtrue_own.allocate(sizeof(double) * ndata);
+        d_true = dtrue_own.as<double>();
     }
     if (!d_smooth) {
-        dsmooth_own.allocate(sizeof(T) * ndata);
-        d_smooth = dsmooth_own.as<T>();
+        dsmooth_own.allocate(sizeof(double) * ndata);
+        d_smooth = dsmooth_own.as<double>();
     }
-    delta.allocate(sizeof(T) * ndata);
-
-    const int64_t nsnap = f16 ? (nt + stride - 1) / stride : nt;
-    DeviceBuffer fsnap, rsnap, amax, inv, M, S2;
-    if (f16) {
-        fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
-        amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
-        amax.zero(s);
-        inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
-    } else {
-        fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
-        if (strict) rsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
-    }
-    if (!strict) {
-        M.allocate(sizeof(double) * n);  // FP64 sums, or compensated FP32 (hi, lo) pairs of the same size
-        S2.allocate(sizeof(double) * n);
-        M.zero(s);
-        if (f16)
-            S2.zero(s);
-        else
-            fill(S2.as<double>(), n, eps, s);
-    }
+    delta.allocate(sizeof(double) * ndata);
+    DeviceBuffer fsnap, rsnap;
+    fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
+    rsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
 
     // forward modelling in the true and the migration model
     timing_begin(s);
     for (int64_t t = 0; t < nt; ++t) {
-        StepIO<T> io;
+        StepIO<double> io;
         io.t = (int)t;
         io.rec = d_true + t * nx;
         A.step(io);
-        StepIO<T> jo;
+        StepIO<double> jo;
         jo.t = (int)t;
         jo.rec = d_smooth + t * nx;
-        if (!f16) {
-            jo.snap = reinterpret_cast<T*>(fsnap.as<double>()) + t * n;
-        } else {
-            if (t % stride == 0) jo.amax = amax.as<unsigned>() + t / stride;
-            if (t >= 1 && (t - 1) % stride == 0) {
-                const int64_t k = (t - 1) / stride;
-                jo.pack = fsnap.as<__half>() + k * n;
-                jo.pack_amax = amax.as<unsigned>() + k;
-                jo.pack_inv_scale_out = inv.as<float>() + k;
-            }
-        }
+        jo.snap = fsnap.as<double>() + t * n;
         B.step(jo);
     }
-    if (f16 && nt >= 1 && (nt - 1) % stride == 0) {
-        const int64_t k = (nt - 1) / stride;
-        launch_pack_f16(reinterpret_cast<const float*>(B.current()), B.ldp(), (int)nz, (int)nx,
-                        amax.as<unsigned>() + k, fsnap.as<__half>() + k * n, inv.as<float>() + k, s);
-    }
     // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse time
-    diff_kernel<T><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<T>(), nx * nt);
+    diff_kernel<double><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<double>(), nx * nt);
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_mark(s);
 
-    // reverse propagation in the true model, imaging
+    // reverse propagation in the true model, every snapshot kept
     A.reset();
     A.set_point_sources(0, nullptr, nullptr, nullptr, (int)nt);
     for (int64_t t = nt - 1; t >= 0; --t) {
-        StepIO<T> io;
+        StepIO<double> io;
         io.t = (int)t;
-        io.src_row = delta.as<T>() + t * nx;
-        if (strict) {
-            io.snap = reinterpret_cast<T*>(rsnap.as<double>()) + t * n;
-        } else if (!f16) {
-            io.img_f64 = fsnap.as<double>() + t * n;
-            io.img_m = M.as<double>();
-            io.img_s2 = S2.as<double>();
-        } else if (t % stride == 0) {
-            io.img_f16 = fsnap.as<__half>() + (t / stride) * n;
-            io.img_inv_scale = inv.as<float>() + t / stride;
-            io.img_m2 = M.as<float2>();
-            io.img_s22 = S2.as<float2>();
-        }
+        io.src_row = delta.as<double>() + t * nx;
+        io.snap = rsnap.as<double>() + t * n;
         A.step(io);
     }
     timing_mark(s);
 
     DeviceView dimg(image, (size_t)n, false, s);
-    if (strict) {
-        image_ascending_kernel<<<152 * 4, 256, 0, s>>>(fsnap.as<double>(), rsnap.as<double>(), n, nt, eps, dimg.ptr);
-    } else {
-        if (f16)
-            image_finish_comp_kernel<<<152 * 4, 256, 0, s>>>(M.as<float2>(), S2.as<float2>(), n, (double)stride, eps,
-                                                              dimg.ptr);
-        else
-            image_finish_kernel<<<152 * 4, 256, 0, s>>>(M.as<double>(), S2.as<double>(), n, 1.0, 0.0, dimg.ptr);
-    }
+    image_ascending_kernel<<<152 * 4, 256, 0, s>>>(fsnap.as<double>(), rsnap.as<double>(), n, nt, eps, dimg.ptr);
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_end(s);
@@ -422,19 +367,29 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     if (!kF16) stride = 1;
     SSSI_REQUIRE(stride >= 1, SSSI_ERR_ARG, "snap_stride must be >= 1");
     Batch2d<T> B(N, dz, dx, s);
-    // forward in v and in vs over batch steps [0, nt); reverse in v over [nt, 2nt)
-    const int kA = B.add_shot(v, nz, nx, nB, dt, (int)nt, 0, false);
-    const int kB = B.add_shot(vs, nz, nx, nB, dt, (int)nt, 0, false);
-    const int kR = B.add_shot_like(kA, (int)nt, (int)nt, true);
+    // Forward over batch steps [0, nt), reverse in v over [nt, 2nt).  FP32: the
+    // field in vs and the residual D = (field in v) - (field in vs) advance as
+    // one residual pair, so dataTrue - dataSmooth (D's row 0) keeps FP32
+    // accuracy relative to itself even where the two fields nearly cancel.
+    // FP64: the two forward shots and their difference, as the reference.
+    int kA = -1, kB = -1, kR = -1;
+    if (kF16) {
+        kB = B.add_pair_shot(vs, v, nz, nx, nB, dt, (int)nt, 0);
+        kR = B.add_shot(v, nz, nx, nB, dt, (int)nt, (int)nt, true);
+    } else {
+        kA = B.add_shot(v, nz, nx, nB, dt, (int)nt, 0, false);
+        kB = B.add_shot(vs, nz, nx, nB, dt, (int)nt, 0, false);
+        kR = B.add_shot_like(kA, (int)nt, (int)nt, true);
+    }
     Staged<T> wav(wavelet, (size_t)nt, true, s);
-    B.set_point_sources(kA, 1, &src_iz, &src_ix, wav.ptr);
+    if (kA >= 0) B.set_point_sources(kA, 1, &src_iz, &src_ix, wav.ptr);
     B.set_point_sources(kB, 1, &src_iz, &src_ix, wav.ptr);
     const size_t ndata = (size_t)(nx * std::max<int64_t>(nt, 1));
     Staged<T> dtrue(data_true, ndata, false, s), dsmooth(data_smooth, ndata, false, s);
     DeviceBuffer dtrue_own, dsmooth_own, delta;
     T* d_true = dtrue.ptr;
     T* d_smooth = dsmooth.ptr;
-    if (!d_true) {
+    if (!d_true && !kF16) {
         dtrue_own.allocate(sizeof(T) * ndata);
         d_true = dtrue_own.as<T>();
     }
@@ -444,12 +399,12 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     }
     delta.allocate(sizeof(T) * ndata);
     const int64_t nsnap = (nt + stride - 1) / stride;
-    DeviceBuffer fsnap, amax, inv, M, S2;
+    const int64_t nblk = ((nz + 31) / 32) * ((nx + 31) / 32);  // FP16 scale blocks of 32 x 32 cells
+    DeviceBuffer fsnap, amax, M, S2;
     if (kF16) {
         fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
-        amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
+        amax.allocate(sizeof(unsigned) * nblk * std::max<int64_t>(nsnap, 1));
         amax.zero(s);
-        inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
     } else {
         fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
     }
@@ -461,15 +416,14 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     else
         fill(S2.as<double>(), n, eps, s);
 
-    ShotTail<T>& a = B.shot(kA);
-    a.rec = d_true;
+    if (kA >= 0) B.shot(kA).rec = d_true;
     ShotTail<T>& b = B.shot(kB);
     b.rec = d_smooth;
+    if (kF16) b.rec_d = delta.as<T>();
     if (kF16) {
         b.stride = stride;
         b.amax = amax.as<unsigned>();
         b.pack = fsnap.as<__half>();
-        b.inv_scale = inv.as<float>();
     } else {
         b.snap = reinterpret_cast<T*>(fsnap.as<double>());
         b.snap_t0 = 0;
@@ -479,7 +433,7 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     if (kF16) {
         r.stride = stride;
         r.img_f16 = fsnap.as<__half>();
-        r.img_inv = inv.as<float>();
+        r.img_amax = amax.as<unsigned>();
         r.img_m2 = M.as<float2>();
         r.img_s22 = S2.as<float2>();
     } else {
@@ -497,14 +451,20 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     if (kF16 && nt >= 1 && (nt - 1) % stride == 0) {
         const int64_t k = (nt - 1) / stride;
         launch_pack_f16(reinterpret_cast<const float*>(B.current_field(kB)), B.ldp(kB), (int)nz, (int)nx,
-                        amax.as<unsigned>() + k, fsnap.as<__half>() + k * n, inv.as<float>() + k, s);
+                        amax.as<unsigned>() + k * nblk, fsnap.as<__half>() + k * n, s);
     }
-    // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse time
-    diff_kernel<T><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<T>(), nx * nt);
-    count_launch();
+    // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse
+    // time: D's row 0 for the residual pair, else the difference of the two
+    if (!kF16) {
+        diff_kernel<T><<<152 * 4, 256, 0, s>>>(d_true, d_smooth, delta.as<T>(), nx * nt);
+        count_launch();
+    } else if (d_true) {
+        sum_kernel<T><<<152 * 4, 256, 0, s>>>(d_smooth, delta.as<T>(), d_true, nx * nt);
+        count_launch();
+    }
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_mark(s);
-    B.enable(kA, false);
+    if (kA >= 0) B.enable(kA, false);
     B.enable(kB, false);
     B.enable(kR, true);
     B.finalize();
@@ -609,7 +569,7 @@ extern "C" int sssi_rtmTimeCpmlFor2dAw(const double* v, const double* vs, int64_
             brtm2d<double>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon, 1,
                            image, data_true, data_smooth);
         else
-            rtm2d<Cpml2d<double, double>>(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz,
-                                          src_ix, epsilon, mode, snap_stride, image, data_true, data_smooth);
+            rtm2d_strict(v, vs, nz, nx, nt, nDiffOrder, nBoundary, dz, dx, dt, wavelet, src_iz, src_ix, epsilon,
+                         image, data_true, data_smooth);
     });
 }

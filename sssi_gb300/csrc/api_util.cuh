@@ -209,5 +209,12 @@ __global__ void diff_kernel(const T* a, const T* b, T* out, int64_t n) {
         out[q] = a[q] - b[q];
 }
 
+// out = a + b in T
+template <typename T>
+__global__ void sum_kernel(const T* a, const T* b, T* out, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = a[q] + b[q];
+}
+
 }  // namespace api
 }  // namespace sssi

@@ -47,21 +47,35 @@ struct alignas(16) ShotTail {
     T* snap;               // slices of nz x nx for tau = snap_t0, ...
     int dense_t0;
     int snap_t0;
-    // RTM, forward shot: at tau % stride == 0 the max |field| goes to amax[tau/stride];
-    // at (tau-1) % stride == 0 the current field (the result of step tau-1) is
-    // stored in FP16 at pack + ((tau-1)/stride) * nz*nx, its 1/scale in inv_scale.
+    // RTM, forward shot: the field is stored in FP16 every `stride` steps with
+    // one power-of-two scale per 32 x 32 block of cells (block (bz, bx) =
+    // rows 32 bz .. 32 bz + 31, columns 32 bx .. 32 bx + 31; index bz + bx * nbz,
+    // nbz = ceil(nz / 32), nblk blocks): at tau % stride == 0 each block's max
+    // |field| goes to amax[(tau/stride) * nblk + block]; at (tau-1) % stride == 0
+    // the current field (the result of step tau-1) is stored at
+    // pack + ((tau-1)/stride) * nz*nx, scaled by its block's scale.
     int stride;
     unsigned* amax;
     __half* pack;
-    float* inv_scale;
-    // RTM, reverse shot: at tau % stride == 0 image against the stored forward field
-    const __half* img_f16;  // stored forward fields (as written by pack)
-    const float* img_inv;   // their 1/scale
+    // RTM, reverse shot: at tau % stride == 0 image against the stored forward
+    // field, unscaled with the block maxima the forward shot recorded
+    const __half* img_f16;     // stored forward fields (as written by pack)
+    const unsigned* img_amax;  // their block maxima
     float2* img_m2;         // compensated FP32 sums
     float2* img_s22;
     const double* img_f64;  // FP64: forward field of every step, nz x nx x nt
     double* img_m;
     double* img_s2;
+    // Residual pair (sched & kSchedPair, FP32 only): the shot advances two
+    // fields in one tile, the field P of the model it was added with (the
+    // migration model of an RTM shot) and the residual D = Q - P, where Q is
+    // the field of a second model (the true model).  D is stored dcol columns
+    // to the right of P in the same buffers ((v dt)^2 holds P's and, dcol
+    // columns on, the difference Q's minus P's); its band coefficients follow
+    // P's (b, b-1 of the second model, then b_Q - b_P) and its memory variables
+    // follow P's, zoff / xoff entries on.  rec_d receives D's row 0.
+    T* rec_d;
+    int dcol;
 };
 
 // Per-tile work flags.  kBandZ, kBandX and point sources inside the tile do
@@ -82,9 +96,11 @@ __host__ __device__ inline unsigned tile_band_flags(int N, int TZ, int TX, int n
     return f;
 }
 
-// ShotTail::sched: bit 0 reverse, bits 1-7 the hooks that are set, stride above.
+// ShotTail::sched: bit 0 reverse, bits 1-7 the hooks that are set, bit 8 a
+// residual pair, the stride from bit 9 on.
 constexpr unsigned kSchedReverse = 1u, kSchedDense = 2u, kSchedRow = 4u, kSchedSnap = 8u, kSchedImg64 = 16u,
-                   kSchedAmax = 32u, kSchedPack = 64u, kSchedImg16 = 128u;
+                   kSchedAmax = 32u, kSchedPack = 64u, kSchedImg16 = 128u, kSchedPair = 256u;
+constexpr int kSchedStrideShift = 9;
 template <typename T>
 inline unsigned sched_word(const ShotTail<T>& d) {
     unsigned w = d.reverse ? kSchedReverse : 0u;
@@ -95,7 +111,8 @@ inline unsigned sched_word(const ShotTail<T>& d) {
     if (d.amax) w |= kSchedAmax;
     if (d.pack) w |= kSchedPack;
     if (d.img_f16) w |= kSchedImg16;
-    return w | ((unsigned)(d.stride > 0 ? d.stride : 1) << 8);
+    if (d.dcol > 0) w |= kSchedPair;
+    return w | ((unsigned)(d.stride > 0 ? d.stride : 1) << kSchedStrideShift);
 }
 
 // A work item: shot k (< 2^24) with the tile's step-independent flags in the
@@ -152,6 +169,13 @@ class Batch2d {
     // Adds a shot on the model of shot k (same grid, bands and dt) with its own
     // state, length and start: the reverse propagation of an RTM shot.
     int add_shot_like(int k, int nt, int t_start, bool reverse);
+    // Adds a residual pair (FP32 only): the field P in model vp and the
+    // residual D = Q - P of the field Q in model vq (same grid), advanced
+    // together so that D keeps FP32 accuracy relative to itself (an RTM
+    // shot's dataTrue - dataSmooth is D's row 0).  P's outputs are set on
+    // shot(k) as for any shot; D's row 0 goes to shot(k).rec_d.
+    int add_pair_shot(const double* vp, const double* vq, int64_t nz, int64_t nx, int nB, double dt, int nt,
+                      int t_start);
     ShotTail<T>& shot(int k) { return shots_[k].desc.s; }
     void set_point_sources(int k, int nsrc, const int64_t* iz, const int64_t* ix, const T* d_wavelet);
     void enable(int k, bool on) {
@@ -204,7 +228,8 @@ class Batch2d {
     cudaStream_t up() const { return upload_ ? upload_ : stream_; }
     int take_slot();
     int add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,
-                    int t_start, bool reverse);
+                    int t_start, bool reverse, const double* vq = nullptr);
+    int pairs_enabled() const;
     BatchConst<T> bc_{};
     std::vector<Shot> shots_;
     void launch_step(const int* base, int offset, cudaStream_t stream);
@@ -214,15 +239,17 @@ class Batch2d {
     struct GraphKey {
         int grid = 0;
         bool split = false;
+        bool pair = false;
         int shape = 0;
         const void *desc = nullptr, *begin = nullptr, *work = nullptr;
         bool operator==(const GraphKey& o) const {
-            return grid == o.grid && split == o.split && shape == o.shape && desc == o.desc && begin == o.begin &&
-                   work == o.work;
+            return grid == o.grid && split == o.split && pair == o.pair && shape == o.shape && desc == o.desc &&
+                   begin == o.begin && work == o.work;
         }
     } graph_key_;
     GraphKey current_key() const {
-        return GraphKey{grid_, split_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(), d_work_[shape_].get()};
+        return GraphKey{grid_, split_, pair_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(),
+                        d_work_[shape_].get()};
     }
     // tile shape: the schedule in use (BatchShape index) and the tuner (times a
     // few steps with each shape when a large schedule is built, keeps the faster)
@@ -235,26 +262,29 @@ class Batch2d {
     void schedule(int shape);  // work lists of the enabled shots for a tile shape
     void use_shape(int shape);
     bool split_ = false;  // the schedule holds half tiles
+    bool pair_ = false;   // enabled residual pairs: the launch uses the pair variant (32 x 32 tiles)
+    int shape_free_ = 0;  // the tile shape to return to when the last pair leaves
     DeviceBuffer d_desc_, d_ctr_;                // d_ctr_: graph step base, zero, error flag
     DeviceBuffer d_cta_begin_[2], d_work_[2];    // the schedule of each tile shape
     int grid_s_[2] = {0, 0}, ntiles_s_[2] = {0, 0};
     bool split_s_[2] = {false, false};
     int grid_ = 0, ntiles_ = 0, step_ = 0;
-    int ctas_per_sm_[2] = {1, 1}, sms_ = 1;
+    int ctas_per_sm_[2] = {1, 1}, ctas_per_sm_pair_ = 1, sms_ = 1;
     cudaGraphExec_t graph_ = nullptr;
 };
 
 // Launches one batch step with the programmatic-serialization attribute.
-// split: the work lists hold half tiles; shape: BatchShape index.
+// split: the work lists hold half tiles; shape: BatchShape index; pair: the
+// batch holds residual pairs (FP32, shape 1, no half tiles).
 template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape, bool pair,
                       cudaStream_t stream);
 template <typename T, int N>
-int batch2d_occupancy_n(int shape);
+int batch2d_occupancy_n(int shape, bool pair);
 template <typename T>
 void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
-                    cudaStream_t stream);
+                    bool pair, cudaStream_t stream);
 template <typename T>
-int batch2d_ctas_per_sm(int N, int shape);
+int batch2d_ctas_per_sm(int N, int shape, bool pair);
 
 }  // namespace sssi

@@ -83,7 +83,8 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
     int dev = 0;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
     SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
-    for (int v = 0; v < kBatchShapes<T>; ++v) ctas_per_sm_[v] = batch2d_ctas_per_sm<T>(N, v);
+    for (int v = 0; v < kBatchShapes<T>; ++v) ctas_per_sm_[v] = batch2d_ctas_per_sm<T>(N, v, false);
+    if (kBatchShapes<T> > 1) ctas_per_sm_pair_ = batch2d_ctas_per_sm<T>(N, 1, true);
 }
 
 template <typename T>
@@ -123,6 +124,35 @@ int Batch2d<T>::add_shot_like(int k, int nt, int t_start, bool reverse) {
 }
 
 template <typename T>
+int Batch2d<T>::add_pair_shot(const double* vp, const double* vq, int64_t nz, int64_t nx, int nB, double dt, int nt,
+                              int t_start) {
+    SSSI_REQUIRE((std::is_same<T, float>::value), SSSI_ERR_INTERNAL, "residual pairs are FP32 only");
+    SSSI_REQUIRE(vp && vq, SSSI_ERR_ARG, "a residual pair needs both models");
+    SSSI_REQUIRE(nz >= 1 && nx >= 1, SSSI_ERR_ARG, "empty model (%lld x %lld)", (long long)nz, (long long)nx);
+    SSSI_REQUIRE(nB >= 0 && nB <= nz && 2 * (int64_t)nB <= nx, SSSI_ERR_ARG,
+                 "nBoundary %d does not fit the model (%lld x %lld): need nBoundary <= nz and 2*nBoundary <= nx", nB,
+                 (long long)nz, (long long)nx);
+    SSSI_REQUIRE(nz <= 65535LL * 32 && nx <= 65535LL * 16, SSSI_ERR_ARG,
+                 "model too large for a residual pair (%lld x %lld)", (long long)nz, (long long)nx);
+    SSSI_REQUIRE(dt > 0 && nt >= 0, SSSI_ERR_ARG, "dt must be positive and nt >= 0");
+    const int slot = take_slot();
+    stale_ = true;
+    try {
+        return add_shot_in(slot, vp, -1, nz, nx, nB, dt, nt, t_start, false, vq);
+    } catch (...) {
+        remove_shot(slot);
+        throw;
+    }
+}
+
+template <typename T>
+int Batch2d<T>::pairs_enabled() const {
+    int n = 0;
+    for (const Shot& S : shots_) n += (!S.free && S.enabled && S.desc.s.dcol > 0) ? 1 : 0;
+    return n;
+}
+
+template <typename T>
 int Batch2d<T>::take_slot() {
     for (int q = 0; q < (int)shots_.size(); ++q)
         if (shots_[q].free) {
@@ -134,13 +164,30 @@ int Batch2d<T>::take_slot() {
     return (int)shots_.size() - 1;
 }
 
+namespace {
+
+// (vq dt)^2 - (vp dt)^2 in FP64, rounded once to T: the residual's source
+// weight, exact to the last bit of T even where the two models nearly agree.
+template <typename T>
+__global__ void vdt2_diff_kernel(const double* vp, const double* vq, int64_t nz, int64_t nx, double dt, T* out,
+                                 int64_t ldz) {
+    const int64_t n = nz * nx;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double a = vq[q] * dt, b = vp[q] * dt;
+        out[(q % nz) + (q / nz) * ldz] = static_cast<T>(a * a - b * b);
+    }
+}
+
+}  // namespace
+
 template <typename T>
 int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,
-                            int t_start, bool reverse) {
+                            int t_start, bool reverse, const double* vq) {
     using Sh = TileShape<T>;
     shots_[slot] = Shot{};
     Shot& S = shots_[slot];
     ShotTail<T>& d = S.desc.s;
+    const bool pair = vq != nullptr;
     const int HZ = tile_halo_rows(N_);
     constexpr int al = Scalar<T>::kAlign;
     const int64_t oz = (std::max(L_, HZ) + al - 1) / al * al;
@@ -148,7 +195,13 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
     const int64_t ldp = (oz + nz_alloc + HZ + al - 1) / al * al;
     S.origin = oz + (int64_t)L_ * ldp;
     const int64_t cols = nx + 2 * L_;
-    const size_t pbytes = sizeof(T) * (size_t)ldp * (size_t)cols;
+    // a residual pair keeps D in the same buffers, dcol columns to the right of
+    // P, past 8 zero columns: a tile box of D that starts left of D's padded
+    // grid (shifted tile columns start up to 8 columns early) reads zeros
+    const int64_t dcol = pair ? cols + 8 : 0;
+    const int64_t cols_all = pair ? dcol + cols : cols;
+    const size_t pbytes = sizeof(T) * (size_t)ldp * (size_t)cols_all;
+    const int64_t nzb = (int64_t)nB * nx, nxb = nz * 2 * (int64_t)nB;  // band sizes (pair: per field)
     for (auto& b : S.P) b.allocate(pbytes);
     if (like >= 0) {
         // the same model as shot `like`: copy its (v dt)^2 and band coefficients
@@ -157,6 +210,7 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
             SSSI_CHECK_CUDA(cudaMemcpyAsync(dst.get(), src.get(), src.bytes(), cudaMemcpyDeviceToDevice, up()));
         };
         const Shot& Q = shots_[like];
+        SSSI_REQUIRE(Q.desc.s.dcol == 0, SSSI_ERR_INTERNAL, "a shot cannot copy a residual pair's model");
         copy(S.vdt2, Q.vdt2);
         copy(S.zb, Q.zb);
         copy(S.zbm1, Q.zbm1);
@@ -166,33 +220,54 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
         // (v dt)^2 on the device, from v where it lies (host models go up once
         // as doubles); the damping bands on the host, from the band strips of v
         const int64_t n = nz * nx;
-        const bool dev = is_device_pointer(v);
-        DeviceBuffer vd;
-        const double* vdev = v;
         S.vdt2.allocate(pbytes);
         S.vdt2.zero(up());
-        if (!dev) {
-            vd.allocate(sizeof(double) * n);
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(vd.get(), v, sizeof(double) * n, cudaMemcpyHostToDevice, up()));
-            vdev = vd.template as<double>();
-        }
-        launch_vdt2<T>(vdev, nz, nx, 1, dt, S.vdt2.template as<T>() + S.origin, ldp, ldp * cols, up());
-        Bands2D bands;
-        if (dev) {
+        auto on_device = [&](const double* m, DeviceBuffer& tmp) {
+            if (is_device_pointer(m)) return m;
+            tmp.allocate(sizeof(double) * n);
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(tmp.get(), m, sizeof(double) * n, cudaMemcpyHostToDevice, up()));
+            return static_cast<const double*>(tmp.template as<double>());
+        };
+        auto bands_of = [&](const double* m) {
+            if (!is_device_pointer(m)) return damping_bands_2d(m, nz, nx, nB, dz_, dx_, dt);
             std::vector<double> bottom((size_t)nB * nx), sides((size_t)nz * 2 * nB);
             if (nB > 0) {
-                SSSI_CHECK_CUDA(cudaMemcpy2DAsync(bottom.data(), sizeof(double) * nB, v + (nz - nB),
+                SSSI_CHECK_CUDA(cudaMemcpy2DAsync(bottom.data(), sizeof(double) * nB, m + (nz - nB),
                                                   sizeof(double) * nz, sizeof(double) * nB, nx,
                                                   cudaMemcpyDeviceToHost, up()));
-                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data(), v, sizeof(double) * nz * nB, cudaMemcpyDeviceToHost,
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data(), m, sizeof(double) * nz * nB, cudaMemcpyDeviceToHost,
                                                 up()));
-                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data() + nz * nB, v + (nx - nB) * nz, sizeof(double) * nz * nB,
+                SSSI_CHECK_CUDA(cudaMemcpyAsync(sides.data() + nz * nB, m + (nx - nB) * nz, sizeof(double) * nz * nB,
                                                 cudaMemcpyDeviceToHost, up()));
             }
             SSSI_CHECK_CUDA(cudaStreamSynchronize(up()));
-            bands = damping_bands_2d_strips(bottom.data(), sides.data(), nz, nx, nB, dz_, dx_, dt);
-        } else {
-            bands = damping_bands_2d(v, nz, nx, nB, dz_, dx_, dt);
+            return damping_bands_2d_strips(bottom.data(), sides.data(), nz, nx, nB, dz_, dx_, dt);
+        };
+        DeviceBuffer vd, vqd;
+        const double* vdev = on_device(v, vd);
+        launch_vdt2<T>(vdev, nz, nx, 1, dt, S.vdt2.template as<T>() + S.origin, ldp, ldp * cols_all, up());
+        Bands2D bands = bands_of(v);
+        std::vector<T> zb, zbm1, xb, xbm1;
+        band_coefficients<T>(bands.zb, bands.zbm1, zb, zbm1);
+        band_coefficients<T>(bands.xb, bands.xbm1, xb, xbm1);
+        if (pair) {
+            // D's (v dt)^2 column block holds (vq dt)^2 - (vp dt)^2; its band
+            // coefficients (b_Q, b_Q - 1, then b_Q - b_P) follow P's
+            const double* vqdev = on_device(vq, vqd);
+            vdt2_diff_kernel<T><<<152 * 4, 256, 0, up()>>>(vdev, vqdev, nz, nx, dt,
+                                                          S.vdt2.template as<T>() + S.origin + dcol * ldp, ldp);
+            count_launch();
+            SSSI_CHECK_CUDA(cudaGetLastError());
+            const Bands2D bq = bands_of(vq);
+            std::vector<T> qzb, qzbm1, qxb, qxbm1;
+            band_coefficients<T>(bq.zb, bq.zbm1, qzb, qzbm1);
+            band_coefficients<T>(bq.xb, bq.xbm1, qxb, qxbm1);
+            zb.insert(zb.end(), qzb.begin(), qzb.end());
+            zbm1.insert(zbm1.end(), qzbm1.begin(), qzbm1.end());
+            xb.insert(xb.end(), qxb.begin(), qxb.end());
+            xbm1.insert(xbm1.end(), qxbm1.begin(), qxbm1.end());
+            for (size_t k = 0; k < bq.zb.size(); ++k) zb.push_back(static_cast<T>(bq.zb[k] - bands.zb[k]));
+            for (size_t k = 0; k < bq.xb.size(); ++k) xb.push_back(static_cast<T>(bq.xb[k] - bands.xb[k]));
         }
         auto upload = [&](DeviceBuffer& buf, const std::vector<T>& h) {
             buf.allocate(sizeof(T) * std::max<size_t>(h.size(), 1));
@@ -200,17 +275,15 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
                 SSSI_CHECK_CUDA(cudaMemcpyAsync(buf.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
                                                 up()));
         };
-        std::vector<T> zb, zbm1, xb, xbm1;
-        band_coefficients<T>(bands.zb, bands.zbm1, zb, zbm1);
-        band_coefficients<T>(bands.xb, bands.xbm1, xb, xbm1);
         upload(S.zb, zb);
         upload(S.zbm1, zbm1);
         upload(S.xb, xb);
         upload(S.xbm1, xbm1);
         SSSI_CHECK_CUDA(cudaStreamSynchronize(up()));  // vd and the host vectors go out of scope
     }
-    const size_t zbytes = sizeof(M) * std::max<size_t>((size_t)nB * nx, 1);
-    const size_t xbytes = sizeof(M) * std::max<size_t>((size_t)nz * 2 * nB, 1);
+    const size_t fields = pair ? 2 : 1;  // memory variables of P, then D's
+    const size_t zbytes = sizeof(M) * std::max<size_t>(fields * (size_t)nzb, 1);
+    const size_t xbytes = sizeof(M) * std::max<size_t>(fields * (size_t)nxb, 1);
     for (auto* bf : {&S.zphi[0], &S.zphi[1], &S.zpsi}) bf->allocate(zbytes);
     for (auto* bf : {&S.xphi[0], &S.xphi[1], &S.xpsi}) bf->allocate(xbytes);
 
@@ -219,14 +292,14 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
         const uint32_t box_rows = tz + 2 * HZ, box_cols = tx + 2 * L_;
         for (int k = 0; k < 2; ++k) {
             SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_box[v][k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp,
-                                              cols, ldp, box_rows, box_cols),
+                                              cols_all, ldp, box_rows, box_cols),
                          SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field halo box");
             SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_tile[v][k], S.P[k].get(), TmaType<T>::kType, sizeof(T), ldp,
-                                              cols, ldp, tz, tx),
+                                              cols_all, ldp, tz, tx),
                          SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the field tile box");
         }
-        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_v[v], S.vdt2.get(), TmaType<T>::kType, sizeof(T), ldp, cols, ldp,
-                                          tz, tx),
+        SSSI_REQUIRE(encode_tensor_map_2d(&S.desc.tm_v[v], S.vdt2.get(), TmaType<T>::kType, sizeof(T), ldp, cols_all,
+                                          ldp, tz, tx),
                      SSSI_ERR_CUDA, "cuTensorMapEncodeTiled failed for (v dt)^2");
     }
     d.field[0] = S.P[0].template as<T>() + S.origin;
@@ -252,6 +325,7 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
     d.nt = nt;
     d.reverse = reverse ? 1 : 0;
     d.stride = 1;
+    d.dcol = (int)dcol;
     reset_shot(slot);
     return slot;
 }
@@ -323,6 +397,18 @@ int Batch2d<T>::tile_x(int shape) const {
 
 template <typename T>
 void Batch2d<T>::finalize() {
+    // residual pairs run in the pair variant of the step, 32 x 32 whole tiles,
+    // for every shot of the batch while any pair is enabled
+    const bool was_pair = pair_;
+    pair_ = pairs_enabled() > 0;
+    if (pair_) {
+        if (!was_pair) shape_free_ = shape_;
+        schedule(1);
+        use_shape(1);
+        stale_ = false;
+        return;
+    }
+    if (was_pair) shape_ = shape_free_;  // the shape in use before the pairs
     // the first large schedule (at least four whole tiles' worth per block) is
     // worth tuning the tile shape for, and one grown eightfold since
     int64_t tiles = 0;
@@ -380,6 +466,7 @@ void Batch2d<T>::schedule(int shape) {
             if (S.enabled) n += (int64_t)((S.desc.s.nz + TZs - 1) / TZs) * ((S.desc.s.nx + TXs - 1) / TXs);
         if (n >= 8LL * sms_ * ctas_per_sm_[shape]) band_w = 2.0f;
     }
+    const int cps = pair_ ? ctas_per_sm_pair_ : ctas_per_sm_[shape];  // resident blocks per SM
     auto tile_item = [&](int k, int z0, int x0, int width) {
         const ShotTail<T>& d = shots_[k].desc.s;
         unsigned f = tile_band_flags(N_, TZs, width, d.nz, d.nx, d.nB, z0, x0);
@@ -390,7 +477,9 @@ void Batch2d<T>::schedule(int shape) {
         const int rows = std::min(z0 + TZs, d.nz) - std::max(z0, 0);
         const int cols = std::max(0, std::min(x0 + width, d.nx) - std::max(x0, 0));
         const float fill = (float)(rows * cols) / (float)(TZs * TXs);
-        return Item{k, z0, x0, f, (0.3f + 0.7f * fill) * (1.0f + (bz ? band_w : 0.0f) + (bx ? band_w : 0.0f))};
+        const float pair_w = d.dcol > 0 ? 2.0f : 1.0f;  // a residual pair's tile advances two fields
+        return Item{k, z0, x0, f,
+                    pair_w * (0.3f + 0.7f * fill) * (1.0f + (bz ? band_w : 0.0f) + (bx ? band_w : 0.0f))};
     };
     // Tile rows of a shot start at row -zs (0 <= zs < TZs, a multiple of one
     // 32-byte sector of rows, so that the tiles' copies stay sector-aligned; the
@@ -471,8 +560,8 @@ void Batch2d<T>::schedule(int shape) {
     {
         float total = 0.0f;
         for (const Item& it : items) total += it.cost;
-        const int blocks = std::max(1, std::min((int)items.size(), sms_ * ctas_per_sm_[shape_]));
-        split_s_[shape] = total < 2.0f * (float)blocks;
+        const int blocks = std::max(1, std::min((int)items.size(), sms_ * cps));
+        split_s_[shape] = !pair_ && total < 2.0f * (float)blocks;  // the pair variant takes whole tiles only
         if (split_s_[shape]) {
             std::vector<Item> split;
             split.reserve(items.size() + items.size() / 4);
@@ -500,7 +589,7 @@ void Batch2d<T>::schedule(int shape) {
         }
     }
     const int ntiles = (int)items.size();
-    const int grid = std::max(1, std::min(ntiles, sms_ * ctas_per_sm_[shape]));
+    const int grid = std::max(1, std::min(ntiles, sms_ * cps));
     ntiles_s_[shape] = ntiles;
     grid_s_[shape] = grid;
     // longest processing time first onto the least loaded CTA
@@ -641,14 +730,14 @@ void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
     BatchConst<T> bc = bc_;
     bc.step_base = base;
     bc.step_offset = offset;
-    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, shape_, stream);
+    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, shape_, pair_, stream);
 }
 
 template <typename T>
 void Batch2d<T>::run(int nsteps) {
     SSSI_REQUIRE(grid_ > 0 && !stale_, SSSI_ERR_INTERNAL, "Batch2d::run: the schedule is out of date (finalize)");
     int q = 0;
-    if (tune_ && nsteps >= kTuneMinRun) {
+    if (tune_ && !pair_ && nsteps >= kTuneMinRun) {
         // tile-shape tuning: kTuneSteps steps with each shape, timed with events,
         // then the faster shape's schedule for the rest (the per-cell arithmetic
         // does not depend on the tiling, so the results do not either)
@@ -728,31 +817,31 @@ void Batch2d<T>::check_errors() {
 
 template <typename T>
 void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
-                    cudaStream_t stream) {
+                    bool pair, cudaStream_t stream) {
     switch (N) {
-        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, shape, stream); break;
-        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, shape, stream); break;
-        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, shape, stream); break;
-        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, shape, stream); break;
-        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, shape, stream); break;
-        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, shape, stream); break;
-        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, shape, stream); break;
-        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, shape, stream); break;
+        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, shape, pair, stream); break;
+        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, shape, pair, stream); break;
+        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, shape, pair, stream); break;
+        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, shape, pair, stream); break;
+        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, shape, pair, stream); break;
+        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, shape, pair, stream); break;
+        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, shape, pair, stream); break;
+        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, shape, pair, stream); break;
         default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
     }
 }
 
 template <typename T>
-int batch2d_ctas_per_sm(int N, int shape) {
+int batch2d_ctas_per_sm(int N, int shape, bool pair) {
     switch (N) {
-        case 1: return batch2d_occupancy_n<T, 1>(shape);
-        case 2: return batch2d_occupancy_n<T, 2>(shape);
-        case 3: return batch2d_occupancy_n<T, 3>(shape);
-        case 4: return batch2d_occupancy_n<T, 4>(shape);
-        case 5: return batch2d_occupancy_n<T, 5>(shape);
-        case 6: return batch2d_occupancy_n<T, 6>(shape);
-        case 7: return batch2d_occupancy_n<T, 7>(shape);
-        default: return batch2d_occupancy_n<T, 8>(shape);
+        case 1: return batch2d_occupancy_n<T, 1>(shape, pair);
+        case 2: return batch2d_occupancy_n<T, 2>(shape, pair);
+        case 3: return batch2d_occupancy_n<T, 3>(shape, pair);
+        case 4: return batch2d_occupancy_n<T, 4>(shape, pair);
+        case 5: return batch2d_occupancy_n<T, 5>(shape, pair);
+        case 6: return batch2d_occupancy_n<T, 6>(shape, pair);
+        case 7: return batch2d_occupancy_n<T, 7>(shape, pair);
+        default: return batch2d_occupancy_n<T, 8>(shape, pair);
     }
 }
 

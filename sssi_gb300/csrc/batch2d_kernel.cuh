@@ -10,6 +10,8 @@
 //   shots that are not active at this batch step are skipped without copies.
 #pragma once
 
+#include <cstddef>
+
 #include "batch2d.cuh"
 
 namespace sssi {
@@ -368,6 +370,138 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
     }
 }
 
+// Stage one of a residual pair's band tile (FP32, whole tiles): the same
+// units as band_stage1, for both fields of the pair at once.  P (box Pb) uses
+// the shot's band coefficients and memory variables; D = Q - P (box Pd) uses
+// the second model's coefficients b_Q, b_Q - 1 (zoff / xoff entries on) and
+// its own memory variables (zoff / xoff on), and takes the coupling term
+//     phi_D <- b_Q phi_D + (b_Q - 1) D+D + (b_Q - b_P) (phi_P + D+P)
+// with phi_P before its update, which is phi_Q - phi_P of the two fields'
+// own recursions written out.  A_P and A_D go to scratch and scratch_d.
+template <typename T, int N, class Sh, int TX>
+__device__ __noinline__ void band_stage1_pair(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb,
+                                              const T* Pd, int z0, int x0, bool bz, bool bx, T* scratch,
+                                              T* scratch_d) {
+    using S = Sh;
+    using B = BandScratch<T, N, Sh>;
+    using M = typename MemVar<T>::type;
+    constexpr int TZ = S::TZ, NT = S::kThreads;
+    constexpr int CXW = TX + 2 * N - 1;
+    constexpr int L = 2 * N - 1;
+    constexpr int HZ = tile_halo_rows(N);
+    constexpr int SP = TZ + 2 * HZ;
+    const int tid = threadIdx.x;
+    const int nz = sh.nz, nx = sh.nx, nB = sh.nB;
+    if (bz) {
+        constexpr int G4 = (B::RZ + 3) / 4;
+        constexpr int UNITS = G4 * TX;
+        constexpr int MU = (UNITS + NT - 1) / NT;
+        const int zb0 = nz - nB;
+        const int64_t zoff = (int64_t)nB * nx;
+        const T* __restrict__ zb = sh.zb;
+        const T* __restrict__ zbm1 = sh.zbm1;
+        const M* __restrict__ phi_in = sh.zphi[ph];
+        M* __restrict__ phi_out = sh.zphi[ph ^ 1];
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int unit = tid + u * NT;
+            if (unit < UNITS) {
+                const int g = unit % G4, c = unit / G4, j = x0 + c;
+                T out[4], outd[4];
+                const T* colp = Pb + (c + L) * SP + 4 * g;
+                const T* cold = Pd + (c + L) * SP + 4 * g;
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    constexpr int C0 = HZ - N;
+                    T d = bc.wz[0] * (colp[C0 + o + 1] - colp[C0 + o]);
+                    T e = bc.wz[0] * (cold[C0 + o + 1] - cold[C0 + o]);
+#pragma unroll
+                    for (int n = 1; n < N; ++n) {
+                        d = fma(bc.wz[n], colp[C0 + o + 1 + n] - colp[C0 + o - n], d);
+                        e = fma(bc.wz[n], cold[C0 + o + 1 + n] - cold[C0 + o - n], e);
+                    }
+                    const int r = 4 * g + o, p = z0 - N + r;
+                    if ((unsigned)j < (unsigned)nx && p >= zb0 && p < nz) {
+                        const int64_t q = (p - zb0) + (int64_t)j * nB;
+                        M m = ldg_t(phi_in + q);
+                        M md = ldg_t(phi_in + zoff + q);
+                        const T cpl = ldg_t(zb + 2 * zoff + q) * ((m.x + m.y) + d);
+                        m = mem_new(ldg_t(zb + q), ldg_t(zbm1 + q), m, d);
+                        md = comp_add(mem_new(ldg_t(zb + zoff + q), ldg_t(zbm1 + zoff + q), md, e), cpl);
+                        d = mem_add(d, m);
+                        e = mem_add(e, md);
+                        if (r >= N && r < N + TZ) {
+                            phi_out[q] = m;
+                            phi_out[zoff + q] = md;
+                        }
+                    }
+                    out[o] = d;
+                    outd[o] = e;
+                }
+                st4(scratch + c * B::ZP + 4 * g, out);
+                st4(scratch_d + c * B::ZP + 4 * g, outd);
+            }
+        }
+    }
+    if (bx) {
+        constexpr int G4 = TZ / 4;
+        constexpr int UNITS = G4 * CXW;
+        constexpr int MU = (UNITS + NT - 1) / NT;
+        const int64_t xoff = (int64_t)nz * 2 * nB;
+        const T* __restrict__ xb = sh.xb;
+        const T* __restrict__ xbm1 = sh.xbm1;
+        const M* __restrict__ phi_in = sh.xphi[ph];
+        M* __restrict__ phi_out = sh.xphi[ph ^ 1];
+        T* xA = scratch + B::kX / sizeof(T);
+        T* xAd = scratch_d + B::kX / sizeof(T);
+#pragma unroll
+        for (int u = 0; u < MU; ++u) {
+            const int unit = tid + u * NT;
+            if (unit < UNITS) {
+                const int g = unit % G4, cx = unit / G4;
+                const int i = z0 + 4 * g, jc = x0 - N + cx;
+                const bool band = i >= 0 && jc >= 0 && jc < nx && (jc < nB || jc >= nx - nB);
+                const int64_t qc = band ? i + (int64_t)(jc < nB ? jc : nB + jc - (nx - nB)) * nz : -1;
+                V4<T> a[2 * N], ad[2 * N];
+#pragma unroll
+                for (int t = 0; t < 2 * N; ++t) {
+                    a[t] = ld4(Pb + (cx + t) * SP + HZ + 4 * g);
+                    ad[t] = ld4(Pd + (cx + t) * SP + HZ + 4 * g);
+                }
+                T out[4], outd[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    T d = bc.wx[0] * (a[N].v[o] - a[N - 1].v[o]);
+                    T e = bc.wx[0] * (ad[N].v[o] - ad[N - 1].v[o]);
+#pragma unroll
+                    for (int n = 1; n < N; ++n) {
+                        d = fma(bc.wx[n], a[N + n].v[o] - a[N - 1 - n].v[o], d);
+                        e = fma(bc.wx[n], ad[N + n].v[o] - ad[N - 1 - n].v[o], e);
+                    }
+                    if (qc >= 0 && i + o < nz) {
+                        const int64_t q = qc + o;
+                        M m = ldg_t(phi_in + q);
+                        M md = ldg_t(phi_in + xoff + q);
+                        const T cpl = ldg_t(xb + 2 * xoff + q) * ((m.x + m.y) + d);
+                        m = mem_new(ldg_t(xb + q), ldg_t(xbm1 + q), m, d);
+                        md = comp_add(mem_new(ldg_t(xb + xoff + q), ldg_t(xbm1 + xoff + q), md, e), cpl);
+                        d = mem_add(d, m);
+                        e = mem_add(e, md);
+                        if (cx >= N && cx < N + TX) {
+                            phi_out[q] = m;
+                            phi_out[xoff + q] = md;
+                        }
+                    }
+                    out[o] = d;
+                    outd[o] = e;
+                }
+                st4(xA + cx * TZ + 4 * g, out);
+                st4(xAd + cx * TZ + 4 * g, outd);
+            }
+        }
+    }
+}
+
 // Optional per-step outputs other than the receiver row (dense snapshots, the
 // RTM FP16 pack and max, the imaging sums).  Out of line for the same reason.
 template <typename T, int RX>
@@ -384,9 +518,13 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
             for (int o = 0; o < nrow; ++o) snap[(i0 + o) + (int64_t)(j0 + c) * nz] = pn.v[c][o];
     }
     const int stride = sh.stride > 0 ? sh.stride : 1;
+    // the thread's cells lie in one 32 x 32 scale block: i0 is a multiple of 4
+    // and j0 of 2, so neither straddles a multiple of 32
+    const int64_t blk = (i0 >> 5) + (int64_t)(j0 >> 5) * ((nz + 31) >> 5);
+    const int64_t nblk = (int64_t)((nz + 31) >> 5) * ((nx + 31) >> 5);
     if (sh.pack && tau >= 1 && (tau - 1) % stride == 0) {
         const int k = (tau - 1) / stride;
-        const float scale = fp16_scale_from_amax(sh.amax[k]);
+        const float scale = fp16_scale_from_amax(sh.amax[k * nblk + blk]);
         __half* pack = sh.pack + (int64_t)k * ncell;
         for (int c = 0; c < ncol; ++c) {
             const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
@@ -403,7 +541,6 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
                 for (int o = 0; o < nrow; ++o) pack[q0 + o] = __float2half_rn(f32(pc.v[c][o]) * scale);
             }
         }
-        if (i0 == 0 && j0 == 0) sh.inv_scale[k] = 1.0f / scale;
     }
     if (sh.amax && tau % stride == 0) {
         for (int c = 0; c < ncol; ++c)
@@ -440,7 +577,7 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
     if (sh.img_f16 && tau % stride == 0) {
         const int k = tau / stride;
         const __half* f16 = sh.img_f16 + (int64_t)k * ncell;
-        const float inv = sh.img_inv[k];
+        const float inv = 1.0f / fp16_scale_from_amax(sh.img_amax[k * nblk + blk]);  // a power of two
         float2* im = sh.img_m2;
         float2* is2 = sh.img_s22;
 #pragma unroll
@@ -523,13 +660,35 @@ __device__ __forceinline__ void add_sources(const ShotTail<T>& sh, int tau, int 
     }
 }
 
+// What the P pass of a residual pair hands to its D pass, per cell of the
+// thread: P's lap with the injected terms, and the coupling terms of the psi
+// recursions, (b_Q - b_P) (psi_P + D- A_P) with psi_P before its update.
+template <typename T, int RX>
+struct PairIO {
+    T lap[RX][4];
+    T cz[RX][4];
+    T cx[RX][4];
+};
+
+// Roles of tile_cells: a single field, or the P / D pass of a residual pair.
+constexpr int kRoleSingle = 0, kRolePairP = 1, kRolePairD = 2;
+
 // All cells of one thread: rows i0..i0+3, columns j0..j0+RX-1.  kBandZ / kBandX:
 // the tile is a band tile in z / x, its first derivatives are in `scratch`;
 // otherwise the composed stencil is used in that direction.
-template <typename T, int N, class Sh, int RX>
+//
+// Residual pairs run it twice per tile: kRolePairP advances P exactly as a
+// single field (its outputs are the shot's) and fills `io`; kRolePairD
+// advances D = Q - P from the D box (Pb), D's previous tile (Ob), P's
+// (v dt)^2 (Vb) and the difference of the two models' (v dt)^2 (Vd):
+//     D_new = wQ (zD + xD) + (wQ - wP) lap_P + 2 D - D_old,   wQ = wP + (wQ - wP),
+// with the second model's band coefficients, D's memory variables and the
+// coupling terms of `io` in the band tiles, and writes D's row 0 to rec_d.
+template <typename T, int N, class Sh, int RX, int kRole = kRoleSingle>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
-                                           unsigned flags, const T* scratch, unsigned& amax_bits) {
+                                           unsigned flags, const T* scratch, unsigned& amax_bits,
+                                           PairIO<T, RX>* io = nullptr, const T* Vd = nullptr) {
     using S = Sh;
     using B = BandScratch<T, N, Sh>;
     using M = typename MemVar<T>::type;
@@ -599,9 +758,12 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         // D- zA (+ psi): zA row r0+t of the scratch is global row i0-N+t
         constexpr int ZW = (2 * N + 3 + 3) / 4;  // 4-vectors covering the 2N+3 rows used
         const int zb0 = nz - nB;
-        const T* zb = sh.zb;
-        const T* zbm1 = sh.zbm1;
-        M* zpsi = sh.zpsi;
+        // a pair's D pass uses the second model's coefficients and D's own psi,
+        // zoff entries after P's; both passes read b_Q - b_P 2 zoff entries on
+        const int64_t zoff = (int64_t)nB * nx;
+        const T* zb = sh.zb + (kRole == kRolePairD ? zoff : 0);
+        const T* zbm1 = sh.zbm1 + (kRole == kRolePairD ? zoff : 0);
+        M* zpsi = sh.zpsi + (kRole == kRolePairD ? zoff : 0);
         bool in[RX][4];
         T pb[RX][4], pbm[RX][4];
         M ps[RX][4];
@@ -614,11 +776,13 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 pb[c][o] = T(0);
                 pbm[c][o] = T(0);
                 ps[c][o] = M{};
+                if constexpr (kRole == kRolePairP) io->cz[c][o] = T(0);
                 if (in[c][o]) {
                     const int64_t q = (i - zb0) + (int64_t)j * nB;
                     pb[c][o] = ldg_t(zb + q);
                     pbm[c][o] = ldg_t(zbm1 + q);
                     ps[c][o] = zpsi[q];
+                    if constexpr (kRole == kRolePairP) io->cz[c][o] = ldg_t(sh.zb + 2 * zoff + q);
                 }
             }
 #pragma unroll
@@ -641,7 +805,9 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 #pragma unroll
                 for (int k = 1; k < N; ++k) d = fma(bc.wz[k], w[o + N + k] - w[o + N - 1 - k], d);
                 if (in[c][o]) {
+                    if constexpr (kRole == kRolePairP) io->cz[c][o] *= mem_add(d, ps[c][o]);
                     ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
+                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], io->cz[c][o]);
                     d = mem_add(d, ps[c][o]);
                 }
                 lz.v[c][o] = d;
@@ -702,9 +868,10 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         }
     } else {
         // D- xA (+ psi): xA column c0+t of the scratch is global column j0-N+t
-        const T* xb = sh.xb;
-        const T* xbm1 = sh.xbm1;
-        M* xpsi = sh.xpsi;
+        const int64_t xoff = (int64_t)nz * 2 * nB;
+        const T* xb = sh.xb + (kRole == kRolePairD ? xoff : 0);
+        const T* xbm1 = sh.xbm1 + (kRole == kRolePairD ? xoff : 0);
+        M* xpsi = sh.xpsi + (kRole == kRolePairD ? xoff : 0);
         int64_t qo[RX];
         T pb[RX][4], pbm[RX][4];
         M ps[RX][4];
@@ -717,11 +884,13 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 pb[c][o] = T(0);
                 pbm[c][o] = T(0);
                 ps[c][o] = M{};
+                if constexpr (kRole == kRolePairP) io->cx[c][o] = T(0);
                 if (qo[c] >= 0 && i0 + o < nz) {
                     const int64_t q = qo[c] + i0 + o;
                     pb[c][o] = ldg_t(xb + q);
                     pbm[c][o] = ldg_t(xbm1 + q);
                     ps[c][o] = xpsi[q];
+                    if constexpr (kRole == kRolePairP) io->cx[c][o] = ldg_t(sh.xb + 2 * xoff + q);
                 }
             }
         }
@@ -737,7 +906,9 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 #pragma unroll
                 for (int k = 1; k < N; ++k) d = fma(bc.wx[k], a[c + N + k].v[o] - a[c + N - 1 - k].v[o], d);
                 if (qo[c] >= 0 && i0 + o < nz) {
+                    if constexpr (kRole == kRolePairP) io->cx[c][o] *= mem_add(d, ps[c][o]);
                     ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
+                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], io->cx[c][o]);
                     d = mem_add(d, ps[c][o]);
                 }
                 lx.v[c][o] = d;
@@ -752,7 +923,7 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
     // ---------------- update ----------------
     const int tau = ti.tau;
     const bool full_rows = i0 + 3 < nz;
-    T* const Pnew = sh.field[ph ^ 1];
+    T* const Pnew = sh.field[ph ^ 1] + (kRole == kRolePairD ? (int64_t)sh.dcol * sh.ldp : 0);
     Blk<T, RX> pn;
 #pragma unroll
     for (int c = 0; c < RX; ++c) {
@@ -773,20 +944,40 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 #pragma unroll
             for (int o = 0; o < 4; ++o) lap[o] = lz.v[c][o] + lx.v[c][o];
         }
-        if (flags & kSource) add_sources<T>(sh, tau, i0, j, lap);
-        if constexpr (kPacked<T>) {
+        if constexpr (kRole == kRolePairD) {
+            // D_new = wQ lap_D + (wQ - wP) lap_P + 2 D - D_old
+            const V4<T> vd = ld4(Vd + (c0 + c) * TZ + r0);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc.v[c][2 * h], pc.v[c][2 * h + 1]),
                                             make_float2(-po.v[2 * h], -po.v[2 * h + 1]));
-                const float2 u = __ffma2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]),
-                                            make_float2(lap[2 * h], lap[2 * h + 1]), t);
-                pn.v[c][2 * h] = u.x;
-                pn.v[c][2 * h + 1] = u.y;
+                const float2 dw = make_float2(vd.v[2 * h], vd.v[2 * h + 1]);
+                const float2 u = __ffma2_rn(dw, make_float2(io->lap[c][2 * h], io->lap[c][2 * h + 1]), t);
+                const float2 wq = __fadd2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]), dw);
+                const float2 r = __ffma2_rn(wq, make_float2(lap[2 * h], lap[2 * h + 1]), u);
+                pn.v[c][2 * h] = r.x;
+                pn.v[c][2 * h + 1] = r.y;
             }
         } else {
+            if (flags & kSource) add_sources<T>(sh, tau, i0, j, lap);
+            if constexpr (kRole == kRolePairP) {
 #pragma unroll
-            for (int o = 0; o < 4; ++o) pn.v[c][o] = fma(vv.v[o], lap[o], fma(T(2), pc.v[c][o], -po.v[o]));
+                for (int o = 0; o < 4; ++o) io->lap[c][o] = lap[o];
+            }
+            if constexpr (kPacked<T>) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc.v[c][2 * h], pc.v[c][2 * h + 1]),
+                                                make_float2(-po.v[2 * h], -po.v[2 * h + 1]));
+                    const float2 u = __ffma2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]),
+                                                make_float2(lap[2 * h], lap[2 * h + 1]), t);
+                    pn.v[c][2 * h] = u.x;
+                    pn.v[c][2 * h + 1] = u.y;
+                }
+            } else {
+#pragma unroll
+                for (int o = 0; o < 4; ++o) pn.v[c][o] = fma(vv.v[o], lap[o], fma(T(2), pc.v[c][o], -po.v[o]));
+            }
         }
         T* dst = Pnew + i0 + (int64_t)j * sh.ldp;
         if (full_rows) {
@@ -797,12 +988,14 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 if (i0 + o < nz) dst[o] = pn.v[c][o];
         }
     }
-    if (sh.rec && i0 == 0) {
-        T* rec = sh.rec + (int64_t)tau * nx;
+    T* const rec = kRole == kRolePairD ? sh.rec_d : sh.rec;
+    if (rec && i0 == 0) {
+        T* r = rec + (int64_t)tau * nx;
         const int ncol = min(RX, nx - j0);
-        for (int c = 0; c < ncol; ++c) rec[j0 + c] = pn.v[c][0];
+        for (int c = 0; c < ncol; ++c) r[j0 + c] = pn.v[c][0];
     }
-    if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
+    if constexpr (kRole != kRolePairD)
+        if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
 }
 
 // Per-tile work flags at step tau, worked out by the preparing thread from
@@ -812,7 +1005,7 @@ __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned 
     if ((sched & kSchedDense) || ((sched & kSchedRow) && z0 <= 0)) f |= kSource;  // z0 <= 0: the tile holds row 0
     bool rare = (sched & (kSchedSnap | kSchedImg64)) != 0u;
     if (sched & (kSchedAmax | kSchedPack | kSchedImg16)) {  // outputs every stride steps
-        const int stride = (int)(sched >> 8);
+        const int stride = (int)(sched >> kSchedStrideShift);
         const bool on_stride = tau % stride == 0;
         if ((sched & kSchedAmax) && on_stride) f |= kAmax;
         rare |= ((sched & kSchedPack) && tau >= 1 && (tau - 1) % stride == 0) ||
@@ -823,7 +1016,10 @@ __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned 
 }
 
 // Shared-memory layout of one pipeline stage (byte offsets, 128-aligned).
-template <typename T, int N, class Sh>
+// kPair: the stage also holds a residual pair's D box (kP2), D's previous
+// tile (kO2) and the (v dt)^2 difference (kV2), and the band scratch is
+// doubled (P's, then D's).
+template <typename T, int N, class Sh, bool kPair = false>
 struct StageLayout {
     using S = Sh;
     static constexpr int L = 2 * N - 1;
@@ -831,28 +1027,37 @@ struct StageLayout {
     static constexpr int SP = S::TZ + 2 * HZ;
     static constexpr unsigned kPBoxBytes = sizeof(T) * SP * (S::TX + 2 * L);
     static constexpr unsigned kTileBytes = sizeof(T) * S::TZ * S::TX;
+    static constexpr unsigned kBoxA = (kPBoxBytes + 127) / 128 * 128;
+    static constexpr unsigned kTileA = (kTileBytes + 127) / 128 * 128;
     static constexpr unsigned kP = 0;
-    static constexpr unsigned kO = (kPBoxBytes + 127) / 128 * 128;
-    static constexpr unsigned kV = kO + (kTileBytes + 127) / 128 * 128;
-    static constexpr unsigned kTail = kV + (kTileBytes + 127) / 128 * 128;
+    static constexpr unsigned kP2 = kPair ? kBoxA : 0;
+    static constexpr unsigned kO = kBoxA * (kPair ? 2 : 1);
+    static constexpr unsigned kO2 = kO + (kPair ? kTileA : 0);
+    static constexpr unsigned kV = kO2 + kTileA;
+    static constexpr unsigned kV2 = kV + (kPair ? kTileA : 0);
+    static constexpr unsigned kTail = kV2 + kTileA;
     static constexpr unsigned kInfo = kTail + (sizeof(ShotTail<T>) + 127) / 128 * 128;
     static constexpr unsigned kStage = kInfo + 128;  // TileInfo (32 bytes) rounded up
-    static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;  // bytes the TMA copies deliver
-    static constexpr int kStages = 2;                             // tiles in the copy pipeline
-    static constexpr unsigned kBar = kStages * kStage;            // one mbarrier per stage
-    static constexpr unsigned kScratch = kBar + 128;              // band scratch
-    static constexpr unsigned kSmem = kScratch + BandScratch<T, N, Sh>::kBytes;
+    static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;          // bytes the TMA copies deliver
+    static constexpr unsigned kTxPair = 2 * kPBoxBytes + 4 * kTileBytes;  // the same for a residual pair
+    static constexpr int kStages = 2;                                     // tiles in the copy pipeline
+    static constexpr unsigned kBar = kStages * kStage;                    // one mbarrier per stage
+    static constexpr unsigned kScratch = kBar + 128;                      // band scratch
+    static constexpr unsigned kScratchD = kScratch + BandScratch<T, N, Sh>::kBytes;  // pairs: D's
+    static constexpr unsigned kSmem = kScratch + (kPair ? 2 : 1) * BandScratch<T, N, Sh>::kBytes;
 };
 
 constexpr unsigned kWaitLimit = 1u << 24;
 
 // kSplit: the work lists may hold half tiles (schedules of small grids); the
 // variant without them keeps the whole-tile path free of their handling.
-template <typename T, int N, bool kSplit, class Sh>
-__global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
+// kPair: the batch holds residual pairs (FP32, whole tiles only).
+template <typename T, int N, bool kSplit, class Sh, bool kPair>
+__global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh::kMinBlocks)
     batch2d_kernel(const ShotDesc<T>* __restrict__ shots, const __grid_constant__ BatchConst<T> bc) {
     using S = Sh;
-    using G = StageLayout<T, N, Sh>;
+    using G = StageLayout<T, N, Sh, kPair>;
+    static_assert(!kPair || (std::is_same<T, float>::value && !kSplit), "residual pairs: FP32 whole tiles");
     constexpr int V = Sh::kIndex;  // tensor maps of this shape
     constexpr int TZ = S::TZ, TX = S::TX, RX = S::RX;
     constexpr int HZ = G::HZ, L = G::L;
@@ -896,23 +1101,38 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
         if (lane == 0 && info->shot >= 0) {
             const ShotTail<T>& g = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
             const int k = info->shot, z0 = info->z0, x0 = info->x0, cur = info->tloc & 1;
+            const bool pair = kPair && (g.sched & kSchedPair);
             inflight |= 1u << s;
             fence_proxy_async_shared();
-            mbar_arrive_expect_tx(&bar[s], G::kTx);
+            mbar_arrive_expect_tx(&bar[s], pair ? G::kTxPair : G::kTx);
             tma_load_2d(st + G::kP, &shots[k].tm_box[V][cur], &bar[s], g.oz + z0 - HZ, x0);
             tma_load_2d(st + G::kO, &shots[k].tm_tile[V][cur ^ 1], &bar[s], g.oz + z0, x0 + L);
             tma_load_2d(st + G::kV, &shots[k].tm_v[V], &bar[s], g.oz + z0, x0 + L);
+            if (pair) {
+                tma_load_2d(st + G::kP2, &shots[k].tm_box[V][cur], &bar[s], g.oz + z0 - HZ, x0 + g.dcol);
+                tma_load_2d(st + G::kO2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], g.oz + z0, x0 + L + g.dcol);
+                tma_load_2d(st + G::kV2, &shots[k].tm_v[V], &bar[s], g.oz + z0, x0 + L + g.dcol);
+            }
         }
     };
     // warp 0: put the prefetched item into stage s (tile = its position in the
     // list); with `copy`, lane 0 also issues the stage's three copies (or the
     // plain arrival).  Lane 0 works from registers: the item and the head of the
     // shot's tail.
+    // a residual pair's column offset of D, from the lane that holds it
+    constexpr int kDcolOff = (int)offsetof(ShotTail<T>, dcol);
+    static_assert(kDcolOff % 4 == 0, "dcol is a 32-bit word");
     auto prepare = [&](int w, int s, bool copy) {
         unsigned char* st = smem + s * G::kStage;
         TileInfo* info = reinterpret_cast<TileInfo*>(st + G::kInfo);
         const int k = item.x >= 0 ? (item.x & 0xffffff) : -1;
         if (k >= 0 && lane < kTailVec) reinterpret_cast<uint4*>(st + G::kTail)[lane] = tail_reg;
+        int dcol = 0;
+        if constexpr (kPair) {
+            constexpr int word = (kDcolOff % 16) / 4;
+            const unsigned x = word == 0 ? tail_reg.x : word == 1 ? tail_reg.y : word == 2 ? tail_reg.z : tail_reg.w;
+            dcol = (int)__shfl_sync(0xffffffffu, x, kDcolOff / 16);
+        }
         if (lane == 0) {
             const int t_start = (int)tail_reg.x, nt = (int)tail_reg.y, oz = (int)tail_reg.w;
             const unsigned sched = tail_reg.z;
@@ -936,12 +1156,18 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
             info->flags = shot >= 0 ? tile_flags(sched, z0, top & 7u, tau) | (half ? kHalf : 0u) : 0u;
             if (copy && shot >= 0) {
                 const int cur = tloc & 1;
+                const bool pair = kPair && (sched & kSchedPair);
                 inflight |= 1u << s;
                 fence_proxy_async_shared();
-                mbar_arrive_expect_tx(&bar[s], G::kTx);
+                mbar_arrive_expect_tx(&bar[s], pair ? G::kTxPair : G::kTx);
                 tma_load_2d(st + G::kP, &shots[k].tm_box[V][cur], &bar[s], oz + z0 - HZ, x0);
                 tma_load_2d(st + G::kO, &shots[k].tm_tile[V][cur ^ 1], &bar[s], oz + z0, x0 + L);
                 tma_load_2d(st + G::kV, &shots[k].tm_v[V], &bar[s], oz + z0, x0 + L);
+                if (pair) {
+                    tma_load_2d(st + G::kP2, &shots[k].tm_box[V][cur], &bar[s], oz + z0 - HZ, x0 + dcol);
+                    tma_load_2d(st + G::kO2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], oz + z0, x0 + L + dcol);
+                    tma_load_2d(st + G::kV2, &shots[k].tm_v[V], &bar[s], oz + z0, x0 + L + dcol);
+                }
             }
         }
         __syncwarp();
@@ -1017,17 +1243,50 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
                 if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx && (!half || c0 < TX / 2))
                     tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
             } else {
-                if (ti.flags & (kBandZ | kBandX)) {
-                    band_stage1<T, N, Sh, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ, ti.flags & kBandX,
-                                          scratch);
-                    __syncthreads();
+                bool done = false;
+                if constexpr (kPair) {
+                    if (sh.sched & kSchedPair) {
+                        // a residual pair: P's and D's cells in one tile, P first
+                        const T* Pd = reinterpret_cast<const T*>(st + G::kP2);
+                        const T* Od = reinterpret_cast<const T*>(st + G::kO2);
+                        const T* Vd = reinterpret_cast<const T*>(st + G::kV2);
+                        T* scratch_d = reinterpret_cast<T*>(smem + G::kScratchD);
+                        if (ti.flags & (kBandZ | kBandX)) {
+                            band_stage1_pair<T, N, Sh, TX>(bc, sh, ti.tloc & 1, Pb, Pd, z0, x0, ti.flags & kBandZ,
+                                                           ti.flags & kBandX, scratch, scratch_d);
+                            __syncthreads();
+                        }
+                        if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx) {
+                            PairIO<T, RX> io;
+                            tile_cells<T, N, Sh, RX, kRolePairP>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags,
+                                                                 scratch, amax_bits, &io);
+                            tile_cells<T, N, Sh, RX, kRolePairD>(bc, sh, ti, Pd, Od, Vb, z0, x0, r0, c0, ti.flags,
+                                                                 scratch_d, amax_bits, &io, Vd);
+                        }
+                        done = true;
+                    }
                 }
-                if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx)
-                    tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+                if (!done) {
+                    if (ti.flags & (kBandZ | kBandX)) {
+                        band_stage1<T, N, Sh, TX>(bc, sh, ti.tloc & 1, Pb, z0, x0, ti.flags & kBandZ,
+                                                  ti.flags & kBandX, scratch);
+                        __syncthreads();
+                    }
+                    if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx)
+                        tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+                }
             }
             if (ti.flags & kAmax) {
-                const unsigned w = __reduce_max_sync(0xffffffffu, amax_bits);
-                if (lane == 0 && w) atomicMax(sh.amax + ti.tau / (sh.stride > 0 ? sh.stride : 1), w);
+                // block maxima: one atomic per group of lanes whose cells share a
+                // 32 x 32 scale block (lanes that computed nothing skip)
+                const int nbz = (sh.nz + 31) >> 5;
+                const int key = amax_bits ? (i0 >> 5) + (j0 >> 5) * nbz : -1;
+                const unsigned peers = __match_any_sync(0xffffffffu, key);
+                const unsigned w = __reduce_max_sync(peers, amax_bits);
+                if (key >= 0 && w && lane == __ffs(peers) - 1) {
+                    const int64_t nblk = (int64_t)nbz * ((sh.nx + 31) >> 5);
+                    atomicMax(sh.amax + (int64_t)(ti.tau / (sh.stride > 0 ? sh.stride : 1)) * nblk + key, w);
+                }
             }
         }
         __syncthreads();
@@ -1045,12 +1304,12 @@ __global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks)
 
 }  // namespace batch
 
-template <typename T, int N, bool kSplit, class Sh>
+template <typename T, int N, bool kSplit, class Sh, bool kPair>
 void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
-    using G = batch::StageLayout<T, N, Sh>;
+    using G = batch::StageLayout<T, N, Sh, kPair>;
     static bool configured = false;
     if (!configured) {
-        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit, Sh>,
+        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit, Sh, kPair>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem));
         configured = true;
     }
@@ -1064,7 +1323,7 @@ void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, i
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit, Sh>, shots, bc));
+    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit, Sh, kPair>, shots, bc));
     count_launch();
 }
 
@@ -1072,33 +1331,39 @@ template <typename T, int N, class Sh>
 void launch_batch2d_shape(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
                           cudaStream_t stream) {
     if (split)
-        launch_batch2d_variant<T, N, true, Sh>(shots, bc, grid, stream);
+        launch_batch2d_variant<T, N, true, Sh, false>(shots, bc, grid, stream);
     else
-        launch_batch2d_variant<T, N, false, Sh>(shots, bc, grid, stream);
+        launch_batch2d_variant<T, N, false, Sh, false>(shots, bc, grid, stream);
 }
 
 template <typename T, int N>
-void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
+void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape, bool pair,
                       cudaStream_t stream) {
     if constexpr (kBatchShapes<T> > 1) {
+        if (pair) {
+            SSSI_REQUIRE(shape == 1 && !split, SSSI_ERR_INTERNAL, "residual pairs run with 32 x 32 whole tiles");
+            launch_batch2d_variant<T, N, false, BatchShape<T, 1>, true>(shots, bc, grid, stream);
+            return;
+        }
         if (shape == 1) {
             launch_batch2d_shape<T, N, BatchShape<T, 1>>(shots, bc, grid, split, stream);
             return;
         }
     }
+    SSSI_REQUIRE(!pair, SSSI_ERR_INTERNAL, "residual pairs are FP32 only");
     SSSI_REQUIRE(shape == 0, SSSI_ERR_INTERNAL, "tile shape %d not built for this type", shape);
     launch_batch2d_shape<T, N, BatchShape<T, 0>>(shots, bc, grid, split, stream);
 }
 
-template <typename T, int N, class Sh>
+template <typename T, int N, class Sh, bool kPair>
 int batch2d_occupancy_shape() {
-    const size_t smem = batch::StageLayout<T, N, Sh>::kSmem;
+    const size_t smem = batch::StageLayout<T, N, Sh, kPair>::kSmem;
     int n = 0;
-    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false, Sh>,
+    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false, Sh, kPair>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false, Sh>, Sh::kThreads,
-                                                          smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false, Sh, kPair>,
+                                                          Sh::kThreads, smem);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
         n = 1;
@@ -1107,15 +1372,17 @@ int batch2d_occupancy_shape() {
 }
 
 template <typename T, int N>
-int batch2d_occupancy_n(int shape) {
+int batch2d_occupancy_n(int shape, bool pair) {
     if constexpr (kBatchShapes<T> > 1) {
-        if (shape == 1) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>>();
+        if (pair) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>, true>();
+        if (shape == 1) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>, false>();
     }
-    return batch2d_occupancy_shape<T, N, BatchShape<T, 0>>();
+    return batch2d_occupancy_shape<T, N, BatchShape<T, 0>, false>();
 }
 
-#define SSSI_BATCH2D_INSTANCE(T, N)                                                                                \
-    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, int, cudaStream_t); \
-    template int batch2d_occupancy_n<T, N>(int);
+#define SSSI_BATCH2D_INSTANCE(T, N)                                                                      \
+    template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, int, bool, \
+                                         cudaStream_t);                                                  \
+    template int batch2d_occupancy_n<T, N>(int, bool);
 
 }  // namespace sssi

@@ -3,9 +3,10 @@
 // One launch advances the whole grid by one time step
 // (src/fd_cmex/fwdTimeCpmlFor2dAw_mex.c:183-290): both first-derivative
 // stages of both axes, the CPML memory-variable updates, the leapfrog update,
-// source injection, receiver gather, snapshot output, FP16 packing of the
-// field for the adjoint pass and the RTM imaging sums, in one pass over the
-// wavefield.
+// source injection, receiver gather and snapshot output, in one pass over the
+// wavefield.  It serves the strict FP64 mode (the reference's rounding
+// sequence) and the no-allocation entry point; the fused FP64 and FP32 modes
+// run on the batched tiled kernel.
 //
 // Work decomposition: a block owns BZ consecutive rows (one row per thread,
 // so a warp reads 32 consecutive z samples of one column: coalesced) and
@@ -94,7 +95,6 @@ __device__ __forceinline__ TA mem_update(TA b, TA m, TA bm1, T d) {
     }
 }
 
-__device__ __forceinline__ float to_f32(double x) { return static_cast<float>(x); }
 
 template <typename T, typename TA, int N, bool STRICT>
 __global__ void cpml2d_step_kernel(const Step2D<T, TA> p) {
@@ -126,16 +126,6 @@ __global__ void cpml2d_step_kernel(const Step2D<T, TA> p) {
     double src_amp[kMaxPointSources];
 #pragma unroll
     for (int s = 0; s < kMaxPointSources; ++s) src_amp[s] = (s < p.nsrc) ? p.src_wavelet[(int64_t)s * p.nt + p.t] : 0.0;
-
-    float pack_scale = 1.0f;
-    if (p.pack) {
-        pack_scale = fp16_scale_from_amax(*p.pack_amax);
-        if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && p.pack_inv_scale_out)
-            *p.pack_inv_scale_out = 1.0f / pack_scale;
-    }
-    float img_inv = 1.0f;
-    if (p.img_f16) img_inv = *p.img_inv_scale;
-    unsigned my_amax = 0u;
 
     T pq[2 * N];  // P(i, k-2N+1 .. k)
     T aq[2 * N];  // xA(i, k-N-2N+1 .. k-N)
@@ -250,29 +240,7 @@ __global__ void cpml2d_step_kernel(const Step2D<T, TA> p) {
 
             if (p.rec && i == 0) p.rec[j] = static_cast<double>(pn);
             if (p.snap) p.snap[q] = static_cast<double>(pn);
-            if (p.pack) p.pack[q] = __float2half_rn(to_f32(static_cast<double>(pc)) * pack_scale);
-            if (p.amax) my_amax = max(my_amax, __float_as_uint(fabsf(to_f32(static_cast<double>(pn)))));
-            if (p.img_f64) {
-                const double f = p.img_f64[q];
-                const double r = static_cast<double>(pn);
-                if constexpr (STRICT) {
-                    p.img_m[q] = __dadd_rn(__dmul_rn(f, r), p.img_m[q]);
-                    p.img_s2[q] = __dadd_rn(__dmul_rn(f, f), p.img_s2[q]);
-                } else {
-                    p.img_m[q] = fma(f, r, p.img_m[q]);
-                    p.img_s2[q] = fma(f, f, p.img_s2[q]);
-                }
-            } else if (p.img_f16) {
-                const float f = __half2float(p.img_f16[q]) * img_inv;
-                const float r = to_f32(static_cast<double>(pn));
-                p.img_m[q] += static_cast<double>(f * r);
-                p.img_s2[q] += static_cast<double>(f * f);
-            }
         }
-    }
-    if (p.amax) {
-        const unsigned w = __reduce_max_sync(0xffffffffu, my_amax);
-        if ((tid & 31) == 0 && w) atomicMax(p.amax, w);
     }
 }
 
@@ -301,15 +269,16 @@ void launch_dispatch(const Step2D<T, TA>& p, int N, int bz, cudaStream_t stream)
     SSSI_CHECK_CUDA(cudaGetLastError());
 }
 
-__global__ void pack_f16_kernel(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
-                                float* inv_scale_out) {
-    const float scale = fp16_scale_from_amax(*amax);
+// FP16 copy of a padded FP32 field, one power-of-two scale per 32 x 32 block
+// (the block maxima amax[bz + bx * nbz], nbz = ceil(nz / 32)).
+__global__ void pack_f16_kernel(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out) {
     const int64_t n = (int64_t)nz * nx;
+    const int nbz = (nz + 31) >> 5;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = q % nz, j = q / nz;
+        const float scale = fp16_scale_from_amax(amax[(i >> 5) + (j >> 5) * nbz]);
         out[q] = __float2half_rn(P[i + j * ldp] * scale);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && inv_scale_out) *inv_scale_out = 1.0f / scale;
 }
 
 }  // namespace
@@ -361,8 +330,8 @@ cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool stric
 }
 
 void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
-                     float* inv_scale_out, cudaStream_t stream) {
-    pack_f16_kernel<<<152 * 4, 256, 0, stream>>>(P, ldp, nz, nx, amax, out, inv_scale_out);
+                     cudaStream_t stream) {
+    pack_f16_kernel<<<152 * 4, 256, 0, stream>>>(P, ldp, nz, nx, amax, out);
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
 }
@@ -487,15 +456,6 @@ void Cpml2d<T, TA>::step(const StepIO<T>& io) {
     p.src_row_sub = nullptr;
     p.rec = io.rec;
     p.snap = io.snap;
-    p.pack = io.pack;
-    p.pack_amax = io.pack_amax;
-    p.pack_inv_scale_out = io.pack_inv_scale_out;
-    p.amax = io.amax;
-    p.img_f64 = io.img_f64;
-    p.img_f16 = io.img_f16;
-    p.img_inv_scale = io.img_inv_scale;
-    p.img_m = io.img_m;
-    p.img_s2 = io.img_s2;
     if (p.nsrc == 0) p.src_wavelet = nullptr;
     launch_cpml2d_step<T, TA>(p, N_, strict_, bz_, stream_);
     cur_ = 1 - cur_;

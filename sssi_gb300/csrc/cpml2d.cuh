@@ -55,18 +55,6 @@ struct Step2D {
     // outputs of this step
     double* rec;   // nx: new field on row 0
     double* snap;  // nz x nx: new field
-    // FP16 copy of the *current* field (the previous step's result), scaled
-    __half* pack;
-    const unsigned* pack_amax;  // bit pattern of max|P| of the field being packed
-    float* pack_inv_scale_out;  // written once: 1/scale of this pack
-    unsigned* amax;             // atomicMax of bit pattern of |new field|, or null
-
-    // imaging against a stored forward field (reverse pass)
-    const double* img_f64;  // nz x nx forward snapshot of this step
-    const __half* img_f16;  // nz x nx FP16 forward snapshot of this step
-    const float* img_inv_scale;  // its 1/scale
-    double* img_m;
-    double* img_s2;
 };
 
 // Power-of-two scale that maps max|P| into [2^14, 2^15) for FP16 storage.
@@ -103,17 +91,6 @@ struct StepIO {
     const T* src_row = nullptr;    // nx values injected on row 0
     T* rec = nullptr;              // nx: new field on row 0
     T* snap = nullptr;             // nz x nx: new field
-    __half* pack = nullptr;
-    const unsigned* pack_amax = nullptr;
-    float* pack_inv_scale_out = nullptr;
-    unsigned* amax = nullptr;
-    const double* img_f64 = nullptr;
-    const __half* img_f16 = nullptr;
-    const float* img_inv_scale = nullptr;
-    double* img_m = nullptr;
-    double* img_s2 = nullptr;
-    float2* img_m2 = nullptr;  // compensated FP32 sums used with img_f16 by the tiled kernel
-    float2* img_s22 = nullptr;
     int t = 0;
 };
 
@@ -170,7 +147,10 @@ template <typename T, typename TA>
 cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool strict, int bz, cudaStream_t stream);
 
 // Packs field P (padded, interior origin) into FP16 with the scale from *amax.
+// FP16 copy of the padded FP32 field P (nz x nx interior, column pitch ldp)
+// with one power-of-two scale per 32 x 32 block, from the block maxima amax
+// (index bz + bx * ceil(nz / 32)).
 void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
-                     float* inv_scale_out, cudaStream_t stream);
+                     cudaStream_t stream);
 
 }  // namespace sssi

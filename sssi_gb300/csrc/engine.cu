@@ -36,6 +36,9 @@ namespace {
 using namespace api;
 using Clock = std::chrono::steady_clock;
 
+// FP16 snapshot scale blocks (32 x 32 cells) of an nz x nx grid.
+inline int64_t nblocks(int64_t nz, int64_t nx) { return ((nz + 31) / 32) * ((nx + 31) / 32); }
+
 // Device array of T -> caller array of doubles (host or device).
 template <typename T>
 void deliver(const T* dev, size_t n, double* out, cudaStream_t s) {
@@ -132,7 +135,7 @@ class Engine final : public EngineBase {
         int kA = -1, kB = -1, kR = -1;
         int64_t s0 = 0;
         int phase = 1;
-        DeviceBuffer wav, recA, recB, delta, fsnap, amax, inv, Mb, S2, img;
+        DeviceBuffer wav, recA, recB, delta, fsnap, amax, Mb, S2, img;
         std::unique_ptr<Prop3d<T>> p3;
         int64_t done3 = 0;
         cudaStream_t s3 = nullptr;  // 3D: the propagation's own stream (runs beside the 2D batch)
@@ -175,7 +178,7 @@ class Engine final : public EngineBase {
             const size_t n = (size_t)(nz * nx);
             const int stride = kF16 ? (r.d.snap_stride > 0 ? r.d.snap_stride : 4) : 1;
             const size_t nsnap = (size_t)((nt + stride - 1) / stride);
-            const size_t snaps = kF16 ? 2 * n * nsnap + 8 * nsnap : 8 * n * (size_t)nt;
+            const size_t snaps = kF16 ? 2 * n * nsnap + 4 * (size_t)nblocks(nz, nx) * nsnap : 8 * n * (size_t)nt;
             return 3 * shot2d() + 3 * ts * (size_t)(nx * nt) + snaps + 16 * n + wav;
         }
         const int64_t vol = (nz + 2 * HZ + 3) * (nx + 2 * L) * (ny + 2 * L);
@@ -236,11 +239,19 @@ class Engine final : public EngineBase {
             const int64_t n = nz * nx;
             const int stride = kF16 ? (d.snap_stride > 0 ? d.snap_stride : 4) : 1;
             const int64_t nsnap = (nt + stride - 1) / stride;
-            u->kA = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
-            u->kB = B_.add_shot(r->vs.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
-            u->kR = B_.add_shot_like(u->kA, (int)nt, (int)(step_ + nt), true);
+            // FP32: the field in vs and the residual (field in v) - (field in vs)
+            // as one residual pair (dataTrue - dataSmooth is the residual's row
+            // 0, accurate relative to itself); FP64: two forward shots
+            if (kF16) {
+                u->kB = B_.add_pair_shot(r->vs.data(), r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_);
+                u->kR = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)(step_ + nt), true);
+            } else {
+                u->kA = B_.add_shot(r->v.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
+                u->kB = B_.add_shot(r->vs.data(), nz, nx, d.nBoundary, d.dt, (int)nt, (int)step_, false);
+                u->kR = B_.add_shot_like(u->kA, (int)nt, (int)(step_ + nt), true);
+                B_.set_point_sources(u->kA, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
+            }
             B_.enable(u->kR, false);
-            B_.set_point_sources(u->kA, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
             B_.set_point_sources(u->kB, 1, r->iz.data(), r->ix.data(), u->wav.template as<T>());
             u->recA.allocate(sizeof(T) * ndata);
             u->recB.allocate(sizeof(T) * ndata);
@@ -250,23 +261,21 @@ class Engine final : public EngineBase {
             u->Mb.zero(up_);
             if (kF16) {
                 u->fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
-                u->amax.allocate(sizeof(unsigned) * std::max<int64_t>(nsnap, 1));
+                u->amax.allocate(sizeof(unsigned) * nblocks(nz, nx) * std::max<int64_t>(nsnap, 1));
                 u->amax.zero(up_);
-                u->inv.allocate(sizeof(float) * std::max<int64_t>(nsnap, 1));
                 u->S2.zero(up_);
             } else {
                 u->fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
                 fill(u->S2.template as<double>(), n, d.epsilon, up_);
             }
-            ShotTail<T>& a = B_.shot(u->kA);
-            a.rec = u->recA.template as<T>();
+            if (u->kA >= 0) B_.shot(u->kA).rec = u->recA.template as<T>();
             ShotTail<T>& b = B_.shot(u->kB);
             b.rec = u->recB.template as<T>();
+            if (kF16) b.rec_d = u->delta.template as<T>();
             if (kF16) {
                 b.stride = stride;
                 b.amax = u->amax.template as<unsigned>();
                 b.pack = u->fsnap.template as<__half>();
-                b.inv_scale = u->inv.template as<float>();
             } else {
                 b.snap = reinterpret_cast<T*>(u->fsnap.template as<double>());
                 b.snap_t0 = 0;
@@ -276,7 +285,7 @@ class Engine final : public EngineBase {
             if (kF16) {
                 rr.stride = stride;
                 rr.img_f16 = u->fsnap.template as<__half>();
-                rr.img_inv = u->inv.template as<float>();
+                rr.img_amax = u->amax.template as<unsigned>();
                 rr.img_m2 = u->Mb.template as<float2>();
                 rr.img_s22 = u->S2.template as<float2>();
             } else {
@@ -433,17 +442,24 @@ class Engine final : public EngineBase {
                 if (kF16 && nt >= 1 && (nt - 1) % stride == 0) {
                     const int64_t k = (nt - 1) / stride;
                     launch_pack_f16(reinterpret_cast<const float*>(B_.current_field(u.kB)), B_.ldp(u.kB), (int)nz,
-                                    (int)nx, u.amax.template as<unsigned>() + k, u.fsnap.template as<__half>() + k * n,
-                                    u.inv.template as<float>() + k, s_);
+                                    (int)nx, u.amax.template as<unsigned>() + k * nblocks(nz, nx),
+                                    u.fsnap.template as<__half>() + k * n, s_);
                 }
                 if (nt > 0) {
-                    diff_kernel<T><<<152 * 4, 256, 0, s_>>>(u.recA.template as<T>(), u.recB.template as<T>(),
-                                                            u.delta.template as<T>(), nx * nt);
-                    count_launch();
+                    // the reverse source dataTrue - dataSmooth: the residual's row 0
+                    // (FP32), or the difference of the two forward shots (FP64);
+                    // dataTrue itself (FP32) as dataSmooth + residual, when wanted
+                    if (!kF16)
+                        diff_kernel<T><<<152 * 4, 256, 0, s_>>>(u.recA.template as<T>(), u.recB.template as<T>(),
+                                                                u.delta.template as<T>(), nx * nt);
+                    else if (d.data)
+                        sum_kernel<T><<<152 * 4, 256, 0, s_>>>(u.recB.template as<T>(), u.delta.template as<T>(),
+                                                               u.recA.template as<T>(), nx * nt);
+                    if (!kF16 || d.data) count_launch();
                     SSSI_CHECK_CUDA(cudaGetLastError());
                 }
                 wait_stream(s_);
-                B_.remove_shot(u.kA);
+                if (u.kA >= 0) B_.remove_shot(u.kA);
                 B_.remove_shot(u.kB);
                 u.kA = u.kB = -1;
                 B_.enable(u.kR, true);

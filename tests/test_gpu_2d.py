@@ -163,8 +163,8 @@ def test_rtm_fast_and_fp16(gpu, golden, oracle_mod):
                                            1e-3, epsilon=float(g["epsilon"]), mode="fp32", snap_stride=1,
                                            want_data=True)
     assert oracle_mod.rel_l2(dtr, g["data_true"]) <= TOL_FP32
-    # FP16 storage of the forward field: image within 1e-3 here (small grid,
-    # few steps); the full-size check with the 1e-4 target is in test_gpu_rtm_full.
+    # FP16 storage of the forward field: image within 1e-3 on this 40 x 60 grid
+    # of 120 steps; the 1e-4 target on realistic grids is in tests/test_gpu_rtm.py
     assert oracle_mod.rel_l2(img32, g["image"]) <= 1e-3
 
 
@@ -223,7 +223,7 @@ def test_mex_gateway_fp32_mode(gpu, golden, oracle_mod, monkeypatch):
     g = golden("fwd2d_rvs2d.npz")
     nz, nx, nt, N, nB, v, src = _case(g, 3)
     monkeypatch.setenv("SSSI_MEX_MODE", "fp32")
-    data, _ = oracle_mod.shim_call(fwd, 1, v, src, N, nB, 10.0, 10.0, 1e-3)
+    data, _ = oracle_mod.shim_call(fwd, 2, v, src, N, nB, 10.0, 10.0, 1e-3)
     assert oracle_mod.rel_l2(data, g["c3_data"]) <= TOL_FP32
 
 
