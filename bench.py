@@ -689,8 +689,14 @@ def bench_serve(S, args):
         z0 = int(rng.integers(0, (1000 if kind != "fwd3d" else 256) - nz + 1))
         x0 = int(rng.integers(0, (3000 if kind != "fwd3d" else 256) - nx + 1))
         reqs.append((t, kind, nz, nx, nt, z0, x0))
-    # outputs: a pinned sink per kind (requests overwrite it in turn), own arrays for the checked sample
-    check = set(int(k) for k in rng.choice(n_req, 8, replace=False))
+    # outputs: a pinned sink per kind (requests overwrite it in turn), own arrays for the checked
+    # sample: a seeded stratified sample of every kind (RTM images weigh most: their reverse
+    # source is a difference of two seismograms)
+    per_kind = {"fwd2d": args.serve_check_fwd, "rtm2d": args.serve_check_rtm, "fwd3d": args.serve_check_3d}
+    check = set()
+    for kind, m in per_kind.items():
+        idx = [k for k, r in enumerate(reqs) if r[1] == kind]
+        check.update(int(k) for k in rng.choice(idx, min(m, len(idx)), replace=False))
 
     def sink(n):
         return torch.empty(n, dtype=torch.float64).pin_memory().numpy()
@@ -703,7 +709,8 @@ def bench_serve(S, args):
 
     tickets, inputs = [], {}
     dt = 8e-4
-    with S.Plan(N_ORDER, DZ, DX, DX, mode="fp32", device_bytes=64 << 30) as plan:
+    S.release_cache()  # the headline's cached FP64 buffers go back before the plan takes its budget
+    with S.Plan(N_ORDER, DZ, DX, DX, mode="fp32", device_bytes=int(args.serve_budget_gb * (1 << 30))) as plan:
         plan.wait(plan.submit_fwd2d(np.asfortranarray(big2d[:200, :300]), 100, [0], [150],
                                     ricker(20.0, 100, dt)[None, :], NB, dt))  # warm-up
         t_start = time.perf_counter()
@@ -719,7 +726,7 @@ def bench_serve(S, args):
             elif kind == "rtm2d":
                 v = np.asfortranarray(big2d[z0:z0 + nz, x0:x0 + nx])
                 vs = np.asfortranarray(smooth2d[z0:z0 + nz, x0:x0 + nx])
-                tk = plan.submit_rtm2d(v, vs, w, 0, nx // 2, NB, dt, epsilon=EPS, snap_stride=STRIDE,
+                tk = plan.submit_rtm2d(v, vs, w, 0, nx // 2, NB, dt, epsilon=EPS, snap_stride=args.serve_stride,
                                        image=view(kind, (nz, nx), own))
             else:
                 v = np.asfortranarray(big3d[z0:z0 + nz, x0:x0 + nx, :nx])
@@ -758,10 +765,13 @@ def bench_serve(S, args):
             "gcell_updates_per_s": round(cells / span / 1e9, 2), "span_s": round(span, 2),
             "offered_rate_per_s": rate, "requests": {k: kinds.count(k) for k in ("fwd2d", "rtm2d", "fwd3d")},
             "rel_l2_vs_fp64": errs, "rel_l2_vs_fp64_max": max(errs.values()) if errs else None,
+            "rel_l2_vs_fp64_max_by_kind": {kd: max([e for k, e in errs.items() if k.endswith(kd)], default=None)
+                                           for kd in ("fwd2d", "rtm2d", "fwd3d")},
+            "checked": {kd: sum(1 for k in errs if k.endswith(kd)) for kd in ("fwd2d", "rtm2d", "fwd3d")},
             "admission_budget_bytes": int(st["device_bytes_budget"]), "failed": int(st["failed"]), "dtype": "fp32",
             "plan_host_s": {k: round(st[k], 3) for k in ("admit_s", "round_s", "gpu_wait_s", "deliver_s")},
             "config": {"workload": "serve-mixed", "fwd2d": "200x300 .. 1000x3000", "rtm2d": "400x800 .. 800x2400, "
-                       "fp16 snapshots every 4 steps", "fwd3d": "128^3 .. 256^3, nB 16", "nt": "U[1000, 4000]",
+                       f"16-bit snapshots every {args.serve_stride} steps", "fwd3d": "128^3 .. 256^3, nB 16", "nt": "U[1000, 4000]",
                        "dt": dt, "arrivals": "Poisson, seeded", "models": "cut from a seeded layered+anomaly 2D "
                        "model (1000x3000) and a seeded dipping-layer 3D model (256^3)"}}
 
@@ -893,6 +903,12 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream line")
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-rate", type=float, default=10.0, help="mean arrivals per second")
+    ap.add_argument("--serve-stride", type=int, default=1,
+                    help="served RTM requests: forward field stored (16-bit) and imaged every this many steps")
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0, help="device memory the serving plan may hold")
+    ap.add_argument("--serve-check-rtm", type=int, default=16, help="served RTM requests checked against FP64")
+    ap.add_argument("--serve-check-fwd", type=int, default=6, help="served 2D forward requests checked")
+    ap.add_argument("--serve-check-3d", type=int, default=3, help="served 3D requests checked")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps requested", file=sys.stderr)

@@ -424,6 +424,7 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
         b.stride = stride;
         b.amax = amax.as<unsigned>();
         b.pack = fsnap.as<__half>();
+        b.s2acc = S2.as<float2>();  // the illumination from the FP32 forward field
     } else {
         b.snap = reinterpret_cast<T*>(fsnap.as<double>());
         b.snap_t0 = 0;
@@ -435,7 +436,6 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
         r.img_f16 = fsnap.as<__half>();
         r.img_amax = amax.as<unsigned>();
         r.img_m2 = M.as<float2>();
-        r.img_s22 = S2.as<float2>();
     } else {
         r.img_f64 = fsnap.as<double>();
         r.img_m = M.as<double>();

@@ -57,8 +57,10 @@ struct alignas(16) ShotTail {
     int stride;
     unsigned* amax;
     __half* pack;
+    float2* s2acc;  // when set: at tau % stride == 0, s2acc += field^2 (compensated), from the FP32 field
     // RTM, reverse shot: at tau % stride == 0 image against the stored forward
-    // field, unscaled with the block maxima the forward shot recorded
+    // field, unscaled with the block maxima the forward shot recorded (the
+    // illumination sum only when img_s22 is set)
     const __half* img_f16;     // stored forward fields (as written by pack)
     const unsigned* img_amax;  // their block maxima
     float2* img_m2;         // compensated FP32 sums
@@ -70,10 +72,11 @@ struct alignas(16) ShotTail {
     // fields in one tile, the field P of the model it was added with (the
     // migration model of an RTM shot) and the residual D = Q - P, where Q is
     // the field of a second model (the true model).  D is stored dcol columns
-    // to the right of P in the same buffers ((v dt)^2 holds P's and, dcol
-    // columns on, the difference Q's minus P's); its band coefficients follow
-    // P's (b, b-1 of the second model, then b_Q - b_P) and its memory variables
-    // follow P's, zoff / xoff entries on.  rec_d receives D's row 0.
+    // to the right of P in the same buffers and P's low part (P = hi + lo)
+    // 2 dcol columns on ((v dt)^2 holds P's and, dcol columns on, the
+    // difference Q's minus P's); the band factors b_Q - b_P follow P's b and
+    // D's memory variables follow P's, zoff / xoff entries on.  rec_d receives
+    // D's row 0.
     T* rec_d;
     int dcol;
 };
@@ -109,7 +112,7 @@ inline unsigned sched_word(const ShotTail<T>& d) {
     if (d.snap) w |= kSchedSnap;
     if (d.img_f64) w |= kSchedImg64;
     if (d.amax) w |= kSchedAmax;
-    if (d.pack) w |= kSchedPack;
+    if (d.pack || d.s2acc) w |= kSchedPack;
     if (d.img_f16) w |= kSchedImg16;
     if (d.dcol > 0) w |= kSchedPair;
     return w | ((unsigned)(d.stride > 0 ? d.stride : 1) << kSchedStrideShift);

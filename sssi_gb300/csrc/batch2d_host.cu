@@ -196,10 +196,11 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
     S.origin = oz + (int64_t)L_ * ldp;
     const int64_t cols = nx + 2 * L_;
     // a residual pair keeps D in the same buffers, dcol columns to the right of
-    // P, past 8 zero columns: a tile box of D that starts left of D's padded
-    // grid (shifted tile columns start up to 8 columns early) reads zeros
+    // P, past 8 zero columns (a tile box of D that starts left of D's padded
+    // grid, as shifted tile columns do by up to 8 columns, reads zeros), and the
+    // low part of P another dcol columns on
     const int64_t dcol = pair ? cols + 8 : 0;
-    const int64_t cols_all = pair ? dcol + cols : cols;
+    const int64_t cols_all = pair ? 2 * dcol + cols : cols;
     const size_t pbytes = sizeof(T) * (size_t)ldp * (size_t)cols_all;
     const int64_t nzb = (int64_t)nB * nx, nxb = nz * 2 * (int64_t)nB;  // band sizes (pair: per field)
     for (auto& b : S.P) b.allocate(pbytes);
@@ -251,21 +252,15 @@ int Batch2d<T>::add_shot_in(int slot, const double* v, int like, int64_t nz, int
         band_coefficients<T>(bands.zb, bands.zbm1, zb, zbm1);
         band_coefficients<T>(bands.xb, bands.xbm1, xb, xbm1);
         if (pair) {
-            // D's (v dt)^2 column block holds (vq dt)^2 - (vp dt)^2; its band
-            // coefficients (b_Q, b_Q - 1, then b_Q - b_P) follow P's
+            // D's (v dt)^2 column block holds (vq dt)^2 - (vp dt)^2 and its band
+            // factors b_Q - b_P follow P's b: the residual uses P's rounded factors
+            // plus these exact differences
             const double* vqdev = on_device(vq, vqd);
             vdt2_diff_kernel<T><<<152 * 4, 256, 0, up()>>>(vdev, vqdev, nz, nx, dt,
                                                           S.vdt2.template as<T>() + S.origin + dcol * ldp, ldp);
             count_launch();
             SSSI_CHECK_CUDA(cudaGetLastError());
             const Bands2D bq = bands_of(vq);
-            std::vector<T> qzb, qzbm1, qxb, qxbm1;
-            band_coefficients<T>(bq.zb, bq.zbm1, qzb, qzbm1);
-            band_coefficients<T>(bq.xb, bq.xbm1, qxb, qxbm1);
-            zb.insert(zb.end(), qzb.begin(), qzb.end());
-            zbm1.insert(zbm1.end(), qzbm1.begin(), qzbm1.end());
-            xb.insert(xb.end(), qxb.begin(), qxb.end());
-            xbm1.insert(xbm1.end(), qxbm1.begin(), qxbm1.end());
             for (size_t k = 0; k < bq.zb.size(); ++k) zb.push_back(static_cast<T>(bq.zb[k] - bands.zb[k]));
             for (size_t k = 0; k < bq.xb.size(); ++k) xb.push_back(static_cast<T>(bq.xb[k] - bands.xb[k]));
         }

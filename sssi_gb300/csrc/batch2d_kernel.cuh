@@ -373,11 +373,15 @@ __device__ __noinline__ void band_stage1(const BatchConst<T>& bc, const ShotTail
 // Stage one of a residual pair's band tile (FP32, whole tiles): the same
 // units as band_stage1, for both fields of the pair at once.  P (box Pb) uses
 // the shot's band coefficients and memory variables; D = Q - P (box Pd) uses
-// the second model's coefficients b_Q, b_Q - 1 (zoff / xoff entries on) and
-// its own memory variables (zoff / xoff on), and takes the coupling term
-//     phi_D <- b_Q phi_D + (b_Q - 1) D+D + (b_Q - b_P) (phi_P + D+P)
-// with phi_P before its update, which is phi_Q - phi_P of the two fields'
-// own recursions written out.  A_P and A_D go to scratch and scratch_d.
+// the same coefficients b_P, b_P - 1, its own memory variables (zoff / xoff
+// entries on) and the difference db = b_Q - b_P (zoff / xoff entries after
+// b_P):
+//     phi_D <- b_P phi_D + (b_P - 1) D+D + db (phi_Q + D+Q),
+//     phi_Q = phi_P + phi_D,  D+Q = D+P + D+D  (phi before the update),
+// which is phi_Q - phi_P of the two fields' own recursions written out.  The
+// second model's factor is thus b_P + db exactly, wherever it multiplies, so
+// Q = P + D sees no rounding of its own model that P does not share.  A_P and
+// A_D go to scratch and scratch_d.
 template <typename T, int N, class Sh, int TX>
 __device__ __noinline__ void band_stage1_pair(const BatchConst<T>& bc, const ShotTail<T>& sh, int ph, const T* Pb,
                                               const T* Pd, int z0, int x0, bool bz, bool bx, T* scratch,
@@ -425,9 +429,10 @@ __device__ __noinline__ void band_stage1_pair(const BatchConst<T>& bc, const Sho
                         const int64_t q = (p - zb0) + (int64_t)j * nB;
                         M m = ldg_t(phi_in + q);
                         M md = ldg_t(phi_in + zoff + q);
-                        const T cpl = ldg_t(zb + 2 * zoff + q) * ((m.x + m.y) + d);
-                        m = mem_new(ldg_t(zb + q), ldg_t(zbm1 + q), m, d);
-                        md = comp_add(mem_new(ldg_t(zb + zoff + q), ldg_t(zbm1 + zoff + q), md, e), cpl);
+                        const T b = ldg_t(zb + q), bm = ldg_t(zbm1 + q);
+                        const T cpl = ldg_t(zb + zoff + q) * (((m.x + m.y) + d) + ((md.x + md.y) + e));
+                        m = mem_new(b, bm, m, d);
+                        md = comp_add(mem_new(b, bm, md, e), cpl);
                         d = mem_add(d, m);
                         e = mem_add(e, md);
                         if (r >= N && r < N + TZ) {
@@ -482,9 +487,10 @@ __device__ __noinline__ void band_stage1_pair(const BatchConst<T>& bc, const Sho
                         const int64_t q = qc + o;
                         M m = ldg_t(phi_in + q);
                         M md = ldg_t(phi_in + xoff + q);
-                        const T cpl = ldg_t(xb + 2 * xoff + q) * ((m.x + m.y) + d);
-                        m = mem_new(ldg_t(xb + q), ldg_t(xbm1 + q), m, d);
-                        md = comp_add(mem_new(ldg_t(xb + xoff + q), ldg_t(xbm1 + xoff + q), md, e), cpl);
+                        const T b = ldg_t(xb + q), bm = ldg_t(xbm1 + q);
+                        const T cpl = ldg_t(xb + xoff + q) * (((m.x + m.y) + d) + ((md.x + md.y) + e));
+                        m = mem_new(b, bm, m, d);
+                        md = comp_add(mem_new(b, bm, md, e), cpl);
                         d = mem_add(d, m);
                         e = mem_add(e, md);
                         if (cx >= N && cx < N + TX) {
@@ -546,6 +552,23 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
         for (int c = 0; c < ncol; ++c)
             for (int o = 0; o < nrow; ++o) amax_bits = max(amax_bits, __float_as_uint(fabsf(f32(pn.v[c][o]))));
     }
+    // illumination sum of the forward field, from the FP32 field itself
+    if (sh.s2acc && tau % stride == 0) {
+        float2* s2 = sh.s2acc;
+        for (int c = 0; c < ncol; ++c) {
+            const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
+            float2 a[4];
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (o < nrow) a[o] = s2[q0 + o];
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+                if (o < nrow) {
+                    const float f = f32(pn.v[c][o]);
+                    s2[q0 + o] = comp_add(a[o], __fmul_rn(f, f));
+                }
+        }
+    }
     // Imaging: the operands of a column's cells are loaded before any of its
     // sums is stored, so those cells share one round trip to memory.
     if constexpr (std::is_same<T, double>::value) {
@@ -597,8 +620,8 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
                 h[3] = __high2half(h23);
                 const float4 ma = *reinterpret_cast<const float4*>(im + q0);
                 const float4 mb = *reinterpret_cast<const float4*>(im + q0 + 2);
-                const float4 sa = *reinterpret_cast<const float4*>(is2 + q0);
-                const float4 sb = *reinterpret_cast<const float4*>(is2 + q0 + 2);
+                const float4 sa = is2 ? *reinterpret_cast<const float4*>(is2 + q0) : make_float4(0, 0, 0, 0);
+                const float4 sb = is2 ? *reinterpret_cast<const float4*>(is2 + q0 + 2) : make_float4(0, 0, 0, 0);
                 m[0] = make_float2(ma.x, ma.y);
                 m[1] = make_float2(ma.z, ma.w);
                 m[2] = make_float2(mb.x, mb.y);
@@ -617,8 +640,10 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
                 }
                 *reinterpret_cast<float4*>(im + q0) = make_float4(mn[0].x, mn[0].y, mn[1].x, mn[1].y);
                 *reinterpret_cast<float4*>(im + q0 + 2) = make_float4(mn[2].x, mn[2].y, mn[3].x, mn[3].y);
-                *reinterpret_cast<float4*>(is2 + q0) = make_float4(sn[0].x, sn[0].y, sn[1].x, sn[1].y);
-                *reinterpret_cast<float4*>(is2 + q0 + 2) = make_float4(sn[2].x, sn[2].y, sn[3].x, sn[3].y);
+                if (is2) {
+                    *reinterpret_cast<float4*>(is2 + q0) = make_float4(sn[0].x, sn[0].y, sn[1].x, sn[1].y);
+                    *reinterpret_cast<float4*>(is2 + q0 + 2) = make_float4(sn[2].x, sn[2].y, sn[3].x, sn[3].y);
+                }
                 continue;
             }
 #pragma unroll
@@ -626,7 +651,7 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
                 if (o < nrow) {
                     h[o] = f16[q0 + o];
                     m[o] = im[q0 + o];
-                    s2[o] = is2[q0 + o];
+                    if (is2) s2[o] = is2[q0 + o];
                 }
 #pragma unroll
             for (int o = 0; o < 4; ++o)
@@ -634,7 +659,7 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
                     const float f = __half2float(h[o]) * inv;
                     const float r = f32(pn.v[c][o]);
                     im[q0 + o] = comp_add(m[o], __fmul_rn(f, r));
-                    is2[q0 + o] = comp_add(s2[o], __fmul_rn(f, f));
+                    if (is2) is2[q0 + o] = comp_add(s2[o], __fmul_rn(f, f));
                 }
         }
     }
@@ -661,14 +686,41 @@ __device__ __forceinline__ void add_sources(const ShotTail<T>& sh, int tau, int 
 }
 
 // What the P pass of a residual pair hands to its D pass, per cell of the
-// thread: P's lap with the injected terms, and the coupling terms of the psi
-// recursions, (b_Q - b_P) (psi_P + D- A_P) with psi_P before its update.
+// thread: P's lap with the injected terms, and psi_P + D- A_P in the z and x
+// bands (psi_P before its update).
 template <typename T, int RX>
 struct PairIO {
     T lap[RX][4];
     T cz[RX][4];
     T cx[RX][4];
+    const T* lo;      // P's low parts, current and previous field (tiles in shared memory)
+    const T* lo_old;
 };
+
+// P of a residual pair is carried as hi + lo (two FP32 words): its rounding
+// noise would otherwise scatter off the model difference into D.  The
+// stencil reads hi only (the lo terms change lap by about an FP32 rounding);
+// the update 2P - P_old + w lap is done with error-free transformations.
+// Returns the new (hi, lo).
+__device__ __forceinline__ float2 pair_update_hi_lo(float hi, float lo, float hi_old, float lo_old, float w,
+                                                    float lap) {
+    // 2 hi - hi_old exactly as s + e (2 hi is exact)
+    const float a = __fmul_rn(2.0f, hi);
+    const float s = __fsub_rn(a, hi_old);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(-hi_old, bb));
+    // w lap exactly as p + pe
+    const float p = __fmul_rn(w, lap);
+    const float pe = fmaf(w, lap, -p);
+    // s + p as h + e2
+    const float h = __fadd_rn(s, p);
+    const float b2 = __fsub_rn(h, s);
+    const float e2 = __fadd_rn(__fsub_rn(s, __fsub_rn(h, b2)), __fsub_rn(p, b2));
+    // the low-order terms, then renormalise
+    const float l = __fadd_rn(__fadd_rn(__fadd_rn(e, pe), e2), __fsub_rn(__fmul_rn(2.0f, lo), lo_old));
+    const float hn = __fadd_rn(h, l);
+    return make_float2(hn, __fsub_rn(l, __fsub_rn(hn, h)));
+}
 
 // Roles of tile_cells: a single field, or the P / D pass of a residual pair.
 constexpr int kRoleSingle = 0, kRolePairP = 1, kRolePairD = 2;
@@ -677,13 +729,17 @@ constexpr int kRoleSingle = 0, kRolePairP = 1, kRolePairD = 2;
 // the tile is a band tile in z / x, its first derivatives are in `scratch`;
 // otherwise the composed stencil is used in that direction.
 //
-// Residual pairs run it twice per tile: kRolePairP advances P exactly as a
-// single field (its outputs are the shot's) and fills `io`; kRolePairD
-// advances D = Q - P from the D box (Pb), D's previous tile (Ob), P's
-// (v dt)^2 (Vb) and the difference of the two models' (v dt)^2 (Vd):
-//     D_new = wQ (zD + xD) + (wQ - wP) lap_P + 2 D - D_old,   wQ = wP + (wQ - wP),
-// with the second model's band coefficients, D's memory variables and the
-// coupling terms of `io` in the band tiles, and writes D's row 0 to rec_d.
+// Residual pairs run it twice per tile: kRolePairP advances P as a single
+// field (its outputs are the shot's) but carries it as hi + lo (the low part
+// 2 dcol columns on) and fills `io`; kRolePairD advances D = Q - P from the D
+// box (Pb), D's previous tile (Ob), P's (v dt)^2 (Vb) and the difference of
+// the two models' (v dt)^2 (Vd):
+//     D_new = wP lap_D + (wQ - wP) (lap_D + lap_P) + 2 D - D_old,
+// with P's band coefficients, D's memory variables and the coupling terms
+// db (psi_Q + D- A_Q) in the band tiles (db = b_Q - b_P, psi_Q = psi_P +
+// psi_D before the update), and writes D's row 0 to rec_d.  Every factor of
+// the second model is P's FP32 factor plus the exact difference, so the
+// rounding of the models is shared by P and Q and cancels in D.
 template <typename T, int N, class Sh, int RX, int kRole = kRoleSingle>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
@@ -761,11 +817,12 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         // a pair's D pass uses the second model's coefficients and D's own psi,
         // zoff entries after P's; both passes read b_Q - b_P 2 zoff entries on
         const int64_t zoff = (int64_t)nB * nx;
-        const T* zb = sh.zb + (kRole == kRolePairD ? zoff : 0);
-        const T* zbm1 = sh.zbm1 + (kRole == kRolePairD ? zoff : 0);
+        const T* zb = sh.zb;
+        const T* zbm1 = sh.zbm1;
         M* zpsi = sh.zpsi + (kRole == kRolePairD ? zoff : 0);
         bool in[RX][4];
         T pb[RX][4], pbm[RX][4];
+        T pdb[kRole == kRolePairD ? RX : 1][4];  // D pass: b_Q - b_P
         M ps[RX][4];
 #pragma unroll
         for (int c = 0; c < RX; ++c)
@@ -776,13 +833,13 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 pb[c][o] = T(0);
                 pbm[c][o] = T(0);
                 ps[c][o] = M{};
-                if constexpr (kRole == kRolePairP) io->cz[c][o] = T(0);
+                if constexpr (kRole == kRolePairD) pdb[c][o] = T(0);
                 if (in[c][o]) {
                     const int64_t q = (i - zb0) + (int64_t)j * nB;
                     pb[c][o] = ldg_t(zb + q);
                     pbm[c][o] = ldg_t(zbm1 + q);
                     ps[c][o] = zpsi[q];
-                    if constexpr (kRole == kRolePairP) io->cz[c][o] = ldg_t(sh.zb + 2 * zoff + q);
+                    if constexpr (kRole == kRolePairD) pdb[c][o] = ldg_t(zb + zoff + q);
                 }
             }
 #pragma unroll
@@ -805,9 +862,13 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 #pragma unroll
                 for (int k = 1; k < N; ++k) d = fma(bc.wz[k], w[o + N + k] - w[o + N - 1 - k], d);
                 if (in[c][o]) {
-                    if constexpr (kRole == kRolePairP) io->cz[c][o] *= mem_add(d, ps[c][o]);
+                    // a pair's P pass hands over psi_P + D- A_P (psi before the update);
+                    // the D pass adds db (psi_Q + D- A_Q) to D's recursion
+                    if constexpr (kRole == kRolePairP) io->cz[c][o] = mem_add(d, ps[c][o]);
+                    T cpl = T(0);
+                    if constexpr (kRole == kRolePairD) cpl = pdb[c][o] * (io->cz[c][o] + mem_add(d, ps[c][o]));
                     ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
-                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], io->cz[c][o]);
+                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], cpl);
                     d = mem_add(d, ps[c][o]);
                 }
                 lz.v[c][o] = d;
@@ -869,11 +930,12 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
     } else {
         // D- xA (+ psi): xA column c0+t of the scratch is global column j0-N+t
         const int64_t xoff = (int64_t)nz * 2 * nB;
-        const T* xb = sh.xb + (kRole == kRolePairD ? xoff : 0);
-        const T* xbm1 = sh.xbm1 + (kRole == kRolePairD ? xoff : 0);
+        const T* xb = sh.xb;
+        const T* xbm1 = sh.xbm1;
         M* xpsi = sh.xpsi + (kRole == kRolePairD ? xoff : 0);
         int64_t qo[RX];
         T pb[RX][4], pbm[RX][4];
+        T pdb[kRole == kRolePairD ? RX : 1][4];  // D pass: b_Q - b_P
         M ps[RX][4];
 #pragma unroll
         for (int c = 0; c < RX; ++c) {
@@ -884,13 +946,13 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
                 pb[c][o] = T(0);
                 pbm[c][o] = T(0);
                 ps[c][o] = M{};
-                if constexpr (kRole == kRolePairP) io->cx[c][o] = T(0);
+                if constexpr (kRole == kRolePairD) pdb[c][o] = T(0);
                 if (qo[c] >= 0 && i0 + o < nz) {
                     const int64_t q = qo[c] + i0 + o;
                     pb[c][o] = ldg_t(xb + q);
                     pbm[c][o] = ldg_t(xbm1 + q);
                     ps[c][o] = xpsi[q];
-                    if constexpr (kRole == kRolePairP) io->cx[c][o] = ldg_t(sh.xb + 2 * xoff + q);
+                    if constexpr (kRole == kRolePairD) pdb[c][o] = ldg_t(xb + xoff + q);
                 }
             }
         }
@@ -906,9 +968,11 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
 #pragma unroll
                 for (int k = 1; k < N; ++k) d = fma(bc.wx[k], a[c + N + k].v[o] - a[c + N - 1 - k].v[o], d);
                 if (qo[c] >= 0 && i0 + o < nz) {
-                    if constexpr (kRole == kRolePairP) io->cx[c][o] *= mem_add(d, ps[c][o]);
+                    if constexpr (kRole == kRolePairP) io->cx[c][o] = mem_add(d, ps[c][o]);
+                    T cpl = T(0);
+                    if constexpr (kRole == kRolePairD) cpl = pdb[c][o] * (io->cx[c][o] + mem_add(d, ps[c][o]));
                     ps[c][o] = mem_new(pb[c][o], pbm[c][o], ps[c][o], d);
-                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], io->cx[c][o]);
+                    if constexpr (kRole == kRolePairD) ps[c][o] = comp_add(ps[c][o], cpl);
                     d = mem_add(d, ps[c][o]);
                 }
                 lx.v[c][o] = d;
@@ -945,16 +1009,19 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
             for (int o = 0; o < 4; ++o) lap[o] = lz.v[c][o] + lx.v[c][o];
         }
         if constexpr (kRole == kRolePairD) {
-            // D_new = wQ lap_D + (wQ - wP) lap_P + 2 D - D_old
+            // D_new = wP lap_D + (wQ - wP) (lap_D + lap_P) + 2 D - D_old, lap_P with
+            // the injected terms: Q's factor is wP + (wQ - wP) exactly
             const V4<T> vd = ld4(Vd + (c0 + c) * TZ + r0);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc.v[c][2 * h], pc.v[c][2 * h + 1]),
                                             make_float2(-po.v[2 * h], -po.v[2 * h + 1]));
                 const float2 dw = make_float2(vd.v[2 * h], vd.v[2 * h + 1]);
-                const float2 u = __ffma2_rn(dw, make_float2(io->lap[c][2 * h], io->lap[c][2 * h + 1]), t);
-                const float2 wq = __fadd2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]), dw);
-                const float2 r = __ffma2_rn(wq, make_float2(lap[2 * h], lap[2 * h + 1]), u);
+                const float2 lq = __fadd2_rn(make_float2(lap[2 * h], lap[2 * h + 1]),
+                                             make_float2(io->lap[c][2 * h], io->lap[c][2 * h + 1]));
+                const float2 u = __ffma2_rn(dw, lq, t);
+                const float2 r = __ffma2_rn(make_float2(vv.v[2 * h], vv.v[2 * h + 1]),
+                                            make_float2(lap[2 * h], lap[2 * h + 1]), u);
                 pn.v[c][2 * h] = r.x;
                 pn.v[c][2 * h + 1] = r.y;
             }
@@ -963,8 +1030,24 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
             if constexpr (kRole == kRolePairP) {
 #pragma unroll
                 for (int o = 0; o < 4; ++o) io->lap[c][o] = lap[o];
-            }
-            if constexpr (kPacked<T>) {
+                const V4<T> lc = ld4(io->lo + (c0 + c) * TZ + r0);
+                const V4<T> lold = ld4(io->lo_old + (c0 + c) * TZ + r0);
+                T lnew[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    const float2 r = pair_update_hi_lo(pc.v[c][o], lc.v[o], po.v[o], lold.v[o], vv.v[o], lap[o]);
+                    pn.v[c][o] = r.x;
+                    lnew[o] = r.y;
+                }
+                T* dlo = Pnew + 2 * (int64_t)sh.dcol * sh.ldp + i0 + (int64_t)j * sh.ldp;
+                if (full_rows) {
+                    st4(dlo, lnew);
+                } else {
+#pragma unroll
+                    for (int o = 0; o < 4; ++o)
+                        if (i0 + o < nz) dlo[o] = lnew[o];
+                }
+            } else if constexpr (kPacked<T>) {
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc.v[c][2 * h], pc.v[c][2 * h + 1]),
@@ -1008,7 +1091,7 @@ __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned 
         const int stride = (int)(sched >> kSchedStrideShift);
         const bool on_stride = tau % stride == 0;
         if ((sched & kSchedAmax) && on_stride) f |= kAmax;
-        rare |= ((sched & kSchedPack) && tau >= 1 && (tau - 1) % stride == 0) ||
+        rare |= ((sched & kSchedPack) && ((tau >= 1 && (tau - 1) % stride == 0) || on_stride)) ||
                 ((sched & (kSchedAmax | kSchedImg16)) && on_stride);
     }
     if (rare) f |= kRare;
@@ -1017,8 +1100,9 @@ __device__ __forceinline__ unsigned tile_flags(unsigned sched, int z0, unsigned 
 
 // Shared-memory layout of one pipeline stage (byte offsets, 128-aligned).
 // kPair: the stage also holds a residual pair's D box (kP2), D's previous
-// tile (kO2) and the (v dt)^2 difference (kV2), and the band scratch is
-// doubled (P's, then D's).
+// tile (kO2), the (v dt)^2 difference (kV2) and the low parts of P's current
+// and previous tiles (kL, kL2), and the band scratch is doubled (P's, then
+// D's).
 template <typename T, int N, class Sh, bool kPair = false>
 struct StageLayout {
     using S = Sh;
@@ -1035,11 +1119,13 @@ struct StageLayout {
     static constexpr unsigned kO2 = kO + (kPair ? kTileA : 0);
     static constexpr unsigned kV = kO2 + kTileA;
     static constexpr unsigned kV2 = kV + (kPair ? kTileA : 0);
-    static constexpr unsigned kTail = kV2 + kTileA;
+    static constexpr unsigned kL = kV2 + kTileA;               // pairs: P's low part, current field
+    static constexpr unsigned kL2 = kL + (kPair ? kTileA : 0);  // pairs: P's low part, previous field
+    static constexpr unsigned kTail = kPair ? kL2 + kTileA : kL;
     static constexpr unsigned kInfo = kTail + (sizeof(ShotTail<T>) + 127) / 128 * 128;
     static constexpr unsigned kStage = kInfo + 128;  // TileInfo (32 bytes) rounded up
     static constexpr unsigned kTx = kPBoxBytes + 2 * kTileBytes;          // bytes the TMA copies deliver
-    static constexpr unsigned kTxPair = 2 * kPBoxBytes + 4 * kTileBytes;  // the same for a residual pair
+    static constexpr unsigned kTxPair = 2 * kPBoxBytes + 6 * kTileBytes;  // the same for a residual pair
     static constexpr int kStages = 2;                                     // tiles in the copy pipeline
     static constexpr unsigned kBar = kStages * kStage;                    // one mbarrier per stage
     static constexpr unsigned kScratch = kBar + 128;                      // band scratch
@@ -1112,6 +1198,8 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
                 tma_load_2d(st + G::kP2, &shots[k].tm_box[V][cur], &bar[s], g.oz + z0 - HZ, x0 + g.dcol);
                 tma_load_2d(st + G::kO2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], g.oz + z0, x0 + L + g.dcol);
                 tma_load_2d(st + G::kV2, &shots[k].tm_v[V], &bar[s], g.oz + z0, x0 + L + g.dcol);
+                tma_load_2d(st + G::kL, &shots[k].tm_tile[V][cur], &bar[s], g.oz + z0, x0 + L + 2 * g.dcol);
+                tma_load_2d(st + G::kL2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], g.oz + z0, x0 + L + 2 * g.dcol);
             }
         }
     };
@@ -1167,6 +1255,8 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
                     tma_load_2d(st + G::kP2, &shots[k].tm_box[V][cur], &bar[s], oz + z0 - HZ, x0 + dcol);
                     tma_load_2d(st + G::kO2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], oz + z0, x0 + L + dcol);
                     tma_load_2d(st + G::kV2, &shots[k].tm_v[V], &bar[s], oz + z0, x0 + L + dcol);
+                    tma_load_2d(st + G::kL, &shots[k].tm_tile[V][cur], &bar[s], oz + z0, x0 + L + 2 * dcol);
+                    tma_load_2d(st + G::kL2, &shots[k].tm_tile[V][cur ^ 1], &bar[s], oz + z0, x0 + L + 2 * dcol);
                 }
             }
         }
@@ -1258,6 +1348,8 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
                         }
                         if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx) {
                             PairIO<T, RX> io;
+                            io.lo = reinterpret_cast<const T*>(st + G::kL);
+                            io.lo_old = reinterpret_cast<const T*>(st + G::kL2);
                             tile_cells<T, N, Sh, RX, kRolePairP>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags,
                                                                  scratch, amax_bits, &io);
                             tile_cells<T, N, Sh, RX, kRolePairD>(bc, sh, ti, Pd, Od, Vb, z0, x0, r0, c0, ti.flags,

@@ -276,6 +276,7 @@ class Engine final : public EngineBase {
                 b.stride = stride;
                 b.amax = u->amax.template as<unsigned>();
                 b.pack = u->fsnap.template as<__half>();
+                b.s2acc = u->S2.template as<float2>();  // the illumination from the FP32 forward field
             } else {
                 b.snap = reinterpret_cast<T*>(u->fsnap.template as<double>());
                 b.snap_t0 = 0;
@@ -287,7 +288,6 @@ class Engine final : public EngineBase {
                 rr.img_f16 = u->fsnap.template as<__half>();
                 rr.img_amax = u->amax.template as<unsigned>();
                 rr.img_m2 = u->Mb.template as<float2>();
-                rr.img_s22 = u->S2.template as<float2>();
             } else {
                 rr.img_f64 = u->fsnap.template as<double>();
                 rr.img_m = u->Mb.template as<double>();

@@ -80,8 +80,8 @@ def test_rtm_fp32_full_size(gpu):
 
 def test_plan_rtm_uniform_top_mix(gpu, oracle_mod):
     """FP32 plan: two uniform-top-layer RTM shots of different sizes mixed with
-    forward shots.  Each image equals its single-shot result exactly and is
-    within 1e-4 of FP64."""
+    forward shots, the forward field stored and imaged every step.  Each image
+    equals its single-shot result exactly and is within 1e-4 of FP64."""
     S = gpu
     shots = []
     for k, (nz0, nx0, top, nt) in enumerate([(140, 220, 80, 1200), (120, 300, 70, 1000)]):
@@ -90,7 +90,7 @@ def test_plan_rtm_uniform_top_mix(gpu, oracle_mod):
         shots.append((V, VS, w, V.shape[1] // 2 + 7 * k))
     with S.Plan(4, 10.0, 10.0, mode="fp32", steps_per_round=48) as plan:
         tf = plan.submit_fwd2d(shots[0][0], 700, [2], [40], oracle_mod.ricker(20.0, 700, 8e-4)[None, :], 20, 8e-4)
-        ts = [plan.submit_rtm2d(V, VS, w, 0, ix, 20, 8e-4, epsilon=1e-3, snap_stride=4, want_data=True)
+        ts = [plan.submit_rtm2d(V, VS, w, 0, ix, 20, 8e-4, epsilon=1e-3, snap_stride=1, want_data=True)
               for (V, VS, w, ix) in shots]
         tg = plan.submit_fwd2d(shots[1][0], 900, [0], [100], oracle_mod.ricker(20.0, 900, 8e-4)[None, :], 20, 8e-4)
         outs = [plan.wait(t) for t in ts]
@@ -98,7 +98,7 @@ def test_plan_rtm_uniform_top_mix(gpu, oracle_mod):
         plan.wait(tg)
     for (V, VS, w, ix), o in zip(shots, outs):
         img, dtr, _ = S.rtmTimeCpmlFor2dAw(V, VS, w, 0, ix, 4, 20, 10.0, 10.0, 8e-4, epsilon=1e-3, mode="fp32",
-                                           snap_stride=4, want_data=True)
+                                           snap_stride=1, want_data=True)
         assert np.array_equal(o["image"], img)
         assert np.array_equal(o["data"], dtr)
         ref = S.rtmTimeCpmlFor2dAw(V, VS, w, 0, ix, 4, 20, 10.0, 10.0, 8e-4, epsilon=1e-3, mode="fp64")
