@@ -400,11 +400,13 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     delta.allocate(sizeof(T) * ndata);
     const int64_t nsnap = (nt + stride - 1) / stride;
     const int64_t nblk = ((nz + 31) / 32) * ((nx + 31) / 32);  // FP16 scale blocks of 32 x 32 cells
-    DeviceBuffer fsnap, amax, M, S2;
+    DeviceBuffer fsnap, amax, perr, M, S2;
     if (kF16) {
         fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
         amax.allocate(sizeof(unsigned) * nblk * std::max<int64_t>(nsnap, 1));
         amax.zero(s);
+        perr.allocate(sizeof(float) * n);
+        perr.zero(s);
     } else {
         fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
     }
@@ -425,6 +427,7 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
         b.amax = amax.as<unsigned>();
         b.pack = fsnap.as<__half>();
         b.s2acc = S2.as<float2>();  // the illumination from the FP32 forward field
+        b.perr = perr.as<float>();
     } else {
         b.snap = reinterpret_cast<T*>(fsnap.as<double>());
         b.snap_t0 = 0;
@@ -451,7 +454,7 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     if (kF16 && nt >= 1 && (nt - 1) % stride == 0) {
         const int64_t k = (nt - 1) / stride;
         launch_pack_f16(reinterpret_cast<const float*>(B.current_field(kB)), B.ldp(kB), (int)nz, (int)nx,
-                        amax.as<unsigned>() + k * nblk, fsnap.as<__half>() + k * n, s);
+                        amax.as<unsigned>() + k * nblk, fsnap.as<__half>() + k * n, perr.as<float>(), s);
     }
     // dataTrue - dataSmooth (mainRtmTimeCpmlFor2dAw.m:252), injected in reverse
     // time: D's row 0 for the residual pair, else the difference of the two

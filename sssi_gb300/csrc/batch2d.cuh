@@ -57,6 +57,7 @@ struct alignas(16) ShotTail {
     int stride;
     unsigned* amax;
     __half* pack;
+    float* perr;    // with pack: each cell's FP16 rounding error, added to its next stored value (nz x nx)
     float2* s2acc;  // when set: at tau % stride == 0, s2acc += field^2 (compensated), from the FP32 field
     // RTM, reverse shot: at tau % stride == 0 image against the stored forward
     // field, unscaled with the block maxima the forward shot recorded (the

@@ -529,22 +529,41 @@ __device__ __noinline__ unsigned rare_outputs(const ShotTail<T>& sh, const TileI
     const int64_t blk = (i0 >> 5) + (int64_t)(j0 >> 5) * ((nz + 31) >> 5);
     const int64_t nblk = (int64_t)((nz + 31) >> 5) * ((nx + 31) >> 5);
     if (sh.pack && tau >= 1 && (tau - 1) % stride == 0) {
+        // FP16 with error feedback: the cell's rounding error of the previous
+        // stored step is added before rounding and the new one kept (FP32), so
+        // the rounding errors of consecutive snapshots cancel in the imaging sum
         const int k = (tau - 1) / stride;
         const float scale = fp16_scale_from_amax(sh.amax[k * nblk + blk]);
+        const float inv = 1.0f / scale;  // a power of two: exact
         __half* pack = sh.pack + (int64_t)k * ncell;
+        float* perr = sh.perr;
         for (int c = 0; c < ncol; ++c) {
             const int64_t q0 = i0 + (int64_t)(j0 + c) * nz;
-            if (nrow == 4 && (q0 & 3) == 0 && (ncell & 3) == 0) {  // four halves in one 8-byte store
-                const __half2 lo = __halves2half2(__float2half_rn(f32(pc.v[c][0]) * scale),
-                                                  __float2half_rn(f32(pc.v[c][1]) * scale));
-                const __half2 hi = __halves2half2(__float2half_rn(f32(pc.v[c][2]) * scale),
-                                                  __float2half_rn(f32(pc.v[c][3]) * scale));
+            if (nrow == 4 && (q0 & 3) == 0 && (ncell & 3) == 0) {  // four cells: 8- and 16-byte accesses
+                float4 e = *reinterpret_cast<const float4*>(perr + q0);
+                const float x[4] = {__fadd_rn(f32(pc.v[c][0]), e.x), __fadd_rn(f32(pc.v[c][1]), e.y),
+                                    __fadd_rn(f32(pc.v[c][2]), e.z), __fadd_rn(f32(pc.v[c][3]), e.w)};
+                __half h[4];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) h[o] = __float2half_rn(__fmul_rn(x[o], scale));
+                e = make_float4(__fsub_rn(x[0], __fmul_rn(__half2float(h[0]), inv)),
+                                __fsub_rn(x[1], __fmul_rn(__half2float(h[1]), inv)),
+                                __fsub_rn(x[2], __fmul_rn(__half2float(h[2]), inv)),
+                                __fsub_rn(x[3], __fmul_rn(__half2float(h[3]), inv)));
+                *reinterpret_cast<float4*>(perr + q0) = e;
+                const __half2 lo = __halves2half2(h[0], h[1]);
+                const __half2 hi = __halves2half2(h[2], h[3]);
                 uint2 w;
                 w.x = *reinterpret_cast<const unsigned*>(&lo);
                 w.y = *reinterpret_cast<const unsigned*>(&hi);
                 *reinterpret_cast<uint2*>(pack + q0) = w;
             } else {
-                for (int o = 0; o < nrow; ++o) pack[q0 + o] = __float2half_rn(f32(pc.v[c][o]) * scale);
+                for (int o = 0; o < nrow; ++o) {
+                    const float x = __fadd_rn(f32(pc.v[c][o]), perr[q0 + o]);
+                    const __half h = __float2half_rn(__fmul_rn(x, scale));
+                    perr[q0 + o] = __fsub_rn(x, __fmul_rn(__half2float(h), inv));
+                    pack[q0 + o] = h;
+                }
             }
         }
     }

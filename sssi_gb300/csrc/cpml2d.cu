@@ -270,14 +270,20 @@ void launch_dispatch(const Step2D<T, TA>& p, int N, int bz, cudaStream_t stream)
 }
 
 // FP16 copy of a padded FP32 field, one power-of-two scale per 32 x 32 block
-// (the block maxima amax[bz + bx * nbz], nbz = ceil(nz / 32)).
-__global__ void pack_f16_kernel(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out) {
+// (the block maxima amax[bz + bx * nbz], nbz = ceil(nz / 32)), with the error
+// feedback of the batched step: err (nz x nx) is added before rounding and
+// receives the new rounding error.
+__global__ void pack_f16_kernel(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
+                                float* err) {
     const int64_t n = (int64_t)nz * nx;
     const int nbz = (nz + 31) >> 5;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = q % nz, j = q / nz;
         const float scale = fp16_scale_from_amax(amax[(i >> 5) + (j >> 5) * nbz]);
-        out[q] = __float2half_rn(P[i + j * ldp] * scale);
+        const float x = __fadd_rn(P[i + j * ldp], err[q]);
+        const __half h = __float2half_rn(__fmul_rn(x, scale));
+        err[q] = __fsub_rn(x, __fmul_rn(__half2float(h), 1.0f / scale));
+        out[q] = h;
     }
 }
 
@@ -329,9 +335,9 @@ cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool stric
     return cudaGetLastError();
 }
 
-void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
+void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out, float* err,
                      cudaStream_t stream) {
-    pack_f16_kernel<<<152 * 4, 256, 0, stream>>>(P, ldp, nz, nx, amax, out);
+    pack_f16_kernel<<<152 * 4, 256, 0, stream>>>(P, ldp, nz, nx, amax, out, err);
     count_launch();
     SSSI_CHECK_CUDA(cudaGetLastError());
 }

@@ -149,8 +149,9 @@ cudaError_t launch_cpml2d_step_nothrow(const Step2D<T, TA>& p, int N, bool stric
 // Packs field P (padded, interior origin) into FP16 with the scale from *amax.
 // FP16 copy of the padded FP32 field P (nz x nx interior, column pitch ldp)
 // with one power-of-two scale per 32 x 32 block, from the block maxima amax
-// (index bz + bx * ceil(nz / 32)).
-void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out,
+// (index bz + bx * ceil(nz / 32)); err (nz x nx) carries each cell's rounding
+// error from one stored step to the next.
+void launch_pack_f16(const float* P, int64_t ldp, int nz, int nx, const unsigned* amax, __half* out, float* err,
                      cudaStream_t stream);
 
 }  // namespace sssi

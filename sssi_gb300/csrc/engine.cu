@@ -135,7 +135,7 @@ class Engine final : public EngineBase {
         int kA = -1, kB = -1, kR = -1;
         int64_t s0 = 0;
         int phase = 1;
-        DeviceBuffer wav, recA, recB, delta, fsnap, amax, Mb, S2, img;
+        DeviceBuffer wav, recA, recB, delta, fsnap, amax, perr, Mb, S2, img;
         std::unique_ptr<Prop3d<T>> p3;
         int64_t done3 = 0;
         cudaStream_t s3 = nullptr;  // 3D: the propagation's own stream (runs beside the 2D batch)
@@ -178,7 +178,7 @@ class Engine final : public EngineBase {
             const size_t n = (size_t)(nz * nx);
             const int stride = kF16 ? (r.d.snap_stride > 0 ? r.d.snap_stride : 4) : 1;
             const size_t nsnap = (size_t)((nt + stride - 1) / stride);
-            const size_t snaps = kF16 ? 2 * n * nsnap + 4 * (size_t)nblocks(nz, nx) * nsnap : 8 * n * (size_t)nt;
+            const size_t snaps = kF16 ? 2 * n * nsnap + 4 * (size_t)nblocks(nz, nx) * nsnap + 4 * n : 8 * n * (size_t)nt;
             return 3 * shot2d() + 3 * ts * (size_t)(nx * nt) + snaps + 16 * n + wav;
         }
         const int64_t vol = (nz + 2 * HZ + 3) * (nx + 2 * L) * (ny + 2 * L);
@@ -263,6 +263,8 @@ class Engine final : public EngineBase {
                 u->fsnap.allocate(sizeof(__half) * n * std::max<int64_t>(nsnap, 1));
                 u->amax.allocate(sizeof(unsigned) * nblocks(nz, nx) * std::max<int64_t>(nsnap, 1));
                 u->amax.zero(up_);
+                u->perr.allocate(sizeof(float) * n);
+                u->perr.zero(up_);
                 u->S2.zero(up_);
             } else {
                 u->fsnap.allocate(sizeof(double) * n * std::max<int64_t>(nt, 1));
@@ -277,6 +279,7 @@ class Engine final : public EngineBase {
                 b.amax = u->amax.template as<unsigned>();
                 b.pack = u->fsnap.template as<__half>();
                 b.s2acc = u->S2.template as<float2>();  // the illumination from the FP32 forward field
+                b.perr = u->perr.template as<float>();
             } else {
                 b.snap = reinterpret_cast<T*>(u->fsnap.template as<double>());
                 b.snap_t0 = 0;
@@ -443,7 +446,7 @@ class Engine final : public EngineBase {
                     const int64_t k = (nt - 1) / stride;
                     launch_pack_f16(reinterpret_cast<const float*>(B_.current_field(u.kB)), B_.ldp(u.kB), (int)nz,
                                     (int)nx, u.amax.template as<unsigned>() + k * nblocks(nz, nx),
-                                    u.fsnap.template as<__half>() + k * n, s_);
+                                    u.fsnap.template as<__half>() + k * n, u.perr.template as<float>(), s_);
                 }
                 if (nt > 0) {
                     // the reverse source dataTrue - dataSmooth: the residual's row 0

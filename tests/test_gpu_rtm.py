@@ -84,12 +84,14 @@ def test_plan_rtm_uniform_top_mix(gpu, oracle_mod):
     equals its single-shot result exactly and is within 1e-4 of FP64."""
     S = gpu
     shots = []
-    for k, (nz0, nx0, top, nt) in enumerate([(140, 220, 80, 1200), (120, 300, 70, 1000)]):
+    # records long enough to hold each model's first reflection (two-way time of
+    # the top layer at 1700 m/s: about 1180 and 1030 steps)
+    for k, (nz0, nx0, top, nt) in enumerate([(140, 220, 80, 1800), (120, 300, 70, 1500)]):
         V, VS = uniform_top_models(nz0, nx0, top, [1700.0, 2500.0, 3100.0], seed=10 + k)
         w = oracle_mod.ricker(15.0, nt, 8e-4)
         shots.append((V, VS, w, V.shape[1] // 2 + 7 * k))
     with S.Plan(4, 10.0, 10.0, mode="fp32", steps_per_round=48) as plan:
-        tf = plan.submit_fwd2d(shots[0][0], 700, [2], [40], oracle_mod.ricker(20.0, 700, 8e-4)[None, :], 20, 8e-4)
+        tf = plan.submit_fwd2d(shots[0][0], 900, [2], [40], oracle_mod.ricker(20.0, 900, 8e-4)[None, :], 20, 8e-4)
         ts = [plan.submit_rtm2d(V, VS, w, 0, ix, 20, 8e-4, epsilon=1e-3, snap_stride=1, want_data=True)
               for (V, VS, w, ix) in shots]
         tg = plan.submit_fwd2d(shots[1][0], 900, [0], [100], oracle_mod.ricker(20.0, 900, 8e-4)[None, :], 20, 8e-4)
