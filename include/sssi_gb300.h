@@ -35,7 +35,8 @@ extern "C" {
 #define SSSI_ERR_NOMEM 3    /* device or host allocation failed */
 #define SSSI_ERR_UNSTABLE 4 /* the wavefield became non-finite (CFL violated) */
 #define SSSI_ERR_BUSY 5     /* admission refused: not enough device memory now */
-#define SSSI_ERR_INTERNAL 6
+#define SSSI_ERR_INTERNAL 6  /* e.g. a step's tile copy did not arrive within the wait limit */
+#define SSSI_ERR_CANCELLED 7 /* the shot was cancelled (sssi_cancel) */
 
 /* ---- arithmetic modes ---- */
 /* FP64 with the reference's rounding sequence (no fused multiply-add,
@@ -240,12 +241,33 @@ int sssi_plan_destroy(sssi_plan *plan);
  * queues it; outputs are written when the shot completes, so data / image
  * must stay valid until then.  *ticket identifies the shot. */
 int sssi_shot_submit(sssi_plan *plan, const sssi_shot_desc *shot, int64_t *ticket);
+/* Cancels a shot: a queued shot leaves the queue at once, a running one at
+ * the plan's next round boundary (its device memory then returns to the
+ * budget); either ends SSSI_SHOT_FAILED with status SSSI_ERR_CANCELLED and
+ * writes no outputs.  Finished shots are left as they are.  No counterpart in
+ * the reference (its shot loops run to completion). */
+int sssi_cancel(sssi_plan *plan, int64_t ticket);
 /* Current state of a shot (never blocks). */
 int sssi_poll(sssi_plan *plan, int64_t ticket, sssi_shot_info *info);
 /* Blocks until the shot is done or failed; returns its status (message in
- * sssi_last_error()).  info may be NULL. */
+ * sssi_last_error()).  info may be NULL.  A shot whose receiver row becomes
+ * non-finite (a time step beyond the stability limit) fails alone with
+ * SSSI_ERR_UNSTABLE; a step whose tile copy does not arrive in time fails
+ * every 2D shot that was advancing in it (SSSI_ERR_INTERNAL), and the plan
+ * goes on with the next ones. */
 int sssi_wait(sssi_plan *plan, int64_t ticket, sssi_shot_info *info);
 int sssi_plan_stats_get(sssi_plan *plan, sssi_plan_stats *stats);
+
+/* ---- test support ---- */
+
+/* No counterpart in the reference: a test knob of the batched 2D step.  At
+ * batch step `step` (counted from 0 in every call or plan that starts after
+ * this one) the first block withholds the tile copies of its first tile, so
+ * that tile's bounded wait runs out after `wait_limit` polls (0: the default
+ * limit) and the failure path is taken: the call returns SSSI_ERR_INTERNAL, a
+ * plan fails the shots of that step, and the device stays usable.  step < 0
+ * turns the knob off. */
+int sssi_debug_withhold_copy(int step, unsigned wait_limit);
 
 /* ---- forward modelling without any allocation ---- */
 

@@ -9,6 +9,7 @@ from .api import (  # noqa: F401
     MODES,
     Plan,
     dampPml,
+    debug_withhold_copy,
     dCoef,
     enable_timing,
     last_timing,

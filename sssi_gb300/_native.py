@@ -57,6 +57,8 @@ SIGNATURES = {
     "sssi_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "sssi_shot_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ShotDesc), ctypes.POINTER(c_i64)]),
     "sssi_poll": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
+    "sssi_cancel": (ctypes.c_int, [ctypes.c_void_p, c_i64]),
+    "sssi_debug_withhold_copy": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint]),
     "sssi_wait": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
     "sssi_plan_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlanStats)]),
     "sssi_last_error": (ctypes.c_char_p, []),

@@ -240,6 +240,14 @@ def measure_fp64_rate() -> float:
     return r.value
 
 
+def debug_withhold_copy(step: int, wait_limit: int = 0) -> None:
+    """Test knob: at batch step ``step`` of later calls and plans, the first
+    block of the batched 2D step withholds one tile's copies, so its bounded
+    wait runs out (after ``wait_limit`` polls) and the call fails cleanly;
+    ``step < 0`` turns it off."""
+    check(lib().sssi_debug_withhold_copy(int(step), int(wait_limit)))
+
+
 def release_cache() -> None:
     check(lib().sssi_release_cache())
 
@@ -362,6 +370,10 @@ class Plan:
         info = ShotInfo()
         check(lib().sssi_poll(self._h, ticket.id, ctypes.byref(info)))
         return self._info(info)
+
+    def cancel(self, ticket):
+        """Cancels a queued or running shot (it ends failed, status SSSI_ERR_CANCELLED)."""
+        check(lib().sssi_cancel(self._h, ticket.id))
 
     def wait(self, ticket):
         """Blocks until the shot completes; returns its outputs (raises on failure)."""

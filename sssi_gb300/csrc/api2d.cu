@@ -1,5 +1,6 @@
 // C-ABI entry points of the 2D propagators and the RTM shot.
 #include <algorithm>
+#include <initializer_list>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -272,6 +273,17 @@ void rtm2d_strict(const double* v, const double* vs, int64_t nz, int64_t nx, int
 }
 
 // ================================================================ batched engine
+// Fails the call with SSSI_ERR_UNSTABLE when a step found a non-finite value on
+// the receiver row of one of the shots ks.
+template <typename T>
+void require_stable(Batch2d<T>& B, std::initializer_list<int> ks) {
+    const std::vector<int> st = B.statuses();
+    for (int k : ks)
+        SSSI_REQUIRE(k < 0 || k >= (int)st.size() || st[k] != SSSI_ERR_UNSTABLE, SSSI_ERR_UNSTABLE,
+                     "the wavefield became non-finite (is dt beyond the stability limit of the grid and the "
+                     "velocities?)");
+}
+
 // Dense copy of a padded field (device) for the reverse pass's model output.
 template <typename T>
 void download_field(const T* field, int64_t ldp, int L, int64_t nz, int64_t nx, double* model, cudaStream_t s) {
@@ -317,6 +329,7 @@ void bfwd2d(const double* v, const double* source, int64_t nz, int64_t nx, int64
     }
     timing_end(s);
     B.check_errors();
+    require_stable(B, {k});
     rec.download(data, s);
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
@@ -347,6 +360,7 @@ void brvs2d(const double* v, const double* data, int64_t nz, int64_t nx, int64_t
     }
     timing_end(s);
     B.check_errors();
+    require_stable(B, {k});
     // the reference returns the field held as "old" after its final rotation:
     // the result of the step before the last one
     if (model) {
@@ -484,6 +498,7 @@ void brtm2d(const double* v, const double* vs, int64_t nz, int64_t nx, int64_t n
     SSSI_CHECK_CUDA(cudaGetLastError());
     timing_end(s);
     B.check_errors();
+    require_stable(B, {kA, kB, kR});
     dimg.download(image, (size_t)n, s);
     if (dtrue.ptr) dtrue.download(data_true, s);
     if (dsmooth.ptr) dsmooth.download(data_smooth, s);

@@ -80,6 +80,9 @@ struct alignas(16) ShotTail {
     // D's row 0.
     T* rec_d;
     int dcol;
+    // the shot's status word: the step sets it to SSSI_ERR_UNSTABLE when a
+    // value of row 0 (the receiver row) is not finite
+    int* status;
 };
 
 // Per-tile work flags.  kBandZ, kBandX and point sources inside the tile do
@@ -142,6 +145,9 @@ struct alignas(128) ShotDesc {
     ShotTail<T> s;
 };
 
+// Polls of a tile copy's barrier before a block gives up and reports failure.
+constexpr unsigned kDefaultWaitLimit = 1u << 24;
+
 template <typename T>
 struct BatchConst {
     T az[16], ax[16];  // composed second-derivative coefficients a_0 .. a_l
@@ -154,6 +160,8 @@ struct BatchConst {
     const int* step_base;  // the launch computes batch step *step_base + step_offset
     int step_offset;
     int* err;              // set when a TMA copy does not arrive in time
+    unsigned wait_limit;   // polls of a copy's barrier before the block gives up
+    int debug_step;        // test knob (-1: off): at this batch step block 0 withholds its first tile's copies
 };
 
 // Device state of a batch of shots sharing the order and the grid spacing.
@@ -204,7 +212,17 @@ class Batch2d {
     // The schedule must be current: finalize() after any add, remove, enable
     // or point-source change.
     void run(int nsteps);
+    // Throws SSSI_ERR_INTERNAL (and clears the flag) when a step's tile copy did
+    // not arrive within the wait limit.
     void check_errors();
+    // Status of shot k set by the steps (SSSI_OK or SSSI_ERR_UNSTABLE), read
+    // after the stream has run; clear_status resets it.
+    std::vector<int> statuses();
+    void clear_status(int k);
+    // Test knob: at batch step `step` block 0 withholds its first tile's copies,
+    // and every barrier wait gives up after `wait_limit` polls (step < 0: off,
+    // the default limit).
+    void set_debug(int step, unsigned wait_limit);
     ~Batch2d();
     Batch2d(const Batch2d&) = delete;
     Batch2d& operator=(const Batch2d&) = delete;
@@ -234,6 +252,7 @@ class Batch2d {
     int add_shot_in(int slot, const double* v, int like, int64_t nz, int64_t nx, int nB, double dt, int nt,
                     int t_start, bool reverse, const double* vq = nullptr);
     int pairs_enabled() const;
+    void ensure_status();
     BatchConst<T> bc_{};
     std::vector<Shot> shots_;
     void launch_step(const int* base, int offset, cudaStream_t stream);
@@ -246,14 +265,16 @@ class Batch2d {
         bool pair = false;
         int shape = 0;
         const void *desc = nullptr, *begin = nullptr, *work = nullptr;
+        int debug_step = -1;
+        unsigned wait_limit = 0;
         bool operator==(const GraphKey& o) const {
             return grid == o.grid && split == o.split && pair == o.pair && shape == o.shape && desc == o.desc &&
-                   begin == o.begin && work == o.work;
+                   begin == o.begin && work == o.work && debug_step == o.debug_step && wait_limit == o.wait_limit;
         }
     } graph_key_;
     GraphKey current_key() const {
         return GraphKey{grid_, split_, pair_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(),
-                        d_work_[shape_].get()};
+                        d_work_[shape_].get(), bc_.debug_step, bc_.wait_limit};
     }
     // tile shape: the schedule in use (BatchShape index) and the tuner (times a
     // few steps with each shape when a large schedule is built, keeps the faster)
@@ -269,6 +290,7 @@ class Batch2d {
     bool pair_ = false;   // enabled residual pairs: the launch uses the pair variant (32 x 32 tiles)
     int shape_free_ = 0;  // the tile shape to return to when the last pair leaves
     DeviceBuffer d_desc_, d_ctr_;                // d_ctr_: graph step base, zero, error flag
+    DeviceBuffer d_status_;                      // one status word per shot slot
     DeviceBuffer d_cta_begin_[2], d_work_[2];    // the schedule of each tile shape
     int grid_s_[2] = {0, 0}, ntiles_s_[2] = {0, 0};
     bool split_s_[2] = {false, false};

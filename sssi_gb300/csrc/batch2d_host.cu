@@ -80,6 +80,14 @@ Batch2d<T>::Batch2d(int N, double dz, double dx, cudaStream_t stream)
     bc_.step_base = d_ctr_.template as<int>() + 1;
     bc_.step_offset = 0;
     bc_.err = d_ctr_.template as<int>() + 2;
+    bc_.wait_limit = kDefaultWaitLimit;
+    bc_.debug_step = -1;
+    {
+        int step = -1;
+        unsigned limit = 0;
+        debug_withhold(&step, &limit);
+        set_debug(step, limit);
+    }
     int dev = 0;
     SSSI_CHECK_CUDA(cudaGetDevice(&dev));
     SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
@@ -360,6 +368,7 @@ void Batch2d<T>::set_point_sources(int k, int nsrc, const int64_t* iz, const int
 
 template <typename T>
 void Batch2d<T>::reset_shot(int k) {
+    clear_status(k);
     Shot& S = shots_[k];
     for (auto& b : S.P) b.zero(up());
     for (auto* b : {&S.zphi[0], &S.zphi[1], &S.zpsi, &S.xphi[0], &S.xphi[1], &S.xpsi}) b->zero(up());
@@ -683,10 +692,11 @@ void Batch2d<T>::schedule(int shape) {
     // descriptors of every slot in one copy
     const size_t nd = std::max<size_t>(shots_.size(), 1);
     if (d_desc_.bytes() < nd * sizeof(ShotDesc<T>)) d_desc_.allocate(nd * sizeof(ShotDesc<T>));
+    ensure_status();
     std::vector<ShotDesc<T>> hdesc(shots_.size());
     for (int k = 0; k < (int)shots_.size(); ++k) {
         ShotTail<T>& d = shots_[k].desc.s;
-        SSSI_REQUIRE(d.stride < (1 << 24), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
+        SSSI_REQUIRE(d.stride < (1 << 22), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
         d.sched = sched_word(d);
         hdesc[k] = shots_[k].desc;
     }
@@ -709,7 +719,7 @@ void Batch2d<T>::schedule(int shape) {
 template <typename T>
 void Batch2d<T>::sync_desc(int k) {
     ShotTail<T>& d = shots_[k].desc.s;
-    SSSI_REQUIRE(d.stride < (1 << 24), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
+    SSSI_REQUIRE(d.stride < (1 << 22), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
     d.sched = sched_word(d);
     SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.template as<ShotDesc<T>>() + k, &shots_[k].desc, sizeof(ShotDesc<T>),
                                     cudaMemcpyHostToDevice, stream_));
@@ -807,7 +817,49 @@ void Batch2d<T>::check_errors() {
     int h = 0;
     SSSI_CHECK_CUDA(cudaMemcpyAsync(&h, bc_.err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
     SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
-    SSSI_REQUIRE(h == 0, SSSI_ERR_INTERNAL, "a tile copy did not arrive within the wait limit (kernel aborted)");
+    if (h != 0) SSSI_CHECK_CUDA(cudaMemsetAsync(bc_.err, 0, sizeof(int), stream_));  // the batch stays usable
+    SSSI_REQUIRE(h == 0, SSSI_ERR_INTERNAL,
+                 "a tile copy did not arrive within the wait limit: the step was aborted and the fields of its "
+                 "shots are incomplete");
+}
+
+template <typename T>
+void Batch2d<T>::ensure_status() {
+    // one status word per slot; the descriptors point at theirs
+    const size_t need = sizeof(int) * std::max<size_t>(shots_.size(), 1);
+    if (d_status_.bytes() < need) {
+        DeviceBuffer fresh(need * 2);
+        fresh.zero(stream_);
+        if (d_status_.bytes())
+            SSSI_CHECK_CUDA(cudaMemcpyAsync(fresh.get(), d_status_.get(), d_status_.bytes(), cudaMemcpyDeviceToDevice,
+                                            stream_));
+        d_status_ = std::move(fresh);
+    }
+    for (int k = 0; k < (int)shots_.size(); ++k) shots_[k].desc.s.status = d_status_.template as<int>() + k;
+}
+
+template <typename T>
+std::vector<int> Batch2d<T>::statuses() {
+    // slots added since the last schedule have not stepped yet: they read as SSSI_OK
+    std::vector<int> h(shots_.size(), 0);
+    const size_t n = std::min(h.size(), d_status_.bytes() / sizeof(int));
+    if (n) {
+        SSSI_CHECK_CUDA(cudaMemcpyAsync(h.data(), d_status_.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, stream_));
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(stream_));
+    }
+    return h;
+}
+
+template <typename T>
+void Batch2d<T>::clear_status(int k) {
+    if (d_status_.bytes() >= sizeof(int) * (size_t)(k + 1))
+        SSSI_CHECK_CUDA(cudaMemsetAsync(d_status_.template as<int>() + k, 0, sizeof(int), stream_));
+}
+
+template <typename T>
+void Batch2d<T>::set_debug(int step, unsigned wait_limit) {
+    bc_.debug_step = step;
+    bc_.wait_limit = step >= 0 && wait_limit ? wait_limit : kDefaultWaitLimit;
 }
 
 template <typename T>

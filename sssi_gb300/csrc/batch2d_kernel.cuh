@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstddef>
+#include <limits>
 
 #include "batch2d.cuh"
 
@@ -1096,6 +1097,16 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
         const int ncol = min(RX, nx - j0);
         for (int c = 0; c < ncol; ++c) r[j0 + c] = pn.v[c][0];
     }
+    if constexpr (kRole != kRolePairD) {
+        // blow-up check on the receiver row: a non-finite value there (a time
+        // step beyond the stability limit grows without bound) fails the shot
+        if (i0 == 0 && sh.status) {
+            const int ncol = min(RX, nx - j0);
+            bool bad = false;
+            for (int c = 0; c < ncol; ++c) bad |= !(fabs(pn.v[c][0]) <= std::numeric_limits<T>::max());
+            if (bad) atomicExch(sh.status, SSSI_ERR_UNSTABLE);
+        }
+    }
     if constexpr (kRole != kRolePairD)
         if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
 }
@@ -1152,7 +1163,6 @@ struct StageLayout {
     static constexpr unsigned kSmem = kScratch + (kPair ? 2 : 1) * BandScratch<T, N, Sh>::kBytes;
 };
 
-constexpr unsigned kWaitLimit = 1u << 24;
 
 // kSplit: the work lists may hold half tiles (schedules of small grids); the
 // variant without them keeps the whole-tile path free of their handling.
@@ -1203,7 +1213,10 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
     auto issue = [&](int s) {
         unsigned char* st = smem + s * G::kStage;
         const TileInfo* info = reinterpret_cast<const TileInfo*>(st + G::kInfo);
-        if (lane == 0 && info->shot >= 0) {
+        // test knob: at bc.debug_step block 0 issues nothing for its first tile, so
+        // that tile's barrier wait runs out and the failure path is exercised
+        const bool withheld = bc.debug_step >= 0 && step == bc.debug_step && blockIdx.x == 0 && s == 0;
+        if (lane == 0 && info->shot >= 0 && !withheld) {
             const ShotTail<T>& g = *reinterpret_cast<const ShotTail<T>*>(st + G::kTail);
             const int k = info->shot, z0 = info->z0, x0 = info->x0, cur = info->tloc & 1;
             const bool pair = kPair && (g.sched & kSchedPair);
@@ -1318,7 +1331,7 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
             fetch(wbeg + k + NS);
         }
         if (ti.shot >= 0) {
-            const bool ok = mbar_wait_bounded(&bar[s], (phase_bits >> s) & 1u, kWaitLimit);
+            const bool ok = mbar_wait_bounded(&bar[s], (phase_bits >> s) & 1u, bc.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -1405,9 +1418,12 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
     if (failed) {
         if (tid == 0) {
             atomicExch(bc.err, 1);
-            // copies issued for stages not yet consumed may still be in flight: wait for them (bounded)
+            // copies issued for stages not yet consumed may still be in flight: wait for
+            // them, bounded by the default limit (a copy that was issued lands); if one
+            // never does, the block leaves with it outstanding and the reported failure
+            // is the only guarantee left
             for (int q = 0; q < NS; ++q)
-                if ((inflight >> q) & 1u) mbar_wait_bounded(&bar[q], (phase_bits >> q) & 1u, kWaitLimit);
+                if ((inflight >> q) & 1u) mbar_wait_bounded(&bar[q], (phase_bits >> q) & 1u, kDefaultWaitLimit);
         }
         __syncthreads();
     }

@@ -16,6 +16,7 @@
 //     per round.
 // Rounds end at the next event of any 2D shot (a phase change or a shot's
 // end), so events always fall on round boundaries.
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -81,6 +82,7 @@ struct PlanRequest {
     double t_submit = 0, t_start = 0, t_done = 0;
     size_t bytes = 0;
     int64_t cells = 0;
+    std::atomic<bool> cancel{false};  // set by sssi_cancel; the worker drops the shot at its next round
 };
 using ReqPtr = std::shared_ptr<PlanRequest>;
 
@@ -109,7 +111,14 @@ class EngineBase {
     virtual void complete(std::vector<Delivery>& out) = 0;
     virtual bool busy() const = 0;
     virtual void fail_all(std::vector<ReqPtr>& fin, const std::string& why) = 0;
+    // Shots that failed on their own (a blow-up) or were cancelled since the
+    // last call; the others keep running.
+    void take_failed(std::vector<ReqPtr>& fin) {
+        fin.insert(fin.end(), failed_.begin(), failed_.end());
+        failed_.clear();
+    }
     virtual int64_t batch_steps() const = 0;
+    std::vector<ReqPtr> failed_;
     double gpu_wait_s = 0;  // host time blocked on the batch stream
     // device time of the batched 2D steps (CUDA events around each round's
     // launches) and the cell-updates they made
@@ -307,6 +316,7 @@ class Engine final : public EngineBase {
     double launch(std::vector<Delivery>& out) override {
         double cells = 0;
         ran2_ = false;
+        drop_cancelled();  // every stream is idle here: the last round has completed
         finish_2d_events(out);  // zero-step shots and events due right at admission
         SSSI_CHECK_CUDA(cudaStreamWaitEvent(s_, up_done_, 0));  // uploads of the shots admitted so far
         // ---- 2D batch: up to the next event of any shot
@@ -357,6 +367,7 @@ class Engine final : public EngineBase {
             batch2d_gpu_s += 1e-3 * ms;
             batch2d_cells += cells2_;
             B_.check_errors();
+            fail_unstable();
             finish_2d_events(out);
         }
         ran2_ = false;
@@ -402,6 +413,54 @@ class Engine final : public EngineBase {
     }
 
   private:
+    // Removes run q of runs2_ (its shots leave the batch) and reports it failed.
+    void fail_run2(size_t q, int status, const std::string& why) {
+        Run& u = *runs2_[q];
+        const int ks[3] = {u.kA, u.kB, u.kR};
+        for (int k : ks)
+            if (k >= 0) B_.remove_shot(k);
+        u.r->status = status;
+        u.r->msg = why;
+        failed_.push_back(u.r);
+        runs2_.erase(runs2_.begin() + q);
+        dirty_ = true;
+    }
+
+    // A shot whose receiver row went non-finite fails alone; the batch goes on.
+    void fail_unstable() {
+        const std::vector<int> st = B_.statuses();
+        auto bad = [&](int k) { return k >= 0 && k < (int)st.size() && st[k] == SSSI_ERR_UNSTABLE; };
+        for (size_t q = 0; q < runs2_.size();) {
+            const Run& u = *runs2_[q];
+            if (bad(u.kA) || bad(u.kB) || bad(u.kR))
+                fail_run2(q, SSSI_ERR_UNSTABLE,
+                          "the wavefield became non-finite (is dt beyond the stability limit of the grid and the "
+                          "velocities?)");
+            else
+                ++q;
+        }
+    }
+
+    // Cancelled shots leave at a round boundary, when none of their work is in flight.
+    void drop_cancelled() {
+        for (size_t q = 0; q < runs2_.size();) {
+            if (runs2_[q]->r->cancel.load())
+                fail_run2(q, SSSI_ERR_CANCELLED, "cancelled");
+            else
+                ++q;
+        }
+        for (size_t q = 0; q < runs3_.size();) {
+            if (runs3_[q]->r->cancel.load()) {
+                runs3_[q]->r->status = SSSI_ERR_CANCELLED;
+                runs3_[q]->r->msg = "cancelled";
+                failed_.push_back(runs3_[q]->r);
+                runs3_.erase(runs3_.begin() + q);
+            } else {
+                ++q;
+            }
+        }
+    }
+
     int64_t next_event(const Run& u) const {
         const int64_t nt = u.r->d.nt;
         if (u.r->d.kind == SSSI_SHOT_RTM2D) return u.s0 + (u.phase == 1 ? nt : 2 * nt);
@@ -678,6 +737,7 @@ struct sssi_plan {
             bool ok = guarded_step(fin, [&] { c = engine->launch(out); });
             admit_queued(fin);  // overlaps the steps just launched
             if (ok) ok = guarded_step(fin, [&] { engine->complete(out); });
+            engine->take_failed(fin);
             {
                 std::lock_guard<std::mutex> lk(mu);
                 if (ok) cells += c;
@@ -826,6 +886,33 @@ extern "C" int sssi_shot_submit(sssi_plan* plan, const sssi_shot_desc* shot, int
             *ticket = r->ticket;
         }
         plan->cv_work.notify_all();
+    });
+}
+
+extern "C" int sssi_cancel(sssi_plan* plan, int64_t ticket) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan, SSSI_ERR_ARG, "plan is NULL");
+        std::lock_guard<std::mutex> lk(plan->mu);
+        auto it = plan->tickets.find(ticket);
+        SSSI_REQUIRE(it != plan->tickets.end(), SSSI_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+        ReqPtr r = it->second;
+        if (r->state == SSSI_SHOT_QUEUED) {
+            // not admitted yet: it leaves the queue now
+            for (auto q = plan->queue.begin(); q != plan->queue.end(); ++q)
+                if (q->get() == r.get()) {
+                    plan->queue.erase(q);
+                    break;
+                }
+            r->status = SSSI_ERR_CANCELLED;
+            r->msg = "cancelled";
+            r->state = SSSI_SHOT_FAILED;
+            r->t_done = plan->now();
+            ++plan->n_failed;
+            plan->cv_done.notify_all();
+        } else if (r->state == SSSI_SHOT_RUNNING) {
+            r->cancel.store(true);  // the worker drops it at its next round
+            plan->cv_work.notify_all();
+        }
     });
 }
 

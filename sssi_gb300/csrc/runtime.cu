@@ -194,6 +194,25 @@ void PinnedBuffer::reserve(size_t bytes) {
 
 }  // namespace sssi
 
+namespace sssi {
+namespace {
+std::atomic<int> g_debug_step{-1};
+std::atomic<unsigned> g_debug_wait{0};
+}  // namespace
+
+void debug_withhold(int* step, unsigned* wait_limit) {
+    *step = g_debug_step.load();
+    *wait_limit = g_debug_wait.load();
+}
+}  // namespace sssi
+
+extern "C" int sssi_debug_withhold_copy(int step, unsigned wait_limit) {
+    sssi::clear_error();
+    sssi::g_debug_step.store(step < 0 ? -1 : step);
+    sssi::g_debug_wait.store(wait_limit);
+    return SSSI_OK;
+}
+
 extern "C" const char* sssi_last_error(void) { return sssi::g_error; }
 
 extern "C" int sssi_version(void) { return 10000 * 0 + 100 * 1 + 0; }

@@ -63,6 +63,8 @@ int guarded(F&& f) {
 
 // ---------------------------------------------------------------- runtime
 void count_launch(int n = 1);
+// The test knob of sssi_debug_withhold_copy (step < 0: off).
+void debug_withhold(int* step, unsigned* wait_limit);
 // One-thread kernels that set / advance a device int (graph step bases).
 void launch_store_int(int* p, int v, cudaStream_t s);
 void launch_add_int(int* p, int v, cudaStream_t s);
