@@ -713,13 +713,9 @@ def bench_serve(S, args):
     with S.Plan(N_ORDER, DZ, DX, DX, mode="fp32", device_bytes=int(args.serve_budget_gb * (1 << 30))) as plan:
         plan.wait(plan.submit_fwd2d(np.asfortranarray(big2d[:200, :300]), 100, [0], [150],
                                     ricker(20.0, 100, dt)[None, :], NB, dt))  # warm-up
-        t_start = time.perf_counter()
-        for k, (ta, kind, nz, nx, nt, z0, x0) in enumerate(reqs):
-            delay = ta - (time.perf_counter() - t_start)
-            if delay > 0:
-                time.sleep(delay)
+        def submit(k, kind, nz, nx, nt, z0, x0, own):
             w = ricker(20.0 if kind != "rtm2d" else 15.0, nt, dt)
-            own = k in check
+            vs = None
             if kind == "fwd2d":
                 v = np.asfortranarray(big2d[z0:z0 + nz, x0:x0 + nx])
                 tk = plan.submit_fwd2d(v, nt, [0], [nx // 2], w[None, :], NB, dt, data=view(kind, (nx, nt), own))
@@ -732,12 +728,35 @@ def bench_serve(S, args):
                 v = np.asfortranarray(big3d[z0:z0 + nz, x0:x0 + nx, :nx])
                 tk = plan.submit_fwd3d(v, nt, [0], [nx // 2], [nx // 2], w[None, :], 16, dt,
                                        data=view(kind, (nx, nx, nt), own))
-            tickets.append(tk)
             if own:
-                inputs[k] = (kind, v, vs if kind == "rtm2d" else None, w, nt)
+                inputs[k] = (kind, v, vs, w, nt)
+            return tk
+
+        t_start = time.perf_counter()
+        for k, (ta, kind, nz, nx, nt, z0, x0) in enumerate(reqs):
+            delay = ta - (time.perf_counter() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append(submit(k, kind, nz, nx, nt, z0, x0, k in check))
         for tk in tickets:
             plan.wait(tk)
         st = plan.stats()
+        # capacity: the first requests of the stream submitted all at once (the plan saturated)
+        sat = []
+        if args.serve_saturate > 0:
+            t0s = time.perf_counter()
+            sat = [submit(k, *reqs[k][1:], False) for k in range(min(args.serve_saturate, n_req))]
+            for tk in sat:
+                plan.wait(tk)
+            sat_wall = time.perf_counter() - t0s
+    saturated = None
+    if sat:
+        sinfo = [tk.info for tk in sat]
+        sat_span = max(i["done_s"] for i in sinfo) - min(i["submit_s"] for i in sinfo)
+        saturated = {"shots": len(sat), "shots_per_s": round(len(sat) / sat_span, 3), "span_s": round(sat_span, 2),
+                     "wall_s": round(sat_wall, 2),
+                     "gcell_updates_per_s": round(sum(i["cell_updates"] for i in sinfo) / sat_span / 1e9, 2),
+                     "note": "the first requests of the same stream submitted at once: the plan's capacity"}
     infos = [tk.info for tk in tickets]
     lat = np.array([i["done_s"] - i["submit_s"] for i in infos])
     span = max(i["done_s"] for i in infos) - min(i["submit_s"] for i in infos)
@@ -764,6 +783,7 @@ def bench_serve(S, args):
             "p99_latency_s": round(float(np.percentile(lat, 99)), 3), "mean_latency_s": round(float(lat.mean()), 3),
             "gcell_updates_per_s": round(cells / span / 1e9, 2), "span_s": round(span, 2),
             "offered_rate_per_s": rate, "requests": {k: kinds.count(k) for k in ("fwd2d", "rtm2d", "fwd3d")},
+            "saturated": saturated,
             "rel_l2_vs_fp64": errs, "rel_l2_vs_fp64_max": max(errs.values()) if errs else None,
             "rel_l2_vs_fp64_max_by_kind": {kd: max([e for k, e in errs.items() if k.endswith(kd)], default=None)
                                            for kd in ("fwd2d", "rtm2d", "fwd3d")},
@@ -906,6 +926,8 @@ def main():
     ap.add_argument("--serve-stride", type=int, default=1,
                     help="served RTM requests: forward field stored (16-bit) and imaged every this many steps")
     ap.add_argument("--serve-budget-gb", type=float, default=160.0, help="device memory the serving plan may hold")
+    ap.add_argument("--serve-saturate", type=int, default=120,
+                    help="requests submitted at once after the stream, to measure the plan's capacity")
     ap.add_argument("--serve-check-rtm", type=int, default=16, help="served RTM requests checked against FP64")
     ap.add_argument("--serve-check-fwd", type=int, default=6, help="served 2D forward requests checked")
     ap.add_argument("--serve-check-3d", type=int, default=3, help="served 3D requests checked")

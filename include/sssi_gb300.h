@@ -207,7 +207,9 @@ typedef struct {
     double epsilon;        /* RTM: imaging stabiliser */
     int snap_stride;       /* RTM in FP32 plans: forward field stored every snap_stride steps (0: 4) */
     double *data;          /* receivers (FWD2D, FWD3D), dataTrue (RTM, may be NULL); host or device */
-    double *image;         /* RTM image, nz x nx; host or device */
+    double *image;         /* RTM image, nz x nx; host or device (may be NULL when stacked) */
+    int64_t stack;         /* RTM: a stack of the plan (sssi_plan_stack_create) the image is added to, or 0 */
+    int64_t stack_z0, stack_x0; /* position of the shot's grid in the stack's grid */
 } sssi_shot_desc;
 
 typedef struct {
@@ -241,6 +243,16 @@ int sssi_plan_destroy(sssi_plan *plan);
  * queues it; outputs are written when the shot completes, so data / image
  * must stay valid until then.  *ticket identifies the shot. */
 int sssi_shot_submit(sssi_plan *plan, const sssi_shot_desc *shot, int64_t *ticket);
+/* A stacked image held on the device by the plan: the sum of the images of
+ * the RTM shots submitted with this stack, each added at its (stack_z0,
+ * stack_x0) window as it completes, as the reference stacks its shots
+ * (Stacked = Stacked + M ./ s2, mainRtmTimeCpmlFor2dAw.m:315).  nz x nx
+ * doubles, zero at creation, counted against the plan's device budget. */
+int sssi_plan_stack_create(sssi_plan *plan, int64_t nz, int64_t nx, int64_t *stack);
+/* Waits until every shot submitted to the stack so far has finished (done,
+ * failed or cancelled: a failed shot adds nothing) and copies the stack to
+ * out (nz x nx, host or device). */
+int sssi_plan_stack_get(sssi_plan *plan, int64_t stack, double *out);
 /* Cancels a shot: a queued shot leaves the queue at once, a running one at
  * the plan's next round boundary (its device memory then returns to the
  * budget); either ends SSSI_SHOT_FAILED with status SSSI_ERR_CANCELLED and

@@ -33,7 +33,8 @@ class ShotDesc(ctypes.Structure):
                 ("nx", c_i64), ("ny", c_i64), ("nt", c_i64), ("nBoundary", ctypes.c_int), ("dt", ctypes.c_double),
                 ("nsrc", ctypes.c_int), ("src_iz", ctypes.c_void_p), ("src_ix", ctypes.c_void_p),
                 ("src_iy", ctypes.c_void_p), ("wavelets", ctypes.c_void_p), ("epsilon", ctypes.c_double),
-                ("snap_stride", ctypes.c_int), ("data", ctypes.c_void_p), ("image", ctypes.c_void_p)]
+                ("snap_stride", ctypes.c_int), ("data", ctypes.c_void_p), ("image", ctypes.c_void_p),
+                ("stack", c_i64), ("stack_z0", c_i64), ("stack_x0", c_i64)]
 
 
 class ShotInfo(ctypes.Structure):
@@ -58,6 +59,8 @@ SIGNATURES = {
     "sssi_shot_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ShotDesc), ctypes.POINTER(c_i64)]),
     "sssi_poll": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
     "sssi_cancel": (ctypes.c_int, [ctypes.c_void_p, c_i64]),
+    "sssi_plan_stack_create": (ctypes.c_int, [ctypes.c_void_p, c_i64, c_i64, ctypes.POINTER(c_i64)]),
+    "sssi_plan_stack_get": (ctypes.c_int, [ctypes.c_void_p, c_i64, c_dp]),
     "sssi_debug_withhold_copy": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint]),
     "sssi_wait": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
     "sssi_plan_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlanStats)]),

@@ -327,9 +327,11 @@ class Plan:
         return self._submit(d, {"data": data}, (kv, kd, iz, ix, w, v))
 
     def submit_rtm2d(self, v, vs, wavelet, src_iz, src_ix, nBoundary, dt, *, epsilon=1e-3, snap_stride=4,
-                     want_data=False, image=None):
-        """One RTM shot (as :func:`rtmTimeCpmlFor2dAw`); outputs: image (nz x nx),
-        and dataTrue (nx x nt) with ``want_data``."""
+                     want_data=False, image=None, stack=0, stack_z0=0, stack_x0=0, want_image=True):
+        """One RTM shot (as :func:`rtmTimeCpmlFor2dAw`); outputs: image (nz x nx)
+        unless ``want_image`` is False, and dataTrue (nx x nt) with ``want_data``.
+        With ``stack`` (from :meth:`stack`) the image is also added to that
+        stack at (``stack_z0``, ``stack_x0``) on the device."""
         from ._native import ShotDesc
 
         pv, kv, vshape = _in(v, "v")
@@ -337,11 +339,15 @@ class Plan:
         nz, nx = vshape
         nt = len(np.asarray(wavelet)) if not _is_torch(wavelet) else wavelet.shape[0]
         iz, ix, w = _points([src_iz], [src_ix], None, np.asarray(wavelet, dtype=np.float64)[None, :], nt)
-        image, ki = _out_like(v, (nz, nx)) if image is None else (image, None)
+        if image is None and want_image:
+            image, ki = _out_like(v, (nz, nx))
+        else:
+            ki = None
         data, kd = _out_like(v, (nx, nt)) if want_data else (None, None)
         d = ShotDesc(kind=SHOT_RTM2D, v=pv, vs=pvs, nz=nz, nx=nx, ny=1, nt=int(nt), nBoundary=int(nBoundary),
                      dt=float(dt), nsrc=1, src_iz=iz.ctypes.data, src_ix=ix.ctypes.data, wavelets=w.ctypes.data,
-                     epsilon=float(epsilon), snap_stride=int(snap_stride), data=_addr(data), image=_addr(image))
+                     epsilon=float(epsilon), snap_stride=int(snap_stride), data=_addr(data), image=_addr(image),
+                     stack=int(stack), stack_z0=int(stack_z0), stack_x0=int(stack_x0))
         return self._submit(d, {"image": image, "data": data}, (kv, kvs, ki, kd, iz, ix, w, v, vs))
 
     def submit_fwd3d(self, v, nt, src_iz, src_ix, src_iy, wavelets, nBoundary, dt, *, data=None):
@@ -370,6 +376,20 @@ class Plan:
         info = ShotInfo()
         check(lib().sssi_poll(self._h, ticket.id, ctypes.byref(info)))
         return self._info(info)
+
+    def stack(self, nz, nx):
+        """A zeroed nz x nx image on the device that RTM shots add to (returns its id)."""
+        from ._native import c_i64
+
+        sid = c_i64()
+        check(lib().sssi_plan_stack_create(self._h, int(nz), int(nx), ctypes.byref(sid)))
+        return int(sid.value)
+
+    def stack_get(self, stack, out):
+        """Waits for the shots submitted to ``stack`` and copies the stacked image
+        into ``out`` (its nz x nx shape, float64 column-major, host or device)."""
+        check(lib().sssi_plan_stack_get(self._h, int(stack), _addr(out)))
+        return out
 
     def cancel(self, ticket):
         """Cancels a queued or running shot (it ends failed, status SSSI_ERR_CANCELLED)."""

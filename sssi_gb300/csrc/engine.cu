@@ -59,6 +59,13 @@ void deliver(const T* dev, size_t n, double* out, cudaStream_t s) {
     SSSI_CHECK_CUDA(cudaStreamSynchronize(s));
 }
 
+// stack[i + j * ld] += img[i + j * nz]: one shot's image into a plan's stack.
+__global__ void stack_add_kernel(const double* img, int64_t nz, int64_t nx, double* stack, int64_t ld) {
+    const int64_t n = nz * nx;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        stack[(q % nz) + (q / nz) * ld] += img[q];
+}
+
 // Host doubles -> new device array of T.
 template <typename T>
 void upload(DeviceBuffer& buf, const std::vector<double>& h, cudaStream_t s) {
@@ -83,6 +90,8 @@ struct PlanRequest {
     size_t bytes = 0;
     int64_t cells = 0;
     std::atomic<bool> cancel{false};  // set by sssi_cancel; the worker drops the shot at its next round
+    double* stack_ptr = nullptr;      // RTM: the stack window the image is added to (ld = stack_ld)
+    int64_t stack_ld = 0;
 };
 using ReqPtr = std::shared_ptr<PlanRequest>;
 
@@ -541,6 +550,12 @@ class Engine final : public EngineBase {
                                                                   n, 1.0, 0.0, u.img.template as<double>());
                 count_launch();
                 SSSI_CHECK_CUDA(cudaGetLastError());
+                if (u.r->stack_ptr) {  // ordered before the delivery's event: done means added
+                    stack_add_kernel<<<152 * 4, 256, 0, s_>>>(u.img.template as<double>(), nz, nx, u.r->stack_ptr,
+                                                              u.r->stack_ld);
+                    count_launch();
+                    SSSI_CHECK_CUDA(cudaGetLastError());
+                }
                 B_.remove_shot(u.kR);
                 const double* img = u.img.template as<double>();
                 const T* rec = u.recA.template as<T>();
@@ -591,6 +606,13 @@ struct sssi_plan {
     std::string fatal_msg;
     std::unique_ptr<sssi::EngineBase> engine;
     std::thread worker;
+    // stacked images (sssi_plan_stack_create): device memory and the shots still to add
+    struct Stack {
+        sssi::DeviceBuffer buf;
+        int64_t nz = 0, nx = 0, pending = 0;
+    };
+    std::map<int64_t, std::unique_ptr<Stack>> stacks;
+    int64_t next_stack = 1;
     // delivery thread: copies finished shots' outputs on its own stream
     cudaStream_t dstream = nullptr;
     std::deque<sssi::Delivery> deliveries;
@@ -603,6 +625,10 @@ struct sssi_plan {
     void finish(std::vector<sssi::ReqPtr>& fin) {
         std::lock_guard<std::mutex> lk(mu);
         for (auto& r : fin) {
+            if (r->d.stack) {
+                auto it = stacks.find(r->d.stack);
+                if (it != stacks.end()) --it->second->pending;
+            }
             r->t_done = now();
             r->state = r->status == SSSI_OK ? SSSI_SHOT_DONE : SSSI_SHOT_FAILED;
             in_use -= std::min(in_use, r->bytes);
@@ -860,7 +886,7 @@ extern "C" int sssi_shot_submit(sssi_plan* plan, const sssi_shot_desc* shot, int
                              (!is3 || (d.src_iy[s] >= 0 && d.src_iy[s] < d.ny)),
                          SSSI_ERR_ARG, "point source %d outside the grid", s);
         if (d.kind == SSSI_SHOT_RTM2D) {
-            SSSI_REQUIRE(d.vs && d.image, SSSI_ERR_ARG, "RTM needs vs and image");
+            SSSI_REQUIRE(d.vs && (d.image || d.stack), SSSI_ERR_ARG, "RTM needs vs, and an image or a stack");
             SSSI_REQUIRE(d.nsrc == 1, SSSI_ERR_ARG, "RTM takes exactly one point source");
             SSSI_REQUIRE(d.snap_stride >= 0, SSSI_ERR_ARG, "snap_stride must be >= 0");
         }
@@ -879,6 +905,20 @@ extern "C" int sssi_shot_submit(sssi_plan* plan, const sssi_shot_desc* shot, int
         {
             std::lock_guard<std::mutex> lk(plan->mu);
             SSSI_REQUIRE(!plan->stop, SSSI_ERR_ARG, "plan is being destroyed");
+            if (d.stack) {
+                SSSI_REQUIRE(d.kind == SSSI_SHOT_RTM2D, SSSI_ERR_ARG, "only RTM shots add to a stack");
+                auto it = plan->stacks.find(d.stack);
+                SSSI_REQUIRE(it != plan->stacks.end(), SSSI_ERR_ARG, "unknown stack %lld", (long long)d.stack);
+                auto& st = *it->second;
+                SSSI_REQUIRE(d.stack_z0 >= 0 && d.stack_x0 >= 0 && d.stack_z0 + d.nz <= st.nz &&
+                                 d.stack_x0 + d.nx <= st.nx,
+                             SSSI_ERR_ARG, "the shot's %lld x %lld grid at (%lld, %lld) leaves the %lld x %lld stack",
+                             (long long)d.nz, (long long)d.nx, (long long)d.stack_z0, (long long)d.stack_x0,
+                             (long long)st.nz, (long long)st.nx);
+                r->stack_ptr = st.buf.as<double>() + d.stack_z0 + d.stack_x0 * st.nz;
+                r->stack_ld = st.nz;
+                ++st.pending;
+            }
             r->ticket = plan->next_ticket++;
             r->t_submit = plan->now();
             plan->tickets[r->ticket] = r;
@@ -886,6 +926,41 @@ extern "C" int sssi_shot_submit(sssi_plan* plan, const sssi_shot_desc* shot, int
             *ticket = r->ticket;
         }
         plan->cv_work.notify_all();
+    });
+}
+
+extern "C" int sssi_plan_stack_create(sssi_plan* plan, int64_t nz, int64_t nx, int64_t* stack) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan && stack, SSSI_ERR_ARG, "plan and stack must not be NULL");
+        SSSI_REQUIRE(nz > 0 && nx > 0 && nz < (int64_t(1) << 30) && nx < (int64_t(1) << 30), SSSI_ERR_ARG,
+                     "bad stack size %lld x %lld", (long long)nz, (long long)nx);
+        int dev = 0;
+        SSSI_CHECK_CUDA(cudaGetDevice(&dev));
+        SSSI_REQUIRE(dev == plan->device, SSSI_ERR_ARG, "the plan lives on device %d, the calling thread uses %d",
+                     plan->device, dev);
+        auto st = std::make_unique<sssi_plan::Stack>();
+        st->nz = nz;
+        st->nx = nx;
+        st->buf.allocate(sizeof(double) * (size_t)(nz * nx));
+        st->buf.zero(plan->stream);  // the worker's stream: ordered before any shot adds to it
+        SSSI_CHECK_CUDA(cudaStreamSynchronize(plan->stream));
+        std::lock_guard<std::mutex> lk(plan->mu);
+        plan->in_use += st->buf.bytes();
+        *stack = plan->next_stack++;
+        plan->stacks[*stack] = std::move(st);
+    });
+}
+
+extern "C" int sssi_plan_stack_get(sssi_plan* plan, int64_t stack, double* out) {
+    return guarded([&] {
+        SSSI_REQUIRE(plan && out, SSSI_ERR_ARG, "plan and out must not be NULL");
+        std::unique_lock<std::mutex> lk(plan->mu);
+        auto it = plan->stacks.find(stack);
+        SSSI_REQUIRE(it != plan->stacks.end(), SSSI_ERR_ARG, "unknown stack %lld", (long long)stack);
+        sssi_plan::Stack& st = *it->second;
+        plan->cv_done.wait(lk, [&] { return st.pending == 0; });
+        // every contribution's kernel ran before its shot was reported finished
+        SSSI_CHECK_CUDA(cudaMemcpy(out, st.buf.get(), sizeof(double) * (size_t)(st.nz * st.nx), cudaMemcpyDefault));
     });
 }
 
@@ -908,6 +983,10 @@ extern "C" int sssi_cancel(sssi_plan* plan, int64_t ticket) {
             r->state = SSSI_SHOT_FAILED;
             r->t_done = plan->now();
             ++plan->n_failed;
+            if (r->d.stack) {
+                auto st = plan->stacks.find(r->d.stack);
+                if (st != plan->stacks.end()) --st->second->pending;
+            }
             plan->cv_done.notify_all();
         } else if (r->state == SSSI_SHOT_RUNNING) {
             r->cancel.store(true);  // the worker drops it at its next round

@@ -114,3 +114,64 @@ def test_plan_errors(gpu):
         t = plan.submit_fwd2d(v, 0, [0], [3], np.zeros((1, 0)), 3, 1e-3)  # nothing to do: completes
         plan.wait(t)
         assert plan.poll(t)["state"] == "done"
+
+
+def test_plan_join_mid_flight(gpu, oracle_mod):
+    """Continuous batching: shot B is submitted while shot A is running and has
+    advanced; B joins the running batch and both give their single-shot results
+    exactly."""
+    import time
+
+    S = gpu
+    rng = np.random.default_rng(21)
+    va, vb = _model(rng, 120, 200), _model(rng, 90, 160)
+    wa = oracle_mod.ricker(25.0, 3000, 1e-3)[None, :]
+    wb = oracle_mod.ricker(25.0, 600, 1e-3)[None, :]
+    with S.Plan(4, 10.0, 10.0, mode="fp32", steps_per_round=16) as plan:
+        ta = plan.submit_fwd2d(va, 3000, [3], [100], wa, 10, 1e-3)
+        for _ in range(4000):
+            if plan.poll(ta)["state"] == "running" and plan.stats()["batch_steps"] >= 64:
+                break
+            time.sleep(0.001)
+        steps_before = plan.stats()["batch_steps"]
+        assert plan.poll(ta)["state"] == "running" and steps_before >= 64
+        tb = plan.submit_fwd2d(vb, 600, [0], [40], wb, 10, 1e-3)
+        db = plan.wait(tb)["data"]
+        da = plan.wait(ta)["data"]
+    ia, ib = ta.info, tb.info
+    assert ia["start_s"] < ib["start_s"] < ia["done_s"]  # B ran while A was running
+    ra, _ = S.fwdTimeCpmlFor2dAwPoint(va, 3000, [3], [100], wa, 4, 10, 10.0, 10.0, 1e-3, mode="fp32")
+    rb, _ = S.fwdTimeCpmlFor2dAwPoint(vb, 600, [0], [40], wb, 4, 10, 10.0, 10.0, 1e-3, mode="fp32")
+    assert np.array_equal(da, ra) and np.array_equal(db, rb)
+
+
+@pytest.mark.parametrize("mode", ["fp32", "fp64"])
+def test_plan_stack(gpu, oracle_mod, mode):
+    """Device-resident stacking (Stacked = Stacked + M ./ s2 of the reference's
+    shot loop): three RTM shots on windows of one model add their images to one
+    stack; the stack equals the sum of the shots' own images placed at their
+    windows."""
+    S = gpu
+    rng = np.random.default_rng(4)
+    nz, nx = 70, 200
+    v = _model(rng, nz, nx)
+    vs = np.asfortranarray(0.5 * (v + v.mean()))
+    nt = 120
+    w = oracle_mod.ricker(25.0, nt, 1e-3)
+    windows = [(0, 0, 100), (0, 50, 120), (10, 120, 80)]  # (z0, x0, width)
+    expect = np.zeros((nz, nx), order="F")
+    with S.Plan(4, 10.0, 10.0, mode=mode) as plan:
+        sid = plan.stack(nz, nx)
+        ts = []
+        for (z0, x0, width) in windows:
+            vv = np.asfortranarray(v[z0:, x0:x0 + width])
+            vvs = np.asfortranarray(vs[z0:, x0:x0 + width])
+            ts.append(plan.submit_rtm2d(vv, vvs, w, 0, width // 2, 6, 1e-3, epsilon=1e-3, snap_stride=1,
+                                        stack=sid, stack_z0=z0, stack_x0=x0))
+            img = S.rtmTimeCpmlFor2dAw(vv, vvs, w, 0, width // 2, 4, 6, 10.0, 10.0, 1e-3, epsilon=1e-3, mode=mode,
+                                       snap_stride=1)
+            expect[z0:, x0:x0 + width] += img
+        out = plan.stack_get(sid, np.zeros((nz, nx), order="F"))
+        for t, (z0, x0, width) in zip(ts, windows):  # each shot also returned its own image
+            assert plan.wait(t)["image"].shape == (nz - z0, width)
+    assert oracle_mod.rel_l2(out, expect) <= 1e-14
