@@ -107,10 +107,10 @@ def cell_updates(nz, nx, nt):
     return 3 * nz * nx * nt
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one forward step of the RTM
-# shot (two 620 x 1240 shots), from `ncu --set full -k regex:batch2d -s 40 -c 1
-# python bench.py --case rtm-short`
-FWD_STEP_DRAM_BYTES = 22_306_816
+# dram__bytes_read.sum + dram__bytes_write.sum of one forward step of the FP32
+# RTM shot (the residual pair on 620 x 1240), from `ncu --set full --clock-control
+# none -k regex:batch2d -s 40 -c 2 python bench.py --case rtm-short`
+FWD_STEP_DRAM_BYTES = 35_389_440
 # the same for one FP64 forward step of the RTM shot (fused FP64), from
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 # --clock-control none -k regex:batch2d -s 40 -c 2 python bench.py --case rtm-short-fp64`
@@ -138,6 +138,16 @@ def step_bytes_per_cell_fp64(nz, nx, nb):
     (v dt)^2 read and P(t+1) written, plus 48 B per damped cell and axis
     (phi and psi read and written, b and b-1 read)."""
     return 32 + 48 * (nb / nz + 2 * nb / nx)
+
+
+def pair_bytes_per_cell(nz, nx, nb, stride):
+    """Algorithmic HBM bytes per cell of one step of the FP32 RTM forward pair:
+    P as hi + lo (current and previous read, new written: 24 B), the residual
+    D (12 B), (v dt)^2 and its difference (8 B); every `stride` steps the FP16
+    snapshot (2 B), its error feedback (4 B read and written) and the FP32
+    illumination sum (8 B read and written); per damped cell and axis the
+    compensated memory variables of both fields (64 B) and b, b-1, b_Q-b_P (12 B)."""
+    return 44 + (2 + 8 + 16) / stride + 76 * (nb / nz + 2 * nb / nx)
 
 
 def step_bytes_per_cell(nz, nx, nb):
@@ -303,10 +313,10 @@ def run_gpu(args):
     # the same for the FP32 step (HBM-bound)
     fwd_ms = float(np.mean([p[0][0] for p in ph32]))
     per_launch_ms = fwd_ms / NT
-    bytes_cell = step_bytes_per_cell(nz, nx, NB)
-    # a forward launch advances the shots in v and in vs, and packs the vs field
-    # to FP16 every STRIDE steps
-    alg_bytes = nz * nx * (2 * bytes_cell + 2.0 / STRIDE)
+    # a forward launch advances the residual pair (the field in vs and the
+    # residual of the field in v)
+    bytes_cell = pair_bytes_per_cell(nz, nx, NB, STRIDE)
+    alg_bytes = nz * nx * bytes_cell
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
 
     line = {
@@ -346,10 +356,11 @@ def run_gpu(args):
                          "api": "sssi_rtmTimeCpmlFor2dAw (host buffers)"},
                  "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                               "frac": round(achieved / peak, 4), "traffic": FWD_STEP_DRAM_BYTES,
-                              "traffic_note": "dram read+write of one forward step from an ncu capture of the same "
-                                              "grid (caches flushed per pass); the timed steps run from L2",
+                              "traffic_note": "dram read+write of one forward pair step from an ncu capture of the "
+                                              "same grid (caches flushed per pass); the timed steps run from L2",
                               "alg_bytes_per_launch": int(alg_bytes), "peak_kind": peak_kind,
-                              "kernel": "batch2d step (fp32, forward phase)", "bytes_per_cell": round(bytes_cell, 2),
+                              "kernel": "batch2d step (fp32 residual pair, forward phase)",
+                              "bytes_per_cell": round(bytes_cell, 2),
                               "launch_ms": round(per_launch_ms, 5)},
                  "phases_ms": {"forward": round(fwd_ms, 2),
                                "reverse+imaging": round(float(np.mean([p[1][0] for p in ph32])), 2),
@@ -856,6 +867,7 @@ CASES = {
     "step2d-fp32-large": (4096, 4096, 6, "fp32"),
     "step2d-fp64-large": (4096, 4096, 4, "fp64"),
     "step2d-strict-large": (4096, 4096, 3, "fp64-strict"),
+    "step2d-strict-c2": (620, 1240, 6, "fp64-strict"),  # the RTM workload's grid, strict FP64
     "step3d-fp32": (272, 288, 6, "fp32"),  # the 3D workload's grid (256^3 + 16-cell CPML)
     "step3d-fp32-nb0": (272, 288, 6, "fp32"),  # the same grid without damped bands
 }
