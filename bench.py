@@ -372,6 +372,8 @@ def run_gpu(args):
         line["c1"] = bench_c1(S, args)
     if rank == 0 and not args.no_3d:
         line["fwd3d"] = bench_3d(S, args)
+    if rank == 0 and not args.no_diffop:
+        line["diff_operator"] = bench_diffop(S, args, fma_rate)
     if rank == 0 and not args.no_batch:
         line["batch2d"] = bench_batch(S, args)
     if rank == 0 and not args.no_serve:
@@ -563,6 +565,48 @@ def bench_3d(S, args):
                        "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
                        "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",
                        "source": "20 Hz Ricker at the surface centre"}}
+
+
+def bench_diffop(S, args, fma_rate):
+    """The stand-alone staggered derivative (diffOperator) of a 272 x 288 x 288
+    array (the 3D workload's grid, 180 MB, larger than L2) along each dimension,
+    8th order (4 coefficients), device arrays.  Fused FP64 does 8 FP64
+    instructions per output (4 subtractions, 4 multiply-adds): bound by the FP64
+    pipe (fraction of the FP64 FMA rate measured in the run); the byte view is 8 B
+    read and 8 B written per output (the stencil's other reads hit L1/L2)."""
+    import torch
+
+    shape = (272, 288, 288)
+    x = torch.randn(tuple(reversed(shape)), dtype=torch.float64, device="cuda").permute(2, 1, 0)
+    c = S.dCoef(4)
+    peak, peak_kind = peaks()
+    out = {"metric": "GB/s (staggered derivative of a 272x288x288 FP64 array, 4 coefficients)",
+           "config": {"workload": "diffOperator-3d", "shape": list(shape), "order": 4}}
+    for mode in ("fp64", "fp64-strict"):
+        for dim in (1, 2, 3):
+            S.diffOperator(x, c, 10.0, dim, mode=mode)  # warm-up
+            ts = []
+            for _ in range(5):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                S.diffOperator(x, c, 10.0, dim, mode=mode)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            nout = np.prod(shape) * (shape[dim - 1] - 7) / shape[dim - 1]
+            gbs = 16.0 * nout / (ms * 1e-3) / 1e9
+            gops = 8.0 * nout / (ms * 1e-3) / 1e9
+            out[f"{mode}_dim{dim}"] = {"ms": round(ms, 3), "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4),
+                                       "fp64_gops": round(gops, 1), "frac_fp64": round(gops * 1e9 / fma_rate, 4)}
+    out["roofline"] = {"bound": "fp64", "peak": round(fma_rate / 1e9, 1), "unit": "Gop/s",
+                       "ops_per_output": 8, "achieved": out["fp64_dim1"]["fp64_gops"],
+                       "frac": out["fp64_dim1"]["frac_fp64"]}
+    out["hbm_peak"] = peak
+    out["hbm_peak_kind"] = peak_kind
+    out["timing"] = "CUDA events around the C-ABI call, inputs and outputs on the device (includes the output allocation)"
+    return out
 
 
 # ---------------------------------------------------------------- batched and served shots (plan API)
@@ -929,6 +973,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the fp32-vs-fp64 error report")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D forward-modelling line")
     ap.add_argument("--no-c1", action="store_true", help="skip the plain forward-modelling (dense API) line")
+    ap.add_argument("--no-diffop", action="store_true", help="skip the stand-alone derivative line")
     ap.add_argument("--nt3d", type=int, default=2000)
     ap.add_argument("--steps3d", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-shot batched line")

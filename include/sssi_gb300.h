@@ -90,6 +90,17 @@ int sssi_dCoef(int order, double *coeff);
  * Replaces dampPml, src/fd_cmex/finiteDifference.c:253-280. */
 int sssi_dampPml(const double *u, const double *v, int64_t count, double L, double *d);
 
+/* Staggered first derivative of a column-major 2D (ndims = 2) or 3D array
+ * (dims[0..ndims-1]) along dimension dim (1-based):
+ *     out(m) = sum_k coeff[k] * (data(m + order + k) - data(m + order - 1 - k)) / dist
+ * for k = 0..order-1, where m runs over the output, whose size along dim is
+ * dims[dim-1] - (2*order - 1) (the other sizes unchanged).  data / out may be
+ * host or device memory.  SSSI_MODE_FP64_STRICT rounds as the reference
+ * (bit-identical results); SSSI_MODE_FP64 folds coeff/dist and fuses.
+ * Replaces diffOperator_mex, src/fd_cmex/diffOperator_mex.c:29-213. */
+int sssi_diffOperator(const double *data, int ndims, const int64_t *dims, const double *coeff, int order, double dist,
+                      int dim, double *out, int mode);
+
 /* ---- drop-in propagators (the MEX gateways' work, plain pointers) ---- */
 
 /* 2D forward modelling.  v: nz x nx; source: nz x nx x nt (dense, as the

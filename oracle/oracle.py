@@ -100,6 +100,7 @@ class COracle:
                                 _dp, _dp]
         L.orc_image_accum.argtypes = [_dp, _dp, _i64, _dp, _dp]
         L.orc_image_stack.argtypes = [_dp, _dp, _i64, _dp]
+        L.orc_diff_operator.argtypes = [_dp, _i64, _i64, _i64, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_num_threads.argtypes = [ctypes.c_int]
 
@@ -108,6 +109,18 @@ class COracle:
 
     def threads(self) -> int:
         return int(self.lib.orc_num_threads())
+
+    def diff_operator(self, data, c, d, dim=1) -> np.ndarray:
+        """diffOperator (src/fd_cmex/diffOperator_mex.c:29-213) of a 2D or 3D array."""
+        data = _f64(data)
+        c = np.ascontiguousarray(np.atleast_1d(np.asarray(c, dtype=np.float64)).ravel())
+        shape = list(data.shape) + [1] * (3 - data.ndim)
+        oshape = list(data.shape)
+        oshape[dim - 1] -= 2 * len(c) - 1
+        out = np.zeros(oshape, order="F")
+        self.lib.orc_diff_operator(_ptr(data), shape[0], shape[1], shape[2], _ptr(c), len(c), float(d), int(dim),
+                                   _ptr(out))
+        return out
 
     def dcoef(self, order: int) -> np.ndarray:
         c = np.zeros(order)

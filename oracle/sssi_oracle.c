@@ -18,6 +18,8 @@
  *                    y=1 slice / top row as that file does)
  *   orc_image_accum  applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:268-275
  *   orc_image_stack  applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:315
+ *   orc_diff_operator src/fd_cmex/diffOperator_mex.c:29-213 (the stand-alone
+ *                    staggered derivative of a 2D/3D array along one dimension)
  *
  * Index algebra of one step (0-based, column-major, l = 2N-1 zero rows and
  * columns of padding on every side of the padded wavefield P):
@@ -58,6 +60,35 @@ static int omp_nthreads(void) {
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------ */
+/* stand-alone staggered derivative along dimension dim (1, 2 or 3) of an  */
+/* n1 x n2 x n3 column-major array: out(m) = sum_k c_k (in(m+order+k) -   */
+/* in(m+order-1-k)) / d, each term rounded separately, summed from 0 in    */
+/* order of k; the output shrinks by 2 order - 1 along dim.               */
+/* ------------------------------------------------------------------ */
+void orc_diff_operator(const double *in, idx_t n1, idx_t n2, idx_t n3, const double *c, int order, double d,
+                       int dim, double *out) {
+    const idx_t l = 2 * (idx_t)order - 1;
+    idx_t o1 = n1, o2 = n2, o3 = n3;
+    if (dim == 1) o1 -= l;
+    else if (dim == 2) o2 -= l;
+    else o3 -= l;
+    const idx_t s = dim == 1 ? 1 : (dim == 2 ? n1 : n1 * n2);
+#pragma omp parallel for schedule(static)
+    for (idx_t k = 0; k < o3; ++k)
+        for (idx_t j = 0; j < o2; ++j)
+            for (idx_t i = 0; i < o1; ++i) {
+                const double *base = in + i + j * n1 + k * n1 * n2 + (idx_t)order * s;
+                double acc = 0.0;
+                for (int t = 0; t < order; ++t) {
+                    const double diff = base[t * s] - base[-(t + 1) * s];
+                    const double term = (c[t] * diff) / d;
+                    acc = acc + term;
+                }
+                out[i + j * o1 + k * o1 * o2] = acc;
+            }
 }
 
 /* ------------------------------------------------------------------ */

@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     dampPml,
     debug_withhold_copy,
     dCoef,
+    diffOperator,
     enable_timing,
     last_timing,
     fwdTimeCpmlFor2dAw,

@@ -73,6 +73,8 @@ SIGNATURES = {
     "sssi_last_timing": (ctypes.c_int, [c_dp, c_dp, ctypes.c_int, c_dp]),
     "sssi_measure_fp64_rate": (ctypes.c_int, [c_dp]),
     "sssi_dCoef": (ctypes.c_int, [ctypes.c_int, c_dp]),
+    "sssi_diffOperator": (ctypes.c_int, [c_dp, ctypes.c_int, c_dp, c_dp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                         c_dp, ctypes.c_int]),
     "sssi_dampPml": (ctypes.c_int, [c_dp, c_dp, c_i64, ctypes.c_double, c_dp]),
     "sssi_fwdTimeCpmlFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_dp,

@@ -95,6 +95,26 @@ def dampPml(u, v, L: float) -> np.ndarray:
     return d
 
 
+def diffOperator(data, c, d, dim=1, *, mode="fp64"):
+    """diffData = diffOperator(data, c, d, dim) (src/fd_cmex/diffOperator.m): staggered
+    first derivative of a 2D or 3D array along dimension ``dim`` (1-based), whose
+    length shrinks by 2 numel(c) - 1."""
+    pd, kd, shape = _in(data, "data")
+    if len(shape) not in (2, 3):
+        raise ValueError("data must be 2D or 3D")
+    cc = np.ascontiguousarray(np.atleast_1d(np.asarray(c, dtype=np.float64)).ravel())
+    order = len(cc)
+    oshape = list(shape)
+    oshape[int(dim) - 1] -= 2 * order - 1
+    if oshape[int(dim) - 1] < 0:
+        raise ValueError("the stencil is longer than the dimension")
+    out, _ = _out_like(data, tuple(oshape))
+    dims = np.asarray(shape, dtype=np.int64)
+    check(lib().sssi_diffOperator(pd, len(shape), dims.ctypes.data, cc.ctypes.data, order, float(d), int(dim),
+                                  _addr(out), _mode(mode)))
+    return out
+
+
 def fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
     """[data, snapshot] = fwdTimeCpmlFor2dAw(v, source, nDiffOrder, nBoundary, dz, dx, dt)."""
     pv, kv, vshape = _in(v, "v")

@@ -15,6 +15,11 @@ Outputs (all float64, MATLAB index order):
   fwd3d.npz     3D forward (24 x 20 x 18, nt = 32, N = 3, nB = 4) from the C
                 restatement (the reference has no C for 3D; its MATLAB file is
                 restated and cross-checked against the numpy restatement here)
+  diffop.npz    the reference's diffOperator_mex on seeded 2D (37 x 53) and 3D
+                (16 x 13 x 11) arrays, orders 1..5, every dimension, plus the
+                gateway's dim rule (a 2D array takes dim 3 as 2, a 3D one dim 7 as 3)
+
+``python tests/golden/make_golden.py diffop`` writes diffop.npz alone.
 """
 from __future__ import annotations
 
@@ -133,5 +138,35 @@ def main() -> None:
         print(f.name, f.stat().st_size)
 
 
+def make_diffop() -> None:
+    O.build(reference=True)
+    ref = O.RefMex("diffOperator_mex")
+    co = O.COracle()
+    rng = np.random.default_rng(77)
+    rec = {}
+    n = 0
+    for shape in [(37, 53), (16, 13, 11)]:
+        x = rng.standard_normal(shape)
+        rec[f"x{len(shape)}"] = x
+        for order in (1, 2, 3, 4, 5):
+            c = co.dcoef(order)
+            rec[f"c{order}"] = c
+            dims = list(range(1, len(shape) + 1)) + [len(shape) == 2 and 3 or 7]  # and one out-of-range dim
+            for dim in dims:
+                eff = dim if dim <= len(shape) else len(shape)
+                if shape[eff - 1] < 2 * order - 1:
+                    continue
+                out = ref.call(1, x, c, 10.0, dim)[0]
+                assert np.array_equal(out, co.diff_operator(x, c, 10.0, eff))
+                rec[f"d{len(shape)}_o{order}_dim{dim}"] = out
+                n += 1
+    np.savez_compressed(OUT / "diffop.npz", **rec)
+    print("diffop.npz", n, "cases")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "diffop":
+        make_diffop()
+    else:
+        main()
+        make_diffop()

@@ -133,3 +133,25 @@ def test_no_alloc_rejects_sizes_out_of_range(lib):
         rc = lib.sssi_fwdTimeCpmlFor2dAwNoAlloc(None, None, nz, nx, nt, 4, 5, 10.0, 10.0, 1e-3, None, None, 1)
         assert rc == 1, (nz, nx, nt)
         assert b"out of range" in lib.sssi_last_error()
+
+
+def test_diff_operator_gateway_error_message():
+    """diffOperator_mex with too few arguments: the reference's message."""
+    from oracle import oracle as O
+
+    gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_diffOperator_mex.so")
+    with pytest.raises(O.MexError, match="Input data, finite difference coefficients and distance per sample"):
+        O.shim_call(gw, 1, np.ones((5, 5)), np.ones(2))
+
+
+def test_diff_operator_bad_arguments(lib):
+    x = np.ones((10, 10), order="F")
+    dims = np.array([10, 10], dtype=np.int64)
+    c = np.array([1.0, 0.1])
+    out = np.zeros((7, 10), order="F")
+    p = lambda a: a.ctypes.data  # noqa: E731
+    assert lib.sssi_diffOperator(p(x), 4, p(dims), p(c), 2, 1.0, 1, p(out), 1) == 1  # ndims
+    assert lib.sssi_diffOperator(p(x), 2, p(dims), p(c), 2, 1.0, 3, p(out), 1) == 1  # dim
+    assert lib.sssi_diffOperator(p(x), 2, p(dims), p(c), 2, 0.0, 1, p(out), 1) == 1  # distance
+    assert lib.sssi_diffOperator(p(x), 2, p(dims), p(c), 2, 1.0, 1, p(out), 2) == 1  # mode
+    assert b"mode" in lib.sssi_last_error()

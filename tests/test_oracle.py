@@ -170,3 +170,32 @@ def test_ext_boundary_and_ricker(oracle_mod):
     assert W3.shape == (3, 5, 6)
     w = oracle_mod.ricker(20.0, 200, 1e-3)
     assert np.argmax(w) == 50 and abs(w[50] - 1.0) < 1e-12
+
+
+def test_diff_operator_restatement_matches_golden(co, golden):
+    """The C restatement of diffOperator_mex reproduces the reference gateway's
+    outputs (golden vectors made from it), including the gateway's dim rule."""
+    g = golden("diffop.npz")
+    n = 0
+    for key in g.files:
+        if not key.startswith("d"):
+            continue
+        nd, order, dim = key[1], int(key.split("_o")[1].split("_")[0]), int(key.split("dim")[1])
+        x = g[f"x{nd}"]
+        eff = dim if dim <= int(nd) else int(nd)
+        assert np.array_equal(co.diff_operator(x, g[f"c{order}"], 10.0, eff), g[key]), key
+        n += 1
+    assert n >= 30
+
+
+def test_diff_operator_reference_live(co, oracle_mod):
+    if not (oracle_mod.REF_DIR / "diffOperator_mex.so").exists():
+        pytest.skip("reference gateways not built here (no reference tree)")
+    ref = oracle_mod.RefMex("diffOperator_mex")
+    rng = np.random.default_rng(8)
+    for shape in [(41, 29), (9, 23, 12)]:
+        x = rng.standard_normal(shape)
+        for order in (2, 4):
+            for dim in range(1, len(shape) + 1):
+                c = co.dcoef(order)
+                assert np.array_equal(ref.call(1, x, c, 7.5, dim)[0], co.diff_operator(x, c, 7.5, dim))
