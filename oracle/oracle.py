@@ -482,8 +482,24 @@ def _run2d(v, source, rdata, N, nB, dz, dx, dt):
     return fdm[0].copy(), snapshot
 
 
-def fwd3d_np(v, source, N, nB, dz, dx, dy, dt):
-    """fwdTimeCpmlFor3dAw.m restated (src/fwdTimeCpmlFor3dAw.m:37-147)."""
+def reference_diff(gateway: "RefMex"):
+    """A derivative function with _diff's signature that calls the reference's
+    own diffOperator_mex (compiled on the shim): the routine the MATLAB path
+    resolves diffOperator to (src/fd_cmex/diffOperator.m shadows
+    src/fd_matlab/diffOperator.m), so the 3D MATLAB file's derivatives come from
+    the reference's C."""
+    def diff(data, c, d, axis):
+        data = np.asfortranarray(data)
+        return gateway.call(1, data, np.asarray(c, dtype=np.float64), float(d), axis + 1)[0].reshape(
+            data.shape[:axis] + (data.shape[axis] - (2 * len(c) - 1),) + data.shape[axis + 1:], order="F")
+    return diff
+
+
+def fwd3d_np(v, source, N, nB, dz, dx, dy, dt, diff=None):
+    """fwdTimeCpmlFor3dAw.m restated (src/fwdTimeCpmlFor3dAw.m:37-147).  ``diff``
+    replaces the derivative routine (default: the restatement _diff; with
+    reference_diff, the reference's compiled diffOperator_mex)."""
+    _diff = diff or globals()["_diff"]
     v = np.asarray(v, dtype=np.float64)
     nz, nx, ny = v.shape
     nt = source.shape[3]

@@ -14,7 +14,10 @@ Outputs (all float64, MATLAB index order):
                 and image = M./s2 with the sums in ascending time order
   fwd3d.npz     3D forward (24 x 20 x 18, nt = 32, N = 3, nB = 4) from the C
                 restatement (the reference has no C for 3D; its MATLAB file is
-                restated and cross-checked against the numpy restatement here)
+                restated and cross-checked against the numpy restatement here,
+                which is run a second time with the reference's own compiled
+                diffOperator_mex for every derivative: the routine the MATLAB
+                file's diffOperator calls resolve to)
   diffop.npz    the reference's diffOperator_mex on seeded 2D (37 x 53) and 3D
                 (16 x 13 x 11) arrays, orders 1..5, every dimension, plus the
                 gateway's dim rule (a 2D array takes dim 3 as 2, a 3D one dim 7 as 3)
@@ -132,6 +135,9 @@ def main() -> None:
     d3, s3 = co.fwd3d(v, src, N, nB, 10.0, 10.0, 10.0, 1e-3)
     d3n, s3n = O.fwd3d_np(v, src, N, nB, 10.0, 10.0, 10.0, 1e-3)
     assert np.array_equal(d3, d3n) and np.array_equal(s3, s3n)
+    # and with the reference's own compiled diffOperator_mex for every derivative
+    d3r, s3r = O.fwd3d_np(v, src, N, nB, 10.0, 10.0, 10.0, 1e-3, diff=O.reference_diff(O.RefMex("diffOperator_mex")))
+    assert np.array_equal(d3, d3r) and np.array_equal(s3, s3r)
     np.savez_compressed(OUT / "fwd3d.npz", params=np.array([nz, nx, ny, nt, N, nB]), v=v, trace=trace, data=d3,
                         snap_last=s3[:, :, :, -1], snap_mid=s3[:, :, :, nt // 2])
     for f in sorted(OUT.glob("*.npz")):

@@ -199,3 +199,22 @@ def test_diff_operator_reference_live(co, oracle_mod):
             for dim in range(1, len(shape) + 1):
                 c = co.dcoef(order)
                 assert np.array_equal(ref.call(1, x, c, 7.5, dim)[0], co.diff_operator(x, c, 7.5, dim))
+
+
+def test_fwd3d_restatement_with_reference_derivatives(oracle_mod, golden):
+    """The 3D MATLAB file (src/fwdTimeCpmlFor3dAw.m) has no C in the reference, but
+    its derivatives are the reference's C: on the MATLAB path diffOperator is
+    src/fd_cmex/diffOperator.m, i.e. diffOperator_mex.c.  The numpy restatement
+    run with that compiled gateway for every derivative reproduces the 3D golden
+    vectors (from the C restatement) bit for bit, so only the file's
+    elementwise statements remain restated."""
+    if not (oracle_mod.REF_DIR / "diffOperator_mex.so").exists():
+        pytest.skip("reference gateways not built here (no reference tree)")
+    g = golden("fwd3d.npz")
+    nz, nx, ny, nt, N, nB = (int(x) for x in g["params"])
+    src = np.zeros((nz, nx, ny, nt), order="F")
+    src[1, nx // 2, ny // 2, :] = g["trace"]
+    diff = oracle_mod.reference_diff(oracle_mod.RefMex("diffOperator_mex"))
+    d, s = oracle_mod.fwd3d_np(g["v"], src, N, nB, 10.0, 10.0, 10.0, 1e-3, diff=diff)
+    assert np.array_equal(d, g["data"])
+    assert np.array_equal(s[:, :, :, -1], g["snap_last"])
