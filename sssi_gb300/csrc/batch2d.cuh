@@ -108,6 +108,8 @@ __host__ __device__ inline unsigned tile_band_flags(int N, int TZ, int TX, int n
 constexpr unsigned kSchedReverse = 1u, kSchedDense = 2u, kSchedRow = 4u, kSchedSnap = 8u, kSchedImg64 = 16u,
                    kSchedAmax = 32u, kSchedPack = 64u, kSchedImg16 = 128u, kSchedPair = 256u;
 constexpr int kSchedStrideShift = 9;
+// hooks written by rare_outputs (or the block maxima) on some steps
+constexpr unsigned kSchedRareOut = kSchedSnap | kSchedImg64 | kSchedAmax | kSchedPack | kSchedImg16;
 template <typename T>
 inline unsigned sched_word(const ShotTail<T>& d) {
     unsigned w = d.reverse ? kSchedReverse : 0u;
@@ -263,17 +265,18 @@ class Batch2d {
         int grid = 0;
         bool split = false;
         bool pair = false;
+        bool lean = false;
         int shape = 0;
         const void *desc = nullptr, *begin = nullptr, *work = nullptr;
         int debug_step = -1;
         unsigned wait_limit = 0;
         bool operator==(const GraphKey& o) const {
-            return grid == o.grid && split == o.split && pair == o.pair && shape == o.shape && desc == o.desc &&
+            return grid == o.grid && split == o.split && pair == o.pair && lean == o.lean && shape == o.shape && desc == o.desc &&
                    begin == o.begin && work == o.work && debug_step == o.debug_step && wait_limit == o.wait_limit;
         }
     } graph_key_;
     GraphKey current_key() const {
-        return GraphKey{grid_, split_, pair_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(),
+        return GraphKey{grid_, split_, pair_, lean_, shape_, d_desc_.get(), d_cta_begin_[shape_].get(),
                         d_work_[shape_].get(), bc_.debug_step, bc_.wait_limit};
     }
     // tile shape: the schedule in use (BatchShape index) and the tuner (times a
@@ -288,6 +291,8 @@ class Batch2d {
     void use_shape(int shape);
     bool split_ = false;  // the schedule holds half tiles
     bool pair_ = false;   // enabled residual pairs: the launch uses the pair variant (32 x 32 tiles)
+    bool lean_ = false;   // no enabled shot has rare outputs: the variant without them
+    void update_lean();   // from the descriptors as uploaded
     int shape_free_ = 0;  // the tile shape to return to when the last pair leaves
     DeviceBuffer d_desc_, d_ctr_;                // d_ctr_: graph step base, zero, error flag
     DeviceBuffer d_status_;                      // one status word per shot slot
@@ -301,15 +306,17 @@ class Batch2d {
 
 // Launches one batch step with the programmatic-serialization attribute.
 // split: the work lists hold half tiles; shape: BatchShape index; pair: the
-// batch holds residual pairs (FP32, shape 1, no half tiles).
+// batch holds residual pairs (FP32, shape 1, no half tiles); lean: no shot
+// writes snapshots, FP16 packs, maxima or imaging sums (the variant without
+// those outputs; whole tiles only).
 template <typename T, int N>
 void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape, bool pair,
-                      cudaStream_t stream);
+                      bool lean, cudaStream_t stream);
 template <typename T, int N>
 int batch2d_occupancy_n(int shape, bool pair);
 template <typename T>
 void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
-                    bool pair, cudaStream_t stream);
+                    bool pair, bool lean, cudaStream_t stream);
 template <typename T>
 int batch2d_ctas_per_sm(int N, int shape, bool pair);
 

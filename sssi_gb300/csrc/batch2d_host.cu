@@ -700,6 +700,7 @@ void Batch2d<T>::schedule(int shape) {
         d.sched = sched_word(d);
         hdesc[k] = shots_[k].desc;
     }
+    update_lean();
     if (!hdesc.empty())
         SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.get(), hdesc.data(), sizeof(ShotDesc<T>) * hdesc.size(),
                                         cudaMemcpyHostToDevice, stream_));
@@ -721,8 +722,20 @@ void Batch2d<T>::sync_desc(int k) {
     ShotTail<T>& d = shots_[k].desc.s;
     SSSI_REQUIRE(d.stride < (1 << 22), SSSI_ERR_ARG, "snapshot stride %d too large", d.stride);
     d.sched = sched_word(d);
+    update_lean();
     SSSI_CHECK_CUDA(cudaMemcpyAsync(d_desc_.template as<ShotDesc<T>>() + k, &shots_[k].desc, sizeof(ShotDesc<T>),
                                     cudaMemcpyHostToDevice, stream_));
+}
+
+template <typename T>
+void Batch2d<T>::update_lean() {
+    // the variant without rare outputs takes whole single-field tiles; a batch
+    // whose enabled shots write no snapshots, packs, maxima or imaging sums
+    // runs it (the descriptors' sched words are current: called on upload)
+    bool rare = false;
+    for (const Shot& S : shots_)
+        if (!S.free && S.enabled) rare |= (S.desc.s.sched & kSchedRareOut) != 0u;
+    lean_ = !rare;
 }
 
 template <typename T>
@@ -735,7 +748,7 @@ void Batch2d<T>::launch_step(const int* base, int offset, cudaStream_t stream) {
     BatchConst<T> bc = bc_;
     bc.step_base = base;
     bc.step_offset = offset;
-    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, shape_, pair_, stream);
+    launch_batch2d<T>(N_, d_desc_.template as<ShotDesc<T>>(), bc, grid_, split_, shape_, pair_, lean_, stream);
 }
 
 template <typename T>
@@ -864,16 +877,16 @@ void Batch2d<T>::set_debug(int step, unsigned wait_limit) {
 
 template <typename T>
 void launch_batch2d(int N, const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape,
-                    bool pair, cudaStream_t stream) {
+                    bool pair, bool lean, cudaStream_t stream) {
     switch (N) {
-        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, shape, pair, stream); break;
-        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, shape, pair, stream); break;
-        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, shape, pair, stream); break;
-        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, shape, pair, stream); break;
-        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, shape, pair, stream); break;
-        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, shape, pair, stream); break;
-        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, shape, pair, stream); break;
-        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, shape, pair, stream); break;
+        case 1: launch_batch2d_n<T, 1>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 2: launch_batch2d_n<T, 2>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 3: launch_batch2d_n<T, 3>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 4: launch_batch2d_n<T, 4>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 5: launch_batch2d_n<T, 5>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 6: launch_batch2d_n<T, 6>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 7: launch_batch2d_n<T, 7>(shots, bc, grid, split, shape, pair, lean, stream); break;
+        case 8: launch_batch2d_n<T, 8>(shots, bc, grid, split, shape, pair, lean, stream); break;
         default: SSSI_REQUIRE(false, SSSI_ERR_ARG, "nDiffOrder %d out of range 1..8", N);
     }
 }

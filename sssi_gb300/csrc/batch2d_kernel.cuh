@@ -760,7 +760,10 @@ constexpr int kRoleSingle = 0, kRolePairP = 1, kRolePairD = 2;
 // psi_D before the update), and writes D's row 0 to rec_d.  Every factor of
 // the second model is P's FP32 factor plus the exact difference, so the
 // rounding of the models is shared by P and Q and cancels in D.
-template <typename T, int N, class Sh, int RX, int kRole = kRoleSingle>
+// kRareOut: the call to rare_outputs is compiled in (a batch without snapshots,
+// FP16 packs or imaging runs a variant without it: the call's register
+// saves cost the whole-tile loop about 10 %).
+template <typename T, int N, class Sh, int RX, int kRole = kRoleSingle, bool kRareOut = true>
 __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTail<T>& sh, const TileInfo& ti,
                                            const T* Pb, const T* Ob, const T* Vb, int z0, int x0, int r0, int c0,
                                            unsigned flags, const T* scratch, unsigned& amax_bits,
@@ -1107,7 +1110,7 @@ __device__ __forceinline__ void tile_cells(const BatchConst<T>& bc, const ShotTa
             if (bad) atomicExch(sh.status, SSSI_ERR_UNSTABLE);
         }
     }
-    if constexpr (kRole != kRolePairD)
+    if constexpr (kRole != kRolePairD && kRareOut)
         if (flags & kRare) amax_bits = max(amax_bits, rare_outputs<T, RX>(sh, ti, i0, j0, pn, pc));
 }
 
@@ -1167,12 +1170,15 @@ struct StageLayout {
 // kSplit: the work lists may hold half tiles (schedules of small grids); the
 // variant without them keeps the whole-tile path free of their handling.
 // kPair: the batch holds residual pairs (FP32, whole tiles only).
-template <typename T, int N, bool kSplit, class Sh, bool kPair>
+// kRareOut: some shot of the batch writes snapshots, FP16 packs, maxima or
+// imaging sums (without: whole tiles only, no call to rare_outputs).
+template <typename T, int N, bool kSplit, class Sh, bool kPair, bool kRareOut>
 __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh::kMinBlocks)
     batch2d_kernel(const ShotDesc<T>* __restrict__ shots, const __grid_constant__ BatchConst<T> bc) {
     using S = Sh;
     using G = StageLayout<T, N, Sh, kPair>;
     static_assert(!kPair || (std::is_same<T, float>::value && !kSplit), "residual pairs: FP32 whole tiles");
+    static_assert(kRareOut || (!kSplit && !kPair), "the variant without rare outputs takes whole single tiles");
     constexpr int V = Sh::kIndex;  // tensor maps of this shape
     constexpr int TZ = S::TZ, TX = S::TX, RX = S::RX;
     constexpr int HZ = G::HZ, L = G::L;
@@ -1397,10 +1403,11 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
                         __syncthreads();
                     }
                     if (i0 < sh.nz && (j0 | i0) >= 0 && j0 < sh.nx)
-                        tile_cells<T, N, Sh, RX>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0, ti.flags, scratch, amax_bits);
+                        tile_cells<T, N, Sh, RX, kRoleSingle, kRareOut>(bc, sh, ti, Pb, Ob, Vb, z0, x0, r0, c0,
+                                                                        ti.flags, scratch, amax_bits);
                 }
             }
-            if (ti.flags & kAmax) {
+            if (kRareOut && (ti.flags & kAmax)) {
                 // block maxima: one atomic per group of lanes whose cells share a
                 // 32 x 32 scale block (lanes that computed nothing skip)
                 const int nbz = (sh.nz + 31) >> 5;
@@ -1431,12 +1438,12 @@ __global__ void __launch_bounds__(Sh::kThreads, kPair ? Sh::kMinBlocks / 2 : Sh:
 
 }  // namespace batch
 
-template <typename T, int N, bool kSplit, class Sh, bool kPair>
+template <typename T, int N, bool kSplit, class Sh, bool kPair, bool kRareOut = true>
 void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, cudaStream_t stream) {
     using G = batch::StageLayout<T, N, Sh, kPair>;
     static bool configured = false;
     if (!configured) {
-        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit, Sh, kPair>,
+        SSSI_CHECK_CUDA(cudaFuncSetAttribute(batch::batch2d_kernel<T, N, kSplit, Sh, kPair, kRareOut>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem));
         configured = true;
     }
@@ -1450,22 +1457,24 @@ void launch_batch2d_variant(const ShotDesc<T>* shots, const BatchConst<T>& bc, i
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit, Sh, kPair>, shots, bc));
+    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, batch::batch2d_kernel<T, N, kSplit, Sh, kPair, kRareOut>, shots, bc));
     count_launch();
 }
 
 template <typename T, int N, class Sh>
-void launch_batch2d_shape(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split,
+void launch_batch2d_shape(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, bool lean,
                           cudaStream_t stream) {
     if (split)
         launch_batch2d_variant<T, N, true, Sh, false>(shots, bc, grid, stream);
+    else if (lean)
+        launch_batch2d_variant<T, N, false, Sh, false, false>(shots, bc, grid, stream);
     else
         launch_batch2d_variant<T, N, false, Sh, false>(shots, bc, grid, stream);
 }
 
 template <typename T, int N>
 void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int grid, bool split, int shape, bool pair,
-                      cudaStream_t stream) {
+                      bool lean, cudaStream_t stream) {
     if constexpr (kBatchShapes<T> > 1) {
         if (pair) {
             SSSI_REQUIRE(shape == 1 && !split, SSSI_ERR_INTERNAL, "residual pairs run with 32 x 32 whole tiles");
@@ -1473,23 +1482,23 @@ void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int gri
             return;
         }
         if (shape == 1) {
-            launch_batch2d_shape<T, N, BatchShape<T, 1>>(shots, bc, grid, split, stream);
+            launch_batch2d_shape<T, N, BatchShape<T, 1>>(shots, bc, grid, split, lean, stream);
             return;
         }
     }
     SSSI_REQUIRE(!pair, SSSI_ERR_INTERNAL, "residual pairs are FP32 only");
     SSSI_REQUIRE(shape == 0, SSSI_ERR_INTERNAL, "tile shape %d not built for this type", shape);
-    launch_batch2d_shape<T, N, BatchShape<T, 0>>(shots, bc, grid, split, stream);
+    launch_batch2d_shape<T, N, BatchShape<T, 0>>(shots, bc, grid, split, lean, stream);
 }
 
 template <typename T, int N, class Sh, bool kPair>
 int batch2d_occupancy_shape() {
     const size_t smem = batch::StageLayout<T, N, Sh, kPair>::kSmem;
     int n = 0;
-    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false, Sh, kPair>,
+    cudaError_t e = cudaFuncSetAttribute(batch::batch2d_kernel<T, N, false, Sh, kPair, true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false, Sh, kPair>,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch::batch2d_kernel<T, N, false, Sh, kPair, true>,
                                                           Sh::kThreads, smem);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
@@ -1509,7 +1518,7 @@ int batch2d_occupancy_n(int shape, bool pair) {
 
 #define SSSI_BATCH2D_INSTANCE(T, N)                                                                      \
     template void launch_batch2d_n<T, N>(const ShotDesc<T>*, const BatchConst<T>&, int, bool, int, bool, \
-                                         cudaStream_t);                                                  \
+                                         bool, cudaStream_t);                                            \
     template int batch2d_occupancy_n<T, N>(int, bool);
 
 }  // namespace sssi
