@@ -169,6 +169,53 @@ int sssi_rtmTimeCpmlFor2dAw(const double *v, const double *vs, int64_t nz, int64
                             const double *wavelet, int64_t src_iz, int64_t src_ix, double epsilon, int mode,
                             int snap_stride, double *image, double *data_true, double *data_smooth);
 
+/* ---- sponge absorbing boundary (second-order five-point propagator) ----
+ *
+ * The MATLAB propagators src/fwdTimeSpongeFor2dAw.m and
+ * src/rvsTimeSpongeFor2dAw.m (and the RTM shot of
+ * applications/rtm_2d_acoustic/mainRtmTimeSpongeFor2dAw.m) on the device:
+ * zero-bordered field, fdm3 = b.*p - past + ax.*(right+left) + az.*(down+up)
+ * - vdtSq.*source, then the sponge factors
+ * boundary(k) = exp(-(0.015 (nB-k+1))^2)^10 on the new past and present
+ * (left/right columns above the bottom band, bottom rows across).  Note the
+ * minus sign on the source term, as in the reference.
+ * SSSI_MODE_FP64_STRICT rounds as the MATLAB expressions are written (no fused
+ * multiply-add); SSSI_MODE_FP64 fuses; SSSI_MODE_FP32 keeps the field in FP32.
+ * nBoundary must be in 0..min(nz, nx). */
+
+/* [data, snapshot] = fwdTimeSpongeFor2dAw(v, source, nBoundary, dz, dx, dt):
+ * v nz x nx, source nz x nx x nt, data nx x nt (row 0 after every step),
+ * snapshot nz x nx x nt (either output may be NULL).
+ * Replaces src/fwdTimeSpongeFor2dAw.m:1-101. */
+int sssi_fwdTimeSpongeFor2dAw(const double *v, const double *source, int64_t nz, int64_t nx, int64_t nt,
+                              int nBoundary, double dz, double dx, double dt, double *data, double *snapshot,
+                              int mode);
+
+/* The same with nsrc (<= 64) point sources: cell (src_iz[s], src_ix[s]) takes
+ * wavelets[s*nt + t] at step t (sources on one cell add up). */
+int sssi_fwdTimeSpongeFor2dAwPoint(const double *v, int64_t nz, int64_t nx, int64_t nt, int nBoundary, double dz,
+                                   double dx, double dt, int nsrc, const int64_t *src_iz, const int64_t *src_ix,
+                                   const double *wavelets, double *data, double *snapshot, int mode);
+
+/* [model, snapshot] = rvsTimeSpongeFor2dAw(v, data, nBoundary, dz, dx, dt):
+ * data nx x nt enters row 0 with time running nt-1..0; snapshot nz x nx x nt;
+ * model nz x nx is the field after the last step (t = 0) -- the reference
+ * declares this output but never assigns it.
+ * Replaces src/rvsTimeSpongeFor2dAw.m:1-103. */
+int sssi_rvsTimeSpongeFor2dAw(const double *v, const double *data, int64_t nz, int64_t nx, int64_t nt,
+                              int nBoundary, double dz, double dx, double dt, double *model, double *snapshot,
+                              int mode);
+
+/* One sponge RTM shot (mainRtmTimeSpongeFor2dAw.m:160-161,247-268,310):
+ * forward modelling of the point source in v and vs, reverse propagation of
+ * dataTrue - dataSmooth in v, image = M ./ s2 with M = sum_t f_t .* r_t,
+ * s2 = epsilon + sum_t f_t.^2 (f: forward field in vs).  FP64 modes only:
+ * strict keeps both snapshot volumes and sums in the reference's order;
+ * SSSI_MODE_FP64 accumulates inside the reverse step. */
+int sssi_rtmTimeSpongeFor2dAw(const double *v, const double *vs, int64_t nz, int64_t nx, int64_t nt, int nBoundary,
+                              double dz, double dx, double dt, const double *wavelet, int64_t src_iz, int64_t src_ix,
+                              double epsilon, int mode, double *image, double *data_true, double *data_smooth);
+
 /* ---- batched and served shots: the plan API ----
  *
  * The reference runs one shot per MEX call and loops over shots in MATLAB

@@ -101,6 +101,9 @@ class COracle:
         L.orc_image_accum.argtypes = [_dp, _dp, _i64, _dp, _dp]
         L.orc_image_stack.argtypes = [_dp, _dp, _i64, _dp]
         L.orc_diff_operator.argtypes = [_dp, _i64, _i64, _i64, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_sponge2d.argtypes = [_dp, _i64, _i64, _i64, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, _dp, ctypes.c_int, ctypes.POINTER(_i64), ctypes.POINTER(_i64), _dp,
+                                   _dp, _dp, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_num_threads.argtypes = [ctypes.c_int]
 
@@ -121,6 +124,31 @@ class COracle:
         self.lib.orc_diff_operator(_ptr(data), shape[0], shape[1], shape[2], _ptr(c), len(c), float(d), int(dim),
                                    _ptr(out))
         return out
+
+    def sponge2d(self, v, nt, nB, dz, dx, dt, *, source=None, point=None, rdata=None, want_snapshot=True):
+        """Sponge propagation (src/fwdTimeSpongeFor2dAw.m, src/rvsTimeSpongeFor2dAw.m):
+        ``source`` dense (nz, nx, nt), or ``point=(iz, ix, wavelets)``, or ``rdata``
+        (nx, nt) for the reverse pass.  Returns (data, snapshot, last)."""
+        v = _f64(v)
+        nz, nx = v.shape
+        src = _f64(source) if source is not None else None
+        iz = ix = w = None
+        nsrc = 0
+        if point is not None:
+            iz = np.ascontiguousarray(np.atleast_1d(point[0]), dtype=np.int64)
+            ix = np.ascontiguousarray(np.atleast_1d(point[1]), dtype=np.int64)
+            w = np.ascontiguousarray(np.atleast_2d(np.asarray(point[2], dtype=np.float64)))
+            nsrc = len(iz)
+        rd = _f64(rdata) if rdata is not None else None
+        data = np.zeros((nx, nt), order="F")
+        snap = np.zeros((nz, nx, nt), order="F") if want_snapshot else None
+        last = np.zeros((nz, nx), order="F")
+        ip = (lambda a: a.ctypes.data_as(ctypes.POINTER(_i64)) if a is not None else None)
+        rc = self.lib.orc_sponge2d(_ptr(v), nz, nx, int(nt), int(nB), float(dz), float(dx), float(dt), _ptr(src),
+                                   nsrc, ip(iz), ip(ix), _ptr(w), _ptr(rd), _ptr(data), _ptr(snap), _ptr(last))
+        if rc:
+            raise MemoryError("orc_sponge2d: allocation failed")
+        return data, snap, last
 
     def dcoef(self, order: int) -> np.ndarray:
         c = np.zeros(order)
@@ -577,6 +605,119 @@ def image_np(fwd_snap, rvs_snap, epsilon):
         m = fwd_snap[:, :, t] * rvs_snap[:, :, t] + m
         s2 = fwd_snap[:, :, t] ** 2 + s2
     return m / s2
+
+
+# ---------------------------------------------------------------- sponge ABC
+# Restatement of src/fwdTimeSpongeFor2dAw.m:36-101 and
+# src/rvsTimeSpongeFor2dAw.m:36-103 (MATLAB only in the reference: parity of
+# this part is unpinned -- no compiled reference exists to check it against).
+SPONGE_ALPHA = 0.015  # src/fwdTimeSpongeFor2dAw.m:45
+
+
+def sponge_profile(nB: int) -> np.ndarray:
+    """boundary = (exp(-((alpha*(nB-iz)).^2))).^10 for iz = 0..nB-1
+    (src/fwdTimeSpongeFor2dAw.m:43-47), with glibc's exp and pow."""
+    out = np.zeros(nB)
+    for iz in range(nB):
+        a = SPONGE_ALPHA * float(nB - iz)
+        out[iz] = math.pow(math.exp(-(a * a)), 10.0)
+    return out
+
+
+def _sponge_run(v, src_slice, nt, nB, dz, dx, dt, reverse=False):
+    """The time loop of the two sponge propagators.  src_slice(it) returns the
+    nz x nx source of step it (or None); returns (data nx x nt, snapshot
+    nz x nx x nt, final present nz x nx)."""
+    v = np.asarray(v, dtype=np.float64)
+    nz, nx = v.shape
+    boundary = sponge_profile(nB)
+    t = v * dt / dx
+    ax = t * t
+    t = v * dt / dz
+    az = t * t
+    t = v * dt
+    vdtSq = t * t
+    b = 2 - 2 * ax - 2 * az
+    fdm = [np.zeros((nz + 2, nx + 2)) for _ in range(3)]
+    data = np.zeros((nx, nt))
+    snapshot = np.zeros((nz, nx, nt))
+    izb = slice(1, nz - nB + 1)  # rows (1:nz-nB)+1 of the padded field, 0-based
+    steps = range(nt - 1, -1, -1) if reverse else range(nt)
+    for it in steps:
+        P = fdm[1]
+        new = b * P[1:-1, 1:-1] - fdm[0][1:-1, 1:-1] + ax * (P[1:-1, 2:] + P[1:-1, :-2]) \
+            + az * (P[2:, 1:-1] + P[:-2, 1:-1])
+        s = src_slice(it)
+        if s is not None:
+            new = new - vdtSq * s
+        fdm[2][1:-1, 1:-1] = new
+        fdm[0] = fdm[1].copy()
+        fdm[1] = fdm[2].copy()
+        for ixb in range(2, nB + 2):  # 1-based padded column ixb
+            c = ixb - 1
+            for f in (fdm[0], fdm[1]):
+                f[izb, c] = boundary[ixb - 2] * f[izb, c]
+            ixb2 = nx - nB + ixb
+            c2 = ixb2 - 1
+            for f in (fdm[0], fdm[1]):
+                f[izb, c2] = boundary[nx - ixb2 + 1] * f[izb, c2]
+            izb2 = nz - nB + ixb
+            r2 = izb2 - 1
+            for f in (fdm[0], fdm[1]):
+                f[r2, :] = boundary[nz - izb2 + 1] * f[r2, :]
+        data[:, it] = fdm[1][1, 1:-1]
+        snapshot[:, :, it] = fdm[1][1:-1, 1:-1]
+    return data, snapshot, fdm[1][1:-1, 1:-1].copy()
+
+
+def fwd_sponge_np(v, source, nB, dz, dx, dt):
+    """[data, snapshot] = fwdTimeSpongeFor2dAw(v, source, nBoundary, dz, dx, dt)."""
+    source = np.asarray(source, dtype=np.float64)
+    data, snap, _ = _sponge_run(v, lambda it: source[:, :, it], source.shape[2], nB, dz, dx, dt)
+    return data, snap
+
+
+def fwd_sponge_point_np(v, nt, src_iz, src_ix, wavelets, nB, dz, dx, dt):
+    """The same with point sources (sources on one cell add up, in order)."""
+    v = np.asarray(v, dtype=np.float64)
+    w = np.atleast_2d(np.asarray(wavelets, dtype=np.float64))
+    iz, ix = np.atleast_1d(src_iz), np.atleast_1d(src_ix)
+
+    def slice_at(it):
+        s = np.zeros(v.shape)
+        seen = set()
+        for k in range(len(iz)):
+            key = (int(iz[k]), int(ix[k]))
+            s[key] = s[key] + w[k, it] if key in seen else w[k, it]
+            seen.add(key)
+        return s
+    data, snap, _ = _sponge_run(v, slice_at, nt, nB, dz, dx, dt)
+    return data, snap
+
+
+def rvs_sponge_np(v, data, nB, dz, dx, dt):
+    """[model, snapshot] = rvsTimeSpongeFor2dAw(v, data, nBoundary, dz, dx, dt);
+    model is the field after the last step (the reference never assigns it)."""
+    v = np.asarray(v, dtype=np.float64)
+    data = np.asarray(data, dtype=np.float64)
+
+    def slice_at(it):
+        s = np.zeros(v.shape)
+        s[0, :] = data[:, it]
+        return s
+    _, snap, model = _sponge_run(v, slice_at, data.shape[1], nB, dz, dx, dt, reverse=True)
+    return model, snap
+
+
+def rtm_sponge_np(v, vs, wavelet, src_iz, src_ix, nB, dz, dx, dt, epsilon):
+    """One shot of mainRtmTimeSpongeFor2dAw.m:160-161,247-268,310: returns
+    (M./s2, dataTrue, dataSmooth)."""
+    w = np.asarray(wavelet, dtype=np.float64).ravel()
+    nt = len(w)
+    d_true, _ = fwd_sponge_point_np(v, nt, [src_iz], [src_ix], w[None, :], nB, dz, dx, dt)
+    d_smooth, f_snap = fwd_sponge_point_np(vs, nt, [src_iz], [src_ix], w[None, :], nB, dz, dx, dt)
+    _, r_snap = rvs_sponge_np(v, d_true - d_smooth, nB, dz, dx, dt)
+    return image_np(f_snap, r_snap, epsilon), d_true, d_smooth
 
 
 def rel_l2(a, b) -> float:

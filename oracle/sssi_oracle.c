@@ -20,6 +20,10 @@
  *   orc_image_stack  applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:315
  *   orc_diff_operator src/fd_cmex/diffOperator_mex.c:29-213 (the stand-alone
  *                    staggered derivative of a 2D/3D array along one dimension)
+ *   orc_sponge2d     src/fwdTimeSpongeFor2dAw.m:36-101 and
+ *                    src/rvsTimeSpongeFor2dAw.m:36-103 (MATLAB only in the
+ *                    reference: second-order five-point update, sponge
+ *                    factors on the new past and present)
  *
  * Index algebra of one step (0-based, column-major, l = 2N-1 zero rows and
  * columns of padding on every side of the padded wavefield P):
@@ -697,6 +701,101 @@ int orc_fwd3d(const double *v, const double *source, const double *src_trace, id
     free(Pb);
     free(Pc);
     free(slice);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Sponge-ABC propagation (forward, or reverse with data on row 0).  The    */
+/* zero-bordered (nz+2) x (nx+2) fields of the MATLAB file, its expression */
+/* order b.*P - Pold + ax.*(R+L) + az.*(D+U) - vdtSq.*src, the rotation     */
+/* and the sponge loop over ixb = 2..nB+1 (left column, right column,       */
+/* bottom row; past then present) as written.  src_dense: nz x nx x nt;     */
+/* point sources: nsrc cells with wavelets[k*nt + t]; rdata (reverse): nx x  */
+/* nt on row 0.  Outputs (each optional): data nx x nt, snapshot nz x nx x  */
+/* nt, last (nz x nx, the present after the final step).                   */
+/* ------------------------------------------------------------------ */
+int orc_sponge2d(const double *v, idx_t nz, idx_t nx, idx_t nt, int nB, double dz, double dx, double dt,
+                 const double *src_dense, int nsrc, const idx_t *src_iz, const idx_t *src_ix, const double *wav,
+                 const double *rdata, double *data, double *snapshot, double *last) {
+    const idx_t Nz = nz + 2, Nx = nx + 2, n = nz * nx;
+    double *bnd = (double *)malloc(sizeof(double) * (nB > 0 ? nB : 1));
+    double *ax = (double *)malloc(sizeof(double) * n), *az = (double *)malloc(sizeof(double) * n);
+    double *vs = (double *)malloc(sizeof(double) * n), *b = (double *)malloc(sizeof(double) * n);
+    double *f1 = (double *)calloc((size_t)(Nz * Nx), sizeof(double));
+    double *f2 = (double *)calloc((size_t)(Nz * Nx), sizeof(double));
+    double *f3 = (double *)calloc((size_t)(Nz * Nx), sizeof(double));
+    double *src = (double *)calloc((size_t)n, sizeof(double));
+    if (!bnd || !ax || !az || !vs || !b || !f1 || !f2 || !f3 || !src) return -1;
+    for (int iz = 0; iz < nB; ++iz) {
+        const double a = 0.015 * (double)(nB - iz);
+        bnd[iz] = pow(exp(-(a * a)), 10.0);
+    }
+    for (idx_t q = 0; q < n; ++q) {
+        double t = v[q] * dt / dx;
+        ax[q] = t * t;
+        t = v[q] * dt / dz;
+        az[q] = t * t;
+        t = v[q] * dt;
+        vs[q] = t * t;
+        b[q] = 2 - 2 * ax[q] - 2 * az[q];
+    }
+    for (idx_t step = 0; step < nt; ++step) {
+        const idx_t it = rdata ? nt - 1 - step : step;
+        const double *sl = NULL;
+        if (src_dense) {
+            sl = src_dense + it * n;
+        } else if (nsrc > 0 || rdata) {
+            memset(src, 0, sizeof(double) * n);
+            if (rdata)
+                for (idx_t j = 0; j < nx; ++j) src[j * nz] = rdata[j + it * nx];
+            for (int k = 0; k < nsrc; ++k) {
+                const idx_t q = src_iz[k] + src_ix[k] * nz;
+                int dup = 0;
+                for (int m = 0; m < k; ++m) dup |= src_iz[m] == src_iz[k] && src_ix[m] == src_ix[k];
+                src[q] = dup ? src[q] + wav[k * nt + it] : wav[k * nt + it];
+            }
+            sl = src;
+        }
+#pragma omp parallel for schedule(static)
+        for (idx_t j = 0; j < nx; ++j)
+            for (idx_t i = 0; i < nz; ++i) {
+                const idx_t p = (i + 1) + (j + 1) * Nz, q = i + j * nz;
+                double r = b[q] * f2[p] - f1[p] + ax[q] * (f2[p + Nz] + f2[p - Nz]) + az[q] * (f2[p + 1] + f2[p - 1]);
+                if (sl) r = r - vs[q] * sl[q];
+                f3[p] = r;
+            }
+        double *tmp = f1; /* fdm1 <- fdm2, fdm2 <- fdm3 (f3 is fully rewritten next step) */
+        f1 = f2;
+        f2 = f3;
+        f3 = tmp;
+        for (int ixb = 2; ixb <= nB + 1; ++ixb) {
+            const idx_t c = ixb - 1, c2 = nx - nB + ixb - 1, r2 = nz - nB + ixb - 1;
+            const double bl = bnd[ixb - 2], br = bnd[nx - (nx - nB + ixb) + 1], bb = bnd[nz - (nz - nB + ixb) + 1];
+            double *fs[2] = {f1, f2};
+            for (int w = 0; w < 2; ++w)
+                for (idx_t i = 1; i <= nz - nB; ++i) fs[w][i + c * Nz] = bl * fs[w][i + c * Nz];
+            for (int w = 0; w < 2; ++w)
+                for (idx_t i = 1; i <= nz - nB; ++i) fs[w][i + c2 * Nz] = br * fs[w][i + c2 * Nz];
+            for (int w = 0; w < 2; ++w)
+                for (idx_t j = 0; j < Nx; ++j) fs[w][r2 + j * Nz] = bb * fs[w][r2 + j * Nz];
+        }
+        if (data)
+            for (idx_t j = 0; j < nx; ++j) data[j + it * nx] = f2[1 + (j + 1) * Nz];
+        if (snapshot)
+            for (idx_t j = 0; j < nx; ++j)
+                memcpy(snapshot + it * n + j * nz, f2 + 1 + (j + 1) * Nz, sizeof(double) * nz);
+    }
+    if (last)
+        for (idx_t j = 0; j < nx; ++j) memcpy(last + j * nz, f2 + 1 + (j + 1) * Nz, sizeof(double) * nz);
+    free(bnd);
+    free(ax);
+    free(az);
+    free(vs);
+    free(b);
+    free(f1);
+    free(f2);
+    free(f3);
+    free(src);
     return 0;
 }
 

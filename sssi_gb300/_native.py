@@ -95,6 +95,16 @@ SIGNATURES = {
     "sssi_fwdTimeCpmlFor2dAwNoAlloc": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_dp,
                                                        ctypes.c_int]),
+    "sssi_fwdTimeSpongeFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double, c_dp, c_dp, ctypes.c_int]),
+    "sssi_fwdTimeSpongeFor2dAwPoint": (ctypes.c_int, [c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_double,
+                                                       ctypes.c_double, ctypes.c_double, ctypes.c_int, c_dp, c_dp,
+                                                       c_dp, c_dp, c_dp, ctypes.c_int]),
+    "sssi_rvsTimeSpongeFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double, c_dp, c_dp, ctypes.c_int]),
+    "sssi_rtmTimeSpongeFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double, c_dp, c_i64, c_i64,
+                                                  ctypes.c_double, ctypes.c_int, c_dp, c_dp, c_dp]),
     "sssi_rtmTimeCpmlFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_i64,
                                                 c_i64, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_dp, c_dp,

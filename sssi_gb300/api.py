@@ -233,6 +233,89 @@ def rtmTimeCpmlFor2dAw(v, vs, wavelet, src_iz, src_ix, nDiffOrder, nBoundary, dz
     return image
 
 
+def fwdTimeSpongeFor2dAw(v, source, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
+    """[data, snapshot] = fwdTimeSpongeFor2dAw(v, source, nBoundary, dz, dx, dt)
+    (src/fwdTimeSpongeFor2dAw.m): second-order five-point propagation with the
+    sponge absorbing boundary."""
+    pv, kv, vshape = _in(v, "v")
+    ps, ks, sshape = _in(source, "source")
+    if vshape is None or len(vshape) != 2:
+        raise ValueError("v must be nz x nx")
+    nz, nx = vshape
+    if sshape is None or len(sshape) != 3 or sshape[:2] != (nz, nx):
+        raise ValueError("source must be nz x nx x nt with the grid of v")
+    nt = sshape[2]
+    data, _ = _out_like(v, (nx, nt))
+    snap, _ = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeSpongeFor2dAw(pv, ps, nz, nx, nt, int(nBoundary), float(dz), float(dx), float(dt),
+                                          _addr(data), _addr(snap), _mode(mode)))
+    return data, snap
+
+
+def fwdTimeSpongeFor2dAwPoint(v, nt, src_iz, src_ix, wavelets, nBoundary, dz, dx, dt, *, mode="fp64",
+                              want_snapshot=False):
+    """Sponge forward modelling with point sources: source s at interior
+    (src_iz[s], src_ix[s]) with amplitude wavelets[s, t].  Returns (data,
+    snapshot or None)."""
+    pv, kv, vshape = _in(v, "v")
+    if vshape is None or len(vshape) != 2:
+        raise ValueError("v must be nz x nx")
+    nz, nx = vshape
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or len(ix) != len(iz):
+        raise ValueError("wavelets must be nsrc x nt and src_iz/src_ix of length nsrc")
+    data, _ = _out_like(v, (nx, nt))
+    snap, _ = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_fwdTimeSpongeFor2dAwPoint(pv, nz, nx, int(nt), int(nBoundary), float(dz), float(dx), float(dt),
+                                               len(iz), iz.ctypes.data, ix.ctypes.data, w.ctypes.data, _addr(data),
+                                               _addr(snap), _mode(mode)))
+    return data, snap
+
+
+def rvsTimeSpongeFor2dAw(v, data, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
+    """[model, snapshot] = rvsTimeSpongeFor2dAw(v, data, nBoundary, dz, dx, dt)
+    (src/rvsTimeSpongeFor2dAw.m).  ``model`` (nz x nx) is the field after the
+    last step; the reference declares that output without assigning it."""
+    pv, kv, vshape = _in(v, "v")
+    pd, kd, dshape = _in(data, "data")
+    if vshape is None or len(vshape) != 2:
+        raise ValueError("v must be nz x nx")
+    nz, nx = vshape
+    if dshape is None or len(dshape) != 2 or dshape[0] != nx:
+        raise ValueError("data must be nx x nt")
+    nt = dshape[1]
+    model, _ = _out_like(v, (nz, nx))
+    snap, _ = _out_like(v, (nz, nx, nt)) if want_snapshot else (None, None)
+    check(lib().sssi_rvsTimeSpongeFor2dAw(pv, pd, nz, nx, nt, int(nBoundary), float(dz), float(dx), float(dt),
+                                          _addr(model), _addr(snap), _mode(mode)))
+    return model, snap
+
+
+def rtmTimeSpongeFor2dAw(v, vs, wavelet, src_iz, src_ix, nBoundary, dz, dx, dt, *, epsilon=1e-3, mode="fp64",
+                         want_data=False):
+    """One sponge RTM shot: image = M./s2 of mainRtmTimeSpongeFor2dAw.m:247-268,310
+    for a point source at interior (src_iz, src_ix).  FP64 modes only.
+    Returns image, or (image, dataTrue, dataSmooth) with ``want_data``."""
+    pv, kv, vshape = _in(v, "v")
+    pvs, kvs, vsshape = _in(vs, "vs")
+    pw, kw, wshape = _in(wavelet, "wavelet")
+    if vshape != vsshape or len(vshape) != 2:
+        raise ValueError("v and vs must be nz x nx of the same size")
+    nz, nx = vshape
+    nt = wshape[0]
+    image, _ = _out_like(v, (nz, nx))
+    dt_, _ = _out_like(v, (nx, nt)) if want_data else (None, None)
+    ds_, _ = _out_like(v, (nx, nt)) if want_data else (None, None)
+    check(lib().sssi_rtmTimeSpongeFor2dAw(pv, pvs, nz, nx, nt, int(nBoundary), float(dz), float(dx), float(dt), pw,
+                                          int(src_iz), int(src_ix), float(epsilon), _mode(mode), _addr(image),
+                                          _addr(dt_), _addr(ds_)))
+    if want_data:
+        return image, dt_, ds_
+    return image
+
+
 def set_stream(stream) -> None:
     """Make the library launch on ``stream`` (a torch.cuda.Stream, a raw handle, or None)."""
     handle = getattr(stream, "cuda_stream", stream) or 0

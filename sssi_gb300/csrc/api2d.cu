@@ -53,21 +53,6 @@ __global__ void padded_to_dense_kernel(const T* base, int64_t ldp, int64_t row0,
     }
 }
 
-// Exact-order imaging: M = f_t*r_t + M, s2 = f_t^2 + s2 for t = 0..nt-1
-// (mainRtmTimeCpmlFor2dAw.m:268-275), then image = M ./ s2.
-__global__ void image_ascending_kernel(const double* f, const double* r, int64_t n, int64_t nt, double eps,
-                                       double* image) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        double m = 0.0, s2 = eps;
-        for (int64_t t = 0; t < nt; ++t) {
-            const double ft = f[q + t * n], rt = r[q + t * n];
-            m = __dadd_rn(__dmul_rn(ft, rt), m);
-            s2 = __dadd_rn(__dmul_rn(ft, ft), s2);
-        }
-        image[q] = __ddiv_rn(m, s2);
-    }
-}
-
 template <class Prop>
 void download_padded(const Prop& st, bool previous, double* model, cudaStream_t s) {
     using T = typename Prop::value_type;

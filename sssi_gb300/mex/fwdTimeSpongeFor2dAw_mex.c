@@ -1,0 +1,65 @@
+/*
+ * fwdTimeSpongeFor2dAw_mex.c -- MEX gateway of 2D acoustic forward modelling
+ * with the sponge absorbing boundary on the GPU.  The reference computes this
+ * in MATLAB only (src/fwdTimeSpongeFor2dAw.m:1-101); with this gateway that
+ * file becomes a one-line wrapper:
+ *
+ *   function [data, snapshot] = fwdTimeSpongeFor2dAw(v, source, nBoundary, dz, dx, dt)
+ *   [data, snapshot] = fwdTimeSpongeFor2dAw_mex(v, source, nBoundary, dz, dx, dt);
+ *
+ *     v        nz x nx         velocity
+ *     source   nz x nx x nt    dense source (subtracted, scaled by (v dt)^2)
+ *     data     nx x nt         top row of every step
+ *     snapshot nz x nx x nt    field of every step (only computed when the
+ *                              caller asks for two outputs)
+ *
+ * The work is done by sssi_fwdTimeSpongeFor2dAw (libsssi_gb300) in fused FP64
+ * unless the environment variable SSSI_MEX_MODE is "strict" (the MATLAB
+ * file's rounding sequence) or "fp32".
+ *
+ * Build against MATLAB:  mex -I<repo>/include fwdTimeSpongeFor2dAw_mex.c -L<lib> -lsssi_gb300
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "mex.h"
+#include "sssi_gb300.h"
+
+static int sssi_mex_mode(void) {
+    const char *m = getenv("SSSI_MEX_MODE");
+    if (m && !strcmp(m, "strict")) return SSSI_MODE_FP64_STRICT;
+    if (m && !strcmp(m, "fp32")) return SSSI_MODE_FP32;
+    return SSSI_MODE_FP64;
+}
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
+    const mwSize *dims;
+    mwSize nd, nz, nx, nt, snapdims[3];
+    int boundary, rc;
+    double *snap = NULL;
+
+    if (nrhs < 6) mexErrMsgTxt("All 6 input arguments shall be provided!");
+
+    dims = mxGetDimensions(prhs[1]);
+    nd = mxGetNumberOfDimensions(prhs[1]);
+    nz = dims[0];
+    nx = dims[1];
+    nt = nd >= 3 ? dims[2] : 1;
+    if (mxGetM(prhs[0]) != nz || mxGetN(prhs[0]) != nx)
+        mexErrMsgTxt("Velocity model and source grids should have the same z-axis and x-axis grids!");
+    boundary = (int)*mxGetPr(prhs[2]);
+
+    plhs[0] = mxCreateDoubleMatrix(nx, nt, mxREAL);
+    if (nlhs >= 2) {
+        snapdims[0] = nz;
+        snapdims[1] = nx;
+        snapdims[2] = nt;
+        plhs[1] = mxCreateNumericArray(3, snapdims, mxDOUBLE_CLASS, mxREAL);
+        snap = mxGetPr(plhs[1]);
+    }
+
+    rc = sssi_fwdTimeSpongeFor2dAw(mxGetPr(prhs[0]), mxGetPr(prhs[1]), (int64_t)nz, (int64_t)nx, (int64_t)nt,
+                                   boundary, *mxGetPr(prhs[3]), *mxGetPr(prhs[4]), *mxGetPr(prhs[5]),
+                                   mxGetPr(plhs[0]), snap, sssi_mex_mode());
+    if (rc != SSSI_OK) mexErrMsgIdAndTxt("sssi:fwdTimeSpongeFor2dAw", "%s", sssi_last_error());
+}

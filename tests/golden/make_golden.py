@@ -22,7 +22,17 @@ Outputs (all float64, MATLAB index order):
                 (16 x 13 x 11) arrays, orders 1..5, every dimension, plus the
                 gateway's dim rule (a 2D array takes dim 3 as 2, a 3D one dim 7 as 3)
 
-``python tests/golden/make_golden.py diffop`` writes diffop.npz alone.
+  sponge2d.npz  sponge-ABC forward and reverse (src/fwdTimeSpongeFor2dAw.m,
+                src/rvsTimeSpongeFor2dAw.m; MATLAB only in the reference) on
+                four grids (side bands overlapping when nx < 2 nB, nx == nB,
+                no sponge) and one sponge RTM shot, from the numpy restatement,
+                which must agree bit for bit with the C restatement first.
+                These two restatements are the only pin of that part: no
+                compiled reference exists for it.
+
+``python tests/golden/make_golden.py diffop`` writes diffop.npz alone; ``sponge``
+writes sponge2d.npz alone (it needs only the two restatements, not the
+reference tree).
 """
 from __future__ import annotations
 
@@ -170,9 +180,62 @@ def make_diffop() -> None:
     print("diffop.npz", n, "cases")
 
 
+SPONGE_CASES = [(33, 47, 60, 6), (40, 30, 50, 18), (25, 20, 40, 20), (30, 41, 50, 0)]
+
+
+def make_sponge() -> None:
+    O.build(reference=False)
+    co = O.COracle()
+    rec = {}
+    for k, (nz, nx, nt, nB) in enumerate(SPONGE_CASES):
+        rng = np.random.default_rng(3000 + k)
+        v = rng.uniform(1500.0, 4000.0, (nz, nx))
+        trace, imp, amp = source_2d(rng, nz, nx, nt)
+        src = dense_source(nz, nx, nt, trace, imp, amp)
+        dz, dx, dt = 10.0, 12.0, 1e-3
+        data, snap = O.fwd_sponge_np(v, src, nB, dz, dx, dt)
+        model, rsnap = O.rvs_sponge_np(v, data, nB, dz, dx, dt)
+        dc, sc, _ = co.sponge2d(v, nt, nB, dz, dx, dt, source=src)
+        _, rc, mc = co.sponge2d(v, nt, nB, dz, dx, dt, rdata=data)
+        assert np.array_equal(dc, data) and np.array_equal(sc, snap)
+        assert np.array_equal(mc, model) and np.array_equal(rc, rsnap)
+        pre = f"c{k}_"
+        rec.update({pre + "params": np.array([nz, nx, nt, nB]), pre + "v": v, pre + "trace": trace,
+                    pre + "imp": imp, pre + "amp": amp, pre + "data": data, pre + "snap_mid": snap[:, :, nt // 2],
+                    pre + "snap_last": snap[:, :, -1], pre + "model": model, pre + "rsnap_first": rsnap[:, :, 0],
+                    pre + "rsnap_mid": rsnap[:, :, nt // 2]})
+    rec["ncases"] = np.array(len(SPONGE_CASES))
+    rec["dzdxdt"] = np.array([10.0, 12.0, 1e-3])
+    # one sponge RTM shot
+    nz, nx, nt, nB = 40, 60, 150, 10
+    rng = np.random.default_rng(4040)
+    v = np.full((nz, nx), 2000.0)
+    v[18:, :] = 2600.0
+    v[30:, :] = 3300.0
+    v += rng.uniform(-50, 50, (nz, nx))
+    vs = v.copy()
+    for _ in range(4):
+        vs[1:-1, 1:-1] = 0.2 * (vs[1:-1, 1:-1] + vs[:-2, 1:-1] + vs[2:, 1:-1] + vs[1:-1, :-2] + vs[1:-1, 2:])
+    trace = O.ricker(30.0, nt, 1e-3)
+    image, d_true, d_smooth = O.rtm_sponge_np(v, vs, trace, 0, nx // 2, nB, 10.0, 10.0, 1e-3, 1e-3)
+    dct, _, _ = co.sponge2d(v, nt, nB, 10.0, 10.0, 1e-3, point=([0], [nx // 2], trace[None, :]), want_snapshot=False)
+    dcs, fcs, _ = co.sponge2d(vs, nt, nB, 10.0, 10.0, 1e-3, point=([0], [nx // 2], trace[None, :]))
+    _, rcs, _ = co.sponge2d(v, nt, nB, 10.0, 10.0, 1e-3, rdata=dct - dcs)
+    assert np.array_equal(dct, d_true) and np.array_equal(dcs, d_smooth)
+    assert np.array_equal(O.image_np(fcs, rcs, 1e-3), image)
+    rec.update({"rtm_params": np.array([nz, nx, nt, nB]), "rtm_v": v, "rtm_vs": vs, "rtm_trace": trace,
+                "rtm_src_ix": np.array(nx // 2), "rtm_image": image, "rtm_data_true": d_true,
+                "rtm_data_smooth": d_smooth})
+    np.savez_compressed(OUT / "sponge2d.npz", **rec)
+    print("sponge2d.npz", (OUT / "sponge2d.npz").stat().st_size)
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "diffop":
         make_diffop()
+    elif len(sys.argv) > 1 and sys.argv[1] == "sponge":
+        make_sponge()
     else:
         main()
         make_diffop()
+        make_sponge()

@@ -102,7 +102,8 @@ def test_mex_gateways_export_mexfunction():
     import subprocess
 
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "mexgw"], check=True)
-    for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex", "fwdTimeCpmlFor3dAw_mex"):
+    for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex", "fwdTimeCpmlFor3dAw_mex",
+                 "fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex"):
         gw = ctypes.CDLL(str(ROOT / "oracle" / "_build" / f"mexgw_{name}.so"), mode=ctypes.RTLD_LOCAL)
         assert hasattr(gw, "mexFunction")
 
@@ -155,3 +156,36 @@ def test_diff_operator_bad_arguments(lib):
     assert lib.sssi_diffOperator(p(x), 2, p(dims), p(c), 2, 0.0, 1, p(out), 1) == 1  # distance
     assert lib.sssi_diffOperator(p(x), 2, p(dims), p(c), 2, 1.0, 1, p(out), 2) == 1  # mode
     assert b"mode" in lib.sssi_last_error()
+
+
+def test_sponge_bad_arguments(lib):
+    v = np.full((20, 30), 2000.0, order="F")
+    src = np.zeros((20, 30, 5), order="F")
+    out = np.zeros((30, 5), order="F")
+    p = lambda a: a.ctypes.data  # noqa: E731
+    # the sponge must lie inside the grid
+    rc = lib.sssi_fwdTimeSpongeFor2dAw(p(v), p(src), 20, 30, 5, 21, 10.0, 10.0, 1e-3, p(out), None, 1)
+    assert rc == 1 and b"nBoundary" in lib.sssi_last_error()
+    rc = lib.sssi_rvsTimeSpongeFor2dAw(p(v), p(out), 20, 30, 5, 3, 10.0, 0.0, 1e-3, None, None, 1)
+    assert rc == 1
+    rc = lib.sssi_fwdTimeSpongeFor2dAw(p(v), p(src), 20, 30, 5, 3, 10.0, 10.0, 1e-3, p(out), None, 7)
+    assert rc == 1 and b"mode" in lib.sssi_last_error()
+    img = np.zeros((20, 30), order="F")
+    w = np.zeros(5)
+    rc = lib.sssi_rtmTimeSpongeFor2dAw(p(v), p(v), 20, 30, 5, 3, 10.0, 10.0, 1e-3, p(w), 2, 3, 1e-3, 2, p(img),
+                                       None, None)
+    assert rc == 1 and b"FP64" in lib.sssi_last_error()  # the sponge RTM shot is FP64 only
+    iz = np.array([25], dtype=np.int64)
+    ix = np.array([3], dtype=np.int64)
+    rc = lib.sssi_fwdTimeSpongeFor2dAwPoint(p(v), 20, 30, 5, 3, 10.0, 10.0, 1e-3, 65, p(iz), p(ix), p(w), p(out),
+                                            None, 1)
+    assert rc == 1 and b"nsrc" in lib.sssi_last_error()
+
+
+def test_sponge_gateway_error_messages():
+    from oracle import oracle as O
+
+    for name in ("fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex"):
+        gw = O.load_shim_library(ROOT / "oracle" / "_build" / f"mexgw_{name}.so")
+        with pytest.raises(O.MexError, match="All 6 input arguments shall be provided!"):
+            O.shim_call(gw, 2, np.ones((3, 3)), np.zeros((3, 3, 2)))

@@ -218,3 +218,62 @@ def test_fwd3d_restatement_with_reference_derivatives(oracle_mod, golden):
     d, s = oracle_mod.fwd3d_np(g["v"], src, N, nB, 10.0, 10.0, 10.0, 1e-3, diff=diff)
     assert np.array_equal(d, g["data"])
     assert np.array_equal(s[:, :, :, -1], g["snap_last"])
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_sponge_restatements_match_golden(co, oracle_mod, golden, k):
+    """The two sponge restatements (numpy and C; the reference's sponge
+    propagators are MATLAB only, so these are its only pin) reproduce the
+    committed vectors bit for bit, including the overlapping side bands
+    (nx < 2 nB), nx == nB and the case without a sponge."""
+    g = golden("sponge2d.npz")
+    nz, nx, nt, nB = (int(x) for x in g[f"c{k}_params"])
+    dz, dx, dt = (float(x) for x in g["dzdxdt"])
+    v = g[f"c{k}_v"]
+    src = dense_source(nz, nx, nt, g[f"c{k}_trace"], g[f"c{k}_imp"], g[f"c{k}_amp"])
+    data, snap = oracle_mod.fwd_sponge_np(v, src, nB, dz, dx, dt)
+    assert np.array_equal(data, g[f"c{k}_data"])
+    assert np.array_equal(snap[:, :, nt // 2], g[f"c{k}_snap_mid"])
+    assert np.array_equal(snap[:, :, -1], g[f"c{k}_snap_last"])
+    dc, sc, _ = co.sponge2d(v, nt, nB, dz, dx, dt, source=src)
+    assert np.array_equal(dc, data) and np.array_equal(sc, snap)
+    _, rs, model = co.sponge2d(v, nt, nB, dz, dx, dt, rdata=data)
+    assert np.array_equal(model, g[f"c{k}_model"])
+    assert np.array_equal(rs[:, :, 0], g[f"c{k}_rsnap_first"])
+    assert np.array_equal(rs[:, :, nt // 2], g[f"c{k}_rsnap_mid"])
+
+
+def test_sponge_rtm_golden(co, oracle_mod, golden):
+    g = golden("sponge2d.npz")
+    nz, nx, nt, nB = (int(x) for x in g["rtm_params"])
+    image, d_true, d_smooth = oracle_mod.rtm_sponge_np(g["rtm_v"], g["rtm_vs"], g["rtm_trace"], 0,
+                                                       int(g["rtm_src_ix"]), nB, 10.0, 10.0, 1e-3, 1e-3)
+    assert np.array_equal(image, g["rtm_image"])
+    assert np.array_equal(d_true, g["rtm_data_true"]) and np.array_equal(d_smooth, g["rtm_data_smooth"])
+
+
+def test_sponge_point_source_equals_dense(co, oracle_mod):
+    """Point sources are the dense source with zeros elsewhere (the term
+    vdtSq .* 0 subtracts nothing); two sources on one cell add up."""
+    rng = np.random.default_rng(9)
+    nz, nx, nt, nB = 21, 26, 30, 5
+    v = rng.uniform(1500.0, 4000.0, (nz, nx))
+    w = rng.standard_normal((3, nt))
+    iz, ix = [2, 7, 7], [5, 11, 11]
+    src = np.zeros((nz, nx, nt), order="F")
+    for k in range(3):
+        src[iz[k], ix[k], :] += w[k]
+    d1, s1 = oracle_mod.fwd_sponge_np(v, src, nB, 10.0, 10.0, 1e-3)
+    d2, s2 = oracle_mod.fwd_sponge_point_np(v, nt, iz, ix, w, nB, 10.0, 10.0, 1e-3)
+    d3, s3, _ = co.sponge2d(v, nt, nB, 10.0, 10.0, 1e-3, point=(iz, ix, w))
+    assert np.array_equal(d1, d2) and np.array_equal(s1, s2)
+    assert np.array_equal(d2, d3) and np.array_equal(s2, s3)
+
+
+def test_sponge_profile_values(oracle_mod):
+    """boundary(k) = exp(-(0.015 (nB - k + 1))^2)^10: strongest at the outer
+    cell, rising towards 1 inside."""
+    b = oracle_mod.sponge_profile(20)
+    assert b.shape == (20,)
+    assert np.all(np.diff(b) > 0) and b[-1] < 1.0
+    assert abs(b[0] - np.exp(-(0.3 ** 2)) ** 10) < 1e-15
