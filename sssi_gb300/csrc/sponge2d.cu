@@ -20,9 +20,9 @@
 // GB300 layout and launch: each field is (ldp rows) x (nx + 2 columns) with a
 // zero border (row -1 and row nz, columns -1 and nx), every column's interior
 // starting on a 32-element boundary; the coefficient arrays share the layout.
-// A block of 8 warps takes a tile of 32 rows x 8 columns (one warp per
-// column, coalesced along z) so that the x neighbours of the inner columns
-// come from L1; tiles run z-fastest over a persistent grid.  One step
+// A warp takes 32 rows (coalesced along z) and marches along x over a run
+// of columns, so that each value of the present is fetched once; warps take
+// tiles z-fastest from a persistent grid.  One step
 // is one launch; runs of kSpGraphSteps steps replay a CUDA graph that reads the
 // step number and the chunked hooks (sources, snapshots) from device memory.
 //
@@ -44,8 +44,8 @@ namespace {
 
 using namespace api;
 
-constexpr int kSpRows = 32, kSpCols = 8;  // a tile: one warp per column
-constexpr int kSpThreads = kSpRows * kSpCols;
+constexpr int kSpRows = 32;              // a warp's rows (one per lane)
+constexpr int kSpThreads = 256;          // 8 warps, each an independent worker
 constexpr int kSpOrgRow = 32;             // interior row 0 within a column (row -1 is zero padding)
 constexpr int kSpGraphSteps = 32;
 constexpr double kSpongeAlpha = 0.015;    // src/fwdTimeSpongeFor2dAw.m:45
@@ -74,8 +74,9 @@ struct SpongeParams {
     int nz, nx, nB, nt;
     int64_t ldp;
     int ntz, ntiles;
+    int march;                  // columns a warp marches over (a multiple of kSpAhead)
     int reverse;                // time runs nt-1 .. 0 and row 0 takes src_row
-    T kx, kz;                   // FP32: 1/dx^2, 1/dz^2 (ax = vdt2 kx, az = vdt2 kz)
+    T kx, kz, kxz2;             // FP32: 1/dx^2, 1/dz^2 (ax = vdt2 kx, az = vdt2 kz), 2 (kx + kz)
     // point sources (forward): cell (src_iz[k], src_ix[k]) adds wavelets[k * nt + t]
     int nsrc;
     const int* src_iz;
@@ -93,11 +94,18 @@ struct SpongeParams {
 // cell is hit by the bottom rows alone or by the side columns of its row;
 // both side columns hit it only when nx < 2 nB (the right one first unless
 // nx == nB).
+// The grid's sizes and the profile come by value (a reference to the
+// __grid_constant__ parameter block would be read through generic loads,
+// repeated after every store).
+struct SpongeGeom {
+    int nz, nx, nB;
+};
+
 template <typename T, int kMode>
-__device__ __forceinline__ T sponge(T x, int i, int j, const SpongeParams<T>& p) {
-    const int nB = p.nB;
-    if (i >= p.nz - nB) return kMode == SSSI_MODE_FP32 ? x * p.bnd[p.nz - 1 - i] : __dmul_rn(p.bnd[p.nz - 1 - i], x);
-    const bool left = j < nB, right = j >= p.nx - nB;
+__device__ __forceinline__ T sponge(T x, int i, int j, SpongeGeom g, const T* __restrict__ bnd) {
+    const int nB = g.nB;
+    if (i >= g.nz - nB) return kMode == SSSI_MODE_FP32 ? x * bnd[g.nz - 1 - i] : __dmul_rn(bnd[g.nz - 1 - i], x);
+    const bool left = j < nB, right = j >= g.nx - nB;
     if (!(left | right)) return x;
     auto mul = [](T a, T b) -> T {
         if constexpr (kMode == SSSI_MODE_FP32)
@@ -106,14 +114,191 @@ __device__ __forceinline__ T sponge(T x, int i, int j, const SpongeParams<T>& p)
             return __dmul_rn(a, b);
     };
     if (left && right) {
-        const T bl = p.bnd[j], br = p.bnd[p.nx - 1 - j];
-        return p.nx > nB ? mul(bl, mul(br, x)) : mul(br, mul(bl, x));
+        const T bl = bnd[j], br = bnd[g.nx - 1 - j];
+        return g.nx > nB ? mul(bl, mul(br, x)) : mul(br, mul(bl, x));
     }
-    return mul(p.bnd[left ? j : p.nx - 1 - j], x);
+    return mul(bnd[left ? j : g.nx - 1 - j], x);
 }
 
+// Loads issued ahead per thread in the FP32 step: the columns a warp fetches
+// before it computes them (memory-level parallelism of the HBM-bound stream).
+template <typename T>
+constexpr int kSpAhead = 4;
+
+// The update of one cell from its five present values, its own previous
+// present po (not yet damped) and its coefficients; kGeneral adds the sponge
+// factors and the injected value src (has_src), which interior tiles without
+// sources skip.
+template <typename T>
+struct SpongeK {
+    T kx, kz, kxz2;  // FP32 mode: ax = vdt2 kx, az = vdt2 kz, b = 2 - vdt2 kxz2
+};
+
+template <typename T, int kMode, bool kGeneral>
+__device__ __forceinline__ T sponge_cell(SpongeGeom g, const T* __restrict__ bnd, SpongeK<T> k, int i, int j, T c,
+                                         T up, T dn, T lf, T rt, T po, T vdt2, T cb, T cx, T cz, bool has_src,
+                                         T src) {
+    const T past = kGeneral ? sponge<T, kMode>(po, i, j, g, bnd) : po;
+    T r;
+    if constexpr (kMode == SSSI_MODE_FP64_STRICT) {
+        r = __dsub_rn(__dmul_rn(cb, c), past);
+        r = __dadd_rn(r, __dmul_rn(cx, __dadd_rn(rt, lf)));
+        r = __dadd_rn(r, __dmul_rn(cz, __dadd_rn(dn, up)));
+        if (kGeneral && has_src) r = __dsub_rn(r, __dmul_rn(vdt2, src));
+    } else if constexpr (kMode == SSSI_MODE_FP64) {
+        r = fma(cb, c, -past);
+        r = fma(cx, rt + lf, r);
+        r = fma(cz, dn + up, r);
+        if (kGeneral && has_src) r = fma(-vdt2, src, r);
+    } else {
+        const T ax = vdt2 * k.kx, az = vdt2 * k.kz;
+        const T b = fmaf(-vdt2, k.kxz2, T(2));  // 2 - 2 ax - 2 az
+        r = fmaf(b, c, -past);
+        r = fmaf(ax, rt + lf, r);
+        r = fmaf(az, dn + up, r);
+        if (kGeneral && has_src) r = fmaf(-vdt2, src, r);
+    }
+    return kGeneral ? sponge<T, kMode>(r, i, j, g, bnd) : r;
+}
+
+// One step.  A warp owns 32 rows (one per lane) and marches along x over
+// p.march columns, keeping left / centre / right in registers (each value of
+// the present is fetched once by its owner); up and down come from lane
+// shuffles, the tile's edge rows from two predicated loads.  Lanes below the
+// grid fetch zero padding and store nothing.  A tile clear of the sponge
+// bands and of every source (the common case) takes the lean update.
 template <typename T, int kMode>
-__global__ void __launch_bounds__(kSpThreads) sponge2d_step_kernel(const __grid_constant__ SpongeParams<T> p) {
+__global__ void __launch_bounds__(kSpThreads, 4) sponge2d_march_kernel(const __grid_constant__ SpongeParams<T> p) {
+    constexpr int U = kSpAhead<T>;
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int step = *reinterpret_cast<volatile const int*>(p.step_base) + p.step_offset;
+    const int t = p.reverse ? p.nt - 1 - step : step;
+    const T* __restrict__ cur = p.field[step & 1];
+    T* __restrict__ nxt = p.field[(step & 1) ^ 1];
+    const SpongeHooks<T> h = *p.hooks;
+    const int64_t n = (int64_t)p.nz * p.nx;
+    const T* src_dense = h.src_dense ? h.src_dense + (int64_t)(t - h.dense_t0) * n : nullptr;
+    T* snap = h.snap ? h.snap + (int64_t)(t - h.snap_t0) * n : nullptr;
+    const T* fsnap = h.fsnap ? h.fsnap + (int64_t)(t - h.fsnap_t0) * n : nullptr;
+    const bool per_cell_out = snap || fsnap || src_dense;  // outputs / inputs in the dense nz x nx layout
+    const int lane = threadIdx.x & 31;
+    const int64_t ldp = p.ldp;
+    const int nwarps = gridDim.x * (kSpThreads / 32);
+    const SpongeGeom g{p.nz, p.nx, p.nB};
+    const SpongeK<T> kk{p.kx, p.kz, p.kxz2};
+    const T* __restrict__ bnd = p.bnd;
+    for (int tile = blockIdx.x * (kSpThreads / 32) + (threadIdx.x >> 5); tile < p.ntiles; tile += nwarps) {
+        const int tz = tile % p.ntz, tx = tile / p.ntz;
+        const int i0 = tz * kSpRows, i = i0 + lane, j0 = tx * p.march;
+        const int jend = min(j0 + p.march, p.nx);
+        const bool row_ok = i < p.nz;
+        // warp-uniform: does the tile touch a sponge band, row 0's injection or a point source?
+        bool general = i0 + kSpRows > p.nz - p.nB || j0 < p.nB || jend > p.nx - p.nB || src_dense ||
+                       ((p.src_row || p.rec) && i0 == 0);
+        for (int k = 0; k < p.nsrc; ++k) {
+            const int si = p.src_iz[k], sj = p.src_ix[k];
+            general |= si >= i0 && si < i0 + kSpRows && sj >= j0 && sj < jend;
+        }
+        const int64_t q0 = i + (int64_t)j0 * ldp;
+        const T* pc = cur + q0;  // (i, j) of the column being computed
+        T* pn = nxt + q0;
+        const T* pv = p.cvdt2 + q0;
+        const T* pb = kMode != SSSI_MODE_FP32 ? p.cb + q0 : nullptr;
+        const T* px = kMode != SSSI_MODE_FP32 ? p.cax + q0 : nullptr;
+        const T* pz = kMode != SSSI_MODE_FP32 ? p.caz + q0 : nullptr;
+        T lf = __ldg(pc - ldp);
+        T c = __ldg(pc);
+        for (int jb = j0; jb < jend; jb += U) {
+            T rt[U], po[U], vd[U], eg[U], cb[U], cx[U], cz[U];
+            const bool whole = jb + U <= jend;  // warp-uniform; a partial group only at the grid's last column
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                // past the end: a repeat of the last column, unused
+                const int64_t o = whole ? (int64_t)u * ldp : (int64_t)min(u, jend - 1 - jb) * ldp;
+                rt[u] = __ldg(pc + o + ldp);
+                po[u] = pn[o];
+                vd[u] = __ldg(pv + o);
+                eg[u] = lane == 0 ? __ldg(pc + o - 1) : (lane == 31 ? __ldg(pc + o + 1) : T(0));
+                if constexpr (kMode != SSSI_MODE_FP32) {
+                    cb[u] = __ldg(pb + o);
+                    cx[u] = __ldg(px + o);
+                    cz[u] = __ldg(pz + o);
+                } else {
+                    cb[u] = cx[u] = cz[u] = T(0);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = jb + u;
+                if (j >= jend) break;  // warp-uniform
+                const T up_s = __shfl_up_sync(0xffffffffu, c, 1), dn_s = __shfl_down_sync(0xffffffffu, c, 1);
+                const T up = lane == 0 ? eg[u] : up_s, dn = lane == 31 ? eg[u] : dn_s;
+                const int64_t o = (int64_t)u * ldp;
+                if (row_ok) {
+                    T out;
+                    if (!general) {
+                        out = sponge_cell<T, kMode, false>(g, bnd, kk, i, j, c, up, dn, lf, rt[u], po[u], vd[u],
+                                                           cb[u], cx[u], cz[u], false, T(0));
+                    } else {
+                        // the injected value of the cell at step t (dense slice, row 0, point sources)
+                        T src = T(0);
+                        bool has_src = false;
+                        if (src_dense) {
+                            src = src_dense[i + (int64_t)j * p.nz];
+                            has_src = true;
+                        }
+                        if (p.src_row && i == 0) {
+                            src = p.src_row[j + (int64_t)t * p.nx];
+                            has_src = true;
+                        }
+                        for (int k = 0; k < p.nsrc; ++k)
+                            if (p.src_iz[k] == i && p.src_ix[k] == j) {
+                                const T w = p.wavelets[(int64_t)k * p.nt + t];
+                                src = has_src ? src + w : w;
+                                has_src = true;
+                            }
+                        out = sponge_cell<T, kMode, true>(g, bnd, kk, i, j, c, up, dn, lf, rt[u], po[u], vd[u],
+                                                          cb[u], cx[u], cz[u], has_src, src);
+                    }
+                    pn[o] = out;
+                    if (general && p.rec && i == 0) p.rec[j + (int64_t)t * p.nx] = out;
+                    if (per_cell_out) {
+                        const int64_t qd = i + (int64_t)j * p.nz;
+                        if (snap) snap[qd] = out;
+                        if constexpr (kMode == SSSI_MODE_FP64) {
+                            if (fsnap) {
+                                const double f = fsnap[qd];
+                                p.im[qd] = fma(f, (double)out, p.im[qd]);
+                                p.is2[qd] = fma(f, f, p.is2[qd]);
+                            }
+                        }
+                    }
+                }
+                lf = c;
+                c = rt[u];
+            }
+            const int64_t adv = (int64_t)U * ldp;
+            pc += adv;
+            pn += adv;
+            pv += adv;
+            if constexpr (kMode != SSSI_MODE_FP32) {
+                pb += adv;
+                px += adv;
+                pz += adv;
+            }
+        }
+    }
+}
+
+// The FP64 step: FP64 is bound by its pipe (about 5 to 8 FP64 operations a
+// cell), so every thread takes one cell of a 32-row x 8-column block tile
+// (one warp per column) and the SM holds as many warps as it can; the x
+// neighbours of a tile's inner columns come from L1.
+constexpr int kSpCellCols = kSpThreads / 32;
+
+template <typename T, int kMode>
+__global__ void __launch_bounds__(kSpThreads) sponge2d_cell_kernel(const __grid_constant__ SpongeParams<T> p) {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const int step = *reinterpret_cast<volatile const int*>(p.step_base) + p.step_offset;
@@ -127,60 +312,59 @@ __global__ void __launch_bounds__(kSpThreads) sponge2d_step_kernel(const __grid_
     const T* fsnap = h.fsnap ? h.fsnap + (int64_t)(t - h.fsnap_t0) * n : nullptr;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t ldp = p.ldp;
+    const SpongeGeom g{p.nz, p.nx, p.nB};
+    const SpongeK<T> kk{p.kx, p.kz, p.kxz2};
+    const T* __restrict__ bnd = p.bnd;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int tz = tile % p.ntz, tx = tile / p.ntz;
-        const int i = tz * kSpRows + lane, j = tx * kSpCols + w;
+        const int i0 = tz * kSpRows, j0 = tx * kSpCellCols;
+        const int i = i0 + lane, j = j0 + w;
+        // block-uniform: does the tile touch a sponge band, row 0 or a point source?
+        bool general = i0 + kSpRows > p.nz - p.nB || j0 < p.nB || j0 + kSpCellCols > p.nx - p.nB || src_dense ||
+                       i0 == 0;
+        for (int k = 0; k < p.nsrc; ++k) {
+            const int si = p.src_iz[k], sj = p.src_ix[k];
+            general |= si >= i0 && si < i0 + kSpRows && sj >= j0 && sj < j0 + kSpCellCols;
+        }
         if (i >= p.nz || j >= p.nx) continue;
         const int64_t q = i + (int64_t)j * ldp;
         const T c = __ldg(cur + q), up = __ldg(cur + q - 1), dn = __ldg(cur + q + 1);
         const T lf = __ldg(cur + q - ldp), rt = __ldg(cur + q + ldp);
-        const T past = sponge<T, kMode>(nxt[q], i, j, p);
-        const T vdt2 = __ldg(p.cvdt2 + q);
-        // the injected value of the cell at step t (dense slice, point sources, or row 0)
-        T src = T(0);
-        bool has_src = false;
-        if (src_dense) {
-            src = src_dense[i + (int64_t)j * p.nz];
-            has_src = true;
-        }
-        if (p.src_row && i == 0) {
-            src = p.src_row[j + (int64_t)t * p.nx];
-            has_src = true;
-        }
-        for (int k = 0; k < p.nsrc; ++k)
-            if (p.src_iz[k] == i && p.src_ix[k] == j) {
-                src = has_src ? src + p.wavelets[(int64_t)k * p.nt + t] : p.wavelets[(int64_t)k * p.nt + t];
+        const T po = nxt[q], vdt2 = __ldg(p.cvdt2 + q);
+        const T cb = __ldg(p.cb + q), cx = __ldg(p.cax + q), cz = __ldg(p.caz + q);
+        T out;
+        if (!general) {
+            out = sponge_cell<T, kMode, false>(g, bnd, kk, i, j, c, up, dn, lf, rt, po, vdt2, cb, cx, cz, false, T(0));
+        } else {
+            T src = T(0);
+            bool has_src = false;
+            if (src_dense) {
+                src = src_dense[i + (int64_t)j * p.nz];
                 has_src = true;
             }
-        T r;
-        if constexpr (kMode == SSSI_MODE_FP64_STRICT) {
-            r = __dsub_rn(__dmul_rn(__ldg(p.cb + q), c), past);
-            r = __dadd_rn(r, __dmul_rn(__ldg(p.cax + q), __dadd_rn(rt, lf)));
-            r = __dadd_rn(r, __dmul_rn(__ldg(p.caz + q), __dadd_rn(dn, up)));
-            if (has_src) r = __dsub_rn(r, __dmul_rn(vdt2, src));
-        } else if constexpr (kMode == SSSI_MODE_FP64) {
-            r = fma(__ldg(p.cb + q), c, -past);
-            r = fma(__ldg(p.cax + q), rt + lf, r);
-            r = fma(__ldg(p.caz + q), dn + up, r);
-            if (has_src) r = fma(-vdt2, src, r);
-        } else {
-            const T ax = vdt2 * p.kx, az = vdt2 * p.kz;
-            const T b = (T(2) - T(2) * ax) - T(2) * az;
-            r = fmaf(b, c, -past);
-            r = fmaf(ax, rt + lf, r);
-            r = fmaf(az, dn + up, r);
-            if (has_src) r = fmaf(-vdt2, src, r);
+            if (p.src_row && i == 0) {
+                src = p.src_row[j + (int64_t)t * p.nx];
+                has_src = true;
+            }
+            for (int k = 0; k < p.nsrc; ++k)
+                if (p.src_iz[k] == i && p.src_ix[k] == j) {
+                    const T wv = p.wavelets[(int64_t)k * p.nt + t];
+                    src = has_src ? src + wv : wv;
+                    has_src = true;
+                }
+            out = sponge_cell<T, kMode, true>(g, bnd, kk, i, j, c, up, dn, lf, rt, po, vdt2, cb, cx, cz, has_src, src);
+            if (p.rec && i == 0) p.rec[j + (int64_t)t * p.nx] = out;
         }
-        const T out = sponge<T, kMode>(r, i, j, p);
         nxt[q] = out;
-        const int64_t qd = i + (int64_t)j * p.nz;
-        if (p.rec && i == 0) p.rec[j + (int64_t)t * p.nx] = out;
-        if (snap) snap[qd] = out;
-        if constexpr (kMode == SSSI_MODE_FP64) {
-            if (fsnap) {
-                const double f = fsnap[qd];
-                p.im[qd] = fma(f, (double)out, p.im[qd]);
-                p.is2[qd] = fma(f, f, p.is2[qd]);
+        if (snap || fsnap) {
+            const int64_t qd = i + (int64_t)j * p.nz;
+            if (snap) snap[qd] = out;
+            if constexpr (kMode == SSSI_MODE_FP64) {
+                if (fsnap) {
+                    const double f = fsnap[qd];
+                    p.im[qd] = fma(f, (double)out, p.im[qd]);
+                    p.is2[qd] = fma(f, f, p.is2[qd]);
+                }
             }
         }
     }
@@ -197,7 +381,10 @@ void launch_sponge_step(const SpongeParams<T>& p, int grid, cudaStream_t s) {
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, sponge2d_step_kernel<T, kMode>, p));
+    if constexpr (kMode == SSSI_MODE_FP32)
+        SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, sponge2d_march_kernel<T, kMode>, p));
+    else
+        SSSI_CHECK_CUDA(cudaLaunchKernelEx(&cfg, sponge2d_cell_kernel<T, kMode>, p));
     count_launch();
 }
 
@@ -212,15 +399,40 @@ std::vector<double> sponge_profile(int nB) {
     return b;
 }
 
+// ax = (v dt/dx)^2, az = (v dt/dz)^2, vdtSq = (v dt)^2 and b = 2 - 2ax - 2az
+// rounded as the MATLAB expressions are written (explicit round-to-nearest
+// operations: nothing is fused), into the padded layout (interior origin
+// applied to the outputs; b, ax, az only in the FP64 modes).
+template <typename T>
+__global__ void sponge_coef_kernel(const double* v, int nz, int nx, int64_t ldp, double dz, double dx, double dt,
+                                   T* vdt2, T* b, T* ax, T* az) {
+    const int64_t n = (int64_t)nz * nx;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = q % nz, j = q / nz, o = i + j * ldp;
+        const double vdt = __dmul_rn(v[q], dt);
+        const double tx = __ddiv_rn(vdt, dx), tz = __ddiv_rn(vdt, dz);
+        const double cx = __dmul_rn(tx, tx), cz = __dmul_rn(tz, tz);
+        vdt2[o] = (T)__dmul_rn(vdt, vdt);
+        if (b) {
+            ax[o] = (T)cx;
+            az[o] = (T)cz;
+            b[o] = (T)__dsub_rn(__dsub_rn(2.0, __dmul_rn(2.0, cx)), __dmul_rn(2.0, cz));
+        }
+    }
+}
+
 // One propagation (forward or reverse) of one shot: fields, coefficients,
 // hooks and the step loop (graphs of kSpGraphSteps steps).
 template <typename T>
 class Sponge2d {
   public:
+    // v: the velocity model in device memory (nz x nx doubles)
     Sponge2d(const double* v, int64_t nz, int64_t nx, int nB, double dz, double dx, double dt, int mode, int64_t nt,
              bool reverse, cudaStream_t s)
         : nz_((int)nz), nx_((int)nx), mode_(mode), s_(s) {
-        ldp_ = ((int64_t)kSpOrgRow + nz + 1 + 31) / 32 * 32;
+        // rows: kSpOrgRow above the interior, then the interior rounded up to whole
+        // 32-row tiles plus one more row of zeros (row nz and the lanes below the grid)
+        ldp_ = (int64_t)kSpOrgRow + (nz + 31) / 32 * 32 + 32;
         const int64_t cols = nx + 2;
         const size_t cells = (size_t)(ldp_ * cols);
         org_ = kSpOrgRow + ldp_;  // interior (0, 0): row kSpOrgRow of column 1
@@ -228,37 +440,24 @@ class Sponge2d {
             f.allocate(cells * sizeof(T));
             f.zero(s);
         }
-        // coefficients as the reference forms them (src/fwdTimeSpongeFor2dAw.m:51-55)
+        // coefficients as the reference forms them (src/fwdTimeSpongeFor2dAw.m:51-55),
+        // on the device from v (device memory, nz x nx); the padding stays zero
         const bool fp64 = mode != SSSI_MODE_FP32;
-        std::vector<T> hb, hax, haz, hv(cells, T(0));
-        if (fp64) {
-            hb.assign(cells, T(0));
-            hax.assign(cells, T(0));
-            haz.assign(cells, T(0));
-        }
-        for (int64_t j = 0; j < nx; ++j)
-            for (int64_t i = 0; i < nz; ++i) {
-                const double vv = v[i + j * nz];
-                const double vdt = vv * dt;
-                const double ax = (vdt / dx) * (vdt / dx), az = (vdt / dz) * (vdt / dz);
-                const size_t q = (size_t)(org_ + i + j * ldp_);
-                hv[q] = (T)(vdt * vdt);
-                if (fp64) {
-                    hax[q] = (T)ax;
-                    haz[q] = (T)az;
-                    hb[q] = (T)((2.0 - 2.0 * ax) - 2.0 * az);
-                }
-            }
-        auto upload = [&](DeviceBuffer& d, const std::vector<T>& h) {
+        auto make = [&](DeviceBuffer& d) {
             d.allocate(cells * sizeof(T));
-            SSSI_CHECK_CUDA(cudaMemcpyAsync(d.get(), h.data(), cells * sizeof(T), cudaMemcpyHostToDevice, s));
+            d.zero(s);
+            return d.template as<T>() + org_;
         };
-        upload(vdt2_, hv);
+        T* dv2 = make(vdt2_);
+        T *db = nullptr, *dax = nullptr, *daz = nullptr;
         if (fp64) {
-            upload(b_, hb);
-            upload(ax_, hax);
-            upload(az_, haz);
+            db = make(b_);
+            dax = make(ax_);
+            daz = make(az_);
         }
+        sponge_coef_kernel<T><<<152 * 4, 256, 0, s>>>(v, (int)nz, (int)nx, ldp_, dz, dx, dt, dv2, db, dax, daz);
+        count_launch();
+        SSSI_CHECK_CUDA(cudaGetLastError());
         const std::vector<double> prof = sponge_profile(nB);
         std::vector<T> hp(prof.begin(), prof.end());
         bnd_.allocate(std::max<size_t>(hp.size(), 1) * sizeof(T));
@@ -286,14 +485,37 @@ class Sponge2d {
         p_.nt = (int)nt;
         p_.ldp = ldp_;
         p_.ntz = (nz_ + kSpRows - 1) / kSpRows;
-        p_.ntiles = p_.ntz * ((nx_ + kSpCols - 1) / kSpCols);
         p_.reverse = reverse ? 1 : 0;
         p_.kx = (T)(1.0 / (dx * dx));
         p_.kz = (T)(1.0 / (dz * dz));
+        p_.kxz2 = (T)(2.0 * (1.0 / (dx * dx) + 1.0 / (dz * dz)));
         int dev = 0, sms = 0;
         SSSI_CHECK_CUDA(cudaGetDevice(&dev));
         SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        grid_ = std::max(1, std::min(p_.ntiles, sms * 8));  // 8 blocks of 256 threads per SM
+        int per_sm = 0;
+        if (mode == SSSI_MODE_FP32) {
+            // FP32: the longest march that still gives every resident warp a tile
+            // (short marches re-fetch the column left of each tile; grids that fit
+            // in L2 need many warps in flight more than they need long marches)
+            SSSI_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, (const void*)sponge2d_march_kernel<float, SSSI_MODE_FP32>, kSpThreads, 0));
+            per_sm = std::max(per_sm, 1);
+            const int64_t warps = (int64_t)sms * per_sm * (kSpThreads / 32);
+            int march = 32;
+            while (march > 4 && (int64_t)p_.ntz * ((nx_ + march - 1) / march) < warps) march /= 2;
+            p_.march = march;
+            p_.ntiles = p_.ntz * ((nx_ + march - 1) / march);
+            grid_ = (int)std::max<int64_t>(1, std::min<int64_t>((p_.ntiles + kSpThreads / 32 - 1) / (kSpThreads / 32),
+                                                                 (int64_t)sms * per_sm));
+        } else {
+            // FP64: block tiles of 32 x 8 cells over a persistent grid
+            SSSI_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, (const void*)sponge2d_cell_kernel<double, SSSI_MODE_FP64_STRICT>, kSpThreads, 0));
+            per_sm = std::max(per_sm, 1);
+            p_.march = kSpCellCols;
+            p_.ntiles = p_.ntz * ((nx_ + kSpCellCols - 1) / kSpCellCols);
+            grid_ = std::max(1, std::min(p_.ntiles, sms * per_sm));
+        }
         set_hooks(SpongeHooks<T>{});
     }
     ~Sponge2d() {
@@ -389,8 +611,8 @@ void sponge_fwd(const double* v, const double* source, int64_t nz, int64_t nx, i
                 const double* wavelets, double* data, double* snapshot) {
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    std::vector<double> vh = host_copy(v, (size_t)n, s);
-    Sponge2d<T> P(vh.data(), nz, nx, nB, dz, dx, dt, mode, nt, false, s);
+    DeviceView dv(v, (size_t)n, true, s);
+    Sponge2d<T> P(dv.ptr, nz, nx, nB, dz, dx, dt, mode, nt, false, s);
     Staged<T> rec(data, (size_t)(nx * nt), false, s);
     Staged<T> wav(wavelets, (size_t)(nsrc * nt), true, s);
     DeviceBuffer d_iz, d_ix;
@@ -451,8 +673,8 @@ void sponge_rvs(const double* v, const double* data, int64_t nz, int64_t nx, int
                 double dx, double dt, int mode, double* model, double* snapshot) {
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    std::vector<double> vh = host_copy(v, (size_t)n, s);
-    Sponge2d<T> P(vh.data(), nz, nx, nB, dz, dx, dt, mode, nt, true, s);
+    DeviceView dv(v, (size_t)n, true, s);
+    Sponge2d<T> P(dv.ptr, nz, nx, nB, dz, dx, dt, mode, nt, true, s);
     Staged<T> rows(data, (size_t)(nx * nt), true, s);
     P.params().src_row = data ? rows.ptr : nullptr;
     const int64_t K = snapshot ? chunk_steps(nt, n) : std::max<int64_t>(nt, 1);
@@ -491,7 +713,7 @@ void sponge_rtm(const double* v, const double* vs, int64_t nz, int64_t nx, int64
                  (long long)siz, (long long)six);
     cudaStream_t s = current_stream();
     const int64_t n = nz * nx;
-    std::vector<double> vh = host_copy(v, (size_t)n, s), vsh = host_copy(vs, (size_t)n, s);
+    DeviceView dv(v, (size_t)n, true, s), dvs(vs, (size_t)n, true, s);
     Staged<double> wav(wavelet, (size_t)nt, true, s);
     DeviceBuffer d_src(2 * sizeof(int));
     const int hsrc[2] = {(int)siz, (int)six};
@@ -502,7 +724,7 @@ void sponge_rtm(const double* v, const double* vs, int64_t nz, int64_t nx, int64
     const bool strict = mode == SSSI_MODE_FP64_STRICT;
     timing_begin(s);
     for (int pass = 0; pass < 2; ++pass) {
-        Sponge2d<double> P(pass == 0 ? vh.data() : vsh.data(), nz, nx, nB, dz, dx, dt, mode, nt, false, s);
+        Sponge2d<double> P(pass == 0 ? dv.ptr : dvs.ptr, nz, nx, nB, dz, dx, dt, mode, nt, false, s);
         SpongeParams<double>& p = P.params();
         p.nsrc = 1;
         p.src_iz = d_src.as<int>();
@@ -522,7 +744,7 @@ void sponge_rtm(const double* v, const double* vs, int64_t nz, int64_t nx, int64
     SSSI_CHECK_CUDA(cudaGetLastError());
     DeviceView img(image, (size_t)n, false, s);
     {
-        Sponge2d<double> R(vh.data(), nz, nx, nB, dz, dx, dt, mode, nt, true, s);
+        Sponge2d<double> R(dv.ptr, nz, nx, nB, dz, dx, dt, mode, nt, true, s);
         R.params().src_row = delta.as<double>();
         DeviceBuffer rsnap, msum, ssum;
         SpongeHooks<double> h{};
