@@ -374,6 +374,8 @@ def run_gpu(args):
         line["fwd3d"] = bench_3d(S, args)
     if rank == 0 and not args.no_diffop:
         line["diff_operator"] = bench_diffop(S, args, fma_rate)
+    if rank == 0 and not args.no_sponge:
+        line["sponge"] = bench_sponge(S, args, fma_rate)
     if rank == 0 and not args.no_batch:
         line["batch2d"] = bench_batch(S, args)
     if rank == 0 and not args.no_serve:
@@ -606,6 +608,87 @@ def bench_diffop(S, args, fma_rate):
     out["hbm_peak"] = peak
     out["hbm_peak_kind"] = peak_kind
     out["timing"] = "CUDA events around the C-ABI call, inputs and outputs on the device (includes the output allocation)"
+    return out
+
+
+def bench_sponge(S, args, fma_rate):
+    """One sponge-ABC RTM shot (applications/rtm_2d_acoustic/mainRtmTimeSpongeFor2dAw.m:
+    forward in V and VS, reverse of dataTrue - dataSmooth, zero-lag imaging) on
+    the RTM workload's 620 x 1240 model, dt from that file's rule
+    0.75 min(dz / v / sqrt(2)), nt = 4000, through sssi_rtmTimeSpongeFor2dAw
+    with host buffers (e2e).  Fused FP64 is the line's value; strict FP64
+    (the MATLAB rounding sequence) beside it, and FP32 forward modelling of the
+    same shot with its seismogram error against FP64.  The fused step does 5
+    FP64 operations a cell (2 additions, 3 multiply-adds), the reverse step 2
+    more for the imaging sums: bound by the FP64 pipe."""
+    from oracle import oracle as O
+
+    V, VS, _, siz, six, nz, nx = workload()
+    nt = 4000
+    dt = 0.75 * float(np.min(DZ / V / np.sqrt(2.0)))
+    w = ricker(20.0, nt, dt)
+    cells = 3.0 * nz * nx * nt
+    out = {"metric": "Gcell-updates/s (sponge-ABC RTM shot, 620x1240, nt=4000, 3 propagations)",
+           "config": {"workload": "rtm-sponge", "nz": nz, "nx": nx, "nt": nt, "dt": dt, "nBoundary": NB,
+                      "source": "20 Hz Ricker at row 0", "epsilon": 1e-3}}
+    # warm-up (short), then one shot per mode
+    S.rtmTimeSpongeFor2dAw(V, VS, w[:64], siz, six, NB, DZ, DX, dt, epsilon=1e-3, mode="fp64")
+    imgs = {}
+    for mode in ("fp64", "fp64-strict"):
+        S.enable_timing(True)
+        t0 = time.perf_counter()
+        img, d_true, d_smooth = S.rtmTimeSpongeFor2dAw(V, VS, w, siz, six, NB, DZ, DX, dt, epsilon=1e-3, mode=mode,
+                                                       want_data=True)
+        wall = time.perf_counter() - t0
+        ph = S.last_timing()
+        S.enable_timing(False)
+        dev_ms = sum(p[0] for p in ph)
+        imgs[mode] = img
+        out[mode] = {"value": round(cells / wall / 1e9, 3), "unit": UNIT, "wall_ms": round(wall * 1e3, 2),
+                     "device_ms": round(dev_ms, 2), "device_value": round(cells / (dev_ms * 1e-3) / 1e9, 3),
+                     "launches": int(sum(p[1] for p in ph))}
+    ops = nz * nx * nt * (5.0 + 5.0 + 7.0)
+    dev_s = out["fp64"]["device_ms"] * 1e-3
+    bytes_cell = (56.0 + 64.0 + 96.0) / 3.0  # fwd V; fwd VS + snapshot write; rvs + snapshot read + sums
+    peak, peak_kind = peaks()
+    out["value"] = out["fp64"]["value"]
+    out["unit"] = UNIT
+    out["e2e"] = {"value": out["fp64"]["value"], "unit": UNIT, "h2d_bytes_per_step": int(2 * nz * nx * 8 + nt * 8),
+                  "d2h_bytes_per_step": int(nz * nx * 8 + 2 * nx * nt * 8),
+                  "api": "sssi_rtmTimeSpongeFor2dAw (host buffers)"}
+    out["roofline"] = {"bound": "fp64", "achieved": round(ops / dev_s / 1e9, 1), "peak": round(fma_rate / 1e9, 1),
+                       "unit": "Gop/s", "frac": round(ops / dev_s / fma_rate, 4),
+                       "ops_per_cell": round((5.0 + 5.0 + 7.0) / 3.0, 3),
+                       "peak_kind": "measured in this run: FP64 fused multiply-adds per second",
+                       "kernel": "sponge2d cell step (fused fp64), all three propagations",
+                       "hbm": {"achieved": round(cells * bytes_cell / dev_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                               "frac": round(cells * bytes_cell / dev_s / 1e9 / peak, 4), "peak_kind": peak_kind,
+                               "bytes_per_cell": round(bytes_cell, 2)}}
+    out["accuracy"] = {"image_rel_l2_fused_vs_strict": O.rel_l2(imgs["fp64"], imgs["fp64-strict"])}
+    # FP32 forward modelling of the same shot against FP64
+    d64, _ = S.fwdTimeSpongeFor2dAwPoint(V, nt, [siz], [six], w[None, :], NB, DZ, DX, dt, mode="fp64")
+    t0 = time.perf_counter()
+    d32, _ = S.fwdTimeSpongeFor2dAwPoint(V, nt, [siz], [six], w[None, :], NB, DZ, DX, dt, mode="fp32")
+    wall32 = time.perf_counter() - t0
+    out["fp32_forward"] = {"value": round(nz * nx * nt / wall32 / 1e9, 3), "unit": UNIT,
+                           "seismogram_rel_l2_vs_fp64": O.rel_l2(d32, d64), "bound": 1e-4}
+    # parity at a bounded nt: strict GPU image equal to the C restatement's
+    if not args.no_cpu:
+        ntc = min(args.cpu_nt, nt)
+        co = O.COracle()
+        img_g = S.rtmTimeSpongeFor2dAw(V, VS, w[:ntc], siz, six, NB, DZ, DX, dt, epsilon=1e-3, mode="fp64-strict")
+        t0 = time.perf_counter()
+        dct, _, _ = co.sponge2d(V, ntc, NB, DZ, DX, dt, point=([siz], [six], w[None, :ntc]), want_snapshot=False)
+        dcs, fcs, _ = co.sponge2d(VS, ntc, NB, DZ, DX, dt, point=([siz], [six], w[None, :ntc]))
+        _, rcs, _ = co.sponge2d(V, ntc, NB, DZ, DX, dt, rdata=dct - dcs)
+        img_c = O.image_np(fcs, rcs, 1e-3)
+        cpu_s = time.perf_counter() - t0
+        out["accuracy"]["strict_equals_c_restatement"] = bool(np.array_equal(img_g, img_c))
+        out["accuracy"]["checked_nt"] = ntc
+        out["cpu_baseline"] = {"value": round(3.0 * nz * nx * ntc / cpu_s / 1e9, 4), "unit": UNIT,
+                               "cores": co.threads(), "kind": "port",
+                               "sample": f"the same shot for nt={ntc}: the C restatement of the MATLAB sponge "
+                                         "propagators (OpenMP) plus numpy imaging"}
     return out
 
 
@@ -935,6 +1018,17 @@ def run_case(name):
             outs = [plan.wait(t)["data"] for t in tickets]
         print(f"case {name}: 64 shots ok, data max {max(float(np.abs(o).max()) for o in outs):.3e}")
         return
+    if name.startswith("sponge-2000x4000"):
+        # 24 steps of sponge forward modelling (one point source, 20-cell sponge)
+        mode = name.rsplit("-", 1)[1]
+        rng = np.random.default_rng(1)
+        nz, nx, nt = 2000, 4000, 24
+        v = rng.uniform(1500.0, 4000.0, (nz, nx))
+        w = np.sin(np.arange(nt) * 0.05)[None, :]
+        d, _ = S.fwdTimeSpongeFor2dAwPoint(v, nt, [1], [nx // 2], w, 20, 10.0, 10.0, 8e-4, mode=mode)
+        torch.cuda.synchronize()
+        print(f"case {name}: ok, data max {np.abs(d).max():.3e}")
+        return
     if name in ("rtm-short", "rtm-short-fp64"):
         V, VS, w, siz, six, nz, nx = workload()
         fp64 = name.endswith("fp64")
@@ -962,7 +1056,8 @@ def run_case(name):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short", "rtm-short-fp64", "batch64"],
+    ap.add_argument("--case", choices=sorted(CASES) + ["rtm-short", "rtm-short-fp64", "batch64",
+                                                       "sponge-2000x4000-fp64", "sponge-2000x4000-fp32"],
                     help="run one small fixed workload for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -974,6 +1069,7 @@ def main():
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D forward-modelling line")
     ap.add_argument("--no-c1", action="store_true", help="skip the plain forward-modelling (dense API) line")
     ap.add_argument("--no-diffop", action="store_true", help="skip the stand-alone derivative line")
+    ap.add_argument("--no-sponge", action="store_true", help="skip the sponge-ABC RTM line")
     ap.add_argument("--nt3d", type=int, default=2000)
     ap.add_argument("--steps3d", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-shot batched line")
