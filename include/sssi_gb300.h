@@ -216,6 +216,31 @@ int sssi_rtmTimeSpongeFor2dAw(const double *v, const double *vs, int64_t nz, int
                               double dz, double dx, double dt, const double *wavelet, int64_t src_iz, int64_t src_ix,
                               double epsilon, int mode, double *image, double *data_true, double *data_smooth);
 
+/* ---- 2D elastic propagation (simplified PML) ----
+ *
+ * [snapshotVzp, snapshotVxp, snapshotVzs, snapshotVxs] =
+ *     fwdTimeSpmlFor2dEw(vp, vs, source, nDiffOrder, nBoundary, dz, dx, dt)
+ * of src/fwdTimeSpmlFor2dEw.m:1-103 (MATLAB only in the reference): the
+ * velocity split into P and S parts through two potentials, staggered
+ * derivatives of half-order nDiffOrder (diffOperator), damping from dampPml in
+ * cell units on the side columns (x) and bottom rows (z), the source added to
+ * both P components.  vp, vs: nz x nx; source: nz x nx x nt; each snapshot
+ * nz x nx x nt (any may be NULL).  nBoundary must be in 0..min(nz, nx/2).
+ * SSSI_MODE_FP64_STRICT rounds as the MATLAB file and diffOperator_mex do;
+ * SSSI_MODE_FP64 folds c_k/d and fuses; SSSI_MODE_FP32 is the fused form in FP32. */
+int sssi_fwdTimeSpmlFor2dEw(const double *vp, const double *vs, const double *source, int64_t nz, int64_t nx,
+                            int64_t nt, int nDiffOrder, int nBoundary, double dz, double dx, double dt,
+                            double *snapshotVzp, double *snapshotVxp, double *snapshotVzs, double *snapshotVxs,
+                            int mode);
+
+/* The same with nsrc (<= 64) point sources: cell (src_iz[s], src_ix[s]) takes
+ * wavelets[s*nt + t] at step t (sources on one cell add up). */
+int sssi_fwdTimeSpmlFor2dEwPoint(const double *vp, const double *vs, int64_t nz, int64_t nx, int64_t nt,
+                                 int nDiffOrder, int nBoundary, double dz, double dx, double dt, int nsrc,
+                                 const int64_t *src_iz, const int64_t *src_ix, const double *wavelets,
+                                 double *snapshotVzp, double *snapshotVxp, double *snapshotVzs, double *snapshotVxs,
+                                 int mode);
+
 /* ---- batched and served shots: the plan API ----
  *
  * The reference runs one shot per MEX call and loops over shots in MATLAB

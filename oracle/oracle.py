@@ -607,6 +607,73 @@ def image_np(fwd_snap, rvs_snap, epsilon):
     return m / s2
 
 
+# ---------------------------------------------------------------- elastic SPML
+def fwd_elastic2d_np(vp, vs, source, N, nB, dz, dx, dt, diff=None):
+    """src/fwdTimeSpmlFor2dEw.m:38-103 restated statement by statement (three
+    time levels per field, as the file keeps them).  ``diff`` replaces the
+    derivative routine (default: the restatement _diff; with reference_diff,
+    the reference's compiled diffOperator_mex, which the file's diffOperator
+    calls resolve to).  Returns (snapshotVzp, snapshotVxp, snapshotVzs,
+    snapshotVxs), each nz x nx x nt."""
+    D = diff or _diff
+    vp = np.asarray(vp, dtype=np.float64)
+    vs = np.asarray(vs, dtype=np.float64)
+    source = np.asarray(source, dtype=np.float64)
+    nz, nx, nt = source.shape
+    c = dcoef(N)
+    iz = slice(N, nz + N)
+    ix = slice(N, nx + N)
+    xDamp = np.zeros((nz, nx))
+    zDamp = np.zeros((nz, nx))
+    if nB:
+        L = float(nB)
+        ixb = np.arange(1, nB + 1, dtype=float)
+        xDamp[:, :nB] = damp_pml_m(np.tile(ixb[::-1], (nz, 1)), vp[:, :nB], L)
+        xDamp[:, nx - nB:] = damp_pml_m(np.tile(ixb, (nz, 1)), vp[:, nx - nB:], L)
+        zDamp[nz - nB:, :] = damp_pml_m(np.tile(ixb[:, None], (1, nx)), vp[nz - nB:, :], L)
+    shape = (3, nz + 2 * N, nx + 2 * N)
+    A_z, A_x, A, B_z, B_x, B = (np.zeros(shape) for _ in range(6))
+    Vxp, Vxs, Vx, Vzp, Vzs, Vz = (np.zeros(shape) for _ in range(6))
+    vpSq = np.pad(vp * vp, N, mode="edge")
+    vsSq = np.pad(vs * vs, N, mode="edge")
+    out = [np.zeros((nz, nx, nt)) for _ in range(4)]
+    zi = np.arange(N, nz + N)[:, None]
+    xi = np.arange(N, nx + N)[None, :]
+    for it in range(nt):
+        A_x[1][iz, ix] = (1 - 0.5 * xDamp * dt) / (1 + 0.5 * xDamp * dt) * A_x[0][iz, ix] \
+            + dt / (1 + 0.5 * xDamp * dt) * D(Vx[1][iz, :-1], c, dx, 1)
+        A_z[1][iz, ix] = (1 - 0.5 * zDamp * dt) / (1 + 0.5 * zDamp * dt) * A_z[0][iz, ix] \
+            + dt / (1 + 0.5 * zDamp * dt) * D(Vz[1][:-1, ix], c, dz, 0)
+        A[1][iz, ix] = A_x[1][iz, ix] + A_z[1][iz, ix]
+        B_z[1][iz, ix] = (1 - 0.5 * zDamp * dt) / (1 + 0.5 * zDamp * dt) * B_z[0][iz, ix] \
+            + dt / (1 + 0.5 * zDamp * dt) * D(Vx[1][1:, ix], c, dz, 0)
+        B_x[1][iz, ix] = (1 - 0.5 * xDamp * dt) / (1 + 0.5 * xDamp * dt) * B_x[0][iz, ix] \
+            - dt / (1 + 0.5 * xDamp * dt) * D(Vz[1][iz, 1:], c, dx, 1)
+        B[1][iz, ix] = B_z[1][iz, ix] + B_x[1][iz, ix]
+        Vzp[2][iz, ix] = (1 - 0.5 * zDamp * dt) / (1 + 0.5 * zDamp * dt) * Vzp[1][iz, ix] \
+            + 0.25 * (vpSq[zi, xi] + vpSq[zi + 1, xi] + vpSq[zi + 1, xi - 1] + vpSq[zi, xi - 1]) * dt \
+            / (1 + 0.5 * zDamp * dt) * D(A[1][1:, ix], c, dz, 0) \
+            + dt / (1 + 0.5 * zDamp * dt) * source[:, :, it]
+        Vxp[2][iz, ix] = (1 - 0.5 * xDamp * dt) / (1 + 0.5 * xDamp * dt) * Vxp[1][iz, ix] \
+            + vpSq[iz, ix] * dt / (1 + 0.5 * xDamp * dt) * D(A[1][iz, 1:], c, dx, 1) \
+            + dt / (1 + 0.5 * xDamp * dt) * source[:, :, it]
+        Vzs[2][iz, ix] = (1 - 0.5 * xDamp * dt) / (1 + 0.5 * xDamp * dt) * Vzs[1][iz, ix] \
+            - vsSq[iz, ix] * dt / (1 + 0.5 * xDamp * dt) * D(B[1][iz, :-1], c, dx, 1)
+        Vxs[2][iz, ix] = (1 - 0.5 * zDamp * dt) / (1 + 0.5 * zDamp * dt) * Vxs[1][iz, ix] \
+            + 0.25 * (vsSq[zi, xi] + vsSq[zi, xi + 1] + vsSq[zi - 1, xi + 1] + vsSq[zi - 1, xi]) * dt \
+            / (1 + 0.5 * zDamp * dt) * D(B[1][:-1, ix], c, dz, 0)
+        Vx[2][iz, ix] = Vxp[2][iz, ix] + Vxs[2][iz, ix]
+        Vz[2][iz, ix] = Vzp[2][iz, ix] + Vzs[2][iz, ix]
+        for f in (A_z, A_x, A, B_z, B_x, B, Vxp, Vzp, Vxs, Vzs, Vx, Vz):
+            f[0] = f[1].copy()
+            f[1] = f[2].copy()
+        out[1][:, :, it] = Vxp[1][iz, ix]
+        out[0][:, :, it] = Vzp[1][iz, ix]
+        out[3][:, :, it] = Vxs[1][iz, ix]
+        out[2][:, :, it] = Vzs[1][iz, ix]
+    return tuple(out)
+
+
 # ---------------------------------------------------------------- sponge ABC
 # Restatement of src/fwdTimeSpongeFor2dAw.m:36-101 and
 # src/rvsTimeSpongeFor2dAw.m:36-103 (MATLAB only in the reference: parity of

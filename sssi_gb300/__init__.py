@@ -1,4 +1,4 @@
-"""sssi_gb300 -- SSSI's acoustic finite-difference core (CPML and sponge) on GB300 (sm_103a).
+"""sssi_gb300 -- SSSI's finite-difference core (acoustic CPML and sponge, elastic SPML) on GB300 (sm_103a).
 
 Host side of the drop-in: the MATLAB-shaped functions in :mod:`sssi_gb300.api`
 call the C ABI of ``libsssi_gb300.so`` (``include/sssi_gb300.h``), whose
@@ -18,6 +18,8 @@ from .api import (  # noqa: F401
     fwdTimeCpmlFor2dAwPoint,
     fwdTimeCpmlFor3dAw,
     fwdTimeCpmlFor3dAwPoint,
+    fwdTimeSpmlFor2dEw,
+    fwdTimeSpmlFor2dEwPoint,
     fwdTimeSpongeFor2dAw,
     fwdTimeSpongeFor2dAwPoint,
     launch_count,

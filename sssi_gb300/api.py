@@ -316,6 +316,51 @@ def rtmTimeSpongeFor2dAw(v, vs, wavelet, src_iz, src_ix, nBoundary, dz, dx, dt, 
     return image
 
 
+def fwdTimeSpmlFor2dEw(vp, vs, source, nDiffOrder, nBoundary, dz, dx, dt, *, mode="fp64", want_snapshot=True):
+    """[snapshotVzp, snapshotVxp, snapshotVzs, snapshotVxs] =
+    fwdTimeSpmlFor2dEw(vp, vs, source, nDiffOrder, nBoundary, dz, dx, dt)
+    (src/fwdTimeSpmlFor2dEw.m): 2D elastic propagation with the simplified PML.
+    ``want_snapshot`` may be a sequence of four booleans (which snapshots to return;
+    the others come back as None)."""
+    pp, kp, pshape = _in(vp, "vp")
+    ps_, ks_, sshape_ = _in(vs, "vs")
+    pr, kr, rshape = _in(source, "source")
+    if pshape is None or len(pshape) != 2 or sshape_ != pshape:
+        raise ValueError("vp and vs must be nz x nx of the same size")
+    nz, nx = pshape
+    if rshape is None or len(rshape) != 3 or rshape[:2] != (nz, nx):
+        raise ValueError("source must be nz x nx x nt with the grid of vp")
+    nt = rshape[2]
+    want = [bool(want_snapshot)] * 4 if isinstance(want_snapshot, bool) else [bool(w) for w in want_snapshot]
+    outs = [(_out_like(vp, (nz, nx, nt))[0] if w else None) for w in want]
+    check(lib().sssi_fwdTimeSpmlFor2dEw(pp, ps_, pr, nz, nx, nt, int(nDiffOrder), int(nBoundary), float(dz),
+                                        float(dx), float(dt), *[_addr(o) for o in outs], _mode(mode)))
+    return tuple(outs)
+
+
+def fwdTimeSpmlFor2dEwPoint(vp, vs, nt, src_iz, src_ix, wavelets, nDiffOrder, nBoundary, dz, dx, dt, *,
+                            mode="fp64", want_snapshot=True):
+    """The elastic propagation with point sources: source s at interior
+    (src_iz[s], src_ix[s]) with amplitude wavelets[s, t].  Returns the four
+    snapshots (Vzp, Vxp, Vzs, Vxs)."""
+    pp, kp, pshape = _in(vp, "vp")
+    ps_, ks_, sshape_ = _in(vs, "vs")
+    if pshape is None or len(pshape) != 2 or sshape_ != pshape:
+        raise ValueError("vp and vs must be nz x nx of the same size")
+    nz, nx = pshape
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or len(ix) != len(iz):
+        raise ValueError("wavelets must be nsrc x nt and src_iz/src_ix of length nsrc")
+    want = [bool(want_snapshot)] * 4 if isinstance(want_snapshot, bool) else [bool(x) for x in want_snapshot]
+    outs = [(_out_like(vp, (nz, nx, nt))[0] if x else None) for x in want]
+    check(lib().sssi_fwdTimeSpmlFor2dEwPoint(pp, ps_, nz, nx, int(nt), int(nDiffOrder), int(nBoundary), float(dz),
+                                             float(dx), float(dt), len(iz), iz.ctypes.data, ix.ctypes.data,
+                                             w.ctypes.data, *[_addr(o) for o in outs], _mode(mode)))
+    return tuple(outs)
+
+
 def set_stream(stream) -> None:
     """Make the library launch on ``stream`` (a torch.cuda.Stream, a raw handle, or None)."""
     handle = getattr(stream, "cuda_stream", stream) or 0

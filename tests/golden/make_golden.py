@@ -30,7 +30,15 @@ Outputs (all float64, MATLAB index order):
                 These two restatements are the only pin of that part: no
                 compiled reference exists for it.
 
-``python tests/golden/make_golden.py diffop`` writes diffop.npz alone; ``sponge``
+  elastic2d.npz 2D elastic SPML propagation (src/fwdTimeSpmlFor2dEw.m; MATLAB only in
+                the reference) on four grids (nDiffOrder 1..4, no sponge, side
+                bands meeting at nx = 2 nB): the numpy restatement, run twice --
+                with its own diffOperator and with the reference's compiled
+                diffOperator_mex for every derivative (the routine the file's
+                diffOperator calls resolve to) -- which must agree bit for bit.
+
+``python tests/golden/make_golden.py diffop`` writes diffop.npz alone; ``elastic``
+elastic2d.npz alone (it needs the reference tree); ``sponge``
 writes sponge2d.npz alone (it needs only the two restatements, not the
 reference tree).
 """
@@ -180,6 +188,35 @@ def make_diffop() -> None:
     print("diffop.npz", n, "cases")
 
 
+ELASTIC_CASES = [(30, 44, 40, 3, 8), (27, 33, 30, 2, 0), (25, 40, 35, 4, 10), (33, 34, 30, 1, 17)]
+
+
+def make_elastic() -> None:
+    O.build(reference=True)
+    refdiff = O.reference_diff(O.RefMex("diffOperator_mex"))
+    rec = {}
+    for k, (nz, nx, nt, N, nB) in enumerate(ELASTIC_CASES):
+        rng = np.random.default_rng(5000 + k)
+        vp = rng.uniform(2000.0, 4000.0, (nz, nx))
+        vs = vp / np.sqrt(3.0) * rng.uniform(0.95, 1.05, (nz, nx))
+        trace, imp, amp = source_2d(rng, nz, nx, nt)
+        src = dense_source(nz, nx, nt, trace, imp, amp)
+        dz, dx, dt = 10.0, 12.0, 5e-4
+        snaps = O.fwd_elastic2d_np(vp, vs, src, N, nB, dz, dx, dt)
+        snaps_ref = O.fwd_elastic2d_np(vp, vs, src, N, nB, dz, dx, dt, diff=refdiff)
+        assert all(np.array_equal(a, b) for a, b in zip(snaps, snaps_ref))
+        pre = f"c{k}_"
+        rec.update({pre + "params": np.array([nz, nx, nt, N, nB]), pre + "vp": vp, pre + "vs": vs,
+                    pre + "trace": trace, pre + "imp": imp, pre + "amp": amp})
+        for name, a in zip(("Vzp", "Vxp", "Vzs", "Vxs"), snaps):
+            rec[pre + name + "_mid"] = a[:, :, nt // 2]
+            rec[pre + name + "_last"] = a[:, :, -1]
+    rec["ncases"] = np.array(len(ELASTIC_CASES))
+    rec["dzdxdt"] = np.array([10.0, 12.0, 5e-4])
+    np.savez_compressed(OUT / "elastic2d.npz", **rec)
+    print("elastic2d.npz", (OUT / "elastic2d.npz").stat().st_size)
+
+
 SPONGE_CASES = [(33, 47, 60, 6), (40, 30, 50, 18), (25, 20, 40, 20), (30, 41, 50, 0)]
 
 
@@ -235,7 +272,10 @@ if __name__ == "__main__":
         make_diffop()
     elif len(sys.argv) > 1 and sys.argv[1] == "sponge":
         make_sponge()
+    elif len(sys.argv) > 1 and sys.argv[1] == "elastic":
+        make_elastic()
     else:
         main()
         make_diffop()
         make_sponge()
+        make_elastic()

@@ -103,7 +103,7 @@ def test_mex_gateways_export_mexfunction():
 
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "mexgw"], check=True)
     for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex", "fwdTimeCpmlFor3dAw_mex",
-                 "fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex"):
+                 "fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex", "fwdTimeSpmlFor2dEw_mex"):
         gw = ctypes.CDLL(str(ROOT / "oracle" / "_build" / f"mexgw_{name}.so"), mode=ctypes.RTLD_LOCAL)
         assert hasattr(gw, "mexFunction")
 
@@ -189,3 +189,24 @@ def test_sponge_gateway_error_messages():
         gw = O.load_shim_library(ROOT / "oracle" / "_build" / f"mexgw_{name}.so")
         with pytest.raises(O.MexError, match="All 6 input arguments shall be provided!"):
             O.shim_call(gw, 2, np.ones((3, 3)), np.zeros((3, 3, 2)))
+
+
+def test_elastic_bad_arguments(lib):
+    v = np.full((20, 30), 2000.0, order="F")
+    src = np.zeros((20, 30, 5), order="F")
+    p = lambda a: a.ctypes.data  # noqa: E731
+    # side bands may not overlap (the reference concatenates [left, zeros(nx - 2nB), right])
+    rc = lib.sssi_fwdTimeSpmlFor2dEw(p(v), p(v), p(src), 20, 30, 5, 3, 16, 10.0, 10.0, 1e-3, None, None, None, None, 1)
+    assert rc == 1 and b"nBoundary" in lib.sssi_last_error()
+    rc = lib.sssi_fwdTimeSpmlFor2dEw(p(v), p(v), p(src), 20, 30, 5, 9, 3, 10.0, 10.0, 1e-3, None, None, None, None, 1)
+    assert rc == 1 and b"nDiffOrder" in lib.sssi_last_error()
+    rc = lib.sssi_fwdTimeSpmlFor2dEw(p(v), p(v), p(src), 20, 30, 5, 3, 3, 10.0, 10.0, 1e-3, None, None, None, None, 5)
+    assert rc == 1 and b"mode" in lib.sssi_last_error()
+
+
+def test_elastic_gateway_error_message():
+    from oracle import oracle as O
+
+    gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeSpmlFor2dEw_mex.so")
+    with pytest.raises(O.MexError, match="All 8 input arguments shall be provided!"):
+        O.shim_call(gw, 4, np.ones((3, 3)), np.ones((3, 3)), np.zeros((3, 3, 2)))

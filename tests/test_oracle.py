@@ -277,3 +277,35 @@ def test_sponge_profile_values(oracle_mod):
     assert b.shape == (20,)
     assert np.all(np.diff(b) > 0) and b[-1] < 1.0
     assert abs(b[0] - np.exp(-(0.3 ** 2)) ** 10) < 1e-15
+
+
+def _elastic_case(golden, k):
+    g = golden("elastic2d.npz")
+    nz, nx, nt, N, nB = (int(x) for x in g[f"c{k}_params"])
+    dz, dx, dt = (float(x) for x in g["dzdxdt"])
+    src = dense_source(nz, nx, nt, g[f"c{k}_trace"], g[f"c{k}_imp"], g[f"c{k}_amp"])
+    return g, nz, nx, nt, N, nB, dz, dx, dt, g[f"c{k}_vp"], g[f"c{k}_vs"], src
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_elastic_restatement_matches_golden(oracle_mod, golden, k):
+    """The numpy restatement of src/fwdTimeSpmlFor2dEw.m reproduces the committed
+    vectors (made with the reference's compiled diffOperator_mex for every
+    derivative) bit for bit."""
+    g, nz, nx, nt, N, nB, dz, dx, dt, vp, vs, src = _elastic_case(golden, k)
+    snaps = oracle_mod.fwd_elastic2d_np(vp, vs, src, N, nB, dz, dx, dt)
+    for name, a in zip(("Vzp", "Vxp", "Vzs", "Vxs"), snaps):
+        assert np.array_equal(a[:, :, nt // 2], g[f"c{k}_{name}_mid"]), name
+        assert np.array_equal(a[:, :, -1], g[f"c{k}_{name}_last"]), name
+
+
+def test_elastic_restatement_with_reference_derivatives(oracle_mod, golden):
+    """Live, where the reference tree exists: the restatement run with the
+    reference's own diffOperator_mex equals the one with its own derivative."""
+    if not oracle_mod.available_reference():
+        pytest.skip("reference gateways not built (SSSI_REFERENCE_SRC unset)")
+    g, nz, nx, nt, N, nB, dz, dx, dt, vp, vs, src = _elastic_case(golden, 0)
+    diff = oracle_mod.reference_diff(oracle_mod.RefMex("diffOperator_mex"))
+    a = oracle_mod.fwd_elastic2d_np(vp, vs, src, N, nB, dz, dx, dt)
+    b = oracle_mod.fwd_elastic2d_np(vp, vs, src, N, nB, dz, dx, dt, diff=diff)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
