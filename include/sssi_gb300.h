@@ -1,8 +1,9 @@
 /*
  * sssi_gb300.h -- C ABI of libsssi_gb300, a GB300 (sm_103a) implementation of
- * SSSI's acoustic finite-difference time-domain core with a convolutional
- * perfectly matched layer (CPML) and the reverse-time-migration imaging
- * condition.
+ * SSSI's finite-difference time-domain core: acoustic propagation with a
+ * convolutional perfectly matched layer (CPML) and with a sponge boundary,
+ * elastic propagation with a simplified PML, the stand-alone staggered
+ * derivative, and the reverse-time-migration imaging condition.
  *
  * Conventions shared by every entry point
  *   - Arrays are column-major (MATLAB order) double precision unless stated:
@@ -240,6 +241,29 @@ int sssi_fwdTimeSpmlFor2dEwPoint(const double *vp, const double *vs, int64_t nz,
                                  const int64_t *src_iz, const int64_t *src_ix, const double *wavelets,
                                  double *snapshotVzp, double *snapshotVxp, double *snapshotVzs, double *snapshotVxs,
                                  int mode);
+
+/* [snapshotVzp, snapshotVxp, snapshotVyp, snapshotVzs, snapshotVxs, snapshotVys] =
+ *     fwdTimeSpmlFor3dEw(vp, vs, source_x, source_y, source_z, nDiffOrder, nBoundary, dz, dx, dy, dt)
+ * of src/fwdTimeSpmlFor3dEw.m:1-236 (MATLAB only in the reference): the 3D
+ * form of the above, damping profiles as that file takes them (x and z from
+ * the y = 1 slice of vp, y from its top row).  vp, vs: nz x nx x ny; each
+ * source nz x nx x ny x nt (NULL: none); each snapshot nz x nx x ny x nt (NULL:
+ * not returned).  nBoundary must be in 0..min(nz, nx/2, ny/2). */
+int sssi_fwdTimeSpmlFor3dEw(const double *vp, const double *vs, const double *source_x, const double *source_y,
+                            const double *source_z, int64_t nz, int64_t nx, int64_t ny, int64_t nt, int nDiffOrder,
+                            int nBoundary, double dz, double dx, double dy, double dt, double *snapshotVzp,
+                            double *snapshotVxp, double *snapshotVyp, double *snapshotVzs, double *snapshotVxs,
+                            double *snapshotVys, int mode);
+
+/* The same with nsrc (<= 64) point sources: cell (src_iz[s], src_ix[s],
+ * src_iy[s]) takes wavelets[s*nt + t] into the component src_component[s]
+ * (0: x, 1: y, 2: z) at step t. */
+int sssi_fwdTimeSpmlFor3dEwPoint(const double *vp, const double *vs, int64_t nz, int64_t nx, int64_t ny, int64_t nt,
+                                 int nDiffOrder, int nBoundary, double dz, double dx, double dy, double dt, int nsrc,
+                                 const int64_t *src_iz, const int64_t *src_ix, const int64_t *src_iy,
+                                 const int *src_component, const double *wavelets, double *snapshotVzp,
+                                 double *snapshotVxp, double *snapshotVyp, double *snapshotVzs, double *snapshotVxs,
+                                 double *snapshotVys, int mode);
 
 /* ---- batched and served shots: the plan API ----
  *

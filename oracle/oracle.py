@@ -674,6 +674,102 @@ def fwd_elastic2d_np(vp, vs, source, N, nB, dz, dx, dt, diff=None):
     return tuple(out)
 
 
+def fwd_elastic3d_np(vp, vs, source_x, source_y, source_z, N, nB, dz, dx, dy, dt, diff=None):
+    """src/fwdTimeSpmlFor3dEw.m:40-236 restated statement by statement (three
+    time levels per field).  Damping as the file takes it: x and z profiles from
+    the y = 1 slice of vp, y profiles from its top row, each replicated along
+    the missing axis.  ``diff`` as in fwd_elastic2d_np.  Returns the six
+    snapshots (Vzp, Vxp, Vyp, Vzs, Vxs, Vys), each nz x nx x ny x nt."""
+    D = diff or _diff
+    vp = np.asarray(vp, dtype=np.float64)
+    vs = np.asarray(vs, dtype=np.float64)
+    sx_, sy_, sz_ = (np.asarray(a, dtype=np.float64) for a in (source_x, source_y, source_z))
+    nz, nx, ny, nt = sx_.shape
+    c = dcoef(N)
+    xDamp = np.zeros((nz, nx, ny))
+    yDamp = np.zeros((nz, nx, ny))
+    zDamp = np.zeros((nz, nx, ny))
+    if nB:
+        L = float(nB)
+        b = np.arange(1, nB + 1, dtype=float)
+        xDamp[:, :nB, :] = damp_pml_m(np.tile(b[::-1], (nz, 1)), vp[:, :nB, 0], L)[:, :, None]
+        xDamp[:, nx - nB:, :] = damp_pml_m(np.tile(b, (nz, 1)), vp[:, nx - nB:, 0], L)[:, :, None]
+        yDamp[:, :, :nB] = damp_pml_m(np.tile(b[::-1][None, :], (nx, 1)), vp[0, :, :nB], L)[None, :, :]
+        yDamp[:, :, ny - nB:] = damp_pml_m(np.tile(b[None, :], (nx, 1)), vp[0, :, ny - nB:], L)[None, :, :]
+        zDamp[nz - nB:, :, :] = damp_pml_m(np.tile(b[:, None], (1, nx)), vp[nz - nB:, :, 0], L)[:, :, None]
+    shape = (3, nz + 2 * N, nx + 2 * N, ny + 2 * N)
+    names = ("A_x", "A_y", "A_z", "A", "B1_y", "B1_z", "B1", "B2_z", "B2_x", "B2", "B3_x", "B3_y", "B3",
+             "Vxp", "Vxs_y", "Vxs_z", "Vxs", "Vx", "Vyp", "Vys_x", "Vys_z", "Vys", "Vy",
+             "Vzp", "Vzs_x", "Vzs_y", "Vzs", "Vz")
+    F = {k: np.zeros(shape) for k in names}
+    vpSq = np.pad(vp * vp, N, mode="edge")
+    vsSq = np.pad(vs * vs, N, mode="edge")
+    I = (slice(N, nz + N), slice(N, nx + N), slice(N, ny + N))
+
+    def sh(a, oz, ox, oy):  # a(iz + oz, ix + ox, iy + oy)
+        return a[N + oz:nz + N + oz, N + ox:nx + N + ox, N + oy:ny + N + oy]
+
+    def r_(d):
+        return (1 - 0.5 * d * dt) / (1 + 0.5 * d * dt)
+
+    def s_(d):
+        return dt / (1 + 0.5 * d * dt)
+
+    def cur(k):
+        return F[k][1]
+
+    out = [np.zeros((nz, nx, ny, nt)) for _ in range(6)]
+    for it in range(nt):
+        Vx, Vy, Vz = cur("Vx"), cur("Vy"), cur("Vz")
+        F["A_x"][1][I] = r_(xDamp) * F["A_x"][0][I] + s_(xDamp) * D(Vx[N:nz + N, :-1, N:ny + N], c, dx, 1)
+        F["A_y"][1][I] = r_(yDamp) * F["A_y"][0][I] + s_(yDamp) * D(Vy[N:nz + N, N:nx + N, :-1], c, dy, 2)
+        F["A_z"][1][I] = r_(zDamp) * F["A_z"][0][I] + s_(zDamp) * D(Vz[:-1, N:nx + N, N:ny + N], c, dz, 0)
+        F["A"][1][I] = F["A_x"][1][I] + F["A_y"][1][I] + F["A_z"][1][I]
+        F["B1_y"][1][I] = r_(yDamp) * F["B1_y"][0][I] + s_(yDamp) * D(Vz[N:nz + N, N:nx + N, 1:], c, dy, 2)
+        F["B1_z"][1][I] = r_(zDamp) * F["B1_z"][0][I] - s_(zDamp) * D(Vy[1:, N:nx + N, N:ny + N], c, dz, 0)
+        F["B1"][1][I] = F["B1_y"][1][I] + F["B1_z"][1][I]
+        F["B2_z"][1][I] = r_(zDamp) * F["B2_z"][0][I] + s_(zDamp) * D(Vx[1:, N:nx + N, N:ny + N], c, dz, 0)
+        F["B2_x"][1][I] = r_(xDamp) * F["B2_x"][0][I] - s_(xDamp) * D(Vz[N:nz + N, 1:, N:ny + N], c, dx, 1)
+        F["B2"][1][I] = F["B2_z"][1][I] + F["B2_x"][1][I]
+        F["B3_x"][1][I] = r_(xDamp) * F["B3_x"][0][I] + s_(xDamp) * D(Vy[N:nz + N, 1:, N:ny + N], c, dx, 1)
+        F["B3_y"][1][I] = r_(yDamp) * F["B3_y"][0][I] - s_(yDamp) * D(Vx[N:nz + N, N:nx + N, 1:], c, dy, 2)
+        F["B3"][1][I] = F["B3_x"][1][I] + F["B3_y"][1][I]
+        A, B1, B2, B3 = cur("A"), cur("B1"), cur("B2"), cur("B3")
+        avg_zy = lambda q: sh(q, 0, 0, 0) + sh(q, -1, 0, 0) + sh(q, -1, 0, -1) + sh(q, 0, 0, -1)  # noqa: E731
+        avg_zx = lambda q: sh(q, 0, 0, 0) + sh(q, 0, -1, 0) + sh(q, -1, -1, 0) + sh(q, -1, 0, 0)  # noqa: E731
+        avg_xy = lambda q: sh(q, 0, 0, 0) + sh(q, 0, -1, 0) + sh(q, 0, -1, -1) + sh(q, 0, 0, -1)  # noqa: E731
+        F["Vxp"][2][I] = r_(xDamp) * F["Vxp"][1][I] + 0.25 * avg_zy(vpSq) * dt / (1 + 0.5 * xDamp * dt) \
+            * D(A[N:nz + N, 1:, N:ny + N], c, dx, 1) + s_(xDamp) * sx_[:, :, :, it]
+        F["Vyp"][2][I] = r_(yDamp) * F["Vyp"][1][I] + 0.25 * avg_zx(vpSq) * dt / (1 + 0.5 * yDamp * dt) \
+            * D(A[N:nz + N, N:nx + N, 1:], c, dy, 2) + s_(yDamp) * sy_[:, :, :, it]
+        F["Vzp"][2][I] = r_(zDamp) * F["Vzp"][1][I] + 0.25 * avg_xy(vpSq) * dt / (1 + 0.5 * zDamp * dt) \
+            * D(A[1:, N:nx + N, N:ny + N], c, dz, 0) + s_(zDamp) * sz_[:, :, :, it]
+        F["Vxs_y"][2][I] = r_(yDamp) * F["Vxs_y"][1][I] - 0.25 * avg_zy(vsSq) * dt / (1 + 0.5 * yDamp * dt) \
+            * D(B3[N:nz + N, N:nx + N, :-1], c, dy, 2)
+        F["Vxs_z"][2][I] = r_(zDamp) * F["Vxs_z"][1][I] + 0.25 * avg_zy(vsSq) * dt / (1 + 0.5 * zDamp * dt) \
+            * D(B2[:-1, N:nx + N, N:ny + N], c, dz, 0)
+        F["Vxs"][2][I] = F["Vxs_y"][2][I] + F["Vxs_z"][2][I]
+        F["Vys_x"][2][I] = r_(xDamp) * F["Vys_x"][1][I] + 0.25 * avg_zx(vsSq) * dt / (1 + 0.5 * xDamp * dt) \
+            * D(B3[N:nz + N, :-1, N:ny + N], c, dx, 1)
+        F["Vys_z"][2][I] = r_(zDamp) * F["Vys_z"][1][I] - 0.25 * avg_zx(vsSq) * dt / (1 + 0.5 * zDamp * dt) \
+            * D(B1[:-1, N:nx + N, N:ny + N], c, dz, 0)
+        F["Vys"][2][I] = F["Vys_x"][2][I] + F["Vys_z"][2][I]
+        F["Vzs_x"][2][I] = r_(xDamp) * F["Vzs_x"][1][I] - 0.25 * avg_xy(vsSq) * dt / (1 + 0.5 * xDamp * dt) \
+            * D(B2[N:nz + N, :-1, N:ny + N], c, dx, 1)
+        F["Vzs_y"][2][I] = r_(yDamp) * F["Vzs_y"][1][I] + 0.25 * avg_xy(vsSq) * dt / (1 + 0.5 * yDamp * dt) \
+            * D(B1[N:nz + N, N:nx + N, :-1], c, dy, 2)
+        F["Vzs"][2][I] = F["Vzs_x"][2][I] + F["Vzs_y"][2][I]
+        F["Vx"][2][I] = F["Vxp"][2][I] + F["Vxs"][2][I]
+        F["Vy"][2][I] = F["Vyp"][2][I] + F["Vys"][2][I]
+        F["Vz"][2][I] = F["Vzp"][2][I] + F["Vzs"][2][I]
+        for k in names:
+            F[k][0] = F[k][1].copy()
+            F[k][1] = F[k][2].copy()
+        for o, k in zip(out, ("Vzp", "Vxp", "Vyp", "Vzs", "Vxs", "Vys")):
+            o[:, :, :, it] = F[k][1][I]
+    return tuple(out)
+
+
 # ---------------------------------------------------------------- sponge ABC
 # Restatement of src/fwdTimeSpongeFor2dAw.m:36-101 and
 # src/rvsTimeSpongeFor2dAw.m:36-103 (MATLAB only in the reference: parity of

@@ -20,6 +20,8 @@ from .api import (  # noqa: F401
     fwdTimeCpmlFor3dAwPoint,
     fwdTimeSpmlFor2dEw,
     fwdTimeSpmlFor2dEwPoint,
+    fwdTimeSpmlFor3dEw,
+    fwdTimeSpmlFor3dEwPoint,
     fwdTimeSpongeFor2dAw,
     fwdTimeSpongeFor2dAwPoint,
     launch_count,

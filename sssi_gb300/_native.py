@@ -111,6 +111,14 @@ SIGNATURES = {
     "sssi_fwdTimeSpmlFor2dEwPoint": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                                      c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, ctypes.c_int]),
+    "sssi_fwdTimeSpmlFor3dEw": (ctypes.c_int, [c_dp, c_dp, c_dp, c_dp, c_dp, c_i64, c_i64, c_i64, c_i64,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp,
+                                                ctypes.c_int]),
+    "sssi_fwdTimeSpmlFor3dEwPoint": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_int, c_dp, c_dp, c_dp, c_dp, c_dp,
+                                                     c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, ctypes.c_int]),
     "sssi_rtmTimeCpmlFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_i64,
                                                 c_i64, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_dp, c_dp,

@@ -361,6 +361,61 @@ def fwdTimeSpmlFor2dEwPoint(vp, vs, nt, src_iz, src_ix, wavelets, nDiffOrder, nB
     return tuple(outs)
 
 
+def fwdTimeSpmlFor3dEw(vp, vs, source_x, source_y, source_z, nDiffOrder, nBoundary, dz, dx, dy, dt, *,
+                       mode="fp64", want_snapshot=True):
+    """[snapshotVzp, snapshotVxp, snapshotVyp, snapshotVzs, snapshotVxs, snapshotVys] =
+    fwdTimeSpmlFor3dEw(vp, vs, source_x, source_y, source_z, nDiffOrder, nBoundary, dz, dx, dy, dt)
+    (src/fwdTimeSpmlFor3dEw.m).  Any source may be None (no source);
+    ``want_snapshot`` may be a sequence of six booleans."""
+    pp, kp, pshape = _in(vp, "vp")
+    ps_, ks_, sshape_ = _in(vs, "vs")
+    if pshape is None or len(pshape) != 3 or sshape_ != pshape:
+        raise ValueError("vp and vs must be nz x nx x ny of the same size")
+    nz, nx, ny = pshape
+    srcs, keep, nt = [], [], None
+    for name, a in (("source_x", source_x), ("source_y", source_y), ("source_z", source_z)):
+        pa, ka, shp = _in(a, name)
+        if shp is not None:
+            if len(shp) != 4 or shp[:3] != (nz, nx, ny) or (nt is not None and shp[3] != nt):
+                raise ValueError(f"{name} must be nz x nx x ny x nt with the grid of vp")
+            nt = shp[3]
+        srcs.append(pa)
+        keep.append(ka)
+    if nt is None:
+        raise ValueError("at least one source is needed (it sets nt)")
+    want = [bool(want_snapshot)] * 6 if isinstance(want_snapshot, bool) else [bool(w) for w in want_snapshot]
+    outs = [(_out_like(vp, (nz, nx, ny, nt))[0] if w else None) for w in want]
+    check(lib().sssi_fwdTimeSpmlFor3dEw(pp, ps_, *srcs, nz, nx, ny, nt, int(nDiffOrder), int(nBoundary), float(dz),
+                                        float(dx), float(dy), float(dt), *[_addr(o) for o in outs], _mode(mode)))
+    return tuple(outs)
+
+
+def fwdTimeSpmlFor3dEwPoint(vp, vs, nt, src_iz, src_ix, src_iy, src_component, wavelets, nDiffOrder, nBoundary,
+                            dz, dx, dy, dt, *, mode="fp64", want_snapshot=True):
+    """3D elastic propagation with point sources: source s at interior
+    (src_iz[s], src_ix[s], src_iy[s]) into component src_component[s] (0 x, 1 y,
+    2 z) with amplitude wavelets[s, t].  Returns the six snapshots."""
+    pp, kp, pshape = _in(vp, "vp")
+    ps_, ks_, sshape_ = _in(vs, "vs")
+    if pshape is None or len(pshape) != 3 or sshape_ != pshape:
+        raise ValueError("vp and vs must be nz x nx x ny of the same size")
+    nz, nx, ny = pshape
+    iz = np.ascontiguousarray(np.atleast_1d(src_iz), dtype=np.int64)
+    ix = np.ascontiguousarray(np.atleast_1d(src_ix), dtype=np.int64)
+    iy = np.ascontiguousarray(np.atleast_1d(src_iy), dtype=np.int64)
+    cp = np.ascontiguousarray(np.atleast_1d(src_component), dtype=np.int32)
+    w = np.ascontiguousarray(np.atleast_2d(np.asarray(wavelets, dtype=np.float64)))
+    if w.shape != (len(iz), nt) or not (len(ix) == len(iy) == len(cp) == len(iz)):
+        raise ValueError("wavelets must be nsrc x nt and the positions and components of length nsrc")
+    want = [bool(want_snapshot)] * 6 if isinstance(want_snapshot, bool) else [bool(x) for x in want_snapshot]
+    outs = [(_out_like(vp, (nz, nx, ny, nt))[0] if x else None) for x in want]
+    check(lib().sssi_fwdTimeSpmlFor3dEwPoint(pp, ps_, nz, nx, ny, int(nt), int(nDiffOrder), int(nBoundary), float(dz),
+                                             float(dx), float(dy), float(dt), len(iz), iz.ctypes.data, ix.ctypes.data,
+                                             iy.ctypes.data, cp.ctypes.data, w.ctypes.data,
+                                             *[_addr(o) for o in outs], _mode(mode)))
+    return tuple(outs)
+
+
 def set_stream(stream) -> None:
     """Make the library launch on ``stream`` (a torch.cuda.Stream, a raw handle, or None)."""
     handle = getattr(stream, "cuda_stream", stream) or 0

@@ -37,8 +37,12 @@ Outputs (all float64, MATLAB index order):
                 diffOperator_mex for every derivative (the routine the file's
                 diffOperator calls resolve to) -- which must agree bit for bit.
 
+  elastic3d.npz 3D elastic SPML propagation (src/fwdTimeSpmlFor3dEw.m, MATLAB only) on
+                three grids (nDiffOrder 1..3, with and without the sponge), made
+                and pinned the same way.
+
 ``python tests/golden/make_golden.py diffop`` writes diffop.npz alone; ``elastic``
-elastic2d.npz alone (it needs the reference tree); ``sponge``
+elastic2d.npz and elastic3d.npz (it needs the reference tree); ``sponge``
 writes sponge2d.npz alone (it needs only the two restatements, not the
 reference tree).
 """
@@ -217,6 +221,39 @@ def make_elastic() -> None:
     print("elastic2d.npz", (OUT / "elastic2d.npz").stat().st_size)
 
 
+ELASTIC3D_CASES = [(14, 16, 18, 12, 3, 4), (12, 10, 10, 10, 2, 0), (10, 12, 12, 8, 1, 5)]
+
+
+def make_elastic3d() -> None:
+    O.build(reference=True)
+    refdiff = O.reference_diff(O.RefMex("diffOperator_mex"))
+    rec = {}
+    for k, (nz, nx, ny, nt, N, nB) in enumerate(ELASTIC3D_CASES):
+        rng = np.random.default_rng(6000 + k)
+        vp = rng.uniform(2000.0, 4000.0, (nz, nx, ny))
+        vs = vp / np.sqrt(3.0) * rng.uniform(0.95, 1.05, (nz, nx, ny))
+        tr = O.ricker(30.0, nt, 5e-4)
+        srcs = [np.zeros((nz, nx, ny, nt), order="F") for _ in range(3)]
+        for c, s_ in enumerate(srcs):
+            s_[0, nx // 2, ny // 2, :] = tr * (1.0, 0.5, -0.25)[c]
+            for _ in range(4):
+                s_[rng.integers(nz), rng.integers(nx), rng.integers(ny), rng.integers(nt)] += rng.standard_normal()
+        dz, dx, dy, dt = 10.0, 11.0, 12.0, 5e-4
+        snaps = O.fwd_elastic3d_np(vp, vs, *srcs, N, nB, dz, dx, dy, dt)
+        snaps_ref = O.fwd_elastic3d_np(vp, vs, *srcs, N, nB, dz, dx, dy, dt, diff=refdiff)
+        assert all(np.array_equal(a, b) for a, b in zip(snaps, snaps_ref))
+        pre = f"c{k}_"
+        rec.update({pre + "params": np.array([nz, nx, ny, nt, N, nB]), pre + "vp": vp, pre + "vs": vs,
+                    pre + "src_x": srcs[0], pre + "src_y": srcs[1], pre + "src_z": srcs[2]})
+        for name, a in zip(("Vzp", "Vxp", "Vyp", "Vzs", "Vxs", "Vys"), snaps):
+            rec[pre + name + "_mid"] = a[:, :, :, nt // 2]
+            rec[pre + name + "_last"] = a[:, :, :, -1]
+    rec["ncases"] = np.array(len(ELASTIC3D_CASES))
+    rec["spacing"] = np.array([10.0, 11.0, 12.0, 5e-4])
+    np.savez_compressed(OUT / "elastic3d.npz", **rec)
+    print("elastic3d.npz", (OUT / "elastic3d.npz").stat().st_size)
+
+
 SPONGE_CASES = [(33, 47, 60, 6), (40, 30, 50, 18), (25, 20, 40, 20), (30, 41, 50, 0)]
 
 
@@ -274,8 +311,10 @@ if __name__ == "__main__":
         make_sponge()
     elif len(sys.argv) > 1 and sys.argv[1] == "elastic":
         make_elastic()
+        make_elastic3d()
     else:
         main()
         make_diffop()
         make_sponge()
         make_elastic()
+        make_elastic3d()

@@ -103,7 +103,8 @@ def test_mex_gateways_export_mexfunction():
 
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "mexgw"], check=True)
     for name in ("fwdTimeCpmlFor2dAw_mex", "rvsTimeCpmlFor2dAw_mex", "fwdTimeCpmlFor3dAw_mex",
-                 "fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex", "fwdTimeSpmlFor2dEw_mex"):
+                 "fwdTimeSpongeFor2dAw_mex", "rvsTimeSpongeFor2dAw_mex", "fwdTimeSpmlFor2dEw_mex",
+                 "fwdTimeSpmlFor3dEw_mex"):
         gw = ctypes.CDLL(str(ROOT / "oracle" / "_build" / f"mexgw_{name}.so"), mode=ctypes.RTLD_LOCAL)
         assert hasattr(gw, "mexFunction")
 
@@ -210,3 +211,16 @@ def test_elastic_gateway_error_message():
     gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeSpmlFor2dEw_mex.so")
     with pytest.raises(O.MexError, match="All 8 input arguments shall be provided!"):
         O.shim_call(gw, 4, np.ones((3, 3)), np.ones((3, 3)), np.zeros((3, 3, 2)))
+
+
+def test_elastic3d_bad_arguments_and_gateway_message(lib):
+    from oracle import oracle as O
+
+    v = np.full((10, 12, 14), 2000.0, order="F")
+    p = lambda a: a.ctypes.data  # noqa: E731
+    rc = lib.sssi_fwdTimeSpmlFor3dEw(p(v), p(v), None, None, None, 10, 12, 14, 5, 3, 7, 10.0, 10.0, 10.0, 1e-3,
+                                     None, None, None, None, None, None, 1)
+    assert rc == 1 and b"nBoundary" in lib.sssi_last_error()  # 2 nB > nx
+    gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeSpmlFor3dEw_mex.so")
+    with pytest.raises(O.MexError, match="All 11 input arguments shall be provided!"):
+        O.shim_call(gw, 6, v, v)
