@@ -376,6 +376,8 @@ def run_gpu(args):
         line["diff_operator"] = bench_diffop(S, args, fma_rate)
     if rank == 0 and not args.no_sponge:
         line["sponge"] = bench_sponge(S, args, fma_rate)
+    if rank == 0 and not args.no_elastic:
+        line["elastic2d"] = bench_elastic(S, args, fma_rate)
     if rank == 0 and not args.no_batch:
         line["batch2d"] = bench_batch(S, args)
     if rank == 0 and not args.no_serve:
@@ -689,6 +691,90 @@ def bench_sponge(S, args, fma_rate):
                                "cores": co.threads(), "kind": "port",
                                "sample": f"the same shot for nt={ntc}: the C restatement of the MATLAB sponge "
                                          "propagators (OpenMP) plus numpy imaging"}
+    return out
+
+
+def bench_elastic(S, args, fma_rate):
+    """2D elastic SPML forward modelling (src/fwdTimeSpmlFor2dEw.m, the work of
+    applications/wave_2d_elastic/mainWaveTimeSpmlFor2dEw.m:102) on the RTM
+    workload's 620 x 1240 model as vp, vs = vp / sqrt(3) (a Poisson solid; the
+    application's own models are .mat files that are not available here),
+    nDiffOrder 3, nBoundary 20, dt = 0.5 min(dx, dz) / vpmax / sqrt(2) (the
+    application's rule), 20 Hz Ricker at row 0, nt = 2000, through
+    sssi_fwdTimeSpmlFor2dEwPoint.  The application keeps all four snapshot
+    volumes (4 x 620 x 1240 x 2000 doubles = 49 GB); the timed runs keep them
+    on none (the step's work is the same; the snapshot stores are 32 B a cell
+    more).  Fused FP64: about 80 FP64 instructions a cell-step (8 staggered
+    derivatives of 3 terms, the split updates): bound by the FP64 pipe."""
+    from oracle import oracle as O
+
+    V, _, _, _, _, nz, nx = workload()
+    vs = V / np.sqrt(3.0)
+    N, nt = 3, 2000
+    dt = 0.5 * min(DX, DZ) / float(V.max()) / np.sqrt(2.0)
+    w = ricker(20.0, nt, dt)[None, :]
+    six = NB + 49
+    cells = float(nz * nx * nt)
+    out = {"metric": "Gcell-updates/s (2D elastic SPML forward, 620x1240, nt=2000)",
+           "config": {"workload": "elastic-2d", "nz": nz, "nx": nx, "nt": nt, "nDiffOrder": N, "nBoundary": NB,
+                      "dt": dt, "vs": "vp / sqrt(3)", "snapshots": "none kept in the timed runs"}}
+    S.fwdTimeSpmlFor2dEwPoint(V, vs, 32, [0], [six], w[:, :32], N, NB, DZ, DX, dt, mode="fp64", want_snapshot=False)
+    res = {}
+    for mode in ("fp64", "fp64-strict", "fp32"):
+        S.enable_timing(True)
+        t0 = time.perf_counter()
+        r = S.fwdTimeSpmlFor2dEwPoint(V, vs, nt, [0], [six], w, N, NB, DZ, DX, dt, mode=mode,
+                                      want_snapshot=(True, False, False, False) if mode != "fp64-strict" else False)
+        wall = time.perf_counter() - t0
+        ph = S.last_timing()
+        S.enable_timing(False)
+        dev_ms = sum(p[0] for p in ph)
+        res[mode] = r
+        out[mode] = {"value": round(cells / wall / 1e9, 3), "wall_ms": round(wall * 1e3, 1),
+                     "device_ms": round(dev_ms, 1), "device_value": round(cells / (dev_ms * 1e-3) / 1e9, 3)}
+    out["fp64"]["note"] = "these two runs keep the Vzp snapshot (8 B a cell more), to compare FP32 with FP64"
+    out["value"] = out["fp64"]["value"]
+    out["unit"] = UNIT
+    ops = 80.0 * cells
+    dev_s = out["fp64"]["device_ms"] * 1e-3
+    out["roofline"] = {"bound": "fp64", "achieved": round(ops / dev_s / 1e9, 1), "peak": round(fma_rate / 1e9, 1),
+                       "unit": "Gop/s", "frac": round(ops / dev_s / fma_rate, 4), "ops_per_cell": 80,
+                       "peak_kind": "measured in this run: FP64 fused multiply-adds per second",
+                       "kernel": "elastic2d phase 1 + phase 2 (fused fp64)"}
+    out["accuracy"] = {"vzp_snapshot_rel_l2_fp32_vs_fp64": O.rel_l2(res["fp32"][0], res["fp64"][0]), "bound": 1e-4}
+    # 3D (src/fwdTimeSpmlFor3dEw.m, the work of applications/wave_3d_elastic/
+    # mainWaveTimeSpmlFor3dEw.m): a 148^3 grid with 10-cell bands, nDiffOrder 3, dt by the
+    # application's rule 0.5 min(d) / vpmax / sqrt(3), a z-force at the top centre
+    n3, nt3, nb3 = 148, 200, 10
+    rng = np.random.default_rng(20240801)
+    vp3 = np.sort(rng.uniform(2000.0, 4000.0, n3))[:, None, None] * np.ones((n3, n3, n3))
+    vs3 = vp3 / np.sqrt(3.0)
+    dt3 = 0.5 * 10.0 / float(vp3.max()) / np.sqrt(3.0)
+    w3 = ricker(20.0, nt3, dt3)[None, :]
+    S.fwdTimeSpmlFor3dEwPoint(vp3, vs3, 16, [0], [n3 // 2], [n3 // 2], [2], w3[:, :16], 3, nb3, 10.0, 10.0, 10.0,
+                              dt3, mode="fp64", want_snapshot=False)
+    out["3d"] = {"config": {"workload": "elastic-3d", "n": n3, "nt": nt3, "nBoundary": nb3, "nDiffOrder": 3,
+                            "dt": dt3, "model": "layered vp sorted uniform(2000, 4000), vs = vp / sqrt(3)",
+                            "snapshots": "none kept"}}
+    for mode in ("fp64", "fp64-strict", "fp32"):
+        S.enable_timing(True)
+        S.fwdTimeSpmlFor3dEwPoint(vp3, vs3, nt3, [0], [n3 // 2], [n3 // 2], [2], w3, 3, nb3, 10.0, 10.0, 10.0, dt3,
+                                  mode=mode, want_snapshot=False)
+        ph = S.last_timing()
+        S.enable_timing(False)
+        dev_ms = sum(p[0] for p in ph)
+        out["3d"][mode] = {"device_ms": round(dev_ms, 1),
+                           "device_value": round(n3 ** 3 * nt3 / (dev_ms * 1e-3) / 1e9, 3)}
+    if not args.no_cpu:
+        ntc = 10
+        src = np.zeros((nz, nx, ntc), order="F")
+        src[0, six, :] = w[0, :ntc]
+        t0 = time.perf_counter()
+        O.fwd_elastic2d_np(V, vs, src, N, NB, DZ, DX, dt)
+        cpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nz * nx * ntc / cpu_s / 1e9, 4), "unit": UNIT, "cores": 1,
+                               "kind": "port", "sample": f"the same model for nt={ntc}: the numpy restatement of "
+                                                         "the MATLAB file (vectorised statements, one core)"}
     return out
 
 
@@ -1070,6 +1156,7 @@ def main():
     ap.add_argument("--no-c1", action="store_true", help="skip the plain forward-modelling (dense API) line")
     ap.add_argument("--no-diffop", action="store_true", help="skip the stand-alone derivative line")
     ap.add_argument("--no-sponge", action="store_true", help="skip the sponge-ABC RTM line")
+    ap.add_argument("--no-elastic", action="store_true", help="skip the elastic forward-modelling line")
     ap.add_argument("--nt3d", type=int, default=2000)
     ap.add_argument("--steps3d", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-shot batched line")
