@@ -265,6 +265,28 @@ int sssi_fwdTimeSpmlFor3dEwPoint(const double *vp, const double *vs, int64_t nz,
                                  double *snapshotVxp, double *snapshotVyp, double *snapshotVzs, double *snapshotVxs,
                                  double *snapshotVys, int mode);
 
+/* ---- MAT-file persistence ----
+ *
+ * The applications save seismograms, snapshots and images with MATLAB's
+ * save and read them back with load
+ * (applications/rtm_2d_acoustic/mainRtmTimeCpmlFor2dAw.m:170-183,250-266,348-351).
+ * These write and read Level-5 MAT-files (what save(..., '-v6') writes and
+ * every MATLAB load reads): real double arrays of 1 to 8 dimensions, each at
+ * most 4 GiB, streamed from / to host or device memory through a bounded
+ * staging buffer.  Compressed (v7) and HDF5 (v7.3) files are refused with a
+ * message. */
+
+/* Writes nvars variables to path (created or truncated): variable v is
+ * names[v] (1..63 characters), arrays[v] (column-major doubles, host or device)
+ * of ndims[v] dimensions dims[v][0..ndims[v]-1]. */
+int sssi_mat_write(const char *path, int nvars, const char *const *names, const double *const *arrays,
+                   const int *ndims, const int64_t *const *dims);
+
+/* Reads variable `name` of path: *ndims and dims[0..7] receive its shape; with
+ * out != NULL its values (converted to double from the stored type) go to out
+ * (host or device), which must hold `capacity` elements. */
+int sssi_mat_read(const char *path, const char *name, double *out, int64_t capacity, int *ndims, int64_t *dims);
+
 /* ---- batched and served shots: the plan API ----
  *
  * The reference runs one shot per MEX call and loops over shots in MATLAB

@@ -25,6 +25,8 @@ from .api import (  # noqa: F401
     fwdTimeSpongeFor2dAw,
     fwdTimeSpongeFor2dAwPoint,
     launch_count,
+    mat_read,
+    mat_write,
     measure_fp64_rate,
     release_cache,
     rtmTimeCpmlFor2dAw,

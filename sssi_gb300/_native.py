@@ -119,6 +119,8 @@ SIGNATURES = {
                                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                      ctypes.c_double, ctypes.c_int, c_dp, c_dp, c_dp, c_dp, c_dp,
                                                      c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, ctypes.c_int]),
+    "sssi_mat_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, c_dp, c_dp, c_dp, c_dp]),
+    "sssi_mat_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, c_dp, c_i64, c_dp, c_dp]),
     "sssi_rtmTimeCpmlFor2dAw": (ctypes.c_int, [c_dp, c_dp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_i64,
                                                 c_i64, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_dp, c_dp,

@@ -416,6 +416,46 @@ def fwdTimeSpmlFor3dEwPoint(vp, vs, nt, src_iz, src_ix, src_iy, src_component, w
     return tuple(outs)
 
 
+def mat_write(path, variables):
+    """save(path, names..., '-v6'): writes a dict {name: array} (numpy arrays or
+    CUDA tensors, column-major doubles) to a Level-5 MAT-file that MATLAB's load
+    and scipy.io.loadmat read.  Device arrays are streamed without a full host
+    copy."""
+    names = list(variables)
+    keep, ptrs, nds, dimarrs = [], [], [], []
+    for name in names:
+        p, k, shape = _in(variables[name], name)
+        keep.append(k)
+        ptrs.append(p or 0)
+        nds.append(max(len(shape), 1))
+        dimarrs.append(np.asarray(shape if len(shape) else (1,), dtype=np.int64))
+    n = len(names)
+    cnames = (ctypes.c_char_p * max(n, 1))(*[x.encode() for x in names])
+    carrs = (ctypes.c_void_p * max(n, 1))(*ptrs)
+    cnd = (ctypes.c_int * max(n, 1))(*nds)
+    cdims = (ctypes.c_void_p * max(n, 1))(*[d.ctypes.data for d in dimarrs])
+    check(lib().sssi_mat_write(str(path).encode(), n, ctypes.addressof(cnames), ctypes.addressof(carrs),
+                               ctypes.addressof(cnd), ctypes.addressof(cdims)))
+
+
+def mat_read(path, name, *, out=None):
+    """load(path, name) for one real numeric variable of a Level-5 MAT-file:
+    returns a column-major float64 numpy array, or fills ``out`` (a numpy array
+    or CUDA tensor of the same number of elements, column-major) and returns it."""
+    nd = ctypes.c_int(0)
+    dims = np.zeros(8, dtype=np.int64)
+    check(lib().sssi_mat_read(str(path).encode(), name.encode(), None, 0, ctypes.addressof(nd), dims.ctypes.data))
+    shape = tuple(int(x) for x in dims[:nd.value])
+    if out is None:
+        out = np.zeros(shape, order="F")
+    capacity = int(out.numel()) if _is_torch(out) else int(np.asarray(out).size)
+    if not _is_torch(out) and out.ndim > 1 and not out.flags.f_contiguous:
+        raise ValueError("out must be column-major (Fortran ordered)")
+    check(lib().sssi_mat_read(str(path).encode(), name.encode(), _addr(out), capacity, ctypes.addressof(nd),
+                              dims.ctypes.data))
+    return out
+
+
 def set_stream(stream) -> None:
     """Make the library launch on ``stream`` (a torch.cuda.Stream, a raw handle, or None)."""
     handle = getattr(stream, "cuda_stream", stream) or 0

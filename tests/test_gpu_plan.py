@@ -175,3 +175,31 @@ def test_plan_stack(gpu, oracle_mod, mode):
         for t, (z0, x0, width) in zip(ts, windows):  # each shot also returned its own image
             assert plan.wait(t)["image"].shape == (nz - z0, width)
     assert oracle_mod.rel_l2(out, expect) <= 1e-14
+
+
+def test_stack_to_mat_file(gpu, tmp_path):
+    """The device-resident stacked image of a plan goes to a MAT-file straight
+    from device memory (StackedRTM, mainRtmTimeCpmlFor2dAw.m:348-351) and reads
+    back equal, on the host and into a device tensor."""
+    import torch
+    import scipy.io as sio
+
+    nz, nx, nt = 60, 90, 200
+    rng = np.random.default_rng(3)
+    v = np.full((nz, nx), 2000.0)
+    v[30:, :] = 2600.0
+    vs = v.copy()
+    w = np.sin(np.arange(nt) * 0.2) * np.exp(-((np.arange(nt) - 30) / 10.0) ** 2)
+    with gpu.Plan(4, 10.0, 10.0, mode="fp64") as plan:
+        st = plan.stack(nz, nx)
+        t = plan.submit_rtm2d(v + rng.uniform(-5, 5, v.shape), vs, w, 0, nx // 2, 8, 1e-3, stack=st)
+        plan.wait(t)
+        dev = torch.zeros((nx, nz), dtype=torch.float64, device="cuda").T
+        plan.stack_get(st, dev)
+    path = tmp_path / "StackedRTM.mat"
+    gpu.mat_write(path, {"StackedRTM": dev})
+    host = sio.loadmat(path)["StackedRTM"]
+    assert np.array_equal(host, dev.cpu().numpy()) and np.abs(host).max() > 0
+    back = torch.zeros((nx, nz), dtype=torch.float64, device="cuda").T
+    gpu.mat_read(path, "StackedRTM", out=back)
+    assert torch.equal(back, dev)
