@@ -360,6 +360,11 @@ typedef struct {
     /* device time of the batched 2D steps (events around each round's
      * launches) and the cell-updates made in it */
     double batch2d_gpu_s, batch2d_cell_updates;
+    /* the batched step's tile shape in use (0: 64 x 32, 1: 32 x 32, 2: 128 x 16
+     * cells in FP32; FP64 has 32 x 32 only) and the tuner's last timing of each
+     * (milliseconds for its trial steps; 0: not timed) */
+    int batch2d_tile_shape;
+    double batch2d_tune_ms[3];
 } sssi_plan_stats;
 
 /* Creates a plan on the current device.  Native form of the submit/poll/wait
@@ -409,6 +414,13 @@ int sssi_plan_stats_get(sssi_plan *plan, sssi_plan_stats *stats);
  * plan fails the shots of that step, and the device stays usable.  step < 0
  * turns the knob off. */
 int sssi_debug_withhold_copy(int step, unsigned wait_limit);
+
+/* No counterpart in the reference: a test knob of the batched 2D step.  With
+ * shape >= 0, batches built after this call use that tile shape (0: 64 x 32,
+ * 1: 32 x 32, 2: 128 x 16 cells; a shape the element type lacks is ignored)
+ * instead of timing the shapes; shape < 0 hands the choice back to the tuner.
+ * Results do not depend on the shape: the tests use this to show it. */
+int sssi_debug_tile_shape(int shape);
 
 /* ---- forward modelling without any allocation ---- */
 

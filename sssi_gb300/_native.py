@@ -49,7 +49,8 @@ class PlanStats(ctypes.Structure):
                 ("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_budget", ctypes.c_size_t),
                 ("batch_steps", c_i64), ("cell_updates", ctypes.c_double), ("admit_s", ctypes.c_double),
                 ("round_s", ctypes.c_double), ("gpu_wait_s", ctypes.c_double), ("deliver_s", ctypes.c_double),
-                ("batch2d_gpu_s", ctypes.c_double), ("batch2d_cell_updates", ctypes.c_double)]
+                ("batch2d_gpu_s", ctypes.c_double), ("batch2d_cell_updates", ctypes.c_double),
+                ("batch2d_tile_shape", ctypes.c_int), ("batch2d_tune_ms", ctypes.c_double * 3)]
 
 
 # name -> (restype, argtypes)
@@ -62,6 +63,7 @@ SIGNATURES = {
     "sssi_plan_stack_create": (ctypes.c_int, [ctypes.c_void_p, c_i64, c_i64, ctypes.POINTER(c_i64)]),
     "sssi_plan_stack_get": (ctypes.c_int, [ctypes.c_void_p, c_i64, c_dp]),
     "sssi_debug_withhold_copy": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint]),
+    "sssi_debug_tile_shape": (ctypes.c_int, [ctypes.c_int]),
     "sssi_wait": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
     "sssi_plan_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlanStats)]),
     "sssi_last_error": (ctypes.c_char_p, []),

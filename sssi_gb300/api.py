@@ -491,6 +491,13 @@ def debug_withhold_copy(step: int, wait_limit: int = 0) -> None:
     check(lib().sssi_debug_withhold_copy(int(step), int(wait_limit)))
 
 
+def debug_tile_shape(shape: int) -> None:
+    """Test knob: batches built from now on use tile shape ``shape`` (0: 64 x 32,
+    1: 32 x 32, 2: 128 x 16 cells) instead of the tuner's choice; -1 restores
+    the tuner.  Results do not depend on the shape."""
+    check(lib().sssi_debug_tile_shape(int(shape)))
+
+
 def release_cache() -> None:
     check(lib().sssi_release_cache())
 
@@ -652,7 +659,9 @@ class Plan:
 
         st = PlanStats()
         check(lib().sssi_plan_stats_get(self._h, ctypes.byref(st)))
-        return {k: getattr(st, k) for k, _ in PlanStats._fields_}
+        out = {k: getattr(st, k) for k, _ in PlanStats._fields_}
+        out["batch2d_tune_ms"] = list(out["batch2d_tune_ms"])
+        return out
 
 
 def _points(src_iz, src_ix, src_iy, wavelets, nt):

@@ -128,7 +128,7 @@ inline unsigned sched_word(const ShotTail<T>& d) {
 // top byte; the tile's first row z0 and first column x0 (a shot's tiles may
 // start above row 0 and left of column 0, see Batch2d::schedule) as
 // (z0 + kZBias) / 4 and (x0 + kXBias) / 2, 16 bits each.
-constexpr int kZBias = 64, kXBias = 64;
+constexpr int kZBias = 128, kXBias = 64;  // z0 >= -(TZ - 1) of the deepest tile shape
 constexpr int kMaxTileRow = 4 * 0xffff - kZBias;  // largest z0
 constexpr int kMaxTileCol = 2 * 0xffff - kXBias;  // largest x0
 __host__ __device__ inline int2 pack_work_item(int k, unsigned flags, int z0, int x0) {
@@ -141,9 +141,9 @@ __host__ __device__ inline int work_item_x0(int2 item) { return (int)((unsigned)
 template <typename T>
 struct alignas(128) ShotDesc {
     // per tile shape (BatchShape index)
-    CUtensorMap tm_box[2][2];   // halo box of field k
-    CUtensorMap tm_tile[2][2];  // tile box of field k
-    CUtensorMap tm_v[2];        // tile box of (v dt)^2
+    CUtensorMap tm_box[kMaxBatchShapes][2];   // halo box of field k
+    CUtensorMap tm_tile[kMaxBatchShapes][2];  // tile box of field k
+    CUtensorMap tm_v[kMaxBatchShapes];        // tile box of (v dt)^2
     ShotTail<T> s;
 };
 
@@ -219,6 +219,9 @@ class Batch2d {
     void check_errors();
     // Status of shot k set by the steps (SSSI_OK or SSSI_ERR_UNSTABLE), read
     // after the stream has run; clear_status resets it.
+    // the tile shape in use (BatchShape index) and the tuner's last timings
+    int tile_shape() const { return shape_; }
+    float tuned_ms(int v) const { return tuned_ms_[v]; }
     std::vector<int> statuses();
     void clear_status(int k);
     // Test knob: at batch step `step` block 0 withholds its first tile's copies,
@@ -284,6 +287,7 @@ class Batch2d {
     int shape_ = 0;
     bool tune_ = false;
     int tuned_tiles_ = 0;
+    float tuned_ms_[kMaxBatchShapes] = {};  // the tuner's last timing of each shape
     static constexpr int kTuneSteps = 6, kTuneMinRun = 64;  // steps per shape; shortest run that tunes
     int tile_z(int shape) const;
     int tile_x(int shape) const;
@@ -296,11 +300,11 @@ class Batch2d {
     int shape_free_ = 0;  // the tile shape to return to when the last pair leaves
     DeviceBuffer d_desc_, d_ctr_;                // d_ctr_: graph step base, zero, error flag
     DeviceBuffer d_status_;                      // one status word per shot slot
-    DeviceBuffer d_cta_begin_[2], d_work_[2];    // the schedule of each tile shape
-    int grid_s_[2] = {0, 0}, ntiles_s_[2] = {0, 0};
-    bool split_s_[2] = {false, false};
+    DeviceBuffer d_cta_begin_[kMaxBatchShapes], d_work_[kMaxBatchShapes];  // the schedule of each tile shape
+    int grid_s_[kMaxBatchShapes] = {}, ntiles_s_[kMaxBatchShapes] = {};
+    bool split_s_[kMaxBatchShapes] = {};
     int grid_ = 0, ntiles_ = 0, step_ = 0;
-    int ctas_per_sm_[2] = {1, 1}, ctas_per_sm_pair_ = 1, sms_ = 1;
+    int ctas_per_sm_[kMaxBatchShapes] = {1, 1, 1}, ctas_per_sm_pair_ = 1, sms_ = 1;
     cudaGraphExec_t graph_ = nullptr;
 };
 

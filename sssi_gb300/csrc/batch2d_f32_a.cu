@@ -1,9 +1,7 @@
-// Batched 2D CPML step, float, orders 1-4.
+// Batched 2D CPML step, float, orders 1-2.
 #include "batch2d_kernel.cuh"
 
 namespace sssi {
 SSSI_BATCH2D_INSTANCE(float, 1)
 SSSI_BATCH2D_INSTANCE(float, 2)
-SSSI_BATCH2D_INSTANCE(float, 3)
-SSSI_BATCH2D_INSTANCE(float, 4)
 }  // namespace sssi

@@ -1,9 +1,7 @@
-// Batched 2D CPML step, float, orders 5-8.
+// Batched 2D CPML step, float, orders 3-4.
 #include "batch2d_kernel.cuh"
 
 namespace sssi {
-SSSI_BATCH2D_INSTANCE(float, 5)
-SSSI_BATCH2D_INSTANCE(float, 6)
-SSSI_BATCH2D_INSTANCE(float, 7)
-SSSI_BATCH2D_INSTANCE(float, 8)
+SSSI_BATCH2D_INSTANCE(float, 3)
+SSSI_BATCH2D_INSTANCE(float, 4)
 }  // namespace sssi

@@ -387,15 +387,19 @@ void Batch2d<T>::drop_graph() {
 
 template <typename T>
 int Batch2d<T>::tile_z(int shape) const {
-    if constexpr (kBatchShapes<T> > 1)
+    if constexpr (kBatchShapes<T> > 2) {
         if (shape == 1) return BatchShape<T, 1>::TZ;
+        if (shape == 2) return BatchShape<T, 2>::TZ;
+    }
     return TileShape<T>::TZ;
 }
 
 template <typename T>
 int Batch2d<T>::tile_x(int shape) const {
-    if constexpr (kBatchShapes<T> > 1)
+    if constexpr (kBatchShapes<T> > 2) {
         if (shape == 1) return BatchShape<T, 1>::TX;
+        if (shape == 2) return BatchShape<T, 2>::TX;
+    }
     return TileShape<T>::TX;
 }
 
@@ -420,12 +424,16 @@ void Batch2d<T>::finalize() {
         if (S.enabled)
             tiles += ((int64_t)(S.desc.s.nz + TileShape<T>::TZ - 1) / TileShape<T>::TZ) *
                      ((S.desc.s.nx + TileShape<T>::TX - 1) / TileShape<T>::TX);
-    if (kBatchShapes<T> > 1 && tiles >= 4LL * sms_ * ctas_per_sm_[0] && tiles > 8LL * tuned_tiles_) {
+    const int forced = forced_tile_shape();
+    if (forced >= 0 && forced < kBatchShapes<T>) {  // test knob: a fixed shape, no tuning
+        tune_ = false;
+        shape_ = forced;
+    } else if (kBatchShapes<T> > 1 && tiles >= 4LL * sms_ * ctas_per_sm_[0] && tiles > 8LL * tuned_tiles_) {
         tune_ = true;
         tuned_tiles_ = (int)std::min<int64_t>(tiles, 1 << 30);
     }
     if (tune_)
-        for (int v = 0; v < kBatchShapes<T>; ++v) schedule(v);  // both, for the tuner
+        for (int v = 0; v < kBatchShapes<T>; ++v) schedule(v);  // every shape, for the tuner
     else
         schedule(shape_);
     use_shape(shape_);
@@ -760,8 +768,8 @@ void Batch2d<T>::run(int nsteps) {
         // then the faster shape's schedule for the rest (the per-cell arithmetic
         // does not depend on the tiling, so the results do not either)
         tune_ = false;
-        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-        float ms[2] = {0.0f, 0.0f};
+        cudaEvent_t ev[2 * kMaxBatchShapes] = {};
+        float ms[kMaxBatchShapes] = {};
         cudaError_t e = cudaSuccess;
         for (auto& x : ev)
             if (e == cudaSuccess) e = cudaEventCreate(&x);
@@ -777,7 +785,11 @@ void Batch2d<T>::run(int nsteps) {
         for (auto& x : ev)
             if (x) cudaEventDestroy(x);
         SSSI_CHECK_CUDA(e);
-        use_shape((kBatchShapes<T> > 1 && ms[1] < ms[0]) ? 1 : 0);
+        int best = 0;
+        for (int v = 1; v < kBatchShapes<T>; ++v)
+            if (ms[v] < ms[best]) best = v;
+        use_shape(best);
+        for (int v = 0; v < kBatchShapes<T>; ++v) tuned_ms_[v] = ms[v];
     }
     if (nsteps - q >= kGraphSteps) {
         int* base = d_ctr_.template as<int>();

@@ -1485,6 +1485,11 @@ void launch_batch2d_n(const ShotDesc<T>* shots, const BatchConst<T>& bc, int gri
             launch_batch2d_shape<T, N, BatchShape<T, 1>>(shots, bc, grid, split, lean, stream);
             return;
         }
+        if constexpr (kBatchShapes<T> > 2)
+            if (shape == 2) {
+                launch_batch2d_shape<T, N, BatchShape<T, 2>>(shots, bc, grid, split, lean, stream);
+                return;
+            }
     }
     SSSI_REQUIRE(!pair, SSSI_ERR_INTERNAL, "residual pairs are FP32 only");
     SSSI_REQUIRE(shape == 0, SSSI_ERR_INTERNAL, "tile shape %d not built for this type", shape);
@@ -1512,6 +1517,8 @@ int batch2d_occupancy_n(int shape, bool pair) {
     if constexpr (kBatchShapes<T> > 1) {
         if (pair) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>, true>();
         if (shape == 1) return batch2d_occupancy_shape<T, N, BatchShape<T, 1>, false>();
+        if constexpr (kBatchShapes<T> > 2)
+            if (shape == 2) return batch2d_occupancy_shape<T, N, BatchShape<T, 2>, false>();
     }
     return batch2d_occupancy_shape<T, N, BatchShape<T, 0>, false>();
 }

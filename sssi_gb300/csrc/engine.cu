@@ -132,6 +132,9 @@ class EngineBase {
     // device time of the batched 2D steps (CUDA events around each round's
     // launches) and the cell-updates they made
     double batch2d_gpu_s = 0, batch2d_cells = 0;
+    // the batched step's tile shape in use and the tuner's timings of each
+    int tile_shape = 0;
+    double tune_ms[3] = {0, 0, 0};
 
   protected:
     // Waits for the batch stream, counting the time.
@@ -375,6 +378,8 @@ class Engine final : public EngineBase {
             SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms, ev2_[0], ev2_[1]));
             batch2d_gpu_s += 1e-3 * ms;
             batch2d_cells += cells2_;
+            tile_shape = B_.tile_shape();
+            for (int v = 0; v < 3; ++v) tune_ms[v] = v < kBatchShapes<T> ? B_.tuned_ms(v) : 0.0f;
             B_.check_errors();
             fail_unstable();
             finish_2d_events(out);
@@ -601,6 +606,8 @@ struct sssi_plan {
     int64_t n_running = 0, n_done = 0, n_failed = 0, batch_steps = 0;
     double cells = 0, admit_s = 0, round_s = 0, gpu_wait_s = 0, deliver_s = 0, batch2d_gpu_s = 0,
            batch2d_cells = 0;
+    int tile_shape = 0;
+    double tune_ms[3] = {0, 0, 0};
     bool stop = false;
     int fatal = SSSI_OK;
     std::string fatal_msg;
@@ -772,6 +779,8 @@ struct sssi_plan {
                 gpu_wait_s = engine->gpu_wait_s;
                 batch2d_gpu_s = engine->batch2d_gpu_s;
                 batch2d_cells = engine->batch2d_cells;
+                tile_shape = engine->tile_shape;
+                for (int v = 0; v < 3; ++v) tune_ms[v] = engine->tune_ms[v];
             }
             hand_over(out);
             if (!fin.empty()) finish(fin);
@@ -1041,6 +1050,8 @@ extern "C" int sssi_plan_stats_get(sssi_plan* plan, sssi_plan_stats* stats) {
         stats->gpu_wait_s = plan->gpu_wait_s;
         stats->batch2d_gpu_s = plan->batch2d_gpu_s;
         stats->batch2d_cell_updates = plan->batch2d_cells;
+        stats->batch2d_tile_shape = plan->tile_shape;
+        for (int v = 0; v < 3; ++v) stats->batch2d_tune_ms[v] = plan->tune_ms[v];
         stats->deliver_s = plan->deliver_s;
     });
 }

@@ -198,7 +198,10 @@ namespace sssi {
 namespace {
 std::atomic<int> g_debug_step{-1};
 std::atomic<unsigned> g_debug_wait{0};
+std::atomic<int> g_forced_shape{-1};
 }  // namespace
+
+int forced_tile_shape() { return g_forced_shape.load(); }
 
 void debug_withhold(int* step, unsigned* wait_limit) {
     *step = g_debug_step.load();
@@ -210,6 +213,12 @@ extern "C" int sssi_debug_withhold_copy(int step, unsigned wait_limit) {
     sssi::clear_error();
     sssi::g_debug_step.store(step < 0 ? -1 : step);
     sssi::g_debug_wait.store(wait_limit);
+    return SSSI_OK;
+}
+
+extern "C" int sssi_debug_tile_shape(int shape) {
+    sssi::clear_error();
+    sssi::g_forced_shape.store(shape < 0 ? -1 : shape);
     return SSSI_OK;
 }
 

@@ -65,6 +65,8 @@ int guarded(F&& f) {
 void count_launch(int n = 1);
 // The test knob of sssi_debug_withhold_copy (step < 0: off).
 void debug_withhold(int* step, unsigned* wait_limit);
+// The test knob of sssi_debug_tile_shape (-1: the tuner chooses).
+int forced_tile_shape();
 // One-thread kernels that set / advance a device int (graph step bases).
 void launch_store_int(int* p, int v, cudaStream_t s);
 void launch_add_int(int* p, int v, cudaStream_t s);

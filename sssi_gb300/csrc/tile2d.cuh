@@ -44,8 +44,11 @@ struct TileShape<double> {
 };
 
 // Tile shapes of the batched step: shape 0 is TileShape<T>; FP32 also has
-// shape 1, 32 x 32 tiles with four blocks per SM, which the batch's tuner
-// picks when it steps faster (large single grids).
+// shape 1, 32 x 32 tiles with four blocks per SM, and shape 2, 128 x 16 tiles
+// (a z-block twice as deep as shape 0's, half as wide).  The batch's tuner
+// times the shapes on the first steps of a large schedule and keeps the
+// fastest: the z-block depth (32, 64 or 128 rows) and the width that goes
+// with it.
 template <typename T, int V>
 struct BatchShape;
 template <typename T>
@@ -58,8 +61,15 @@ struct BatchShape<float, 1> {
     static constexpr int kThreads = (TZ / 4) * (TX / RX), kMinBlocks = 4;
     static constexpr int kIndex = 1;
 };
+template <>
+struct BatchShape<float, 2> {
+    static constexpr int TZ = 128, TX = 16, RX = 2;
+    static constexpr int kThreads = (TZ / 4) * (TX / RX), kMinBlocks = 2;
+    static constexpr int kIndex = 2;
+};
+constexpr int kMaxBatchShapes = 3;
 template <typename T>
-constexpr int kBatchShapes = std::is_same<T, float>::value ? 2 : 1;
+constexpr int kBatchShapes = std::is_same<T, float>::value ? 3 : 1;
 
 template <typename T>
 struct MemVar;

@@ -68,3 +68,48 @@ def test_tiled_multiple_point_sources(gpu, co, oracle_mod):
     d_ref, _ = co.fwd2d(v, src, N, nB, 10.0, 10.0, 1e-3, want_snapshot=False)
     d, _ = S.fwdTimeCpmlFor2dAwPoint(v, nt, iz, ix, w, N, nB, 10.0, 10.0, 1e-3, mode="fp64")
     assert oracle_mod.rel_l2(d, d_ref) <= TOL_FP64
+
+
+def test_tile_shapes_give_identical_results(gpu):
+    """Every tile shape of the batched FP32 step -- 64 x 32, 32 x 32 and the deep
+    128 x 16 z-blocks the tuner also considers -- computes each cell by the same
+    formula: forward modelling (the variant without rare outputs), a run with
+    snapshots (rare outputs), and an RTM shot are bit-identical across shapes."""
+    rng = np.random.default_rng(17)
+    nz, nx, nt, N, nB = 301, 413, 120, 4, 20
+    v = rng.uniform(1500.0, 4000.0, (nz, nx))
+    w = np.sin(np.arange(nt) * 0.3)[None, :]
+    src = np.zeros((nz, nx, 40), order="F")
+    src[3, 200, :] = np.cos(np.arange(40) * 0.2)
+    outs = []
+    try:
+        for shape in (0, 1, 2):
+            gpu.debug_tile_shape(shape)
+            d, _ = gpu.fwdTimeCpmlFor2dAwPoint(v, nt, [2], [nx // 2], w, N, nB, 10.0, 10.0, 8e-4, mode="fp32")
+            d2, s2 = gpu.fwdTimeCpmlFor2dAw(v, src, N, nB, 10.0, 10.0, 8e-4, mode="fp32")
+            img = gpu.rtmTimeCpmlFor2dAw(v, v * 0.98, w[0, :80], 0, nx // 2, N, nB, 10.0, 10.0, 8e-4, mode="fp32",
+                                         snap_stride=1)
+            outs.append((d, d2, s2, img))
+    finally:
+        gpu.debug_tile_shape(-1)
+    for k in (1, 2):
+        for a, b in zip(outs[0], outs[k]):
+            assert np.array_equal(a, b), k
+
+
+def test_tuner_times_every_shape(gpu):
+    """A batch large enough to tune times all three tile shapes (the tuner's
+    z-block depth choice) and keeps the fastest; the plan reports both."""
+    rng = np.random.default_rng(23)
+    nt = 400
+    models = [rng.uniform(1500.0, 4000.0, (700, 1300)) for _ in range(6)]  # ready before the first submit
+    w = np.sin(np.arange(nt) * 0.2)[None, :]
+    with gpu.Plan(4, 10.0, 10.0, mode="fp32") as plan:
+        tickets = [plan.submit_fwd2d(v, nt, [2], [650], w, 20, 8e-4) for v in models]
+        for t in tickets:
+            plan.wait(t)
+        st = plan.stats()
+    assert st["batch_steps"] < 6 * nt  # the shots ran together
+    ms = st["batch2d_tune_ms"]
+    assert all(x > 0 for x in ms), ms
+    assert st["batch2d_tile_shape"] == int(np.argmin(ms))
