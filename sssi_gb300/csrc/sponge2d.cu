@@ -161,120 +161,123 @@ __device__ __forceinline__ T sponge_cell(SpongeGeom g, const T* __restrict__ bnd
     return kGeneral ? sponge<T, kMode>(r, i, j, g, bnd) : r;
 }
 
-// One step.  A warp owns 32 rows (one per lane) and marches along x over
-// p.march columns, keeping left / centre / right in registers (each value of
-// the present is fetched once by its owner); up and down come from lane
-// shuffles, the tile's edge rows from two predicated loads.  Lanes below the
-// grid fetch zero padding and store nothing.  A tile clear of the sponge
-// bands and of every source (the common case) takes the lean update.
+// The FP32 step.  A warp owns 64 rows, two consecutive ones per lane (one
+// 8-byte access), and marches along x over p.march columns, keeping left /
+// centre / right of the present in registers (each value of the present is
+// fetched once by its owner); the neighbours across lanes come from shuffles,
+// the tile's edge rows from two predicated loads, and the update of a lane's
+// two cells is one packed two-lane sequence.  Lanes below the grid fetch zero
+// padding and store nothing.  A tile clear of the sponge bands, row 0 and every
+// source (the common case) takes the lean update; the others go cell by cell.
+constexpr int kSpMarchRows = 64;
+
 template <typename T, int kMode>
-__global__ void __launch_bounds__(kSpThreads, 4) sponge2d_march_kernel(const __grid_constant__ SpongeParams<T> p) {
+__global__ void __launch_bounds__(kSpThreads, 3) sponge2d_march_kernel(const __grid_constant__ SpongeParams<T> p) {
+    static_assert(kMode == SSSI_MODE_FP32 && std::is_same<T, float>::value, "the marching step is the FP32 form");
     constexpr int U = kSpAhead<T>;
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const int step = *reinterpret_cast<volatile const int*>(p.step_base) + p.step_offset;
     const int t = p.reverse ? p.nt - 1 - step : step;
-    const T* __restrict__ cur = p.field[step & 1];
-    T* __restrict__ nxt = p.field[(step & 1) ^ 1];
-    const SpongeHooks<T> h = *p.hooks;
+    const float* __restrict__ cur = p.field[step & 1];
+    float* __restrict__ nxt = p.field[(step & 1) ^ 1];
+    const SpongeHooks<float> h = *p.hooks;
     const int64_t n = (int64_t)p.nz * p.nx;
-    const T* src_dense = h.src_dense ? h.src_dense + (int64_t)(t - h.dense_t0) * n : nullptr;
-    T* snap = h.snap ? h.snap + (int64_t)(t - h.snap_t0) * n : nullptr;
-    const T* fsnap = h.fsnap ? h.fsnap + (int64_t)(t - h.fsnap_t0) * n : nullptr;
-    const bool per_cell_out = snap || fsnap || src_dense;  // outputs / inputs in the dense nz x nx layout
+    const float* src_dense = h.src_dense ? h.src_dense + (int64_t)(t - h.dense_t0) * n : nullptr;
+    float* snap = h.snap ? h.snap + (int64_t)(t - h.snap_t0) * n : nullptr;
     const int lane = threadIdx.x & 31;
     const int64_t ldp = p.ldp;
     const int nwarps = gridDim.x * (kSpThreads / 32);
     const SpongeGeom g{p.nz, p.nx, p.nB};
-    const SpongeK<T> kk{p.kx, p.kz, p.kxz2};
-    const T* __restrict__ bnd = p.bnd;
+    const SpongeK<float> kk{p.kx, p.kz, p.kxz2};
+    const float* __restrict__ bnd = p.bnd;
+    const float2 kx2 = make_float2(p.kx, p.kx), kz2 = make_float2(p.kz, p.kz), kxz2 = make_float2(p.kxz2, p.kxz2);
+    const float2 two = make_float2(2.0f, 2.0f);
     for (int tile = blockIdx.x * (kSpThreads / 32) + (threadIdx.x >> 5); tile < p.ntiles; tile += nwarps) {
         const int tz = tile % p.ntz, tx = tile / p.ntz;
-        const int i0 = tz * kSpRows, i = i0 + lane, j0 = tx * p.march;
+        const int i0 = tz * kSpMarchRows, i = i0 + 2 * lane, j0 = tx * p.march;
         const int jend = min(j0 + p.march, p.nx);
-        const bool row_ok = i < p.nz;
-        // warp-uniform: does the tile touch a sponge band, row 0's injection or a point source?
-        bool general = i0 + kSpRows > p.nz - p.nB || j0 < p.nB || jend > p.nx - p.nB || src_dense ||
-                       ((p.src_row || p.rec) && i0 == 0);
+        const bool ok0 = i < p.nz, ok1 = i + 1 < p.nz;
+        // warp-uniform: does the tile touch a sponge band, row 0 or a point source?
+        bool general = i0 + kSpMarchRows > p.nz - p.nB || j0 < p.nB || jend > p.nx - p.nB || src_dense ||
+                       ((p.src_row || p.rec) && i0 == 0) || snap;
         for (int k = 0; k < p.nsrc; ++k) {
             const int si = p.src_iz[k], sj = p.src_ix[k];
-            general |= si >= i0 && si < i0 + kSpRows && sj >= j0 && sj < jend;
+            general |= si >= i0 && si < i0 + kSpMarchRows && sj >= j0 && sj < jend;
         }
         const int64_t q0 = i + (int64_t)j0 * ldp;
-        const T* pc = cur + q0;  // (i, j) of the column being computed
-        T* pn = nxt + q0;
-        const T* pv = p.cvdt2 + q0;
-        const T* pb = kMode != SSSI_MODE_FP32 ? p.cb + q0 : nullptr;
-        const T* px = kMode != SSSI_MODE_FP32 ? p.cax + q0 : nullptr;
-        const T* pz = kMode != SSSI_MODE_FP32 ? p.caz + q0 : nullptr;
-        T lf = __ldg(pc - ldp);
-        T c = __ldg(pc);
+        const float* pc = cur + q0;  // (i, j) of the column being computed
+        float* pn = nxt + q0;
+        const float* pv = p.cvdt2 + q0;
+        float2 lf = __ldg(reinterpret_cast<const float2*>(pc - ldp));
+        float2 c = __ldg(reinterpret_cast<const float2*>(pc));
         for (int jb = j0; jb < jend; jb += U) {
-            T rt[U], po[U], vd[U], eg[U], cb[U], cx[U], cz[U];
+            float2 rt[U], po[U], vd[U];
+            float eg[U];
             const bool whole = jb + U <= jend;  // warp-uniform; a partial group only at the grid's last column
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 // past the end: a repeat of the last column, unused
                 const int64_t o = whole ? (int64_t)u * ldp : (int64_t)min(u, jend - 1 - jb) * ldp;
-                rt[u] = __ldg(pc + o + ldp);
-                po[u] = pn[o];
-                vd[u] = __ldg(pv + o);
-                eg[u] = lane == 0 ? __ldg(pc + o - 1) : (lane == 31 ? __ldg(pc + o + 1) : T(0));
-                if constexpr (kMode != SSSI_MODE_FP32) {
-                    cb[u] = __ldg(pb + o);
-                    cx[u] = __ldg(px + o);
-                    cz[u] = __ldg(pz + o);
-                } else {
-                    cb[u] = cx[u] = cz[u] = T(0);
-                }
+                rt[u] = __ldg(reinterpret_cast<const float2*>(pc + o + ldp));
+                po[u] = *reinterpret_cast<const float2*>(pn + o);
+                vd[u] = __ldg(reinterpret_cast<const float2*>(pv + o));
+                eg[u] = lane == 0 ? __ldg(pc + o - 1) : (lane == 31 ? __ldg(pc + o + 2) : 0.0f);
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int j = jb + u;
                 if (j >= jend) break;  // warp-uniform
-                const T up_s = __shfl_up_sync(0xffffffffu, c, 1), dn_s = __shfl_down_sync(0xffffffffu, c, 1);
-                const T up = lane == 0 ? eg[u] : up_s, dn = lane == 31 ? eg[u] : dn_s;
+                const float up_s = __shfl_up_sync(0xffffffffu, c.y, 1), dn_s = __shfl_down_sync(0xffffffffu, c.x, 1);
+                const float up0 = lane == 0 ? eg[u] : up_s;   // row i - 1
+                const float dn1 = lane == 31 ? eg[u] : dn_s;  // row i + 2
                 const int64_t o = (int64_t)u * ldp;
-                if (row_ok) {
-                    T out;
-                    if (!general) {
-                        out = sponge_cell<T, kMode, false>(g, bnd, kk, i, j, c, up, dn, lf, rt[u], po[u], vd[u],
-                                                           cb[u], cx[u], cz[u], false, T(0));
-                    } else {
-                        // the injected value of the cell at step t (dense slice, row 0, point sources)
-                        T src = T(0);
+                float2 out;
+                if (!general) {
+                    const float2 v = vd[u];
+                    const float2 ax = __fmul2_rn(v, kx2), az = __fmul2_rn(v, kz2);
+                    const float2 b = __ffma2_rn(make_float2(-v.x, -v.y), kxz2, two);  // 2 - 2 ax - 2 az
+                    float2 r = __ffma2_rn(b, c, make_float2(-po[u].x, -po[u].y));
+                    r = __ffma2_rn(ax, __fadd2_rn(rt[u], lf), r);
+                    r = __ffma2_rn(az, __fadd2_rn(make_float2(c.y, dn1), make_float2(up0, c.x)), r);
+                    out = r;
+                } else {
+                    // the general update of each of the lane's two cells
+                    float res[2] = {0.0f, 0.0f};
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int ii = i + e;
+                        if (ii >= p.nz) continue;
+                        const float cc = e ? c.y : c.x, up = e ? c.x : up0, dn = e ? dn1 : c.y;
+                        const float lfe = e ? lf.y : lf.x, rte = e ? rt[u].y : rt[u].x;
+                        const float poe = e ? po[u].y : po[u].x, vde = e ? vd[u].y : vd[u].x;
+                        float src = 0.0f;
                         bool has_src = false;
                         if (src_dense) {
-                            src = src_dense[i + (int64_t)j * p.nz];
+                            src = src_dense[ii + (int64_t)j * p.nz];
                             has_src = true;
                         }
-                        if (p.src_row && i == 0) {
+                        if (p.src_row && ii == 0) {
                             src = p.src_row[j + (int64_t)t * p.nx];
                             has_src = true;
                         }
                         for (int k = 0; k < p.nsrc; ++k)
-                            if (p.src_iz[k] == i && p.src_ix[k] == j) {
-                                const T w = p.wavelets[(int64_t)k * p.nt + t];
-                                src = has_src ? src + w : w;
+                            if (p.src_iz[k] == ii && p.src_ix[k] == j) {
+                                const float wv = p.wavelets[(int64_t)k * p.nt + t];
+                                src = has_src ? src + wv : wv;
                                 has_src = true;
                             }
-                        out = sponge_cell<T, kMode, true>(g, bnd, kk, i, j, c, up, dn, lf, rt[u], po[u], vd[u],
-                                                          cb[u], cx[u], cz[u], has_src, src);
+                        res[e] = sponge_cell<float, kMode, true>(g, bnd, kk, ii, j, cc, up, dn, lfe, rte, poe, vde,
+                                                                 0.0f, 0.0f, 0.0f, has_src, src);
+                        if (p.rec && ii == 0) p.rec[j + (int64_t)t * p.nx] = res[e];
+                        if (snap) snap[ii + (int64_t)j * p.nz] = res[e];
                     }
-                    pn[o] = out;
-                    if (general && p.rec && i == 0) p.rec[j + (int64_t)t * p.nx] = out;
-                    if (per_cell_out) {
-                        const int64_t qd = i + (int64_t)j * p.nz;
-                        if (snap) snap[qd] = out;
-                        if constexpr (kMode == SSSI_MODE_FP64) {
-                            if (fsnap) {
-                                const double f = fsnap[qd];
-                                p.im[qd] = fma(f, (double)out, p.im[qd]);
-                                p.is2[qd] = fma(f, f, p.is2[qd]);
-                            }
-                        }
-                    }
+                    out = make_float2(res[0], res[1]);
                 }
+                if (ok1)
+                    *reinterpret_cast<float2*>(pn + o) = out;
+                else if (ok0)
+                    pn[o] = out.x;
                 lf = c;
                 c = rt[u];
             }
@@ -282,11 +285,6 @@ __global__ void __launch_bounds__(kSpThreads, 4) sponge2d_march_kernel(const __g
             pc += adv;
             pn += adv;
             pv += adv;
-            if constexpr (kMode != SSSI_MODE_FP32) {
-                pb += adv;
-                px += adv;
-                pz += adv;
-            }
         }
     }
 }
@@ -432,7 +430,10 @@ class Sponge2d {
         : nz_((int)nz), nx_((int)nx), mode_(mode), s_(s) {
         // rows: kSpOrgRow above the interior, then the interior rounded up to whole
         // 32-row tiles plus one more row of zeros (row nz and the lanes below the grid)
-        ldp_ = (int64_t)kSpOrgRow + (nz + 31) / 32 * 32 + 32;
+        // interior rows rounded up to whole tiles (64 rows in FP32, 32 in FP64),
+        // plus one more tile row of zeros (row nz and the lanes below the grid)
+        const int trows = mode == SSSI_MODE_FP32 ? kSpMarchRows : kSpRows;
+        ldp_ = (int64_t)kSpOrgRow + (nz + trows - 1) / trows * trows + trows;
         const int64_t cols = nx + 2;
         const size_t cells = (size_t)(ldp_ * cols);
         org_ = kSpOrgRow + ldp_;  // interior (0, 0): row kSpOrgRow of column 1
@@ -484,7 +485,7 @@ class Sponge2d {
         p_.nB = nB;
         p_.nt = (int)nt;
         p_.ldp = ldp_;
-        p_.ntz = (nz_ + kSpRows - 1) / kSpRows;
+        p_.ntz = mode == SSSI_MODE_FP32 ? (nz_ + kSpMarchRows - 1) / kSpMarchRows : (nz_ + kSpRows - 1) / kSpRows;
         p_.reverse = reverse ? 1 : 0;
         p_.kx = (T)(1.0 / (dx * dx));
         p_.kz = (T)(1.0 / (dz * dz));
@@ -494,15 +495,23 @@ class Sponge2d {
         SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         int per_sm = 0;
         if (mode == SSSI_MODE_FP32) {
-            // FP32: the longest march that still gives every resident warp a tile
-            // (short marches re-fetch the column left of each tile; grids that fit
-            // in L2 need many warps in flight more than they need long marches)
             SSSI_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &per_sm, (const void*)sponge2d_march_kernel<float, SSSI_MODE_FP32>, kSpThreads, 0));
             per_sm = std::max(per_sm, 1);
+            // each warp takes every nwarps-th tile, so the step lasts ceil(tiles / warps)
+            // tiles of (march + 1) column loads (the +1: the column left of a tile):
+            // the march with the smallest such cost, the longer one on a tie
             const int64_t warps = (int64_t)sms * per_sm * (kSpThreads / 32);
-            int march = 32;
-            while (march > 4 && (int64_t)p_.ntz * ((nx_ + march - 1) / march) < warps) march /= 2;
+            int march = 4;
+            int64_t best = -1;
+            for (int m = 64; m >= 4; m /= 2) {
+                const int64_t tiles = (int64_t)p_.ntz * ((nx_ + m - 1) / m);
+                const int64_t cost = (tiles + warps - 1) / warps * (m + 1);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    march = m;
+                }
+            }
             p_.march = march;
             p_.ntiles = p_.ntz * ((nx_ + march - 1) / march);
             grid_ = (int)std::max<int64_t>(1, std::min<int64_t>((p_.ntiles + kSpThreads / 32 - 1) / (kSpThreads / 32),
