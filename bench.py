@@ -542,6 +542,7 @@ def bench_3d(S, args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     ms = float(np.mean(times))
+    sched, sched_ms = S.debug_schedule3d()
     d64 = torch.zeros((nt, ny, nx), dtype=torch.float64, device="cuda").permute(2, 1, 0)
     t0 = time.perf_counter()
     run("fp64", d64)
@@ -565,6 +566,8 @@ def bench_3d(S, args):
                          "traffic_note": "dram read+write of one step from an ncu capture of the same grid (cold)"},
             "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "ms_per_shot": round(ms64, 1)},
             "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (144 x 144)",
+            "schedule": sched, "schedule_tune_ms": [round(t, 3) for t in sched_ms],
+            "schedule_candidates": "even / cost-cut chunks along y, about 3 then about 2 items per resident block",
             "config": {"workload": "fwd3d-point-source", "grid": [nz, nx, ny], "physical": [256, 256, 256],
                        "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
                        "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",

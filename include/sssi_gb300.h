@@ -422,6 +422,14 @@ int sssi_debug_withhold_copy(int step, unsigned wait_limit);
  * Results do not depend on the shape: the tests use this to show it. */
 int sssi_debug_tile_shape(int shape);
 
+/* No counterpart in the reference: what the 3D propagator's schedule tuner
+ * chose.  A 3D propagation of at least 64 steps times four candidate
+ * work-item schedules on its first steps (even or cost-cut chunks along y, each
+ * with about three or about two items per resident block) and keeps the
+ * fastest; this reports the choice of the last one to finish tuning in
+ * *schedule (-1 before any) and the four timed runs in ms[0..3] (ms). */
+int sssi_debug_schedule3d(int* schedule, float* ms);
+
 /* ---- forward modelling without any allocation ---- */
 
 /* Size of the fixed working array behind sssi_fwdTimeCpmlFor2dAwNoAlloc. */

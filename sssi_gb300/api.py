@@ -498,6 +498,16 @@ def debug_tile_shape(shape: int) -> None:
     check(lib().sssi_debug_tile_shape(int(shape)))
 
 
+def debug_schedule3d() -> tuple[int, list[float]]:
+    """The 3D schedule tuner's last choice (-1 before any) and its four timed
+    runs in ms (even / cost-cut chunks at about three, then about two items per
+    resident block)."""
+    sched = ctypes.c_int(-1)
+    ms = (ctypes.c_float * 4)()
+    check(lib().sssi_debug_schedule3d(ctypes.byref(sched), ms))
+    return sched.value, [float(x) for x in ms]
+
+
 def release_cache() -> None:
     check(lib().sssi_release_cache())
 

@@ -47,6 +47,9 @@ struct Shape3D<double> {
     static constexpr int kMinBlocks = 1;
 };
 
+// Candidate work-item schedules of a 3D propagation, timed on its first steps.
+constexpr int kSchedules3 = kSchedules3Max;
+
 template <typename T>
 struct Desc3 {
     using M = typename MemVar<T>::type;
@@ -60,8 +63,8 @@ struct Desc3 {
     int nz, nx, ny, nB, nt;
     int ntz, ntx;          // tiles along z and x
     int zs;                // tile rows start at row -zs (Prop3d: the bottom band's rows in one tile row)
-    const int2* order[2];  // work items (tile, y0 | y1 << 16: planes y0 .. y1-1), most expensive first, of
-                           // the two candidate schedules (Const3::sched picks one)
+    const int2* order[kSchedules3];  // work items (tile, y0 | y1 << 16: planes y0 .. y1-1), most expensive
+                                     // first, of each candidate schedule (Const3::sched picks one)
     int* next;             // two counters: items taken at steps of parity 0 / 1
     // band coefficients (2D) and memory variables (3D), see the file header
     const T *zb, *zbm1, *xb, *xbm1, *yb, *ybm1;
@@ -112,11 +115,13 @@ class Prop3d {
     void set_stream(cudaStream_t s) { stream_ = s; }
     void sync_desc();
     // Whole runs of kGraphSteps go through a CUDA graph.  The first steps of a
-    // long run time the two candidate schedules (even chunks along y, or chunks
-    // cut by estimated cost per tile); the faster one is kept.
+    // long run time the candidate schedules (even chunks along y, or chunks cut
+    // by estimated cost per tile, each with about three or about two items per
+    // resident block); the fastest is kept.
     void run(int nsteps);
     void check_errors();
     int schedule() const { return cc_.sched; }
+    float tune_ms(int c) const { return tune_ms_[c]; }
     const T* current_field() const { return desc_.field[step_ & 1]; }
     int step() const { return step_; }
     static constexpr int kGraphSteps = 16;
@@ -129,15 +134,17 @@ class Prop3d {
     Desc3<T> desc_{};
     Const3<T> cc_{};
     DeviceBuffer P_[2], vdt2_, zb_, zbm1_, xb_, xbm1_, yb_, ybm1_, zphi_[2], zpsi_, xphi_[2], xpsi_, yphi_[2], ypsi_;
-    DeviceBuffer d_desc_, d_ctr_, d_order_[2], d_next_;
-    int nitems_[2] = {0, 0}, grid_c_[2] = {1, 1};
+    DeviceBuffer d_desc_, d_ctr_, d_order_[kSchedules3], d_next_;
+    int nitems_[kSchedules3] = {}, grid_c_[kSchedules3] = {};
     int grid_ = 0, step_ = 0;
     cudaGraphExec_t graph_ = nullptr;
-    // schedule tuning: phase 0 warm-up, 1 / 2 timing schedule 0 / 1, 3 waiting
-    // for the timings, 4 done
-    static constexpr int kTuneSteps = 6, kTuneMinSteps = 48;
+    // schedule tuning: phase 0 warm-up, 1 .. kSchedules3 timing schedule
+    // phase-1, kTuneWait waiting for the timings, kTuneDone done
+    static constexpr int kTuneSteps = 6, kTuneMinSteps = 64;
+    static constexpr int kTuneWait = kSchedules3 + 1, kTuneDone = kSchedules3 + 2;
     int tune_ = 0, tune_left_ = 2;
-    cudaEvent_t tev_[4] = {nullptr, nullptr, nullptr, nullptr};  // start and end of the two timed runs
+    cudaEvent_t tev_[2 * kSchedules3] = {};  // start and end of each timed run
+    float tune_ms_[kSchedules3] = {};        // the timed runs (ms), 0 until tuned
 };
 
 template <typename T, int N>

@@ -281,15 +281,18 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     cc_.step_base = d_ctr_.template as<int>() + 1;
     cc_.step_offset = 0;
     cc_.err = d_ctr_.template as<int>() + 2;
-    // Two candidate schedules of work items, each item a (z, x) tile and a chunk
-    // of planes; the dynamic schedule takes the most expensive first.  Cost
+    // Candidate schedules of work items, each item a (z, x) tile and a chunk of
+    // planes; the dynamic schedule takes the most expensive first.  Cost
     // model: a plane costs 1, 1.6 next to a z or x band (cooperative pass per
     // plane), +0.4 in a y band (memory-variable traffic); every chunk also
     // fills its queues from 2N-1 planes (0.3 each).
-    //   0: even chunks along y, enough items for about three per resident
-    //      block, 8 to 64 planes;
-    //   1: each tile's planes cut into chunks of about equal estimated cost
-    //      (tiles next to a band get shorter chunks), 4 to 64 planes.
+    //   0, 2: even chunks along y, enough items for about three (0) or two (2)
+    //         per resident block, 8 to 64 planes;
+    //   1, 3: each tile's planes cut into chunks of about equal estimated cost
+    //         (tiles next to a band get shorter chunks), about three (1) or
+    //         two (3) per resident block, 4 to 64 planes.
+    // Fewer, longer chunks fill the queues less often; more chunks balance the
+    // blocks better.
     {
         SSSI_REQUIRE(ny < 65536, SSSI_ERR_ARG, "ny must be below 65536");
         const int ntile = d.ntz * d.ntx;
@@ -308,22 +311,23 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
             int2 item;
             float cost;
         };
-        for (int c = 0; c < 2; ++c) {
+        for (int c = 0; c < kSchedules3; ++c) {
             std::vector<It> its;
+            const int64_t per = c < 2 ? 3 : 2;  // items per resident block
             auto chunk = [&](int t, int y0, int y1) {
                 float cost = warm;
                 for (int y = y0; y < y1; ++y) cost += plane_cost(bzx[t], y);
                 its.push_back({make_int2(t, y0 | (y1 << 16)), cost});
             };
-            if (c == 0) {
-                int64_t yc = std::max<int64_t>(8, (ny * ntile + 3 * slots - 1) / (3 * (int64_t)slots));
+            if (c % 2 == 0) {
+                int64_t yc = std::max<int64_t>(8, (ny * ntile + per * slots - 1) / (per * (int64_t)slots));
                 yc = std::min<int64_t>(yc, 64);
                 const int64_t nch = (ny + yc - 1) / yc;
                 const int ychunk = (int)((ny + nch - 1) / nch);  // even chunks
                 for (int t = 0; t < ntile; ++t)
                     for (int y0 = 0; y0 < ny; y0 += ychunk) chunk(t, y0, (int)std::min<int64_t>(y0 + ychunk, ny));
             } else {
-                const float target = std::max(4.0f, (float)(total / (3.0 * slots)));
+                const float target = std::max(4.0f, (float)(total / ((double)per * slots)));
                 for (int t = 0; t < ntile; ++t) {
                     int y0 = 0;
                     while (y0 < ny) {
@@ -358,7 +362,7 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
         d_next_.zero(stream_);
         d.next = d_next_.template as<int>();
         use_schedule(0);
-        if (nt < kTuneMinSteps) tune_ = 4;  // short runs keep schedule 0
+        if (nt < kTuneMinSteps) tune_ = kTuneDone;  // short runs keep schedule 0
         for (auto& e : tev_) SSSI_CHECK_CUDA(cudaEventCreate(&e));
     }
     sync_desc();
@@ -417,12 +421,12 @@ template <typename T>
 void Prop3d<T>::run(int nsteps) {
     int q = 0;
     // schedule tuning (single launches, events around the timed runs)
-    while (q < nsteps && tune_ < 3) {
+    while (q < nsteps && tune_ < kTuneWait) {
         if (tune_left_ == (tune_ == 0 ? 2 : kTuneSteps)) {
             // a timed run must lie within this call: the caller may queue other
             // work on the stream between calls
             if (tune_ > 0 && nsteps - q < kTuneSteps) break;
-            use_schedule(tune_ == 2 ? 1 : 0);
+            use_schedule(tune_ > 0 ? tune_ - 1 : 0);
             if (tune_ > 0) SSSI_CHECK_CUDA(cudaEventRecord(tev_[2 * (tune_ - 1)], stream_));  // start
         }
         const int k = std::min(nsteps - q, tune_left_);
@@ -435,16 +439,20 @@ void Prop3d<T>::run(int nsteps) {
             tune_left_ = kTuneSteps;
         }
     }
-    if (tune_ == 3) {
+    if (tune_ == kTuneWait) {
         // steps left in this call: wait for the timings (once per propagation),
         // else look without waiting and decide at a later call
-        const cudaError_t e = q < nsteps ? cudaEventSynchronize(tev_[3]) : cudaEventQuery(tev_[3]);
+        cudaEvent_t last = tev_[2 * kSchedules3 - 1];
+        const cudaError_t e = q < nsteps ? cudaEventSynchronize(last) : cudaEventQuery(last);
         if (e == cudaSuccess) {
-            float ms0 = 0, ms1 = 0;
-            SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms0, tev_[0], tev_[1]));
-            SSSI_CHECK_CUDA(cudaEventElapsedTime(&ms1, tev_[2], tev_[3]));
-            use_schedule(ms1 < ms0 ? 1 : 0);
-            tune_ = 4;
+            int best = 0;
+            for (int c = 0; c < kSchedules3; ++c) {
+                SSSI_CHECK_CUDA(cudaEventElapsedTime(&tune_ms_[c], tev_[2 * c], tev_[2 * c + 1]));
+                if (tune_ms_[c] < tune_ms_[best]) best = c;
+            }
+            use_schedule(best);
+            record_schedule3d(best, tune_ms_, kSchedules3);
+            tune_ = kTuneDone;
         } else if (e != cudaErrorNotReady) {
             SSSI_CHECK_CUDA(e);
         } else {

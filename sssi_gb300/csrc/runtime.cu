@@ -199,9 +199,18 @@ namespace {
 std::atomic<int> g_debug_step{-1};
 std::atomic<unsigned> g_debug_wait{0};
 std::atomic<int> g_forced_shape{-1};
+std::mutex g_sched3_mutex;
+int g_sched3 = -1;
+float g_sched3_ms[kSchedules3Max] = {};
 }  // namespace
 
 int forced_tile_shape() { return g_forced_shape.load(); }
+
+void record_schedule3d(int chosen, const float* ms, int n) {
+    std::lock_guard<std::mutex> lock(g_sched3_mutex);
+    g_sched3 = chosen;
+    for (int c = 0; c < kSchedules3Max; ++c) g_sched3_ms[c] = c < n ? ms[c] : 0.0f;
+}
 
 void debug_withhold(int* step, unsigned* wait_limit) {
     *step = g_debug_step.load();
@@ -219,6 +228,18 @@ extern "C" int sssi_debug_withhold_copy(int step, unsigned wait_limit) {
 extern "C" int sssi_debug_tile_shape(int shape) {
     sssi::clear_error();
     sssi::g_forced_shape.store(shape < 0 ? -1 : shape);
+    return SSSI_OK;
+}
+
+extern "C" int sssi_debug_schedule3d(int* schedule, float* ms) {
+    sssi::clear_error();
+    if (!schedule || !ms) {
+        sssi::set_error("sssi_debug_schedule3d: null argument");
+        return SSSI_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(sssi::g_sched3_mutex);
+    *schedule = sssi::g_sched3;
+    for (int c = 0; c < sssi::kSchedules3Max; ++c) ms[c] = sssi::g_sched3_ms[c];
     return SSSI_OK;
 }
 

@@ -67,6 +67,9 @@ void count_launch(int n = 1);
 void debug_withhold(int* step, unsigned* wait_limit);
 // The test knob of sssi_debug_tile_shape (-1: the tuner chooses).
 int forced_tile_shape();
+// The last 3D schedule choice and the timed runs behind it (sssi_debug_schedule3d).
+constexpr int kSchedules3Max = 4;
+void record_schedule3d(int chosen, const float* ms, int n);
 // One-thread kernels that set / advance a device int (graph step bases).
 void launch_store_int(int* p, int v, cudaStream_t s);
 void launch_add_int(int* p, int v, cudaStream_t s);

@@ -87,6 +87,9 @@ def test_fwd3d_long_run_reaches_bands(gpu, co, oracle_mod):
                                          1e-3, mode=mode)
         err = oracle_mod.rel_l2(d, d_ref)
         assert err <= tol, (mode, err)
+        # 260 steps: the schedule tuner timed its four candidates and kept the fastest
+        sched, ms = S.debug_schedule3d()
+        assert 0 <= sched < 4 and all(t > 0 for t in ms) and ms[sched] == min(ms), (mode, sched, ms)
 
 
 def test_fwd3d_errors(gpu):
