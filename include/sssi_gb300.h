@@ -430,6 +430,14 @@ int sssi_debug_tile_shape(int shape);
  * *schedule (-1 before any) and the four timed runs in ms[0..3] (ms). */
 int sssi_debug_schedule3d(int* schedule, float* ms);
 
+/* No counterpart in the reference: a test entry of the division the strict
+ * FP64 forms use for their per-term division by the grid spacing (a
+ * reciprocal, a correction and an exact check, the IEEE division otherwise).
+ * For each of the n dividends a[k] (host or device memory) it writes that
+ * quotient by d to fast[k] and the IEEE quotient to ieee[k]; the two must
+ * agree bit for bit. */
+int sssi_debug_divide(const double* a, int64_t n, double d, double* fast, double* ieee);
+
 /* ---- forward modelling without any allocation ---- */
 
 /* Size of the fixed working array behind sssi_fwdTimeCpmlFor2dAwNoAlloc. */

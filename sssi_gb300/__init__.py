@@ -9,6 +9,7 @@ from .api import (  # noqa: F401
     MODES,
     Plan,
     dampPml,
+    debug_divide,
     debug_schedule3d,
     debug_tile_shape,
     debug_withhold_copy,

@@ -65,6 +65,8 @@ SIGNATURES = {
     "sssi_debug_withhold_copy": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint]),
     "sssi_debug_tile_shape": (ctypes.c_int, [ctypes.c_int]),
     "sssi_debug_schedule3d": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]),
+    "sssi_debug_divide": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
     "sssi_wait": (ctypes.c_int, [ctypes.c_void_p, c_i64, ctypes.POINTER(ShotInfo)]),
     "sssi_plan_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlanStats)]),
     "sssi_last_error": (ctypes.c_char_p, []),

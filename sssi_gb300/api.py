@@ -508,6 +508,16 @@ def debug_schedule3d() -> tuple[int, list[float]]:
     return sched.value, [float(x) for x in ms]
 
 
+def debug_divide(a, d: float):
+    """Test entry: the strict forms' division of each element of ``a`` by ``d``
+    and the IEEE division, as two float64 arrays (equal bit for bit)."""
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    fast = np.empty_like(a)
+    ieee = np.empty_like(a)
+    check(lib().sssi_debug_divide(a.ctypes.data, a.size, float(d), fast.ctypes.data, ieee.ctypes.data))
+    return fast, ieee
+
+
 def release_cache() -> None:
     check(lib().sssi_release_cache())
 

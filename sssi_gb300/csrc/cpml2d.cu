@@ -35,10 +35,11 @@ struct Arith;
 template <>
 struct Arith<double, true> {
     template <int N>
-    __device__ __forceinline__ static double dsum(const double* c, double d, const double* a, const double* b) {
-        double s = __ddiv_rn(__dmul_rn(c[0], __dsub_rn(a[0], b[0])), d);
+    __device__ __forceinline__ static double dsum(const double* c, const Divisor<double>& d, const double* a,
+                                                  const double* b) {
+        double s = div_rn(__dmul_rn(c[0], __dsub_rn(a[0], b[0])), d);
 #pragma unroll
-        for (int k = 1; k < N; ++k) s = __dadd_rn(s, __ddiv_rn(__dmul_rn(c[k], __dsub_rn(a[k], b[k])), d));
+        for (int k = 1; k < N; ++k) s = __dadd_rn(s, div_rn(__dmul_rn(c[k], __dsub_rn(a[k], b[k])), d));
         return s;
     }
     // b*m + bm1*d
@@ -56,7 +57,7 @@ struct Arith<double, true> {
 template <typename T>
 struct ArithFast {
     template <int N>
-    __device__ __forceinline__ static T dsum(const T* w, T, const T* a, const T* b) {
+    __device__ __forceinline__ static T dsum(const T* w, const Divisor<T>&, const T* a, const T* b) {
         T s = w[0] * (a[0] - b[0]);
 #pragma unroll
         for (int k = 1; k < N; ++k) s = fma(w[k], a[k] - b[k], s);
@@ -376,8 +377,8 @@ Cpml2d<T, TA>::Cpml2d(const double* v, int64_t nz, int64_t nx, int N, int nB, do
             tmpl_.cx[k] = static_cast<T>(c[k] / dx);
         }
     }
-    tmpl_.dz = static_cast<T>(dz);
-    tmpl_.dx = static_cast<T>(dx);
+    tmpl_.dz = make_divisor<T>(dz);
+    tmpl_.dx = make_divisor<T>(dx);
 
     // (v dt)^2 and damping bands
     const int64_t n = nz * nx;

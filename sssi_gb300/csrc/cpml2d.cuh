@@ -3,6 +3,7 @@
 
 #include <cuda_fp16.h>
 
+#include "divide.cuh"
 #include "sssi_internal.h"
 
 namespace sssi {
@@ -41,7 +42,7 @@ struct Step2D {
     // strict: c_k and the divisors; fast: w_k = c_k/d (divisors unused)
     T cz[kMaxOrder];
     T cx[kMaxOrder];
-    T dz, dx;
+    Divisor<T> dz, dx;
 
     // sources added inside vdt2*(Pz + Px + src)
     const double* src_dense;  // nz x nx slice of this step, or null

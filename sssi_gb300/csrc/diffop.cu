@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include "api_util.cuh"
+#include "divide.cuh"
 
 namespace sssi {
 namespace {
@@ -23,7 +24,7 @@ constexpr int kMaxDiffOrder = 32;
 
 struct DiffParams {
     double c[kMaxDiffOrder];  // strict: c_k; fused: c_k / d
-    double d;
+    Divisor<double> d;
     int order;
     int64_t n1o, n2o;  // output sizes of the first two dimensions
     int64_t jk;        // output j x k extent (second by third dimension)
@@ -44,7 +45,7 @@ __global__ void diffop_kernel(const double* __restrict__ in, double* __restrict_
         for (int t = 0; t < p.order; ++t) {
             const double a = __ldg(base + t * p.s), b = __ldg(base - (t + 1) * p.s);
             if (STRICT)
-                acc = __dadd_rn(acc, __ddiv_rn(__dmul_rn(p.c[t], __dsub_rn(a, b)), p.d));
+                acc = __dadd_rn(acc, div_rn(__dmul_rn(p.c[t], __dsub_rn(a, b)), p.d));
             else
                 acc = fma(p.c[t], a - b, acc);
         }
@@ -88,7 +89,7 @@ extern "C" int sssi_diffOperator(const double* data, int ndims, const int64_t* d
         const bool strict = mode == SSSI_MODE_FP64_STRICT;
         DiffParams p{};
         for (int t = 0; t < order; ++t) p.c[t] = strict ? coeff[t] : coeff[t] / dist;
-        p.d = dist;
+        p.d = make_divisor<double>(dist);
         p.order = order;
         p.n1o = no[0];
         p.n2o = no[1];

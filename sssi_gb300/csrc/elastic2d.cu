@@ -86,7 +86,7 @@ struct ElParams {
     T c[kElMaxOrder];   // strict: coefficients, divided by dz / dx per term
     T wz[kElMaxOrder];  // fused: c_k / dz, c_k / dx
     T wx[kElMaxOrder];
-    T dz, dx;
+    Divisor<T> dz, dx;  // strict: the spacings the terms are divided by
     int nz, nx, nB, nt;
     int64_t ldp;
     int ntz, ntiles;
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase1_kernel(const __gr
         wz[k] = p.wz[k];
         wx[k] = p.wx[k];
     }
-    const T dz = p.dz, dx = p.dx;
+    const Divisor<T> dz = p.dz, dx = p.dx;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int i = (tile % p.ntz) * kElRows + lane, j = (tile / p.ntz) * kElCols + w;
         if (i >= p.nz || j >= p.nx) continue;
@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase2_kernel(const __gr
         wz[k] = p.wz[k];
         wx[k] = p.wx[k];
     }
-    const T dz = p.dz, dx = p.dx, dt = p.dt;
+    const Divisor<T> dz = p.dz, dx = p.dx;
+    const T dt = p.dt;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int i = (tile % p.ntz) * kElRows + lane, j = (tile / p.ntz) * kElCols + w;
         if (i >= p.nz || j >= p.nx) continue;
@@ -407,8 +408,8 @@ class Elastic2d {
             p_.wz[k] = (T)(cf[k] / dz);
             p_.wx[k] = (T)(cf[k] / dx);
         }
-        p_.dz = (T)dz;
-        p_.dx = (T)dx;
+        p_.dz = make_divisor<T>(dz);
+        p_.dx = make_divisor<T>(dx);
         p_.nz = (int)nz;
         p_.nx = (int)nx;
         p_.nB = nB;

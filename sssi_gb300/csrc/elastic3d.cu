@@ -69,7 +69,7 @@ struct E3Params {
     T wz[kE3MaxOrder];
     T wx[kE3MaxOrder];
     T wy[kE3MaxOrder];
-    T dz, dx, dy;
+    Divisor<T> dz, dx, dy;  // strict: the spacings the terms are divided by
     int nz, nx, ny, nB, nt;
     int64_t ldp, ps;  // column pitch, plane stride
     int ntz, ntx, ntiles;
@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kE3Threads) elastic3d_phase1_kernel(const __gr
         wx[k] = p.wx[k];
         wy[k] = p.wy[k];
     }
-    const T dz = p.dz, dx = p.dx, dy = p.dy, dt = p.dt;
+    const Divisor<T> dz = p.dz, dx = p.dx, dy = p.dy;
+    const T dt = p.dt;
     const int nz = p.nz, nx = p.nx, ny = p.ny, nB = p.nB;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int tz = tile % p.ntz, rest = tile / p.ntz;
@@ -180,7 +181,8 @@ __global__ void __launch_bounds__(kE3Threads) elastic3d_phase2_kernel(const __gr
         wx[k] = p.wx[k];
         wy[k] = p.wy[k];
     }
-    const T dz = p.dz, dx = p.dx, dy = p.dy, dt = p.dt;
+    const Divisor<T> dz = p.dz, dx = p.dx, dy = p.dy;
+    const T dt = p.dt;
     const int nz = p.nz, nx = p.nx, ny = p.ny, nB = p.nB;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int tz = tile % p.ntz, rest = tile / p.ntz;
@@ -402,9 +404,9 @@ class Elastic3d {
             p_.wx[k] = (T)(cf[k] / dx);
             p_.wy[k] = (T)(cf[k] / dy);
         }
-        p_.dz = (T)dz;
-        p_.dx = (T)dx;
-        p_.dy = (T)dy;
+        p_.dz = make_divisor<T>(dz);
+        p_.dx = make_divisor<T>(dx);
+        p_.dy = make_divisor<T>(dy);
         p_.nz = (int)nz;
         p_.nx = (int)nx;
         p_.ny = (int)ny;

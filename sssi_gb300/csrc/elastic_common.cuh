@@ -7,6 +7,7 @@
 
 #include <cmath>
 
+#include "divide.cuh"
 #include "sssi_gb300.h"
 
 namespace sssi {
@@ -16,14 +17,15 @@ namespace elastic {
 // (strict) or as fused multiply-adds with w_k = c_k / d.  s1: the axis stride,
 // forward (D+): f(q+(1+k)s) - f(q-ks); backward (D-): f(q+ks) - f(q-(1+k)s).
 template <typename T, int N, int kMode, bool kForward>
-__device__ __forceinline__ T el_diff(const T* __restrict__ f, int64_t q, int64_t s, const T* c, const T* w, T d) {
+__device__ __forceinline__ T el_diff(const T* __restrict__ f, int64_t q, int64_t s, const T* c, const T* w,
+                                     const Divisor<T>& d) {
     T acc = T(0);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
         const T a = __ldg(f + q + (kForward ? (1 + k) : k) * s);
         const T b = __ldg(f + q - (kForward ? k : (1 + k)) * s);
         if constexpr (kMode == SSSI_MODE_FP64_STRICT)
-            acc = __dadd_rn(acc, __ddiv_rn(__dmul_rn(c[k], __dsub_rn(a, b)), d));
+            acc = __dadd_rn(acc, div_rn(__dmul_rn(c[k], __dsub_rn(a, b)), d));
         else
             acc = fma(w[k], a - b, acc);
     }

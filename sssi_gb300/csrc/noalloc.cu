@@ -310,8 +310,8 @@ int run(const double* v, const double* source, int64_t nz, int64_t nx, int64_t n
         p.cz[k] = strict ? c[k] : c[k] / dz;
         p.cx[k] = strict ? c[k] : c[k] / dx;
     }
-    p.dz = dz;
-    p.dx = dx;
+    p.dz = make_divisor<double>(dz);
+    p.dx = make_divisor<double>(dx);
     const int64_t n = nz * nx;
     int cur = 0;
     for (int64_t t = 0; t < nt; ++t) {
