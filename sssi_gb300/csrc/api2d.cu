@@ -18,17 +18,24 @@ using namespace api;
 // Launch shape for a grid: rows per block (a power of two <= 256) and the
 // number of columns each block marches over.
 void pick_launch(int64_t nz, int64_t nx, int& bz, int& w) {
-    bz = nz >= 512 ? 128 : (nz >= 96 ? 64 : 32);
+    // widest march (least halo recomputation: 2N-1 extra columns per block) that
+    // still gives about eight warps per SM; small grids, which reach that with no
+    // shape, take the most warps (32-row blocks, 4-column marches)
     const int64_t target_warps = 152 * 8;
-    const int64_t zblocks = (nz + bz - 1) / bz;
-    w = 16;
-    for (int cand : {256, 128, 64, 32}) {
-        const int64_t blocks = zblocks * ((nx + cand - 1) / cand);
-        if (blocks * (bz / 32) >= target_warps) {
-            w = cand;
-            break;
+    for (int cbz : {128, 64, 32}) {
+        if ((cbz == 128 && nz < 512) || (cbz == 64 && nz < 96)) continue;
+        const int64_t zblocks = (nz + cbz - 1) / cbz;
+        for (int cand : {256, 128, 64, 32, 16, 8}) {
+            const int64_t blocks = zblocks * ((nx + cand - 1) / cand);
+            if (blocks * (cbz / 32) >= target_warps) {
+                bz = cbz;
+                w = cand;
+                return;
+            }
         }
     }
+    bz = 32;
+    w = 4;
 }
 
 void check_common(int64_t nz, int64_t nx, int64_t nt, int N, int nB, double dz, double dx, double dt, int mode) {
