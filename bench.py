@@ -567,7 +567,7 @@ def bench_3d(S, args):
             "fp64": {"value": round(cells / (ms64 * 1e-3) / 1e9, 3), "ms_per_shot": round(ms64, 1)},
             "receivers_rel_l2_vs_fp64": err, "receivers": "surface grid every 2 cells (144 x 144)",
             "schedule": sched, "schedule_tune_ms": [round(t, 3) for t in sched_ms],
-            "schedule_candidates": "even / cost-cut chunks along y, about 3 then about 2 items per resident block",
+            "schedule_candidates": "0: even chunks along y, ~3 items per resident block; 1/2/3: cost-cut chunks, ~3/2/4",
             "config": {"workload": "fwd3d-point-source", "grid": [nz, nx, ny], "physical": [256, 256, 256],
                        "nt": nt, "nDiffOrder": N_ORDER, "nBoundary": nb,
                        "dt": dt3, "dx": 10.0, "model": "seeded 5-layer dipping-interface model, 1500-4500 m/s",

@@ -424,10 +424,11 @@ int sssi_debug_tile_shape(int shape);
 
 /* No counterpart in the reference: what the 3D propagator's schedule tuner
  * chose.  A 3D propagation of at least 64 steps times four candidate
- * work-item schedules on its first steps (even or cost-cut chunks along y, each
- * with about three or about two items per resident block) and keeps the
- * fastest; this reports the choice of the last one to finish tuning in
- * *schedule (-1 before any) and the four timed runs in ms[0..3] (ms). */
+ * work-item schedules on its first steps (0: even chunks along y, about three
+ * items per resident block; 1, 2, 3: chunks cut by estimated cost, about three,
+ * two or four items per resident block) and keeps the fastest; this reports
+ * the choice of the last one to finish tuning in *schedule (-1 before any) and
+ * the four timed runs in ms[0..3] (ms). */
 int sssi_debug_schedule3d(int* schedule, float* ms);
 
 /* No counterpart in the reference: a test entry of the division the strict

@@ -500,8 +500,8 @@ def debug_tile_shape(shape: int) -> None:
 
 def debug_schedule3d() -> tuple[int, list[float]]:
     """The 3D schedule tuner's last choice (-1 before any) and its four timed
-    runs in ms (even / cost-cut chunks at about three, then about two items per
-    resident block)."""
+    runs in ms (0: even chunks, about three items per resident block; 1, 2, 3:
+    cost-cut chunks, about three, two or four)."""
     sched = ctypes.c_int(-1)
     ms = (ctypes.c_float * 4)()
     check(lib().sssi_debug_schedule3d(ctypes.byref(sched), ms))

@@ -115,9 +115,9 @@ class Prop3d {
     void set_stream(cudaStream_t s) { stream_ = s; }
     void sync_desc();
     // Whole runs of kGraphSteps go through a CUDA graph.  The first steps of a
-    // long run time the candidate schedules (even chunks along y, or chunks cut
-    // by estimated cost per tile, each with about three or about two items per
-    // resident block); the fastest is kept.
+    // long run time the candidate schedules (even chunks along y with about
+    // three items per resident block, or chunks cut by estimated cost per tile
+    // with about three, two or four); the fastest is kept.
     void run(int nsteps);
     void check_errors();
     int schedule() const { return cc_.sched; }

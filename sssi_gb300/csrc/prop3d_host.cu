@@ -282,44 +282,50 @@ Prop3d<T>::Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, in
     cc_.step_offset = 0;
     cc_.err = d_ctr_.template as<int>() + 2;
     // Candidate schedules of work items, each item a (z, x) tile and a chunk of
-    // planes; the dynamic schedule takes the most expensive first.  Cost
-    // model: a plane costs 1, 1.6 next to a z or x band (cooperative pass per
-    // plane), +0.4 in a y band (memory-variable traffic); every chunk also
-    // fills its queues from 2N-1 planes (0.3 each).
-    //   0, 2: even chunks along y, enough items for about three (0) or two (2)
-    //         per resident block, 8 to 64 planes;
-    //   1, 3: each tile's planes cut into chunks of about equal estimated cost
-    //         (tiles next to a band get shorter chunks), about three (1) or
-    //         two (3) per resident block, 4 to 64 planes.
-    // Fewer, longer chunks fill the queues less often; more chunks balance the
-    // blocks better.
+    // planes; the dynamic schedule takes the most expensive first.  Cost model
+    // (plane times measured on 256^3-288^3 grids): a plane costs 1, 2.6 in a
+    // tile next to a z or an x band (cooperative pass per plane), 4 next to
+    // both, +0.5 in a y band (memory-variable traffic); every chunk also fills
+    // its queues from 2N-1 planes (0.4 each).
+    //   0:       even chunks along y, about three items per resident block,
+    //            8 to 64 planes;
+    //   1, 2, 3: each tile's planes cut into chunks of about equal estimated
+    //            cost (tiles next to a band get shorter chunks, each tile ends
+    //            with a shorter one), about three, two or four items per
+    //            resident block, 4 to 64 planes.
+    // Fewer, longer chunks fill the queues less often; more chunks, and short
+    // ones last, balance the blocks better.
     {
         SSSI_REQUIRE(ny < 65536, SSSI_ERR_ARG, "ny must be below 65536");
         const int ntile = d.ntz * d.ntx;
-        auto plane_cost = [&](bool band_zx, int y) {
-            return (band_zx ? 1.6f : 1.0f) + ((nB > 0 && (y < nB || y >= ny - nB)) ? 0.4f : 0.0f);
+        auto plane_cost = [&](int band_zx, int y) {
+            static const float kTile[3] = {1.0f, 2.6f, 4.0f};
+            return kTile[band_zx] + ((nB > 0 && (y < nB || y >= ny - nB)) ? 0.5f : 0.0f);
         };
-        std::vector<char> bzx(ntile);
+        std::vector<char> bzx(ntile);  // 0: no z / x band work, 1: z or x, 2: both
         double total = 0;
         for (int t = 0; t < ntile; ++t) {
             const int z0 = (t % d.ntz) * S::TZ - d.zs, x0 = (t / d.ntz) * S::TX;
-            bzx[t] = nB > 0 && (z0 + S::TZ + N - 1 > nz - nB || x0 - N < nB || x0 + S::TX + N - 2 >= nx - nB);
+            const bool bz = nB > 0 && z0 + S::TZ + N - 1 > nz - nB;
+            const bool bx = nB > 0 && (x0 - N < nB || x0 + S::TX + N - 2 >= nx - nB);
+            bzx[t] = (char)(bz + bx);
             for (int y = 0; y < ny; ++y) total += plane_cost(bzx[t], y);
         }
-        const float warm = 0.3f * (2 * N - 1);
+        const float warm = 0.4f * (2 * N - 1);
         struct It {
             int2 item;
             float cost;
         };
         for (int c = 0; c < kSchedules3; ++c) {
             std::vector<It> its;
-            const int64_t per = c < 2 ? 3 : 2;  // items per resident block
+            static const int kPer[kSchedules3] = {3, 3, 2, 4};  // items per resident block
+            const int64_t per = kPer[c];
             auto chunk = [&](int t, int y0, int y1) {
                 float cost = warm;
                 for (int y = y0; y < y1; ++y) cost += plane_cost(bzx[t], y);
                 its.push_back({make_int2(t, y0 | (y1 << 16)), cost});
             };
-            if (c % 2 == 0) {
+            if (c == 0) {
                 int64_t yc = std::max<int64_t>(8, (ny * ntile + per * slots - 1) / (per * (int64_t)slots));
                 yc = std::min<int64_t>(yc, 64);
                 const int64_t nch = (ny + yc - 1) / yc;
