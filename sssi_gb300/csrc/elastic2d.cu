@@ -24,7 +24,9 @@
 // the step number and the chunked hooks from device memory.  Outside the bands
 // r = 1, s = dt and the divisions by den = 1 are exact no-ops, so the band
 // coefficients live in two small arrays (side columns nz x 2nB, bottom rows
-// nB x nx) and the interior takes the constants.
+// nB x nx), the interior takes the constants and forms no product with r.
+// The velocity updates' coefficients kzp, kxs, kxp, kzs do not change in
+// time: they are formed once per run, with the step's operations, and loaded.
 //
 // Arithmetic: SSSI_MODE_FP64_STRICT rounds as the file (and diffOperator_mex,
 // src/fd_cmex/diffOperator_mex.c:81-92: c_k*(a-b)/d per term, summed from zero)
@@ -74,6 +76,12 @@ struct ElParams {
     T* Vxs;
     const T* vpSq;  // vp.^2 and vs.^2 padded by edge replication (padarray 'replicate')
     const T* vsSq;
+    // the velocity updates' coefficients kzp, kxs, kxp, kzs (constant in time,
+    // formed once by el_coef_kernel), padded layout
+    const T* kzp;
+    const T* kxs;
+    const T* kxp;
+    const T* kzs;
     // band coefficients: side columns (nz x 2 nB, pitch nz; column j < nB, or
     // nB + j - (nx - nB)), bottom rows (nB x nx, pitch nB; row i - (nz - nB))
     const T* xr;
@@ -154,10 +162,11 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase1_kernel(const __gr
         const T dVzz = el_diff<T, N, kMode, false>(p.Vz, q, 1, c, wz, dz);    // Vz(1:end-1, ix), dim 1
         const T dVxz = el_diff<T, N, kMode, true>(p.Vx, q, 1, c, wz, dz);     // Vx(2:end, ix), dim 1
         const T dVzx = el_diff<T, N, kMode, true>(p.Vz, q, ldp, c, wx, dx);   // Vz(iz, 2:end), dim 2
-        const T ax = el_axpby<T, kMode>(rx, p.Ax[q], sx, dVxx);
-        const T az = el_axpby<T, kMode>(rz, p.Az[q], sz, dVzz);
-        const T bz = el_axpby<T, kMode>(rz, p.Bz[q], sz, dVxz);
-        const T bx = el_sub<T, kMode>(el_mul<T, kMode>(rx, p.Bx[q]), el_mul<T, kMode>(sx, dVzx));
+        const bool xb = j < p.nB || j >= p.nx - p.nB, zb = i >= p.nz - p.nB;  // damped along x / z
+        const T ax = el_raxpby<T, kMode>(xb, rx, p.Ax[q], sx, dVxx);
+        const T az = el_raxpby<T, kMode>(zb, rz, p.Az[q], sz, dVzz);
+        const T bz = el_raxpby<T, kMode>(zb, rz, p.Bz[q], sz, dVxz);
+        const T bx = el_sub<T, kMode>(el_rx<T, kMode>(xb, rx, p.Bx[q]), el_mul<T, kMode>(sx, dVzx));
         p.Ax[q] = ax;
         p.Az[q] = az;
         p.Bz[q] = bz;
@@ -189,7 +198,6 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase2_kernel(const __gr
         wx[k] = p.wx[k];
     }
     const Divisor<T> dz = p.dz, dx = p.dx;
-    const T dt = p.dt;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
         const int i = (tile % p.ntz) * kElRows + lane, j = (tile / p.ntz) * kElCols + w;
         if (i >= p.nz || j >= p.nx) continue;
@@ -200,27 +208,8 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase2_kernel(const __gr
         const T dAx = el_diff<T, N, kMode, true>(p.A, q, ldp, c, wx, dx);   // A(iz, 2:end), dim 2
         const T dBx = el_diff<T, N, kMode, false>(p.B, q, ldp, c, wx, dx);  // B(iz, 1:end-1), dim 2
         const T dBz = el_diff<T, N, kMode, false>(p.B, q, 1, c, wz, dz);    // B(1:end-1, ix), dim 1
-        // 0.25 .* (vpSq(iz,ix) + vpSq(iz+1,ix) + vpSq(iz+1,ix-1) + vpSq(iz,ix-1)) * dt ./ den_z, and the others
-        const T p00 = __ldg(p.vpSq + q), s00 = __ldg(p.vsSq + q);
-        const T s4p = el_add<T, kMode>(
-            el_add<T, kMode>(el_add<T, kMode>(p00, __ldg(p.vpSq + q + 1)), __ldg(p.vpSq + q + 1 - ldp)),
-            __ldg(p.vpSq + q - ldp));
-        const T s4s = el_add<T, kMode>(
-            el_add<T, kMode>(el_add<T, kMode>(s00, __ldg(p.vsSq + q + ldp)), __ldg(p.vsSq + q - 1 + ldp)),
-            __ldg(p.vsSq + q - 1));
-        // den = 1 outside the bands: the division is exact there and skipped
-        T kzp = el_mul<T, kMode>(el_mul<T, kMode>(T(0.25), s4p), dt);
-        T kxs = el_mul<T, kMode>(el_mul<T, kMode>(T(0.25), s4s), dt);
-        T kxp = el_mul<T, kMode>(p00, dt);
-        T kzs = el_mul<T, kMode>(s00, dt);
-        if (dnz != T(1)) {
-            kzp = el_div<T, kMode>(kzp, dnz);
-            kxs = el_div<T, kMode>(kxs, dnz);
-        }
-        if (dnx != T(1)) {
-            kxp = el_div<T, kMode>(kxp, dnx);
-            kzs = el_div<T, kMode>(kzs, dnx);
-        }
+        const T kzp = __ldg(p.kzp + q), kxs = __ldg(p.kxs + q), kxp = __ldg(p.kxp + q), kzs = __ldg(p.kzs + q);
+        const bool xb = j < p.nB || j >= p.nx - p.nB, zb = i >= p.nz - p.nB;  // damped along x / z
         T src = T(0);
         bool has_src = false;
         if (src_dense) {
@@ -233,14 +222,14 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase2_kernel(const __gr
                 src = has_src ? src + wv : wv;
                 has_src = true;
             }
-        T vzp = el_axpby<T, kMode>(rz, p.Vzp[q], kzp, dAz);
-        T vxp = el_axpby<T, kMode>(rx, p.Vxp[q], kxp, dAx);
+        T vzp = el_raxpby<T, kMode>(zb, rz, p.Vzp[q], kzp, dAz);
+        T vxp = el_raxpby<T, kMode>(xb, rx, p.Vxp[q], kxp, dAx);
         if (has_src) {
             vzp = el_add<T, kMode>(vzp, el_mul<T, kMode>(sz, src));
             vxp = el_add<T, kMode>(vxp, el_mul<T, kMode>(sx, src));
         }
-        const T vzs = el_sub<T, kMode>(el_mul<T, kMode>(rx, p.Vzs[q]), el_mul<T, kMode>(kzs, dBx));
-        const T vxs = el_axpby<T, kMode>(rz, p.Vxs[q], kxs, dBz);
+        const T vzs = el_sub<T, kMode>(el_rx<T, kMode>(xb, rx, p.Vzs[q]), el_mul<T, kMode>(kzs, dBx));
+        const T vxs = el_raxpby<T, kMode>(zb, rz, p.Vxs[q], kxs, dBz);
         p.Vzp[q] = vzp;
         p.Vxp[q] = vxp;
         p.Vzs[q] = vzs;
@@ -311,6 +300,45 @@ __global__ void el_square_kernel(const double* vp, const double* vs, int nz, int
         const int64_t o = ip + (int64_t)jp * ldp;
         vp2[o] = (T)__dmul_rn(a, a);
         vs2[o] = (T)__dmul_rn(b, b);
+    }
+}
+
+// The velocity updates' coefficients, constant in time, in the step's
+// operation order: kzp = 0.25 (vpSq(iz,ix) + vpSq(iz+1,ix) + vpSq(iz+1,ix-1) +
+// vpSq(iz,ix-1)) dt ./ den_z, kxs = 0.25 (vsSq(iz,ix) + vsSq(iz,ix+1) +
+// vsSq(iz-1,ix+1) + vsSq(iz-1,ix)) dt ./ den_z, kxp = vpSq dt ./ den_x,
+// kzs = vsSq dt ./ den_x (den = 1 outside the bands: the division is exact
+// there and skipped).
+template <typename T, int kMode>
+__global__ void el_coef_kernel(const ElParams<T> p, T* kzp_out, T* kxs_out, T* kxp_out, T* kzs_out) {
+    const int64_t n = (int64_t)p.nz * p.nx, ldp = p.ldp;
+    const T dt = p.dt;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % p.nz), j = (int)(c / p.nz);
+        const int64_t q = i + (int64_t)j * ldp;
+        T rx, sx, dnx, rz, sz, dnz;
+        el_factors(p, i, j, rx, sx, dnx, rz, sz, dnz);
+        const T p00 = p.vpSq[q], s00 = p.vsSq[q];
+        const T s4p = el_add<T, kMode>(el_add<T, kMode>(el_add<T, kMode>(p00, p.vpSq[q + 1]), p.vpSq[q + 1 - ldp]),
+                                       p.vpSq[q - ldp]);
+        const T s4s = el_add<T, kMode>(el_add<T, kMode>(el_add<T, kMode>(s00, p.vsSq[q + ldp]), p.vsSq[q - 1 + ldp]),
+                                       p.vsSq[q - 1]);
+        T kzp = el_mul<T, kMode>(el_mul<T, kMode>(T(0.25), s4p), dt);
+        T kxs = el_mul<T, kMode>(el_mul<T, kMode>(T(0.25), s4s), dt);
+        T kxp = el_mul<T, kMode>(p00, dt);
+        T kzs = el_mul<T, kMode>(s00, dt);
+        if (dnz != T(1)) {
+            kzp = el_div<T, kMode>(kzp, dnz);
+            kxs = el_div<T, kMode>(kxs, dnz);
+        }
+        if (dnx != T(1)) {
+            kxp = el_div<T, kMode>(kxp, dnx);
+            kzs = el_div<T, kMode>(kzs, dnx);
+        }
+        kzp_out[q] = kzp;
+        kxs_out[q] = kxs;
+        kxp_out[q] = kxp;
+        kzs_out[q] = kzs;
     }
 }
 
@@ -423,6 +451,24 @@ class Elastic2d {
         SSSI_CHECK_CUDA(cudaGetDevice(&dev));
         SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         grid_ = std::max(1, std::min(p_.ntiles, sms * 4));
+        // the velocity updates' coefficients, once
+        T* k[4];
+        for (int c = 0; c < 4; ++c) {
+            K_[c].allocate(cells * sizeof(T));
+            k[c] = K_[c].template as<T>() + org_;
+        }
+        p_.kzp = k[0];
+        p_.kxs = k[1];
+        p_.kxp = k[2];
+        p_.kzs = k[3];
+        if constexpr (std::is_same<T, float>::value)
+            el_coef_kernel<T, SSSI_MODE_FP32><<<sms * 4, 256, 0, s>>>(p_, k[0], k[1], k[2], k[3]);
+        else if (mode == SSSI_MODE_FP64_STRICT)
+            el_coef_kernel<T, SSSI_MODE_FP64_STRICT><<<sms * 4, 256, 0, s>>>(p_, k[0], k[1], k[2], k[3]);
+        else
+            el_coef_kernel<T, SSSI_MODE_FP64><<<sms * 4, 256, 0, s>>>(p_, k[0], k[1], k[2], k[3]);
+        count_launch();
+        SSSI_CHECK_CUDA(cudaGetLastError());
         set_hooks(ElHooks<T>{});
     }
     ~Elastic2d() {
@@ -481,7 +527,7 @@ class Elastic2d {
     int N_, mode_;
     cudaStream_t s_;
     int64_t ldp_ = 0, org_ = 0;
-    DeviceBuffer F_[12], V2_[2], band_[6], hooks_dev_, ctr_;
+    DeviceBuffer F_[12], V2_[2], K_[4], band_[6], hooks_dev_, ctr_;
     ElParams<T> p_{};
     int grid_ = 1, step_ = 0;
     cudaGraphExec_t graph_ = nullptr;

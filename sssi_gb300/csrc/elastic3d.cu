@@ -20,6 +20,9 @@
 //
 // GB300 form: as the 2D propagator (elastic2d.cu), with 32 x 8 block tiles on
 // each y plane; the y derivatives read whole planes apart, coalesced along z.
+// The six 0.25 S dt products are constant in time: FP64 forms them once per
+// run and loads them (its step is bound by the FP64 pipe); FP32 forms them per
+// step from the cached neighbours.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -61,6 +64,9 @@ struct E3Params {
     T* f[kE3Fields];  // padded layout, interior origin applied
     const T* vpSq;
     const T* vsSq;
+    // 0.25 S dt of the six 4-point sums of vp^2 (pzy, pzx, pxy) and vs^2 (szy,
+    // szx, sxy), constant in time (formed once by e3_coef_kernel), padded layout
+    const T* kc[6];
     const T* xb[3];  // x band (r, s, den): nz x 2nB, pitch nz (column j < nB, or nB + j - (nx - nB))
     const T* yb[3];  // y band: nx x 2nB, pitch nx (plane k < nB, or nB + k - (ny - nB))
     const T* zb[3];  // z band: nB x nx, pitch nB (row i - (nz - nB))
@@ -117,17 +123,21 @@ __global__ void __launch_bounds__(kE3Threads) elastic3d_phase1_kernel(const __gr
         if (j < nB || j >= nx - nB) e3_band(p.xb, i + (int64_t)(j < nB ? j : nB + j - (nx - nB)) * nz, rx, sx, dnx);
         if (k < nB || k >= ny - nB) e3_band(p.yb, j + (int64_t)(k < nB ? k : nB + k - (ny - nB)) * nx, ry, sy, dny);
         if (i >= nz - nB) e3_band(p.zb, (i - (nz - nB)) + (int64_t)j * nB, rz, sz, dnz);
-        const T ax = el_axpby<T, kMode>(rx, p.f[kAx][q], sx, el_diff<T, N, kMode, false>(p.f[kVx], q, ldp, c, wx, dx));
-        const T ay = el_axpby<T, kMode>(ry, p.f[kAy][q], sy, el_diff<T, N, kMode, false>(p.f[kVy], q, ps, c, wy, dy));
-        const T az = el_axpby<T, kMode>(rz, p.f[kAz][q], sz, el_diff<T, N, kMode, false>(p.f[kVz], q, 1, c, wz, dz));
-        const T b1y = el_axpby<T, kMode>(ry, p.f[kB1y][q], sy, el_diff<T, N, kMode, true>(p.f[kVz], q, ps, c, wy, dy));
-        const T b1z = el_sub<T, kMode>(el_mul<T, kMode>(rz, p.f[kB1z][q]),
+        // damped along x / y / z (r = 1 elsewhere: el_rx)
+        const bool bx = j < nB || j >= nx - nB, by = k < nB || k >= ny - nB, bz = i >= nz - nB;
+        const T ax = el_raxpby<T, kMode>(bx, rx, p.f[kAx][q], sx, el_diff<T, N, kMode, false>(p.f[kVx], q, ldp, c, wx, dx));
+        const T ay = el_raxpby<T, kMode>(by, ry, p.f[kAy][q], sy, el_diff<T, N, kMode, false>(p.f[kVy], q, ps, c, wy, dy));
+        const T az = el_raxpby<T, kMode>(bz, rz, p.f[kAz][q], sz, el_diff<T, N, kMode, false>(p.f[kVz], q, 1, c, wz, dz));
+        const T b1y =
+            el_raxpby<T, kMode>(by, ry, p.f[kB1y][q], sy, el_diff<T, N, kMode, true>(p.f[kVz], q, ps, c, wy, dy));
+        const T b1z = el_sub<T, kMode>(el_rx<T, kMode>(bz, rz, p.f[kB1z][q]),
                                        el_mul<T, kMode>(sz, el_diff<T, N, kMode, true>(p.f[kVy], q, 1, c, wz, dz)));
-        const T b2z = el_axpby<T, kMode>(rz, p.f[kB2z][q], sz, el_diff<T, N, kMode, true>(p.f[kVx], q, 1, c, wz, dz));
-        const T b2x = el_sub<T, kMode>(el_mul<T, kMode>(rx, p.f[kB2x][q]),
+        const T b2z = el_raxpby<T, kMode>(bz, rz, p.f[kB2z][q], sz, el_diff<T, N, kMode, true>(p.f[kVx], q, 1, c, wz, dz));
+        const T b2x = el_sub<T, kMode>(el_rx<T, kMode>(bx, rx, p.f[kB2x][q]),
                                        el_mul<T, kMode>(sx, el_diff<T, N, kMode, true>(p.f[kVz], q, ldp, c, wx, dx)));
-        const T b3x = el_axpby<T, kMode>(rx, p.f[kB3x][q], sx, el_diff<T, N, kMode, true>(p.f[kVy], q, ldp, c, wx, dx));
-        const T b3y = el_sub<T, kMode>(el_mul<T, kMode>(ry, p.f[kB3y][q]),
+        const T b3x =
+            el_raxpby<T, kMode>(bx, rx, p.f[kB3x][q], sx, el_diff<T, N, kMode, true>(p.f[kVy], q, ldp, c, wx, dx));
+        const T b3y = el_sub<T, kMode>(el_rx<T, kMode>(by, ry, p.f[kB3y][q]),
                                        el_mul<T, kMode>(sy, el_diff<T, N, kMode, true>(p.f[kVx], q, ps, c, wy, dy)));
         p.f[kAx][q] = ax;
         p.f[kAy][q] = ay;
@@ -193,14 +203,27 @@ __global__ void __launch_bounds__(kE3Threads) elastic3d_phase2_kernel(const __gr
         if (j < nB || j >= nx - nB) e3_band(p.xb, i + (int64_t)(j < nB ? j : nB + j - (nx - nB)) * nz, rx, sx, dnx);
         if (k < nB || k >= ny - nB) e3_band(p.yb, j + (int64_t)(k < nB ? k : nB + k - (ny - nB)) * nx, ry, sy, dny);
         if (i >= nz - nB) e3_band(p.zb, (i - (nz - nB)) + (int64_t)j * nB, rz, sz, dnz);
-        // 0.25 * S * dt of each pair of sums (the division by den follows per use)
-        const T q4 = T(0.25);
-        const T pzy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -1, -1 - ps, -ps)), dt);
-        const T pzx = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -1 - ldp, -1)), dt);
-        const T pxy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -ldp - ps, -ps)), dt);
-        const T szy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -1, -1 - ps, -ps)), dt);
-        const T szx = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -1 - ldp, -1)), dt);
-        const T sxy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -ldp - ps, -ps)), dt);
+        // 0.25 * S * dt of each pair of sums (the division by den follows per use):
+        // formed once per run in FP64, where the step is bound by the FP64 pipe;
+        // from the cached neighbours in FP32, where six more streams cost more
+        T pzy, pzx, pxy, szy, szx, sxy;
+        if constexpr (kMode == SSSI_MODE_FP32) {
+            const T q4 = T(0.25);
+            pzy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -1, -1 - ps, -ps)), dt);
+            pzx = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -1 - ldp, -1)), dt);
+            pxy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -ldp - ps, -ps)), dt);
+            szy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -1, -1 - ps, -ps)), dt);
+            szx = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -1 - ldp, -1)), dt);
+            sxy = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -ldp - ps, -ps)), dt);
+        } else {
+            pzy = __ldg(p.kc[0] + q);
+            pzx = __ldg(p.kc[1] + q);
+            pxy = __ldg(p.kc[2] + q);
+            szy = __ldg(p.kc[3] + q);
+            szx = __ldg(p.kc[4] + q);
+            sxy = __ldg(p.kc[5] + q);
+        }
+        const bool bx = j < nB || j >= nx - nB, by = k < nB || k >= ny - nB, bz = i >= nz - nB;
         // injected values of the cell at step t
         T sv[3] = {T(0), T(0), T(0)};
         bool hs[3] = {false, false, false};
@@ -220,29 +243,29 @@ __global__ void __launch_bounds__(kE3Threads) elastic3d_phase2_kernel(const __gr
                         hs[u] = true;
                     }
             }
-        T vxp = el_axpby<T, kMode>(rx, p.f[kVxp][q], e3_k<T, kMode>(pzy, dnx),
-                                   el_diff<T, N, kMode, true>(p.f[kA], q, ldp, c, wx, dx));
-        T vyp = el_axpby<T, kMode>(ry, p.f[kVyp][q], e3_k<T, kMode>(pzx, dny),
-                                   el_diff<T, N, kMode, true>(p.f[kA], q, ps, c, wy, dy));
-        T vzp = el_axpby<T, kMode>(rz, p.f[kVzp][q], e3_k<T, kMode>(pxy, dnz),
-                                   el_diff<T, N, kMode, true>(p.f[kA], q, 1, c, wz, dz));
+        T vxp = el_raxpby<T, kMode>(bx, rx, p.f[kVxp][q], e3_k<T, kMode>(pzy, dnx),
+                                    el_diff<T, N, kMode, true>(p.f[kA], q, ldp, c, wx, dx));
+        T vyp = el_raxpby<T, kMode>(by, ry, p.f[kVyp][q], e3_k<T, kMode>(pzx, dny),
+                                    el_diff<T, N, kMode, true>(p.f[kA], q, ps, c, wy, dy));
+        T vzp = el_raxpby<T, kMode>(bz, rz, p.f[kVzp][q], e3_k<T, kMode>(pxy, dnz),
+                                    el_diff<T, N, kMode, true>(p.f[kA], q, 1, c, wz, dz));
         if (hs[0]) vxp = el_add<T, kMode>(vxp, el_mul<T, kMode>(sx, sv[0]));
         if (hs[1]) vyp = el_add<T, kMode>(vyp, el_mul<T, kMode>(sy, sv[1]));
         if (hs[2]) vzp = el_add<T, kMode>(vzp, el_mul<T, kMode>(sz, sv[2]));
         const T vxsy = el_sub<T, kMode>(
-            el_mul<T, kMode>(ry, p.f[kVxsy][q]),
+            el_rx<T, kMode>(by, ry, p.f[kVxsy][q]),
             el_mul<T, kMode>(e3_k<T, kMode>(szy, dny), el_diff<T, N, kMode, false>(p.f[kB3], q, ps, c, wy, dy)));
-        const T vxsz = el_axpby<T, kMode>(rz, p.f[kVxsz][q], e3_k<T, kMode>(szy, dnz),
+        const T vxsz = el_raxpby<T, kMode>(bz, rz, p.f[kVxsz][q], e3_k<T, kMode>(szy, dnz),
                                           el_diff<T, N, kMode, false>(p.f[kB2], q, 1, c, wz, dz));
-        const T vysx = el_axpby<T, kMode>(rx, p.f[kVysx][q], e3_k<T, kMode>(szx, dnx),
+        const T vysx = el_raxpby<T, kMode>(bx, rx, p.f[kVysx][q], e3_k<T, kMode>(szx, dnx),
                                           el_diff<T, N, kMode, false>(p.f[kB3], q, ldp, c, wx, dx));
         const T vysz = el_sub<T, kMode>(
-            el_mul<T, kMode>(rz, p.f[kVysz][q]),
+            el_rx<T, kMode>(bz, rz, p.f[kVysz][q]),
             el_mul<T, kMode>(e3_k<T, kMode>(szx, dnz), el_diff<T, N, kMode, false>(p.f[kB1], q, 1, c, wz, dz)));
         const T vzsx = el_sub<T, kMode>(
-            el_mul<T, kMode>(rx, p.f[kVzsx][q]),
+            el_rx<T, kMode>(bx, rx, p.f[kVzsx][q]),
             el_mul<T, kMode>(e3_k<T, kMode>(sxy, dnx), el_diff<T, N, kMode, false>(p.f[kB2], q, ldp, c, wx, dx)));
-        const T vzsy = el_axpby<T, kMode>(ry, p.f[kVzsy][q], e3_k<T, kMode>(sxy, dny),
+        const T vzsy = el_raxpby<T, kMode>(by, ry, p.f[kVzsy][q], e3_k<T, kMode>(sxy, dny),
                                           el_diff<T, N, kMode, false>(p.f[kB1], q, ps, c, wy, dy));
         const T vxs = el_add<T, kMode>(vxsy, vxsz), vys = el_add<T, kMode>(vysx, vysz);
         const T vzs = el_add<T, kMode>(vzsx, vzsy);
@@ -322,6 +345,27 @@ __global__ void e3_square_kernel(const double* vp, const double* vs, int nz, int
         const int64_t o = ip + (int64_t)jp * ldp + (int64_t)kp * ps;
         vp2[o] = (T)__dmul_rn(a, a);
         vs2[o] = (T)__dmul_rn(b, b);
+    }
+}
+
+// 0.25 S dt of the six 4-point sums the velocity updates use (constant in
+// time), in the step's operation order: pzy, pzx, pxy from vp^2, szy, szx, sxy
+// from vs^2, over the cell and its -z/-y, -x/-z and -x/-y neighbours.
+template <typename T, int kMode>
+__global__ void e3_coef_kernel(const E3Params<T> p, T* k0, T* k1, T* k2, T* k3, T* k4, T* k5) {
+    const int64_t n = (int64_t)p.nz * p.nx * p.ny, ldp = p.ldp, ps = p.ps;
+    const T dt = p.dt, q4 = T(0.25);
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % p.nz);
+        const int64_t r = c / p.nz;
+        const int j = (int)(r % p.nx), k = (int)(r / p.nx);
+        const int64_t q = i + (int64_t)j * ldp + (int64_t)k * ps;
+        k0[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -1, -1 - ps, -ps)), dt);
+        k1[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -1 - ldp, -1)), dt);
+        k2[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vpSq, q, -ldp, -ldp - ps, -ps)), dt);
+        k3[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -1, -1 - ps, -ps)), dt);
+        k4[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -1 - ldp, -1)), dt);
+        k5[q] = el_mul<T, kMode>(el_mul<T, kMode>(q4, e3_sum4<T, kMode>(p.vsSq, q, -ldp, -ldp - ps, -ps)), dt);
     }
 }
 
@@ -425,6 +469,22 @@ class Elastic3d {
         SSSI_CHECK_CUDA(cudaGetDevice(&dev));
         SSSI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         grid_ = std::max(1, std::min(p_.ntiles, sms * 4));
+        // the velocity updates' coefficients, once (FP64; FP32 forms them per step)
+        if constexpr (std::is_same<T, double>::value) {
+            T* kc[6];
+            for (int m = 0; m < 6; ++m) {
+                K_[m].allocate(cells * sizeof(T));
+                kc[m] = K_[m].template as<T>() + org_;
+                p_.kc[m] = kc[m];
+            }
+            if (mode == SSSI_MODE_FP64_STRICT)
+                e3_coef_kernel<T, SSSI_MODE_FP64_STRICT>
+                    <<<sms * 4, 256, 0, s>>>(p_, kc[0], kc[1], kc[2], kc[3], kc[4], kc[5]);
+            else
+                e3_coef_kernel<T, SSSI_MODE_FP64><<<sms * 4, 256, 0, s>>>(p_, kc[0], kc[1], kc[2], kc[3], kc[4], kc[5]);
+            count_launch();
+            SSSI_CHECK_CUDA(cudaGetLastError());
+        }
         set_hooks(E3Hooks<T>{});
     }
     ~Elastic3d() {
@@ -487,7 +547,7 @@ class Elastic3d {
     int N_, mode_;
     cudaStream_t s_;
     int64_t ldp_ = 0, ps_ = 0, org_ = 0;
-    DeviceBuffer F_[kE3Fields], V2_[2], bx_[3], by_[3], bz_[3], hooks_dev_, ctr_;
+    DeviceBuffer F_[kE3Fields], V2_[2], K_[6], bx_[3], by_[3], bz_[3], hooks_dev_, ctr_;
     E3Params<T> p_{};
     int grid_ = 1, step_ = 0;
     cudaGraphExec_t graph_ = nullptr;

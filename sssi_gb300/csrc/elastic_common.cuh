@@ -61,6 +61,24 @@ __device__ __forceinline__ T el_axpby(T r, T x, T s, T y) {
     else
         return fma(s, y, r * x);
 }
+// r * x for a damping factor r that is exactly 1 outside its band: there the
+// product is x itself, and the FP64 forms (bound by the FP64 pipe) do not form
+// it; FP32 multiplies anyway (the same value either way)
+template <typename T, int kMode>
+__device__ __forceinline__ T el_rx(bool damped, T r, T x) {
+    if constexpr (kMode == SSSI_MODE_FP32)
+        return r * x;
+    else
+        return damped ? el_mul<T, kMode>(r, x) : x;
+}
+// el_axpby with r = 1 outside the band (see el_rx)
+template <typename T, int kMode>
+__device__ __forceinline__ T el_raxpby(bool damped, T r, T x, T s, T y) {
+    if constexpr (kMode == SSSI_MODE_FP64_STRICT)
+        return __dadd_rn(el_rx<T, kMode>(damped, r, x), __dmul_rn(s, y));
+    else
+        return fma(s, y, el_rx<T, kMode>(damped, r, x));
+}
 template <typename T, int kMode>
 __device__ __forceinline__ T el_div(T a, T b) {
     if constexpr (kMode == SSSI_MODE_FP64_STRICT)
