@@ -573,7 +573,10 @@ void Batch2d<T>::schedule(int shape) {
         float total = 0.0f;
         for (const Item& it : items) total += it.cost;
         const int blocks = std::max(1, std::min((int)items.size(), sms_ * cps));
-        split_s_[shape] = !pair_ && total < 2.0f * (float)blocks;  // the pair variant takes whole tiles only
+        // FP64 tiles are bound by the FP64 pipe, so a band tile's extra work weighs
+        // more against the step: split up to four tiles' worth per block
+        const float split_below = std::is_same<T, double>::value ? 4.0f : 2.0f;
+        split_s_[shape] = !pair_ && total < split_below * (float)blocks;  // the pair variant takes whole tiles only
         if (split_s_[shape]) {
             std::vector<Item> split;
             split.reserve(items.size() + items.size() / 4);
