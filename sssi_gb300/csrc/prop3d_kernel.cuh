@@ -4,6 +4,8 @@
 // P_new = (v dt)^2 (zP + xP + yP + src) + 2 P - P_old); geometry in prop3d.cuh.
 #pragma once
 
+#include <type_traits>
+
 #include "batch2d_kernel.cuh"
 #include "prop3d.cuh"
 
@@ -525,212 +527,223 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
         __syncthreads();  // the previous item's last planes are no longer read
         for (int q = 0; q < NS - 1; ++q) issue(y0 + q);
 
-        // y queues.  Registers: before the shift of step s, Pq[k] = P(s-1+k)
-        // (k = 0 .. 2N-1); after it Pq[k] = P(s+k).  Shared memory: A_y(p) in
-        // slot (p - ys - N + 1) mod NQ of this thread, at Aq[slot * NT].
-        const int ys = y0 - 2 * N + 1;
-        constexpr int NT = Shape3D<T>::kThreads;
-        T Pq[NQ][RZ];
-        Col<T>* Aq = reinterpret_cast<Col<T>*>(smem + G::kAq) + tid;
+        // Items with no band, source or snapshot work and whole tile rows and
+        // columns inside the grid run a copy of the plane loop without the
+        // per-plane tests for those (kLean).
+        const bool lean = !bz && !bx && !item_yband && !item_src && !item_snap && z0 + TZ <= nz && x0 + TX <= nx;
+        auto plane_loop = [&](auto leanc) {
+            constexpr bool kLean = decltype(leanc)::value;
+            // y queues.  Registers: before the shift of step s, Pq[k] = P(s-1+k)
+            // (k = 0 .. 2N-1); after it Pq[k] = P(s+k).  Shared memory: A_y(p) in
+            // slot (p - ys - N + 1) mod NQ of this thread, at Aq[slot * NT].
+            const int ys = y0 - 2 * N + 1;
+            constexpr int NT = Shape3D<T>::kThreads;
+            T Pq[NQ][RZ];
+            Col<T>* Aq = reinterpret_cast<Col<T>*>(smem + G::kAq) + tid;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k)
+            for (int k = 0; k < NQ; ++k)
 #pragma unroll
-            for (int o = 0; o < RZ; ++o) Pq[k][o] = T(0);
-        // P(ys .. ys+2N-2) (planes below 0 are the zero padding); threads
-        // outside the grid load nothing
-        Col<T> pnext{};
-        if (act) {
+                for (int o = 0; o < RZ; ++o) Pq[k][o] = T(0);
+            // P(ys .. ys+2N-2) (planes below 0 are the zero padding); threads
+            // outside the grid load nothing
+            Col<T> pnext{};
+            if (act) {
 #pragma unroll
-            for (int k = 1; k < NQ; ++k) {
-                const Col<T> v = ldc_nc(P + own + (int64_t)(ys - 1 + k) * ldxy);
+                for (int k = 1; k < NQ; ++k) {
+                    const Col<T> v = ldc_nc(P + own + (int64_t)(ys - 1 + k) * ldxy);
 #pragma unroll
-                for (int o = 0; o < RZ; ++o) Pq[k][o] = v.v[o];
+                    for (int o = 0; o < RZ; ++o) Pq[k][o] = v.v[o];
+                }
+                pnext = ldc_nc(P + own + (int64_t)(ys + NQ - 1) * ldxy);  // P(s+2N-1) for the first step
             }
-            pnext = ldc_nc(P + own + (int64_t)(ys + NQ - 1) * ldxy);  // P(s+2N-1) for the first step
-        }
 
-        int u = 0;        // (s - ys) mod NQ
-        int st_next = 0;  // ring stage of the next output plane
-        for (int s = ys; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
-            {
-                const bool out = s >= y0;
-                const int st = st_next;
-                if (out) st_next = st_next + 1 == NS ? 0 : st_next + 1;
-                Col<T> pin = pnext;  // P(s+2N-1)
-                if (out) {
-                    // output plane y = s: its copies (plane box, P_old, (v dt)^2, and the
-                    // own tile of P at y+2N-1) have arrived once the barrier passes
-                    bool ok = true;
-                    if ((inflight >> st) & 1u) ok = mbar_wait_bounded(&bar[st], (phase_bits >> st) & 1u, kWaitLimit3);
-                    if (__syncthreads_or(!ok)) {
-                        failed = true;
-                        break;
-                    }
-                    phase_bits ^= 1u << st;
-                    inflight &= ~(1u << st);
-                    // every thread is past plane s-1: its stage takes plane s+NS-1
-                    issue(s + NS - 1);
-                    if (act) pin = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kQ) + c0 * TZ + r0);
-                } else if (act && s + 1 < y0) {
-                    pnext = ldc_nc(P + own + (int64_t)(s + NQ) * ldxy);  // the next warm-up step's plane
-                }
-                // queue in: P(s+2N-1)
-#pragma unroll
-                for (int k = 0; k < NQ - 1; ++k)
-#pragma unroll
-                    for (int o = 0; o < RZ; ++o) Pq[k][o] = Pq[k + 1][o];
-#pragma unroll
-                for (int o = 0; o < RZ; ++o) Pq[NQ - 1][o] = pin.v[o];
-                // A_y at plane pa = s+N-1: D+ from P(s .. s+2N-1), phi_y in the y bands
+            int u = 0;        // (s - ys) mod NQ
+            int st_next = 0;  // ring stage of the next output plane
+            for (int s = ys; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
                 {
-                    const int pa = s + N - 1;
-                    T a[RZ];
-                    if constexpr (batch::kPacked<T>) {
-                        // x - y as fma(-1, y, x): the same rounding as the subtraction
-                        const float2 m1 = make_float2(-1.0f, -1.0f);
-#pragma unroll
-                        for (int o = 0; o < RZ; o += 2) {
-                            auto pr = [&](int k) { return make_float2(Pq[k][o], Pq[k][o + 1]); };
-                            float2 dd = __fmul2_rn(cc.wy2[0], __ffma2_rn(m1, pr(N - 1), pr(N)));
-#pragma unroll
-                            for (int k = 1; k < N; ++k)
-                                dd = __ffma2_rn(cc.wy2[k], __ffma2_rn(m1, pr(N - 1 - k), pr(N + k)), dd);
-                            a[o] = dd.x;
-                            a[o + 1] = dd.y;
+                    const bool out = s >= y0;
+                    const int st = st_next;
+                    if (out) st_next = st_next + 1 == NS ? 0 : st_next + 1;
+                    Col<T> pin = pnext;  // P(s+2N-1)
+                    if (out) {
+                        // output plane y = s: its copies (plane box, P_old, (v dt)^2, and the
+                        // own tile of P at y+2N-1) have arrived once the barrier passes
+                        bool ok = true;
+                        if ((inflight >> st) & 1u) ok = mbar_wait_bounded(&bar[st], (phase_bits >> st) & 1u, kWaitLimit3);
+                        if (__syncthreads_or(!ok)) {
+                            failed = true;
+                            break;
                         }
-                    } else {
-#pragma unroll
-                        for (int o = 0; o < RZ; ++o) {
-                            T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
-#pragma unroll
-                            for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
-                            a[o] = dd;
-                        }
+                        phase_bits ^= 1u << st;
+                        inflight &= ~(1u << st);
+                        // every thread is past plane s-1: its stage takes plane s+NS-1
+                        issue(s + NS - 1);
+                        if (act) pin = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kQ) + c0 * TZ + r0);
+                    } else if (act && s + 1 < y0) {
+                        pnext = ldc_nc(P + own + (int64_t)(s + NQ) * ldxy);  // the next warm-up step's plane
                     }
-                    if (item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
-                        Col<T> av;
+                    // queue in: P(s+2N-1)
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) av.v[o] = a[o];
-                        av = y_band_first<T>(d, cur, i0, j, pa, pa >= y0 && pa < y1, av);
+                    for (int k = 0; k < NQ - 1; ++k)
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) a[o] = av.v[o];
-                    }
+                        for (int o = 0; o < RZ; ++o) Pq[k][o] = Pq[k + 1][o];
+#pragma unroll
+                    for (int o = 0; o < RZ; ++o) Pq[NQ - 1][o] = pin.v[o];
+                    // A_y at plane pa = s+N-1: D+ from P(s .. s+2N-1), phi_y in the y bands
                     {
-                        Col<T> w;
-#pragma unroll
-                        for (int o = 0; o < RZ; ++o) w.v[o] = a[o];
-                        Aq[u * NT] = w;
-                    }
-                }
-                if (!out) continue;
-                const int y = s;
-                const T* Pb = reinterpret_cast<const T*>(smem + st * G::kPlane);
-                if (bz || bx) {
-                    band_plane_stage1<T, N>(cc, d, cur, Pb, z0, x0, y, bz, bx, scratch);
-                    __syncthreads();
-                }
-                if (act) {
-                    T lz[RZ], lx[RZ], ly[RZ];
-                    zx_second<T, N>(cc, d, Pb, scratch, bz, bx, i0, j, y, r0, c0, lz, lx);
-                    // D- A_y at plane y from A_y(y-N .. y+N-1) (all 2N slots, weights of
-                    // queue position u), psi_y in the y bands
-                    {
-                        Col<T> a[NQ];
-#pragma unroll
-                        for (int q = 0; q < NQ; ++q) a[q] = Aq[q * NT];
+                        const int pa = s + N - 1;
+                        T a[RZ];
                         if constexpr (batch::kPacked<T>) {
-                            const float2* wq = cc.wyq2 + u * 16;
+                            // x - y as fma(-1, y, x): the same rounding as the subtraction
+                            const float2 m1 = make_float2(-1.0f, -1.0f);
 #pragma unroll
                             for (int o = 0; o < RZ; o += 2) {
-                                float2 dd = __fmul2_rn(wq[0], make_float2(a[0].v[o], a[0].v[o + 1]));
+                                auto pr = [&](int k) { return make_float2(Pq[k][o], Pq[k][o + 1]); };
+                                float2 dd = __fmul2_rn(cc.wy2[0], __ffma2_rn(m1, pr(N - 1), pr(N)));
 #pragma unroll
-                                for (int q = 1; q < NQ; ++q)
-                                    dd = __ffma2_rn(wq[q], make_float2(a[q].v[o], a[q].v[o + 1]), dd);
-                                ly[o] = dd.x;
-                                ly[o + 1] = dd.y;
+                                for (int k = 1; k < N; ++k)
+                                    dd = __ffma2_rn(cc.wy2[k], __ffma2_rn(m1, pr(N - 1 - k), pr(N + k)), dd);
+                                a[o] = dd.x;
+                                a[o + 1] = dd.y;
                             }
                         } else {
-                            const T* wq = cc.wyq + u * 16;
 #pragma unroll
                             for (int o = 0; o < RZ; ++o) {
-                                T dd = wq[0] * a[0].v[o];
+                                T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
 #pragma unroll
-                                for (int q = 1; q < NQ; ++q) dd = fma(wq[q], a[q].v[o], dd);
-                                ly[o] = dd;
+                                for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
+                                a[o] = dd;
                             }
                         }
-                    }
-                    if (item_yband && (y < nB || y >= ny - nB)) {
-                        Col<T> lv;
+                        if (!kLean && item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
+                            Col<T> av;
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) lv.v[o] = ly[o];
-                        lv = y_band_second<T>(d, i0, j, y, lv);
+                            for (int o = 0; o < RZ; ++o) av.v[o] = a[o];
+                            av = y_band_first<T>(d, cur, i0, j, pa, pa >= y0 && pa < y1, av);
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) ly[o] = lv.v[o];
-                    }
-                    // update
-                    const int64_t qi = (int64_t)i0 + (int64_t)j * nz + (int64_t)y * nz * nx;  // interior index
-                    T lap[RZ], pn[RZ];
-                    if constexpr (batch::kPacked<T>) {
-#pragma unroll
-                        for (int o = 0; o < RZ; o += 2) {
-                            const float2 l = __fadd2_rn(__fadd2_rn(make_float2(lz[o], lz[o + 1]), make_float2(lx[o], lx[o + 1])),
-                                                        make_float2(ly[o], ly[o + 1]));
-                            lap[o] = l.x;
-                            lap[o + 1] = l.y;
+                            for (int o = 0; o < RZ; ++o) a[o] = av.v[o];
                         }
-                    } else {
+                        {
+                            Col<T> w;
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) lap[o] = (lz[o] + lx[o]) + ly[o];
-                    }
-                    if (item_src) {
-                        if (d.src_dense) {
-                            const T* sd = d.src_dense + (int64_t)(tau - d.dense_t0) * ((int64_t)nz * nx * ny) + qi;
-#pragma unroll
-                            for (int o = 0; o < RZ; ++o)
-                                if (i0 + o < nz) lap[o] += sd[o];
+                            for (int o = 0; o < RZ; ++o) w.v[o] = a[o];
+                            Aq[u * NT] = w;
                         }
-                        for (int q = 0; q < d.nsrc; ++q)
-                            if (d.src_iy[q] == y && d.src_ix[q] == j && d.src_iz[q] >= i0 && d.src_iz[q] < i0 + RZ) {
+                    }
+                    if (!out) continue;
+                    const int y = s;
+                    const T* Pb = reinterpret_cast<const T*>(smem + st * G::kPlane);
+                    if (!kLean && (bz || bx)) {
+                        band_plane_stage1<T, N>(cc, d, cur, Pb, z0, x0, y, bz, bx, scratch);
+                        __syncthreads();
+                    }
+                    if (act) {
+                        T lz[RZ], lx[RZ], ly[RZ];
+                        zx_second<T, N>(cc, d, Pb, scratch, !kLean && bz, !kLean && bx, i0, j, y, r0, c0, lz, lx);
+                        // D- A_y at plane y from A_y(y-N .. y+N-1) (all 2N slots, weights of
+                        // queue position u), psi_y in the y bands
+                        {
+                            Col<T> a[NQ];
+#pragma unroll
+                            for (int q = 0; q < NQ; ++q) a[q] = Aq[q * NT];
+                            if constexpr (batch::kPacked<T>) {
+                                const float2* wq = cc.wyq2 + u * 16;
+#pragma unroll
+                                for (int o = 0; o < RZ; o += 2) {
+                                    float2 dd = __fmul2_rn(wq[0], make_float2(a[0].v[o], a[0].v[o + 1]));
+#pragma unroll
+                                    for (int q = 1; q < NQ; ++q)
+                                        dd = __ffma2_rn(wq[q], make_float2(a[q].v[o], a[q].v[o + 1]), dd);
+                                    ly[o] = dd.x;
+                                    ly[o + 1] = dd.y;
+                                }
+                            } else {
+                                const T* wq = cc.wyq + u * 16;
+#pragma unroll
+                                for (int o = 0; o < RZ; ++o) {
+                                    T dd = wq[0] * a[0].v[o];
+#pragma unroll
+                                    for (int q = 1; q < NQ; ++q) dd = fma(wq[q], a[q].v[o], dd);
+                                    ly[o] = dd;
+                                }
+                            }
+                        }
+                        if (!kLean && item_yband && (y < nB || y >= ny - nB)) {
+                            Col<T> lv;
+#pragma unroll
+                            for (int o = 0; o < RZ; ++o) lv.v[o] = ly[o];
+                            lv = y_band_second<T>(d, i0, j, y, lv);
+#pragma unroll
+                            for (int o = 0; o < RZ; ++o) ly[o] = lv.v[o];
+                        }
+                        // update
+                        const int64_t qi = (int64_t)i0 + (int64_t)j * nz + (int64_t)y * nz * nx;  // interior index
+                        T lap[RZ], pn[RZ];
+                        if constexpr (batch::kPacked<T>) {
+#pragma unroll
+                            for (int o = 0; o < RZ; o += 2) {
+                                const float2 l = __fadd2_rn(__fadd2_rn(make_float2(lz[o], lz[o + 1]), make_float2(lx[o], lx[o + 1])),
+                                                            make_float2(ly[o], ly[o + 1]));
+                                lap[o] = l.x;
+                                lap[o + 1] = l.y;
+                            }
+                        } else {
+#pragma unroll
+                            for (int o = 0; o < RZ; ++o) lap[o] = (lz[o] + lx[o]) + ly[o];
+                        }
+                        if (!kLean && item_src) {
+                            if (d.src_dense) {
+                                const T* sd = d.src_dense + (int64_t)(tau - d.dense_t0) * ((int64_t)nz * nx * ny) + qi;
 #pragma unroll
                                 for (int o = 0; o < RZ; ++o)
-                                    if (d.src_iz[q] == i0 + o) lap[o] += d.src_wavelet[(int64_t)q * d.nt + tau];
+                                    if (i0 + o < nz) lap[o] += sd[o];
                             }
-                    }
-                    const T* pc = Pq[0];
-                    const Col<T> po = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kO) + c0 * TZ + r0);
-                    const Col<T> vv = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kV) + c0 * TZ + r0);
-                    if constexpr (batch::kPacked<T>) {
+                            for (int q = 0; q < d.nsrc; ++q)
+                                if (d.src_iy[q] == y && d.src_ix[q] == j && d.src_iz[q] >= i0 && d.src_iz[q] < i0 + RZ) {
 #pragma unroll
-                        for (int o = 0; o < RZ; o += 2) {
-                            const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc[o], pc[o + 1]),
-                                                        make_float2(-po.v[o], -po.v[o + 1]));
-                            const float2 r = __ffma2_rn(make_float2(vv.v[o], vv.v[o + 1]), make_float2(lap[o], lap[o + 1]), t);
-                            pn[o] = r.x;
-                            pn[o + 1] = r.y;
+                                    for (int o = 0; o < RZ; ++o)
+                                        if (d.src_iz[q] == i0 + o) lap[o] += d.src_wavelet[(int64_t)q * d.nt + tau];
+                                }
                         }
-                    } else {
+                        const T* pc = Pq[0];
+                        const Col<T> po = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kO) + c0 * TZ + r0);
+                        const Col<T> vv = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kV) + c0 * TZ + r0);
+                        if constexpr (batch::kPacked<T>) {
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o) pn[o] = fma(vv.v[o], lap[o], fma(T(2), pc[o], -po.v[o]));
-                    }
-                    T* dst = Pnew + own + (int64_t)y * ldxy;
-                    if (i0 + RZ <= nz) {
-                        stc(dst, pn);
-                    } else {
+                            for (int o = 0; o < RZ; o += 2) {
+                                const float2 t = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(pc[o], pc[o + 1]),
+                                                            make_float2(-po.v[o], -po.v[o + 1]));
+                                const float2 r = __ffma2_rn(make_float2(vv.v[o], vv.v[o + 1]), make_float2(lap[o], lap[o + 1]), t);
+                                pn[o] = r.x;
+                                pn[o + 1] = r.y;
+                            }
+                        } else {
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o)
-                            if (i0 + o < nz) dst[o] = pn[o];
-                    }
-                    if (rec_here) d.rec[j + (int64_t)y * nx + (int64_t)tau * nx * ny] = pn[0];
-                    if (item_snap) {
-                        T* sn = d.snap + (int64_t)(tau - d.snap_t0) * ((int64_t)nz * nx * ny) + qi;
+                            for (int o = 0; o < RZ; ++o) pn[o] = fma(vv.v[o], lap[o], fma(T(2), pc[o], -po.v[o]));
+                        }
+                        T* dst = Pnew + own + (int64_t)y * ldxy;
+                        if (kLean || i0 + RZ <= nz) {
+                            stc(dst, pn);
+                        } else {
 #pragma unroll
-                        for (int o = 0; o < RZ; ++o)
-                            if (i0 + o < nz) sn[o] = pn[o];
+                            for (int o = 0; o < RZ; ++o)
+                                if (i0 + o < nz) dst[o] = pn[o];
+                        }
+                        if (rec_here) d.rec[j + (int64_t)y * nx + (int64_t)tau * nx * ny] = pn[0];
+                        if (!kLean && item_snap) {
+                            T* sn = d.snap + (int64_t)(tau - d.snap_t0) * ((int64_t)nz * nx * ny) + qi;
+#pragma unroll
+                            for (int o = 0; o < RZ; ++o)
+                                if (i0 + o < nz) sn[o] = pn[o];
+                        }
                     }
                 }
             }
-        }
+        };
+        if (lean)
+            plane_loop(std::true_type{});
+        else
+            plane_loop(std::false_type{});
         __syncthreads();  // every thread has read s_item
         if (tid == 0) s_item = (int)gridDim.x + atomicAdd(next, 1);
         __syncthreads();
