@@ -118,7 +118,7 @@ FWD_STEP_DRAM_BYTES = 35_389_440
 FWD64_STEP_DRAM_BYTES = 42_662_912
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
-STEP3D_DRAM_BYTES = 454_952_448 + 170_105_600
+STEP3D_DRAM_BYTES = 454_435_840 + 169_676_544
 # the same for one batched step of the 64-shot workload while all 64 shots are
 # active (the 301st launch), from `ncu --metrics dram__bytes_read.sum,
 # dram__bytes_write.sum,gpu__time_duration.sum -k regex:batch2d -s 300 -c 2
