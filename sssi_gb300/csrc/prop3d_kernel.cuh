@@ -545,8 +545,11 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
 #pragma unroll
                 for (int o = 0; o < RZ; ++o) Pq[k][o] = T(0);
             // P(ys .. ys+2N-2) (planes below 0 are the zero padding); threads
-            // outside the grid load nothing
-            Col<T> pnext{};
+            // outside the grid load nothing.  The warm-up steps (s < y0) take
+            // P(s+2N-1) from global memory, loaded kAhead steps ahead so that the
+            // short steps do not each wait for a load: pw[k] = P(s+2N-1+k).
+            constexpr int kAhead = 3;
+            Col<T> pw[kAhead] = {};
             if (act) {
 #pragma unroll
                 for (int k = 1; k < NQ; ++k) {
@@ -554,18 +557,79 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
 #pragma unroll
                     for (int o = 0; o < RZ; ++o) Pq[k][o] = v.v[o];
                 }
-                pnext = ldc_nc(P + own + (int64_t)(ys + NQ - 1) * ldxy);  // P(s+2N-1) for the first step
+#pragma unroll
+                for (int k = 0; k < kAhead; ++k)
+                    if (ys + k < y0) pw[k] = ldc_nc(P + own + (int64_t)(ys + NQ - 1 + k) * ldxy);
             }
 
             int u = 0;        // (s - ys) mod NQ
             int st_next = 0;  // ring stage of the next output plane
-            for (int s = ys; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
+            // queue in P(s+2N-1), then A_y at plane s+N-1 into slot u
+            auto queue_in = [&](const Col<T>& pin, int s, int u) {
+                // queue in: P(s+2N-1)
+#pragma unroll
+                for (int k = 0; k < NQ - 1; ++k)
+#pragma unroll
+                    for (int o = 0; o < RZ; ++o) Pq[k][o] = Pq[k + 1][o];
+#pragma unroll
+                for (int o = 0; o < RZ; ++o) Pq[NQ - 1][o] = pin.v[o];
+                // A_y at plane pa = s+N-1: D+ from P(s .. s+2N-1), phi_y in the y bands
                 {
-                    const bool out = s >= y0;
+                    const int pa = s + N - 1;
+                    T a[RZ];
+                    if constexpr (batch::kPacked<T>) {
+                        // x - y as fma(-1, y, x): the same rounding as the subtraction
+                        const float2 m1 = make_float2(-1.0f, -1.0f);
+#pragma unroll
+                        for (int o = 0; o < RZ; o += 2) {
+                            auto pr = [&](int k) { return make_float2(Pq[k][o], Pq[k][o + 1]); };
+                            float2 dd = __fmul2_rn(cc.wy2[0], __ffma2_rn(m1, pr(N - 1), pr(N)));
+#pragma unroll
+                            for (int k = 1; k < N; ++k)
+                                dd = __ffma2_rn(cc.wy2[k], __ffma2_rn(m1, pr(N - 1 - k), pr(N + k)), dd);
+                            a[o] = dd.x;
+                            a[o + 1] = dd.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) {
+                            T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
+#pragma unroll
+                            for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
+                            a[o] = dd;
+                        }
+                    }
+                    if (!kLean && item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
+                        Col<T> av;
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) av.v[o] = a[o];
+                        av = y_band_first<T>(d, cur, i0, j, pa, pa >= y0 && pa < y1, av);
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) a[o] = av.v[o];
+                    }
+                    {
+                        Col<T> w;
+#pragma unroll
+                        for (int o = 0; o < RZ; ++o) w.v[o] = a[o];
+                        Aq[u * NT] = w;
+                    }
+                }
+            };
+            // warm-up: the first 2N-1 planes only fill the queues
+            for (int s = ys; s < y0; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
+                const Col<T> pin = pw[0];  // P(s+2N-1)
+#pragma unroll
+                for (int k = 0; k + 1 < kAhead; ++k) pw[k] = pw[k + 1];
+                if (act && s + kAhead < y0)  // the plane of warm-up step s + kAhead
+                    pw[kAhead - 1] = ldc_nc(P + own + (int64_t)(s + NQ - 1 + kAhead) * ldxy);
+                queue_in(pin, s, u);
+            }
+            for (int s = y0; s < y1 && !failed; ++s, u = (u + 1 == NQ) ? 0 : u + 1) {
+                {
                     const int st = st_next;
-                    if (out) st_next = st_next + 1 == NS ? 0 : st_next + 1;
-                    Col<T> pin = pnext;  // P(s+2N-1)
-                    if (out) {
+                    st_next = st_next + 1 == NS ? 0 : st_next + 1;
+                    Col<T> pin{};  // P(s+2N-1)
+                    {
                         // output plane y = s: its copies (plane box, P_old, (v dt)^2, and the
                         // own tile of P at y+2N-1) have arrived once the barrier passes
                         bool ok = true;
@@ -579,58 +643,8 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                         // every thread is past plane s-1: its stage takes plane s+NS-1
                         issue(s + NS - 1);
                         if (act) pin = ldc(reinterpret_cast<const T*>(smem + st * G::kPlane + G::kQ) + c0 * TZ + r0);
-                    } else if (act && s + 1 < y0) {
-                        pnext = ldc_nc(P + own + (int64_t)(s + NQ) * ldxy);  // the next warm-up step's plane
                     }
-                    // queue in: P(s+2N-1)
-#pragma unroll
-                    for (int k = 0; k < NQ - 1; ++k)
-#pragma unroll
-                        for (int o = 0; o < RZ; ++o) Pq[k][o] = Pq[k + 1][o];
-#pragma unroll
-                    for (int o = 0; o < RZ; ++o) Pq[NQ - 1][o] = pin.v[o];
-                    // A_y at plane pa = s+N-1: D+ from P(s .. s+2N-1), phi_y in the y bands
-                    {
-                        const int pa = s + N - 1;
-                        T a[RZ];
-                        if constexpr (batch::kPacked<T>) {
-                            // x - y as fma(-1, y, x): the same rounding as the subtraction
-                            const float2 m1 = make_float2(-1.0f, -1.0f);
-#pragma unroll
-                            for (int o = 0; o < RZ; o += 2) {
-                                auto pr = [&](int k) { return make_float2(Pq[k][o], Pq[k][o + 1]); };
-                                float2 dd = __fmul2_rn(cc.wy2[0], __ffma2_rn(m1, pr(N - 1), pr(N)));
-#pragma unroll
-                                for (int k = 1; k < N; ++k)
-                                    dd = __ffma2_rn(cc.wy2[k], __ffma2_rn(m1, pr(N - 1 - k), pr(N + k)), dd);
-                                a[o] = dd.x;
-                                a[o + 1] = dd.y;
-                            }
-                        } else {
-#pragma unroll
-                            for (int o = 0; o < RZ; ++o) {
-                                T dd = cc.wy[0] * (Pq[N][o] - Pq[N - 1][o]);
-#pragma unroll
-                                for (int k = 1; k < N; ++k) dd = fma(cc.wy[k], Pq[N + k][o] - Pq[N - 1 - k][o], dd);
-                                a[o] = dd;
-                            }
-                        }
-                        if (!kLean && item_yband && pa >= 0 && pa < ny && (pa < nB || pa >= ny - nB) && act) {
-                            Col<T> av;
-#pragma unroll
-                            for (int o = 0; o < RZ; ++o) av.v[o] = a[o];
-                            av = y_band_first<T>(d, cur, i0, j, pa, pa >= y0 && pa < y1, av);
-#pragma unroll
-                            for (int o = 0; o < RZ; ++o) a[o] = av.v[o];
-                        }
-                        {
-                            Col<T> w;
-#pragma unroll
-                            for (int o = 0; o < RZ; ++o) w.v[o] = a[o];
-                            Aq[u * NT] = w;
-                        }
-                    }
-                    if (!out) continue;
+                    queue_in(pin, s, u);
                     const int y = s;
                     const T* Pb = reinterpret_cast<const T*>(smem + st * G::kPlane);
                     if (!kLean && (bz || bx)) {
