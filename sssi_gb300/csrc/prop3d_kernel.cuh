@@ -546,9 +546,10 @@ __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
                 for (int o = 0; o < RZ; ++o) Pq[k][o] = T(0);
             // P(ys .. ys+2N-2) (planes below 0 are the zero padding); threads
             // outside the grid load nothing.  The warm-up steps (s < y0) take
-            // P(s+2N-1) from global memory, loaded kAhead steps ahead so that the
-            // short steps do not each wait for a load: pw[k] = P(s+2N-1+k).
-            constexpr int kAhead = 3;
+            // P(s+2N-1) from global memory, loaded kAhead steps ahead (all of them
+            // at once up to order 4) so that the short steps do not each wait for
+            // a load: pw[k] = P(s+2N-1+k).
+            constexpr int kAhead = 2 * N - 1 < 7 ? 2 * N - 1 : 7;
             Col<T> pw[kAhead] = {};
             if (act) {
 #pragma unroll
