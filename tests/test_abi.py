@@ -224,3 +224,23 @@ def test_elastic3d_bad_arguments_and_gateway_message(lib):
     gw = O.load_shim_library(ROOT / "oracle" / "_build" / "mexgw_fwdTimeSpmlFor3dEw_mex.so")
     with pytest.raises(O.MexError, match="All 11 input arguments shall be provided!"):
         O.shim_call(gw, 6, v, v)
+
+
+def test_debug_entries_check_arguments(lib):
+    """The test entries of the strict division and the 3D schedule tuner reject
+    bad arguments before touching a GPU; with no 3D propagation tuned yet the
+    schedule query reports -1 (this process has run none)."""
+    fast = np.zeros(4)
+    ieee = np.zeros(4)
+    a = np.ones(4)
+    assert lib.sssi_debug_divide(a.ctypes.data, -1, 10.0, fast.ctypes.data, ieee.ctypes.data) == 1
+    assert lib.sssi_debug_divide(None, 4, 10.0, fast.ctypes.data, ieee.ctypes.data) == 1
+    assert b"NULL" in lib.sssi_last_error()
+    assert lib.sssi_debug_divide(None, 0, 10.0, None, None) == 0  # nothing to divide
+    assert lib.sssi_debug_schedule3d(None, None) == 1
+    import ctypes
+
+    sched = ctypes.c_int(7)
+    ms = (ctypes.c_float * 4)()
+    assert lib.sssi_debug_schedule3d(ctypes.byref(sched), ms) == 0
+    assert sched.value == -1 and list(ms) == [0.0] * 4
