@@ -118,7 +118,7 @@ FWD_STEP_DRAM_BYTES = 35_389_440
 FWD64_STEP_DRAM_BYTES = 42_662_912
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
 # `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
-STEP3D_DRAM_BYTES = 454_435_840 + 169_676_544
+STEP3D_DRAM_BYTES = 394_253_824 + 118_571_008
 # the same for one batched step of the 64-shot workload while all 64 shots are
 # active (the 301st launch), from `ncu --metrics dram__bytes_read.sum,
 # dram__bytes_write.sum,gpu__time_duration.sum -k regex:batch2d -s 300 -c 2
@@ -552,9 +552,9 @@ def bench_3d(S, args):
     err = float(torch.linalg.norm((a - b).flatten()) / torch.linalg.norm(b.flatten()))
     cells = nz * nx * ny * nt
     # algorithmic bytes of one step: 16 B per cell, plus per damped cell and axis
-    # the compensated phi (read, write) and psi (read, write), 32 B (the band
-    # coefficients vary in two dimensions only and stay cached)
-    alg3 = 16.0 * nz * nx * ny + 32.0 * nb * (nx * ny + 2 * nz * ny + 2 * nz * nx)
+    # phi (read, write) and psi (read, write), 16 B (the band coefficients vary in
+    # two dimensions only and stay cached)
+    alg3 = 16.0 * nz * nx * ny + 16.0 * nb * (nx * ny + 2 * nz * ny + 2 * nz * nx)
     return {"metric": "Gcell-updates/s (3D forward shot, 256^3 + 16-cell bands = 272x288x288, nt=%d)" % nt,
             "value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_shot": round(ms, 2),
             "us_per_step": round(ms * 1e3 / nt, 2), "dtype": "fp32", "shots": len(times),

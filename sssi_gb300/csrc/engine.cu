@@ -204,7 +204,8 @@ class Engine final : public EngineBase {
         }
         const int64_t vol = (nz + 2 * HZ + 3) * (nx + 2 * L) * (ny + 2 * L);
         const size_t band3 = (size_t)(nB * nx * ny + nz * 2 * nB * ny + nz * nx * 2 * nB);
-        return 3 * ts * (size_t)vol + 3 * ms * band3 + ts * (size_t)(nx * ny * nt) + wav + 8 * (size_t)(nz * nx * ny);
+        const size_t ms3 = sizeof(typename MemVar3<T>::type);
+        return 3 * ts * (size_t)vol + 3 * ms3 * band3 + ts * (size_t)(nx * ny * nt) + wav + 8 * (size_t)(nz * nx * ny);
     }
 
     void admit(const ReqPtr& r) override {

@@ -47,12 +47,21 @@ struct Shape3D<double> {
     static constexpr int kMinBlocks = 1;
 };
 
+// CPML memory variables of the 3D propagator: one word of the field's type.
+// (The 2D FP32 forms carry theirs as compensated pairs for the RTM residual;
+// the 3D propagator models forward only, where plain FP32 memory variables
+// leave the receivers within a few 1e-7 of FP64.)
+template <typename T>
+struct MemVar3 {
+    using type = T;
+};
+
 // Candidate work-item schedules of a 3D propagation, timed on its first steps.
 constexpr int kSchedules3 = kSchedules3Max;
 
 template <typename T>
 struct Desc3 {
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     CUtensorMap tm_plane[2];  // plane tile of field k with its z/x halo
     CUtensorMap tm_tile[2];   // plane tile of field k without halo (P_old)
     CUtensorMap tm_v;         // plane tile of (v dt)^2
@@ -101,7 +110,7 @@ struct Const3 {
 template <typename T>
 class Prop3d {
   public:
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     Prop3d(const double* v, int64_t nz, int64_t nx, int64_t ny, int N, int nB, double dz, double dx, double dy,
            double dt, int nt, cudaStream_t stream);
     ~Prop3d();

@@ -15,6 +15,9 @@ namespace p3 {
 using batch::ldg_t;
 using batch::mem_add;
 using batch::mem_new;
+// FP32 memory variables (MemVar3): phi <- b phi + (b-1) d, as the FP64 form
+__device__ __forceinline__ float mem_new(float b, float bm1, float m, float d) { return fmaf(b, m, bm1 * d); }
+__device__ __forceinline__ float mem_add(float d, float m) { return d + m; }
 
 // The RZ cells of one thread's column segment: one 16-byte access.
 template <typename T>
@@ -92,7 +95,7 @@ template <typename T, int N>
 __device__ __noinline__ void band_plane_stage1(const Const3<T>& cc, const Desc3<T>& d, int ph, const T* Pb, int z0,
                                                int x0, int y, bool bz, bool bx, T* scratch) {
     using G = Layout3<T, N>;
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int TZ = G::TZ, TX = G::TX, NT = Shape3D<T>::kThreads;
     constexpr int L = G::L, HZ = G::HZ, SP = G::SP;
     const int tid = threadIdx.x;
@@ -206,7 +209,7 @@ template <typename T, int N>
 __device__ __forceinline__ Col<T> z_band_second(const Const3<T>& cc, const Desc3<T>& d, const T* scratch, int i0, int j,
                                              int y, int r0, int c0) {
     using G = Layout3<T, N>;
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int RZ = G::RZ;
     constexpr int ZW = (2 * N + RZ - 1 + RZ - 1) / RZ;
     const int nz = d.nz, nx = d.nx, nB = d.nB;
@@ -259,7 +262,7 @@ template <typename T, int N>
 __device__ __forceinline__ Col<T> x_band_second(const Const3<T>& cc, const Desc3<T>& d, const T* scratch, int i0, int j,
                                              int y, int r0, int c0) {
     using G = Layout3<T, N>;
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int RZ = G::RZ, TZ = G::TZ;
     const int nz = d.nz, nx = d.nx, nB = d.nB;
     M* xpsi = d.xpsi + (int64_t)y * nz * 2 * nB;
@@ -303,7 +306,7 @@ __device__ __forceinline__ Col<T> x_band_second(const Const3<T>& cc, const Desc3
 // plane belongs to this work item.
 template <typename T>
 __device__ __forceinline__ Col<T> y_band_first(const Desc3<T>& d, int cur, int i0, int j, int pa, bool store, Col<T> a) {
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int RZ = Col<T>::R;
     const int nz = d.nz, nx = d.nx, ny = d.ny, nB = d.nB;
     const int cb = pa < nB ? pa : nB + pa - (ny - nB);
@@ -332,7 +335,7 @@ __device__ __forceinline__ Col<T> y_band_first(const Desc3<T>& d, int cur, int i
 // psi_y at plane y (a y band plane): D- A_y + psi.
 template <typename T>
 __device__ __forceinline__ Col<T> y_band_second(const Desc3<T>& d, int i0, int j, int y, Col<T> l) {
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int RZ = Col<T>::R;
     const int nz = d.nz, nx = d.nx, ny = d.ny, nB = d.nB;
     const int cb = y < nB ? y : nB + y - (ny - nB);
@@ -447,7 +450,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(Shape3D<T>::kThreads, Shape3D<T>::kMinBlocks)
     prop3d_kernel(const Desc3<T>* __restrict__ dp, const __grid_constant__ Const3<T> cc) {
     using G = Layout3<T, N>;
-    using M = typename MemVar<T>::type;
+    using M = typename MemVar3<T>::type;
     constexpr int TZ = G::TZ, TX = G::TX, RZ = G::RZ;
     constexpr int NS = G::kStages;
     constexpr int NQ = 2 * N;  // queue length
