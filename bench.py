@@ -117,7 +117,8 @@ FWD_STEP_DRAM_BYTES = 35_389_440
 # (42,652,672 B read, 10,240 B written: the step's writes stay in L2)
 FWD64_STEP_DRAM_BYTES = 42_662_912
 # the same for one 3D step of the 272 x 288 x 288 grid with 16-cell bands, from
-# `ncu --set full -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+# --clock-control none -k regex:prop3d_kernel -s 2 -c 1 python bench.py --case step3d-fp32`
 STEP3D_DRAM_BYTES = 394_253_824 + 118_571_008
 # the same for one batched step of the 64-shot workload while all 64 shots are
 # active (the 301st launch), from `ncu --metrics dram__bytes_read.sum,
