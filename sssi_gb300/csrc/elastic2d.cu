@@ -163,10 +163,10 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase1_kernel(const __gr
         const T dVxz = el_diff<T, N, kMode, true>(p.Vx, q, 1, c, wz, dz);     // Vx(2:end, ix), dim 1
         const T dVzx = el_diff<T, N, kMode, true>(p.Vz, q, ldp, c, wx, dx);   // Vz(iz, 2:end), dim 2
         const bool xb = j < p.nB || j >= p.nx - p.nB, zb = i >= p.nz - p.nB;  // damped along x / z
-        const T ax = el_raxpby<T, kMode>(xb, rx, p.Ax[q], sx, dVxx);
-        const T az = el_raxpby<T, kMode>(zb, rz, p.Az[q], sz, dVzz);
-        const T bz = el_raxpby<T, kMode>(zb, rz, p.Bz[q], sz, dVxz);
-        const T bx = el_sub<T, kMode>(el_rx<T, kMode>(xb, rx, p.Bx[q]), el_mul<T, kMode>(sx, dVzx));
+        const T ax = el_raxpby<T, kMode, true>(xb, rx, p.Ax[q], sx, dVxx);
+        const T az = el_raxpby<T, kMode, true>(zb, rz, p.Az[q], sz, dVzz);
+        const T bz = el_raxpby<T, kMode, true>(zb, rz, p.Bz[q], sz, dVxz);
+        const T bx = el_sub<T, kMode>(el_rx<T, kMode, true>(xb, rx, p.Bx[q]), el_mul<T, kMode>(sx, dVzx));
         p.Ax[q] = ax;
         p.Az[q] = az;
         p.Bz[q] = bz;
@@ -222,14 +222,14 @@ __global__ void __launch_bounds__(kElThreads) elastic2d_phase2_kernel(const __gr
                 src = has_src ? src + wv : wv;
                 has_src = true;
             }
-        T vzp = el_raxpby<T, kMode>(zb, rz, p.Vzp[q], kzp, dAz);
-        T vxp = el_raxpby<T, kMode>(xb, rx, p.Vxp[q], kxp, dAx);
+        T vzp = el_raxpby<T, kMode, true>(zb, rz, p.Vzp[q], kzp, dAz);
+        T vxp = el_raxpby<T, kMode, true>(xb, rx, p.Vxp[q], kxp, dAx);
         if (has_src) {
             vzp = el_add<T, kMode>(vzp, el_mul<T, kMode>(sz, src));
             vxp = el_add<T, kMode>(vxp, el_mul<T, kMode>(sx, src));
         }
-        const T vzs = el_sub<T, kMode>(el_rx<T, kMode>(xb, rx, p.Vzs[q]), el_mul<T, kMode>(kzs, dBx));
-        const T vxs = el_raxpby<T, kMode>(zb, rz, p.Vxs[q], kxs, dBz);
+        const T vzs = el_sub<T, kMode>(el_rx<T, kMode, true>(xb, rx, p.Vzs[q]), el_mul<T, kMode>(kzs, dBx));
+        const T vxs = el_raxpby<T, kMode, true>(zb, rz, p.Vxs[q], kxs, dBz);
         p.Vzp[q] = vzp;
         p.Vxp[q] = vxp;
         p.Vzs[q] = vzs;

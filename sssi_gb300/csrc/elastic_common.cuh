@@ -63,21 +63,22 @@ __device__ __forceinline__ T el_axpby(T r, T x, T s, T y) {
 }
 // r * x for a damping factor r that is exactly 1 outside its band: there the
 // product is x itself, and the FP64 forms (bound by the FP64 pipe) do not form
-// it; FP32 multiplies anyway (the same value either way)
-template <typename T, int kMode>
+// it; FP32 forms it unless kSkip32 (the same value either way: measured, the 2D
+// FP32 step gains from skipping it, the 3D one loses)
+template <typename T, int kMode, bool kSkip32 = false>
 __device__ __forceinline__ T el_rx(bool damped, T r, T x) {
-    if constexpr (kMode == SSSI_MODE_FP32)
+    if constexpr (kMode == SSSI_MODE_FP32 && !kSkip32)
         return r * x;
     else
         return damped ? el_mul<T, kMode>(r, x) : x;
 }
 // el_axpby with r = 1 outside the band (see el_rx)
-template <typename T, int kMode>
+template <typename T, int kMode, bool kSkip32 = false>
 __device__ __forceinline__ T el_raxpby(bool damped, T r, T x, T s, T y) {
     if constexpr (kMode == SSSI_MODE_FP64_STRICT)
         return __dadd_rn(el_rx<T, kMode>(damped, r, x), __dmul_rn(s, y));
     else
-        return fma(s, y, el_rx<T, kMode>(damped, r, x));
+        return fma(s, y, el_rx<T, kMode, kSkip32>(damped, r, x));
 }
 template <typename T, int kMode>
 __device__ __forceinline__ T el_div(T a, T b) {
